@@ -1,0 +1,223 @@
+/*
+ * wukong_gpu.h - C ABI of the GB300-native graph-exploration operator library.
+ *
+ * The operator surface is the per-triple-pattern API of the Wukong+G GPU engine:
+ * a history table of int32 vertex-id rows (row-major, `cols` columns) goes in
+ * together with the pattern's start column, predicate id, direction and a
+ * constant or variable end, and the expanded history comes out.  The library
+ * owns the device store (packed-key hash buckets + per-predicate edge
+ * segments on HBM) and the device history buffers, exactly as the reference's
+ * RCache owns its store and ping-pong result buffers.
+ *
+ * Conventions (all entry points):
+ *   - return an int status: WK_OK (0) or one of the negative WK_E* codes below;
+ *     nothing aborts.  wk_last_error() gives a one-line message for the
+ *     calling thread's last failure.
+ *   - variable ids follow the reference encoding (core/query.hpp:141-154):
+ *     a value >= 0 is a constant vertex id, a value < 0 is variable -v-1
+ *     (column index); direction IN = 0, OUT = 1 (core/gstore.hpp:107).
+ *   - vertex ids are >= 2^17, predicate and type ids are in [1, 2^17)
+ *     (datagen/generate_data.cpp:88-98); pid 1 is rdf:type.
+ *   - a wk_ctx is used by one host thread at a time (the reference's
+ *     one-query-at-a-time GPU lock, core/gpu.hpp:49-61); several contexts may
+ *     share one device store through wk_ctx_share_store.
+ *
+ * No torch or C++ types appear in these signatures.
+ */
+#ifndef WUKONG_GPU_H
+#define WUKONG_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+    WK_OK        = 0,
+    WK_EINVAL    = -1,  /* bad argument or unsupported pattern shape        */
+    WK_ENOMEM    = -2,  /* device or pinned-host allocation failed          */
+    WK_ETIMEDOUT = -3,  /* a bounded device-side wait gave up               */
+    WK_EDEVICE   = -4,  /* CUDA runtime error (no device, launch failure)   */
+    WK_ENOSTORE  = -5,  /* no store has been built/attached to the context  */
+    WK_EOVERFLOW = -6   /* a result exceeded a stated capacity               */
+};
+
+enum { WK_DIR_IN = 0, WK_DIR_OUT = 1 };
+enum { WK_PREDICATE_ID = 0, WK_TYPE_ID = 1 };
+
+typedef struct wk_ctx wk_ctx;
+
+/*
+ * Device history table, the counterpart of request_or_reply's
+ * gpu_history_ptr / gpu_history_table_size / col_num (core/query.hpp:63-65,
+ * :160-174).  `data` is a device pointer owned by the context (never free it);
+ * `size` counts int32 elements (rows * col_num), as in the reference.
+ */
+typedef struct {
+    int32_t *data;      /* device pointer, row-major int32               */
+    int64_t  size;      /* number of int32 elements = rows * col_num     */
+    int32_t  col_num;   /* number of bound columns                       */
+    int32_t  step;      /* number of patterns executed so far            */
+} wk_history;
+
+/* Context configuration (the global_gpu_* knobs of core/config.hpp:66-78). */
+typedef struct {
+    int32_t  device;                 /* CUDA device ordinal                          */
+    int32_t  cache_budget_mb;        /* 0 = whole store resident; > 0 = page
+                                        predicate segments from pinned host memory
+                                        into a device pool of this many MiB
+                                        (core/shard_manager.hpp)                    */
+    int32_t  enable_prefetch;        /* page the next pattern's predicate on a side
+                                        stream (global_gpu_enable_pipeline)         */
+    int32_t  reserved;
+    int64_t  history_capacity;       /* initial int32 capacity of each ping-pong
+                                        history buffer; 0 = 16 Mi elements          */
+} wk_config;
+
+/* ------------------------------------------------------------- context */
+void        wk_config_default(wk_config *cfg);
+int         wk_ctx_create(const wk_config *cfg, wk_ctx **out);
+int         wk_ctx_destroy(wk_ctx *ctx);
+const char *wk_last_error(void);
+const char *wk_status_str(int status);
+int         wk_device_count(int *count);
+
+/* -------------------------------------------------------------- store
+ * Build the device store from ID-form triples (s, p, o), as the reference
+ * loader does from its id_* files (core/dgraph.hpp:268-330,
+ * core/gstore.hpp:600-978): duplicate triples are removed, every non-type
+ * triple is stored in both directions, rdf:type triples (p == 1) become the
+ * per-vertex type list plus the type index, and every predicate gets a
+ * subject index [0|p|IN] and an object index [0|p|OUT].  Adjacency lists are
+ * ascending by neighbour id.  `num_ids` is the number of predicate+type ids
+ * (ids 1..num_ids are valid).
+ */
+int wk_store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o,
+                   int64_t n_triples, int32_t num_ids);
+/* Attach the store of `owner` to `ctx` (read-only sharing, one copy on HBM). */
+int wk_ctx_share_store(wk_ctx *ctx, wk_ctx *owner);
+
+typedef struct {
+    int64_t num_keys;        /* packed (vid,pid,dir) keys                     */
+    int64_t num_edges;       /* int32 edge entries incl. index lists          */
+    int64_t key_bytes;       /* bytes of bucket storage (all predicates)      */
+    int64_t edge_bytes;      /* bytes of edge segments (all predicates)       */
+    int64_t overflow_buckets;/* indirect (overflow) buckets in use            */
+    int64_t device_bytes;    /* bytes of the store resident on the device     */
+    int32_t num_ids;
+    int32_t paged;           /* 1 if predicate segments are paged (cache mode)*/
+} wk_store_info;
+int wk_store_get_info(wk_ctx *ctx, wk_store_info *info);
+
+/* Host-side lookup in the store's host image (no device work): the
+ * counterpart of GStore::get_edges_global (core/gstore.hpp:1129).  Writes at
+ * most `cap` neighbours to `out` and the true degree to *deg. */
+int wk_store_get_edges(wk_ctx *ctx, int64_t vid, int32_t pid, int32_t dir,
+                       int32_t *out, int64_t cap, int64_t *deg);
+
+/* Per-predicate statistics from the built store (GStore::generate_statistic,
+ * core/gstore.hpp:1010-1127): triples, distinct subjects, distinct objects
+ * per id; for class ids the member count is returned in `subjects`. */
+int wk_store_pred_stats(wk_ctx *ctx, int32_t id, int64_t *triples, int64_t *subjects,
+                        int64_t *objects);
+
+/* --------------------------------------------------- per-pattern ops
+ * Counterparts of RCache::{known_to_unknown, known_to_known, known_to_const,
+ * index_to_unknown} (core/rcache.hpp:232, :417, :614, :811) and of the
+ * constant-start step (core/engine.hpp:96-122, done on the host by the
+ * reference GPU engine at core/gpu_engine.hpp:171-189; here on the device).
+ * Each op replaces h->data with a context-owned device buffer holding the
+ * expanded history (ping-pong, like core/rcache.hpp:389-400), updates size and
+ * col_num the way GPU_Engine does (core/gpu_engine.hpp:210-212), and bumps
+ * h->step.  `start` / `end` are reference-encoded ids (negative = variable).
+ */
+int wk_known_to_unknown(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direction,
+                        int32_t predict);
+int wk_known_to_known(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direction,
+                      int32_t predict, int64_t end);
+int wk_known_to_const(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direction,
+                      int32_t predict, int64_t end);
+int wk_index_to_unknown(wk_ctx *ctx, wk_history *h, int32_t index_vertex, int32_t direction);
+int wk_const_to_unknown(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direction,
+                        int32_t predict);
+
+/* History transfer: upload a host table into the context's device buffer
+ * (GPU::load_history_data, core/gpu.hpp:79-88) and download the current
+ * table (the last-step D2H of core/rcache.hpp:402-408). */
+int wk_history_upload(wk_ctx *ctx, wk_history *h, const int32_t *host, int64_t size,
+                      int32_t col_num);
+int wk_history_download(wk_ctx *ctx, const wk_history *h, int32_t *host, int64_t cap);
+void wk_history_init(wk_history *h);
+
+/* ------------------------------------------------------ whole query
+ * Execute every pattern of `cmd_chains` (n_patterns x {start, pid, dir, end},
+ * core/query.hpp:68) with the step dispatch of GPU_Engine::execute_one_step
+ * (core/gpu_engine.hpp:395-467), leaving the final table in *h.  When
+ * `step_rows` is non-null it receives the row count after every step (the
+ * true per-step cardinalities that the estimator trains on).
+ */
+int wk_execute(wk_ctx *ctx, const int64_t *cmd_chains, int32_t n_patterns, wk_history *h,
+               int64_t *step_rows);
+
+/* Per-op timing of the last op (device time from CUDA events, ms) and its
+ * algorithmic bytes (input rows/cols, output rows, adjacency entries read). */
+typedef struct {
+    double  ms;            /* sum of device time of every kernel of the op */
+    double  ms_main;       /* device time of the dominant (expansion) kernel */
+    int64_t rows_in;
+    int64_t rows_out;
+    int32_t cols_in;
+    int32_t kind;          /* 0 k2u, 1 k2k, 2 k2c, 3 i2u, 4 c2u            */
+    int64_t alg_bytes;     /* algorithmic bytes per the roofline formulas   */
+    int64_t kernels;       /* kernel launches of the op                     */
+} wk_op_stats;
+int wk_enable_timing(wk_ctx *ctx, int enable);
+int wk_last_op_stats(wk_ctx *ctx, wk_op_stats *st);
+int64_t wk_kernel_launches(wk_ctx *ctx);   /* cumulative kernel launches */
+int wk_sync(wk_ctx *ctx);
+
+/* ------------------------------------------------ synthetic RDF graphs
+ * Seeded generator of ID-form graphs with the id encoding of
+ * datagen/generate_data.cpp:88-98.  Deterministic across x86_64 and aarch64.
+ * Predicate groups: kind 0 = one-to-many with Zipf(s, cap) out-degree and
+ * uniform objects; kind 1 = functional one-to-one (a bijection); kind 2 =
+ * many-to-one onto a hub set of hub_frac * n_entities vertices.  Each subject
+ * takes part in a predicate with probability `participation`.
+ */
+typedef struct {
+    int32_t kind;
+    int32_t count;
+    double  zipf_s;
+    int32_t zipf_cap;
+    int32_t pad;
+    double  participation;
+    double  hub_frac;
+} wk_pred_group;
+
+typedef struct {
+    uint64_t      seed;
+    int64_t       n_entities;
+    int32_t       n_classes;
+    int32_t       n_groups;
+    wk_pred_group groups[4];
+} wk_graph_spec;
+
+typedef struct wk_graph wk_graph;
+int     wk_graph_generate(const wk_graph_spec *spec, int32_t n_threads, wk_graph **out);
+int64_t wk_graph_size(const wk_graph *g);
+int32_t wk_graph_num_ids(const wk_graph *g);
+int32_t wk_graph_first_class(const wk_graph *g);
+const int32_t *wk_graph_s(const wk_graph *g);
+const int32_t *wk_graph_p(const wk_graph *g);
+const int32_t *wk_graph_o(const wk_graph *g);
+void    wk_graph_free(wk_graph *g);
+/* Build the store straight from a generated graph (no host copies). */
+int     wk_store_build_graph(wk_ctx *ctx, const wk_graph *g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WUKONG_GPU_H */

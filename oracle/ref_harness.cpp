@@ -1,0 +1,189 @@
+// Reference harness -- TEST INFRASTRUCTURE ONLY.
+//
+// Compiles the reference's own store, core/gstore.hpp, from the reference
+// sources in place (see the `ref` target of oracle/Makefile: the reference
+// headers are reached through symlinks, the missing network/RDMA headers and
+// the TBB/boost container names through oracle/ref_shim/).  The store is
+// filled exactly as the reference loader does it for one server:
+//   - triples are split over nthread_parallel_load (11) loader threads by
+//     s % 11 (out-edges) and o % 11 (in-edges), each part sorted with the
+//     reference's edge_sort_by_spo / edge_sort_by_ops and deduplicated
+//     (DGraph::aggregate_data, core/dgraph.hpp:288-325);
+//   - GStore::init sizes the per-predicate main headers (core/gstore.hpp:600);
+//   - the 11 threads run GStore::insert_normal concurrently with its
+//     per-predicate barrier (core/dgraph.hpp:444-463, core/gstore.hpp:665);
+//   - GStore::finish_pred_metas (core/gstore.hpp:957).
+// Lookups go through GStore::get_edges_global with one server.  The CPU
+// engine's step loops (core/engine.hpp:96-255) are restated below over those
+// lookups; they are a few lines each and carry no state of their own.
+#include <pthread.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <new>
+#include <cstdint>
+#include <thread>
+#include <vector>
+
+#include "gstore.hpp"   // the reference store, compiled from its own sources
+
+namespace {
+
+struct RefStore {
+    Mem *mem;
+    GStore *g;
+    int32_t num_ids;
+};
+
+void dedup(std::vector<triple_t> &v) {
+    if (v.size() <= 1) return;
+    size_t n = 1;
+    for (size_t i = 1; i < v.size(); ++i) {
+        if (v[i].s == v[n - 1].s && v[i].p == v[n - 1].p && v[i].o == v[n - 1].o) continue;
+        v[n++] = v[i];
+    }
+    v.resize(n);
+}
+
+int64_t lookup(RefStore *r, int64_t vid, int64_t pid, int64_t dir, edge_t **out) {
+    int sz = 0;
+    *out = r->g->get_edges_global(0, vid, dir, pid, &sz);
+    return sz;
+}
+
+}  // namespace
+
+extern "C" {
+
+void *ref_build(const int32_t *s, const int32_t *p, const int32_t *o, int64_t n, int32_t num_ids,
+                int32_t keys_million, int32_t memstore_mb) {
+    global_num_servers = 1;
+    global_num_engines = 4;
+    global_num_keys_million = keys_million;
+    global_memstore_size_gb = (memstore_mb + 1023) / 1024;
+    RefStore *r = new RefStore();
+    r->num_ids = num_ids;
+    r->mem = new Mem((uint64_t)memstore_mb << 20);
+    // GStore's constructor leaves some counters uninitialised (last_ext among
+    // them, core/gstore.hpp:560-597), so the object is built in zero-filled
+    // storage, the state a fresh process gives it.
+    void *raw = calloc(1, sizeof(GStore));
+    r->g = new (raw) GStore(0, r->mem, num_ids);
+    std::vector<std::vector<triple_t>> spo(nthread_parallel_load), ops(nthread_parallel_load);
+    for (int64_t i = 0; i < n; ++i) {
+        triple_t t((uint64_t)s[i], (uint64_t)p[i], (uint64_t)o[i]);
+        spo[t.s % nthread_parallel_load].push_back(t);
+        ops[t.o % nthread_parallel_load].push_back(t);
+    }
+    for (int t = 0; t < nthread_parallel_load; ++t) {
+        std::sort(spo[t].begin(), spo[t].end(), edge_sort_by_spo());
+        dedup(spo[t]);
+        std::sort(ops[t].begin(), ops[t].end(), edge_sort_by_ops());
+        dedup(ops[t]);
+    }
+    r->g->init(spo, ops);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthread_parallel_load; ++t)
+        th.emplace_back([r, t, &spo, &ops]() { r->g->insert_normal(t, spo[t], ops[t]); });
+    for (auto &x : th) x.join();
+    r->g->finish_pred_metas();
+    return r;
+}
+
+void ref_free(void *h) {
+    RefStore *r = (RefStore *)h;
+    if (!r) return;
+    r->g->~GStore();
+    free(r->g);
+    delete r->mem;
+    delete r;
+}
+
+// degree of [vid|pid|dir]; copies up to cap neighbours into out
+int64_t ref_get_edges(void *h, int64_t vid, int32_t pid, int32_t dir, int32_t *out, int64_t cap) {
+    edge_t *e = nullptr;
+    int64_t sz = lookup((RefStore *)h, vid, pid, dir, &e);
+    for (int64_t k = 0; k < sz && k < cap; ++k) out[k] = (int32_t)e[k].val;
+    return sz;
+}
+
+// Enumerate stored keys: slot cursor in, next data slot out (-1 at the end).
+int64_t ref_next_key(void *h, int64_t cursor, int64_t *vid, int32_t *pid, int32_t *dir, int64_t *deg) {
+    RefStore *r = (RefStore *)h;
+    vertex_t *v = r->g->get_vertices_ptr();
+    const uint64_t ns = r->g->get_num_slots();
+    for (uint64_t i = (uint64_t)cursor; i < ns; ++i) {
+        if (i % 8 == 7) continue;            // link slot of the bucket
+        if (v[i].key.is_empty()) continue;
+        *vid = (int64_t)v[i].key.vid;
+        *pid = (int32_t)v[i].key.pid;
+        *dir = (int32_t)v[i].key.dir;
+        *deg = (int64_t)v[i].ptr.size;
+        return (int64_t)i;
+    }
+    return -1;
+}
+
+// Whole query: the CPU engine's steps with execute_one_step's dispatch
+// (core/gpu_engine.hpp:395-467; index lists taken whole, i.e.
+// global_mt_threshold = 1).  Returns 0, or -1 on an unsupported shape.
+// *out is malloc'ed (free with ref_free_table).
+int ref_execute(void *h, const int64_t *cmd, int32_t npat, int32_t **out, int64_t *rows, int32_t *cols,
+                int64_t *step_rows) {
+    RefStore *r = (RefStore *)h;
+    std::vector<int> table, next;
+    int col = 0;
+    for (int32_t i = 0; i < npat; ++i) {
+        const int64_t start = cmd[i * 4], pid = cmd[i * 4 + 1], d = cmd[i * 4 + 2], end = cmd[i * 4 + 3];
+        next.clear();
+        edge_t *e;
+        auto vt = [&](int64_t v) { return v >= 0 ? 2 : ((-v > col) ? 1 : 0); };
+        if (i == 0 && is_tpid((int)start)) {
+            int sz = 0;
+            e = r->g->get_index_edges_local(0, start, d, &sz);
+            for (int k = 0; k < sz; ++k) next.push_back((int)e[k].val);
+            col = 1;
+        } else if (vt(start) == 2 && vt(end) == 1) {
+            int64_t sz = lookup(r, start, pid, d, &e);
+            for (int64_t k = 0; k < sz; ++k) next.push_back((int)e[k].val);
+            col = 1;
+        } else if (vt(start) == 0 && vt(end) == 1) {
+            const int64_t sc = -start - 1;
+            const size_t nr = col ? table.size() / col : 0;
+            for (size_t rr = 0; rr < nr; ++rr) {
+                int64_t sz = lookup(r, (int64_t)(uint32_t)table[rr * col + sc], pid, d, &e);
+                for (int64_t k = 0; k < sz; ++k) {
+                    next.insert(next.end(), table.begin() + rr * col, table.begin() + (rr + 1) * col);
+                    next.push_back((int)e[k].val);
+                }
+            }
+            col += 1;
+        } else if (vt(start) == 0 && (vt(end) == 0 || vt(end) == 2)) {
+            const int64_t sc = -start - 1;
+            const size_t nr = col ? table.size() / col : 0;
+            for (size_t rr = 0; rr < nr; ++rr) {
+                int64_t sz = lookup(r, (int64_t)(uint32_t)table[rr * col + sc], pid, d, &e);
+                const int target = vt(end) == 0 ? table[rr * col + (-end - 1)] : (int)end;
+                for (int64_t k = 0; k < sz; ++k) {
+                    if ((int)e[k].val == target) {
+                        next.insert(next.end(), table.begin() + rr * col, table.begin() + (rr + 1) * col);
+                        break;
+                    }
+                }
+            }
+        } else {
+            return -1;
+        }
+        table.swap(next);
+        if (step_rows) step_rows[i] = col ? (int64_t)(table.size() / col) : 0;
+    }
+    *rows = col ? (int64_t)(table.size() / col) : 0;
+    *cols = col;
+    *out = (int32_t *)malloc((table.size() + 1) * sizeof(int32_t));
+    if (!table.empty()) std::copy(table.begin(), table.end(), *out);
+    return 0;
+}
+
+void ref_free_table(int32_t *p) { free(p); }
+
+}  // extern "C"

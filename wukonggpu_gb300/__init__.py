@@ -1,0 +1,363 @@
+"""GB300-native per-triple-pattern graph-exploration operator (Wukong+G GPU engine surface).
+
+The compute path is ``libwkgpu.so`` (C++ host runtime + hand-written sm_103a
+kernels) behind the C ABI declared in ``include/wukong_gpu.h``.  This module
+is a thin ctypes mirror of the reference's GPU-engine interface:
+
+* :class:`Request` mirrors ``request_or_reply`` (core/query.hpp:45-175):
+  ``cmd_chains``, ``step``, ``col_num`` and the device history.
+* :class:`RCache` mirrors ``RCache``'s ops (core/rcache.hpp:232, :417, :614,
+  :811) plus the constant start of ``Engine::const_to_unknown``
+  (core/engine.hpp:96-122), and :meth:`RCache.execute` mirrors
+  ``GPU_Engine::execute_request`` (core/gpu_engine.hpp:471-526).
+
+There is no CPU fallback: if the library is missing every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+_LIB_PATH = _PKG / "libwkgpu.so"
+
+WK_OK, WK_EINVAL, WK_ENOMEM, WK_ETIMEDOUT, WK_EDEVICE, WK_ENOSTORE, WK_EOVERFLOW = 0, -1, -2, -3, -4, -5, -6
+IN, OUT = 0, 1
+PREDICATE_ID, TYPE_ID = 0, 1
+VID_BASE = 1 << 17
+
+
+class WkError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+class wk_config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("cache_budget_mb", C.c_int32), ("enable_prefetch", C.c_int32),
+                ("reserved", C.c_int32), ("history_capacity", C.c_int64)]
+
+
+class wk_history(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("size", C.c_int64), ("col_num", C.c_int32), ("step", C.c_int32)]
+
+
+class wk_store_info(C.Structure):
+    _fields_ = [("num_keys", C.c_int64), ("num_edges", C.c_int64), ("key_bytes", C.c_int64),
+                ("edge_bytes", C.c_int64), ("overflow_buckets", C.c_int64), ("device_bytes", C.c_int64),
+                ("num_ids", C.c_int32), ("paged", C.c_int32)]
+
+
+class wk_op_stats(C.Structure):
+    _fields_ = [("ms", C.c_double), ("ms_main", C.c_double), ("rows_in", C.c_int64), ("rows_out", C.c_int64),
+                ("cols_in", C.c_int32), ("kind", C.c_int32), ("alg_bytes", C.c_int64), ("kernels", C.c_int64)]
+
+
+class wk_pred_group(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("count", C.c_int32), ("zipf_s", C.c_double), ("zipf_cap", C.c_int32),
+                ("pad", C.c_int32), ("participation", C.c_double), ("hub_frac", C.c_double)]
+
+
+class wk_graph_spec(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("n_entities", C.c_int64), ("n_classes", C.c_int32),
+                ("n_groups", C.c_int32), ("groups", wk_pred_group * 4)]
+
+
+_P = C.c_void_p
+_I32P = C.POINTER(C.c_int32)
+_I64P = C.POINTER(C.c_int64)
+
+_SIGS = {
+    "wk_config_default": (None, [C.POINTER(wk_config)]),
+    "wk_ctx_create": (C.c_int, [C.POINTER(wk_config), C.POINTER(_P)]),
+    "wk_ctx_destroy": (C.c_int, [_P]),
+    "wk_last_error": (C.c_char_p, []),
+    "wk_status_str": (C.c_char_p, [C.c_int]),
+    "wk_device_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "wk_store_build": (C.c_int, [_P, _I32P, _I32P, _I32P, C.c_int64, C.c_int32]),
+    "wk_ctx_share_store": (C.c_int, [_P, _P]),
+    "wk_store_get_info": (C.c_int, [_P, C.POINTER(wk_store_info)]),
+    "wk_store_get_edges": (C.c_int, [_P, C.c_int64, C.c_int32, C.c_int32, _I32P, C.c_int64, _I64P]),
+    "wk_store_pred_stats": (C.c_int, [_P, C.c_int32, _I64P, _I64P, _I64P]),
+    "wk_known_to_unknown": (C.c_int, [_P, C.POINTER(wk_history), C.c_int64, C.c_int32, C.c_int32]),
+    "wk_known_to_known": (C.c_int, [_P, C.POINTER(wk_history), C.c_int64, C.c_int32, C.c_int32, C.c_int64]),
+    "wk_known_to_const": (C.c_int, [_P, C.POINTER(wk_history), C.c_int64, C.c_int32, C.c_int32, C.c_int64]),
+    "wk_index_to_unknown": (C.c_int, [_P, C.POINTER(wk_history), C.c_int32, C.c_int32]),
+    "wk_const_to_unknown": (C.c_int, [_P, C.POINTER(wk_history), C.c_int64, C.c_int32, C.c_int32]),
+    "wk_history_upload": (C.c_int, [_P, C.POINTER(wk_history), _I32P, C.c_int64, C.c_int32]),
+    "wk_history_download": (C.c_int, [_P, C.POINTER(wk_history), _I32P, C.c_int64]),
+    "wk_history_init": (None, [C.POINTER(wk_history)]),
+    "wk_execute": (C.c_int, [_P, _I64P, C.c_int32, C.POINTER(wk_history), _I64P]),
+    "wk_enable_timing": (C.c_int, [_P, C.c_int]),
+    "wk_last_op_stats": (C.c_int, [_P, C.POINTER(wk_op_stats)]),
+    "wk_kernel_launches": (C.c_int64, [_P]),
+    "wk_sync": (C.c_int, [_P]),
+    "wk_graph_generate": (C.c_int, [C.POINTER(wk_graph_spec), C.c_int32, C.POINTER(_P)]),
+    "wk_graph_size": (C.c_int64, [_P]),
+    "wk_graph_num_ids": (C.c_int32, [_P]),
+    "wk_graph_first_class": (C.c_int32, [_P]),
+    "wk_graph_s": (_I32P, [_P]),
+    "wk_graph_p": (_I32P, [_P]),
+    "wk_graph_o": (_I32P, [_P]),
+    "wk_graph_free": (None, [_P]),
+    "wk_store_build_graph": (C.c_int, [_P, _P]),
+}
+
+_lib = None
+
+
+def lib_path() -> Path:
+    return _LIB_PATH
+
+
+def load_library():
+    """Load libwkgpu.so; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not _LIB_PATH.exists():
+        raise ImportError(f"{_LIB_PATH} is missing: build it with `python -m wukonggpu_gb300.build`")
+    lib = C.CDLL(str(_LIB_PATH))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def _check(status: int):
+    if status != WK_OK:
+        raise WkError(status, load_library().wk_last_error().decode(errors="replace"))
+
+
+def _i32(a: np.ndarray):
+    return a.ctypes.data_as(_I32P)
+
+
+# --------------------------------------------------------------- graphs
+def graph_spec(seed: int, n_entities: int, n_classes: int, groups) -> wk_graph_spec:
+    sp = wk_graph_spec()
+    sp.seed = seed
+    sp.n_entities = n_entities
+    sp.n_classes = n_classes
+    sp.n_groups = len(groups)
+    for i, g in enumerate(groups):
+        sp.groups[i].kind = g.get("kind", 0)
+        sp.groups[i].count = g["count"]
+        sp.groups[i].zipf_s = g.get("zipf_s", 1.0)
+        sp.groups[i].zipf_cap = g.get("zipf_cap", 1)
+        sp.groups[i].participation = g.get("participation", 1.0)
+        sp.groups[i].hub_frac = g.get("hub_frac", 0.01)
+    return sp
+
+
+def spec_small(seed: int = 20240601) -> wk_graph_spec:
+    """200k entities, rdf:type with 10 classes, 15 Zipf(1.2, cap 64) predicates, ~1M triples."""
+    return graph_spec(seed, 200_000, 10, [dict(kind=0, count=15, zipf_s=1.2, zipf_cap=64, participation=0.027)])
+
+
+def spec_single_query(seed: int = 20240602, scale: float = 1.0) -> wk_graph_spec:
+    """2M entities (x scale), 15 classes, 8 one-to-one, 16 Zipf(1.1, cap 4096), 8 many-to-one onto 1% hubs.
+
+    About 100M triples at scale 1.0."""
+    n = int(2_000_000 * scale)
+    return graph_spec(seed, n, 15, [
+        dict(kind=1, count=8, participation=1.0),
+        dict(kind=0, count=16, zipf_s=1.1, zipf_cap=4096, participation=0.0065),
+        dict(kind=2, count=8, participation=1.0, hub_frac=0.01),
+    ])
+
+
+class Graph:
+    """A seeded synthetic ID-form RDF graph (owned by the library)."""
+
+    def __init__(self, spec: wk_graph_spec, n_threads: int = 0):
+        lib = load_library()
+        h = _P()
+        _check(lib.wk_graph_generate(C.byref(spec), n_threads, C.byref(h)))
+        self._h = h
+        self.spec = spec
+        self.n = lib.wk_graph_size(h)
+        self.num_ids = lib.wk_graph_num_ids(h)
+        self.first_class = lib.wk_graph_first_class(h)
+
+    def arrays(self):
+        """(s, p, o) as numpy views into library memory (valid while the graph lives)."""
+        lib = load_library()
+        out = []
+        for f in (lib.wk_graph_s, lib.wk_graph_p, lib.wk_graph_o):
+            ptr = f(self._h)
+            out.append(np.ctypeslib.as_array(ptr, shape=(self.n,)) if self.n else np.zeros(0, np.int32))
+        return tuple(out)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().wk_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------ request / engine
+class Request:
+    """Mirror of request_or_reply (core/query.hpp:45-175) for the GPU path."""
+
+    def __init__(self, cmd_chains):
+        self.cmd_chains = [int(x) for x in cmd_chains]
+        if len(self.cmd_chains) % 4:
+            raise ValueError("cmd_chains must hold 4 values per pattern")
+        self.hist = wk_history()
+        load_library().wk_history_init(C.byref(self.hist))
+        self.result_table = None
+
+    @property
+    def step(self):
+        return self.hist.step
+
+    @property
+    def col_num(self):
+        return self.hist.col_num
+
+    def get_row_num(self):
+        return 0 if self.hist.col_num == 0 else self.hist.size // self.hist.col_num
+
+    def is_finished(self):
+        return self.hist.step * 4 >= len(self.cmd_chains)
+
+
+class RCache:
+    """A device context with its store: the GB300 counterpart of RCache + GPU_Engine."""
+
+    def __init__(self, device: int = 0, cache_budget_mb: int = 0, enable_prefetch: bool = True,
+                 history_capacity: int = 0):
+        lib = load_library()
+        cfg = wk_config()
+        lib.wk_config_default(C.byref(cfg))
+        cfg.device = device
+        cfg.cache_budget_mb = cache_budget_mb
+        cfg.enable_prefetch = 1 if enable_prefetch else 0
+        cfg.history_capacity = history_capacity
+        h = _P()
+        _check(lib.wk_ctx_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    # -- store
+    def build_store(self, s, p, o, num_ids: int):
+        s = np.ascontiguousarray(s, np.int32)
+        p = np.ascontiguousarray(p, np.int32)
+        o = np.ascontiguousarray(o, np.int32)
+        _check(load_library().wk_store_build(self._h, _i32(s), _i32(p), _i32(o), len(s), num_ids))
+
+    def build_store_graph(self, g: Graph):
+        _check(load_library().wk_store_build_graph(self._h, g._h))
+
+    def share_store(self, owner: "RCache"):
+        _check(load_library().wk_ctx_share_store(self._h, owner._h))
+
+    def store_info(self) -> dict:
+        info = wk_store_info()
+        _check(load_library().wk_store_get_info(self._h, C.byref(info)))
+        return {f: getattr(info, f) for f, _ in info._fields_}
+
+    def get_edges(self, vid: int, pid: int, d: int) -> np.ndarray:
+        lib = load_library()
+        deg = C.c_int64()
+        _check(lib.wk_store_get_edges(self._h, vid, pid, d, None, 0, C.byref(deg)))
+        out = np.zeros(max(deg.value, 1), np.int32)
+        _check(lib.wk_store_get_edges(self._h, vid, pid, d, _i32(out), deg.value, C.byref(deg)))
+        return out[:deg.value]
+
+    def pred_stats(self, pid: int):
+        t, s, o = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(load_library().wk_store_pred_stats(self._h, pid, C.byref(t), C.byref(s), C.byref(o)))
+        return t.value, s.value, o.value
+
+    # -- ops (reference names and argument order)
+    def known_to_unknown(self, req: Request, start: int, direction: int, predict: int):
+        _check(load_library().wk_known_to_unknown(self._h, C.byref(req.hist), start, direction, predict))
+
+    def known_to_known(self, req: Request, start: int, direction: int, predict: int, end: int):
+        _check(load_library().wk_known_to_known(self._h, C.byref(req.hist), start, direction, predict, end))
+
+    def known_to_const(self, req: Request, start: int, direction: int, predict: int, end: int):
+        _check(load_library().wk_known_to_const(self._h, C.byref(req.hist), start, direction, predict, end))
+
+    def index_to_unknown(self, req: Request, index_vertex: int, direction: int):
+        _check(load_library().wk_index_to_unknown(self._h, C.byref(req.hist), index_vertex, direction))
+
+    def const_to_unknown(self, req: Request, start: int, direction: int, predict: int):
+        _check(load_library().wk_const_to_unknown(self._h, C.byref(req.hist), start, direction, predict))
+
+    def upload_history(self, req: Request, table: np.ndarray):
+        t = np.ascontiguousarray(table, np.int32)
+        cols = t.shape[1] if t.ndim == 2 else 1
+        _check(load_library().wk_history_upload(self._h, C.byref(req.hist), _i32(t.reshape(-1)), t.size, cols))
+
+    def download(self, req: Request) -> np.ndarray:
+        h = req.hist
+        out = np.zeros(max(h.size, 1), np.int32)
+        _check(load_library().wk_history_download(self._h, C.byref(h), _i32(out), out.size))
+        cols = max(h.col_num, 1)
+        return out[:h.size].reshape(-1, cols)
+
+    def execute(self, cmd_chains, download: bool = True):
+        """Run every pattern on the device; returns (table, per-step row counts)."""
+        req = Request(cmd_chains)
+        n = len(req.cmd_chains) // 4
+        cc = np.asarray(req.cmd_chains, np.int64)
+        rows = np.zeros(n, np.int64)
+        _check(load_library().wk_execute(self._h, cc.ctypes.data_as(_I64P), n, C.byref(req.hist),
+                                         rows.ctypes.data_as(_I64P)))
+        req.result_table = self.download(req) if download else None
+        return req, rows
+
+    def enable_timing(self, on: bool = True):
+        _check(load_library().wk_enable_timing(self._h, 1 if on else 0))
+
+    def last_op_stats(self) -> dict:
+        st = wk_op_stats()
+        _check(load_library().wk_last_op_stats(self._h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def kernel_launches(self) -> int:
+        return load_library().wk_kernel_launches(self._h)
+
+    def sync(self):
+        _check(load_library().wk_sync(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().wk_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def device_count() -> int:
+    n = C.c_int()
+    st = load_library().wk_device_count(C.byref(n))
+    return n.value if st == WK_OK else 0
+
+
+def canonical_rows(table: np.ndarray) -> np.ndarray:
+    """Rows sorted lexicographically (the canonical order used for comparisons)."""
+    t = np.asarray(table)
+    if t.ndim != 2 or t.shape[0] == 0:
+        return t
+    return t[np.lexsort(t.T[::-1])]

@@ -1,0 +1,397 @@
+// The per-pattern ops and the step dispatcher.
+//
+//   wk_known_to_unknown  <-> RCache::known_to_unknown  (core/rcache.hpp:232-414)
+//   wk_known_to_known    <-> RCache::known_to_known    (core/rcache.hpp:417-612)
+//   wk_known_to_const    <-> RCache::known_to_const    (core/rcache.hpp:614-809)
+//   wk_index_to_unknown  <-> RCache::index_to_unknown  (core/rcache.hpp:811-962)
+//   wk_const_to_unknown  <-> Engine::const_to_unknown  (core/engine.hpp:96-122)
+//   wk_execute           <-> GPU_Engine::execute_one_step / execute_request
+//                            (core/gpu_engine.hpp:395-526)
+//
+// Differences from the reference, none of which changes a result row:
+// each op needs at most one host synchronisation (to size the k2u output);
+// k2k/k2c need none before their last kernel; a missing key yields an empty
+// adjacency instead of the reference GPU's out-of-bounds read of slot -1
+// (core/gpu_hash.cu:276-277); tables are not limited to 20 columns or to
+// GPU_MAX_ELEM elements; errors are returned, never asserted.
+#include "wk_runtime.h"
+
+#include <algorithm>
+#include <cstring>
+
+using namespace wk;
+
+namespace {
+
+enum { KIND_K2U = 0, KIND_K2K = 1, KIND_K2C = 2, KIND_I2U = 3, KIND_C2U = 4 };
+
+inline bool is_tpid(int64_t id) { return id > 1 && id < WK_VID_BASE; }   // core/gstore.hpp:111
+
+int check_ctx(wk_ctx *ctx, wk_history *h, const char *what) {
+    if (!ctx || !h) return set_error(WK_EINVAL, "%s: null argument", what);
+    if (!ctx->store) return set_error(WK_ENOSTORE, "%s: no store built", what);
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return WK_OK;
+}
+
+int check_pid(wk_ctx *ctx, int64_t pid, int32_t dir, const char *what) {
+    if (pid < 1 || pid > ctx->store->hs->num_ids)
+        return set_error(WK_EINVAL, "%s: predicate %lld outside [1,%d]", what, (long long)pid, ctx->store->hs->num_ids);
+    if (dir != WK_DIR_IN && dir != WK_DIR_OUT) return set_error(WK_EINVAL, "%s: direction %d", what, dir);
+    return WK_OK;
+}
+
+// ---- per-op timing: a begin/end CUDA event pair around every kernel on the
+// op stream, so host gaps between kernels are never counted
+struct OpClock {
+    wk_ctx *ctx;
+    int main_at = -1;
+    explicit OpClock(wk_ctx *c) : ctx(c) {
+        ctx->tn = 0;
+        ctx->last = wk_op_stats{};
+    }
+    int record() {
+        if (!ctx->timing) return WK_OK;
+        if ((int)ctx->tev.size() <= ctx->tn) {
+            cudaEvent_t ev;
+            cudaError_t e = cudaEventCreate(&ev);
+            if (e != cudaSuccess) return cuda_fail(e, "timing event");
+            ctx->tev.push_back(ev);
+        }
+        cudaError_t e = cudaEventRecord(ctx->tev[(size_t)ctx->tn++], ctx->stream);
+        return e == cudaSuccess ? WK_OK : cuda_fail(e, "timing record");
+    }
+    int begin() { return record(); }
+    int end(bool is_main) {   // after the kernel's launch
+        ++ctx->launches;
+        ++ctx->last.kernels;
+        if (!ctx->timing) return WK_OK;
+        if (is_main) main_at = ctx->tn - 1;   // begin event of this pair
+        return record();
+    }
+    // call after the stream has been synchronised
+    void finish() {
+        if (!ctx->timing) return;
+        double tot = 0.0;
+        for (int i = 0; i + 1 < ctx->tn; i += 2) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ctx->tev[(size_t)i], ctx->tev[(size_t)i + 1]);
+            tot += ms;
+            if (i == main_at) ctx->last.ms_main = ms;
+        }
+        ctx->last.ms = tot;
+    }
+};
+
+int launch_check(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, what);
+}
+
+// output buffer: the ping-pong partner of the input
+wk::DevBuf &out_buf(wk_ctx *ctx, const wk_history *h) {
+    return (h->data == ctx->hbuf[0].ptr) ? ctx->hbuf[1] : ctx->hbuf[0];
+}
+
+int ensure_seg(wk_ctx *ctx, int id, PredView *pv) {
+    DeviceStore &ds = *ctx->store;
+    if (ds.pool) {
+        std::vector<int> prot = ctx->protect;
+        prot.push_back(id);
+        int st = ds.ensure(id, prot, ctx->stream, ctx->stream, nullptr);
+        if (st) return st;
+    }
+    *pv = ds.views[(size_t)id];
+    return WK_OK;
+}
+
+int read_totals(wk_ctx *ctx, int *err_flag) {
+    cudaError_t e = cudaMemcpyAsync(ctx->h_scal, ctx->dscal.ptr, 32, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "totals readback");
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "op sync");
+    *err_flag = (int)(ctx->h_scal[0] & 0xffffffffull);
+    return WK_OK;
+}
+
+int fail_corrupt(wk_ctx *ctx) {
+    cudaMemsetAsync(ctx->dscal.ptr, 0, 8, ctx->stream);
+    return set_error(WK_EDEVICE, "probe found an overflow chain longer than the segment's overflow area (corrupt store)");
+}
+
+// two-pass k2u (count -> scan -> write)
+int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
+    const int C = h->col_num;
+    const int64_t R = h->size / C;
+    OpClock clk(ctx);
+    ctx->last.kind = KIND_K2U;
+    ctx->last.rows_in = R;
+    ctx->last.cols_in = C;
+    PredView pv;
+    int st = ensure_seg(ctx, (int)pid, &pv);
+    if (st) return st;
+    DevBuf &ob = out_buf(ctx, h);
+    if (R == 0) {
+        if ((st = ob.reserve(16))) return st;
+        h->data = ob.as<int32_t>();
+        h->size = 0;
+        h->col_num = C + 1;
+        h->step++;
+        return WK_OK;
+    }
+    const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
+    if ((st = ctx->deg.reserve((size_t)R * 4)) || (st = ctx->off.reserve((size_t)R * 4)) ||
+        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->blk_nz.reserve((size_t)nblk * 4)) ||
+        (st = ctx->cz_pos.reserve((size_t)(R + 1) * 8)))
+        return st;
+    unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
+    int *err = ctx->dscal.as<int>();
+    if ((st = clk.begin())) return st;
+    dev::launch_k2u_probe(h->data, R, C, scol, pid, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
+                          ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), err, ctx->stream);
+    if ((st = launch_check("k2u probe")) || (st = clk.end(false)) || (st = clk.begin())) return st;
+    dev::launch_scan_blocks(ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), nblk, tot,
+                            ctx->cz_pos.as<unsigned long long>(), ctx->stream);
+    if ((st = launch_check("k2u scan")) || (st = clk.end(false))) return st;
+    int errf = 0;
+    if ((st = read_totals(ctx, &errf))) return st;
+    if (errf) return fail_corrupt(ctx);
+    const int64_t R_out = (int64_t)ctx->h_scal[1];
+    const int64_t nz = (int64_t)ctx->h_scal[2];
+    ctx->last.rows_out = R_out;
+    ctx->last.alg_bytes = 4 * R * C + 16 * R + 4 * R_out + 4 * R_out * (C + 1);
+    if (R_out == 0) {
+        if ((st = ob.reserve(16))) return st;
+    } else {
+        const int T = dev::k2u_tile_rows(C + 1);
+        const int64_t ntiles = (R_out + T - 1) / T;
+        if (ntiles > 0x7fffffffll) return set_error(WK_EOVERFLOW, "k2u: %lld output tiles", (long long)ntiles);
+        if ((st = ob.reserve((size_t)R_out * (C + 1) * 4)) || (st = ctx->cz_row.reserve((size_t)nz * 4)) ||
+            (st = ctx->cz_off.reserve((size_t)nz * 4)) || (st = ctx->tile_k0.reserve((size_t)ntiles * 4)))
+            return st;
+        if ((st = clk.begin())) return st;
+        dev::launch_k2u_compact(ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(), R,
+                                ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(),
+                                ctx->cz_row.as<int32_t>(), ctx->cz_pos.as<unsigned long long>(),
+                                ctx->cz_off.as<uint32_t>(), ctx->tile_k0.as<int32_t>(), T, ctx->stream);
+        if ((st = launch_check("k2u compact")) || (st = clk.end(false)) || (st = clk.begin())) return st;
+        dev::launch_k2u_write(h->data, C, pv.edges, ctx->cz_row.as<int32_t>(), ctx->cz_pos.as<unsigned long long>(),
+                              ctx->cz_off.as<uint32_t>(), nz, ctx->tile_k0.as<int32_t>(), ntiles, T, R_out,
+                              ob.as<int32_t>(), ctx->stream);
+        if ((st = launch_check("k2u write")) || (st = clk.end(true))) return st;
+        if (ctx->timing) {
+            cudaError_t e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "k2u sync");
+        }
+    }
+    clk.finish();
+    h->data = ob.as<int32_t>();
+    h->size = R_out * (C + 1);
+    h->col_num = C + 1;
+    h->step++;
+    return WK_OK;
+}
+
+// two-pass k2k / k2c (probe + membership -> scan -> filtered copy)
+int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const, uint32_t pid, uint32_t dir) {
+    const int C = h->col_num;
+    const int64_t R = h->size / C;
+    OpClock clk(ctx);
+    ctx->last.kind = ecol >= 0 ? KIND_K2K : KIND_K2C;
+    ctx->last.rows_in = R;
+    ctx->last.cols_in = C;
+    PredView pv;
+    int st = ensure_seg(ctx, (int)pid, &pv);
+    if (st) return st;
+    DevBuf &ob = out_buf(ctx, h);
+    if (R == 0) {
+        if ((st = ob.reserve(16))) return st;
+        h->data = ob.as<int32_t>();
+        h->size = 0;
+        h->step++;
+        return WK_OK;
+    }
+    const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
+    if ((st = ctx->mask.reserve((size_t)((R + 31) / 32) * 4)) || (st = ctx->blk_sum.reserve((size_t)nblk * 8)) ||
+        (st = ctx->blk_nz.reserve((size_t)nblk * 4)) || (st = ob.reserve((size_t)R * C * 4)))
+        return st;
+    unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
+    int *err = ctx->dscal.as<int>();
+    if ((st = clk.begin())) return st;
+    dev::launch_filter_probe(h->data, R, C, scol, ecol, end_const, pid, dir, pv, ctx->mask.as<uint32_t>(),
+                             ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), err, ctx->stream);
+    if ((st = launch_check("filter probe")) || (st = clk.end(true)) || (st = clk.begin())) return st;
+    dev::launch_scan_blocks(ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), nblk, tot,
+                            nullptr, ctx->stream);
+    if ((st = launch_check("filter scan")) || (st = clk.end(false)) || (st = clk.begin())) return st;
+    dev::launch_filter_write(h->data, R, C, ctx->mask.as<uint32_t>(), ctx->blk_nz.as<unsigned int>(),
+                             ob.as<int32_t>(), ctx->stream);
+    if ((st = launch_check("filter write")) || (st = clk.end(false))) return st;
+    int errf = 0;
+    if ((st = read_totals(ctx, &errf))) return st;
+    if (errf) return fail_corrupt(ctx);
+    const int64_t E = (int64_t)ctx->h_scal[1];
+    const int64_t nz = (int64_t)ctx->h_scal[2];
+    clk.finish();
+    ctx->last.rows_out = nz;
+    ctx->last.alg_bytes = 4 * R * C + 16 * R + 4 * E + 4 * nz * C;
+    h->data = ob.as<int32_t>();
+    h->size = nz * C;
+    h->step++;
+    return WK_OK;
+}
+
+// one adjacency list -> one-column table (index or constant start)
+int op_list(wk_ctx *ctx, wk_history *h, uint64_t vid, uint32_t pid, uint32_t dir, int kind) {
+    OpClock clk(ctx);
+    ctx->last.kind = kind;
+    ctx->last.rows_in = 1;
+    const HostStore &hs = *ctx->store->hs;
+    const int32_t *e = nullptr;
+    const uint64_t deg = hs.lookup(vid, pid, dir, &e);
+    DevBuf &ob = out_buf(ctx, h);
+    int st;
+    if ((st = ob.reserve((size_t)deg * 4 + 16))) return st;
+    if (deg) {
+        PredView pv;
+        if ((st = ensure_seg(ctx, (int)pid, &pv))) return st;
+        const uint64_t off = (uint64_t)(e - (hs.edges + hs.segs[pid].edge_off));
+        if ((st = clk.begin())) return st;
+        dev::launch_copy_list(pv.edges + off, (int64_t)deg, ob.as<int32_t>(), ctx->stream);
+        if ((st = launch_check("list copy")) || (st = clk.end(true))) return st;
+        if (ctx->timing) {
+            cudaError_t ce = cudaStreamSynchronize(ctx->stream);
+            if (ce != cudaSuccess) return cuda_fail(ce, "list sync");
+        }
+    }
+    clk.finish();
+    ctx->last.rows_out = (int64_t)deg;
+    ctx->last.alg_bytes = 16 + 8 * (int64_t)deg;
+    h->data = ob.as<int32_t>();
+    h->size = (int64_t)deg;
+    h->col_num = 1;
+    h->step++;
+    return WK_OK;
+}
+
+int known_col(const wk_history *h, int64_t v, const char *what, int *col) {
+    if (v >= 0 || -v > h->col_num)
+        return set_error(WK_EINVAL, "%s: %lld is not a bound variable (col_num %d)", what, (long long)v, h->col_num);
+    *col = (int)(-v - 1);
+    return WK_OK;
+}
+
+int check_table(const wk_history *h, const char *what) {
+    if (h->col_num <= 0 || h->size < 0 || h->size % h->col_num != 0 || (h->size > 0 && !h->data))
+        return set_error(WK_EINVAL, "%s: malformed history (size %lld, col_num %d)", what, (long long)h->size,
+                         h->col_num);
+    return WK_OK;
+}
+
+}  // namespace
+
+extern "C" int wk_known_to_unknown(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direction, int32_t predict) {
+    int st, scol;
+    if ((st = check_ctx(ctx, h, "known_to_unknown")) || (st = check_table(h, "known_to_unknown")) ||
+        (st = check_pid(ctx, predict, direction, "known_to_unknown")) ||
+        (st = known_col(h, start, "known_to_unknown start", &scol)))
+        return st;
+    return op_k2u(ctx, h, scol, (uint32_t)predict, (uint32_t)direction);
+}
+
+extern "C" int wk_known_to_known(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direction, int32_t predict,
+                                 int64_t end) {
+    int st, scol, ecol;
+    if ((st = check_ctx(ctx, h, "known_to_known")) || (st = check_table(h, "known_to_known")) ||
+        (st = check_pid(ctx, predict, direction, "known_to_known")) ||
+        (st = known_col(h, start, "known_to_known start", &scol)) ||
+        (st = known_col(h, end, "known_to_known end", &ecol)))
+        return st;
+    return op_filter(ctx, h, scol, ecol, 0, (uint32_t)predict, (uint32_t)direction);
+}
+
+extern "C" int wk_known_to_const(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direction, int32_t predict,
+                                 int64_t end) {
+    int st, scol;
+    if ((st = check_ctx(ctx, h, "known_to_const")) || (st = check_table(h, "known_to_const")) ||
+        (st = check_pid(ctx, predict, direction, "known_to_const")) ||
+        (st = known_col(h, start, "known_to_const start", &scol)))
+        return st;
+    if (end < 0 || end > 0x7fffffffll) return set_error(WK_EINVAL, "known_to_const: end %lld is not a constant", (long long)end);
+    return op_filter(ctx, h, scol, -1, (int32_t)end, (uint32_t)predict, (uint32_t)direction);
+}
+
+extern "C" int wk_index_to_unknown(wk_ctx *ctx, wk_history *h, int32_t index_vertex, int32_t direction) {
+    int st;
+    if ((st = check_ctx(ctx, h, "index_to_unknown")) || (st = check_pid(ctx, index_vertex, direction, "index_to_unknown")))
+        return st;
+    if (h->col_num != 0) return set_error(WK_EINVAL, "index_to_unknown: history already has %d columns", h->col_num);
+    return op_list(ctx, h, 0, (uint32_t)index_vertex, (uint32_t)direction, KIND_I2U);
+}
+
+extern "C" int wk_const_to_unknown(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direction, int32_t predict) {
+    int st;
+    if ((st = check_ctx(ctx, h, "const_to_unknown")) || (st = check_pid(ctx, predict, direction, "const_to_unknown")))
+        return st;
+    if (h->col_num != 0) return set_error(WK_EINVAL, "const_to_unknown: history already has %d columns", h->col_num);
+    if (start < WK_VID_BASE || start > 0xffffffffll)
+        return set_error(WK_EINVAL, "const_to_unknown: start %lld is not a vertex id", (long long)start);
+    return op_list(ctx, h, (uint64_t)start, (uint32_t)predict, (uint32_t)direction, KIND_C2U);
+}
+
+// GPU_Engine::execute_one_step dispatch (core/gpu_engine.hpp:395-467) with the
+// variable typing of request_or_reply::variable_type (core/query.hpp:141-149).
+static int vtype(int64_t v, int col_num) {   // 0 known, 1 unknown, 2 const
+    if (v >= 0) return 2;
+    return (-v > col_num) ? 1 : 0;
+}
+
+extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history *h, int64_t *step_rows) {
+    if (!ctx || !cmd || !h || n <= 0) return set_error(WK_EINVAL, "wk_execute: bad arguments");
+    if (!ctx->store) return set_error(WK_ENOSTORE, "wk_execute: no store");
+    wk_history_init(h);
+    ctx->protect.clear();
+    DeviceStore &ds = *ctx->store;
+    int st = WK_OK;
+    for (int i = 0; i < n && st == WK_OK; ++i) {
+        const int64_t start = cmd[i * 4], pid = cmd[i * 4 + 1], d = cmd[i * 4 + 2], end = cmd[i * 4 + 3];
+        // the segment of the next pattern is paged in on the side stream
+        if (ds.pool && ctx->cfg.enable_prefetch && i + 1 < n) {
+            const int64_t np = cmd[(i + 1) * 4 + 1];
+            const int64_t cp = (i == 0 && is_tpid(cmd[0])) ? cmd[0] : pid;
+            if (np >= 1 && np <= ds.hs->num_ids && cp >= 1 && cp <= ds.hs->num_ids) {
+                std::vector<int> prot{(int)cp, (int)np};
+                ds.ensure((int)np, prot, ctx->side, ctx->stream, ctx->use_ready);
+                ctx->protect = prot;
+            }
+        }
+        if (i == 0 && is_tpid(start)) {
+            if (end != -1) return set_error(WK_EINVAL, "wk_execute: index pattern must bind variable -1");
+            st = wk_index_to_unknown(ctx, h, (int32_t)start, (int32_t)d);
+        } else {
+            if (pid < 0) return set_error(WK_EINVAL, "wk_execute: variable predicates are not supported");
+            const int ts = vtype(start, h->col_num), te = vtype(end, h->col_num);
+            if (ts == 2 && te == 1) {
+                if (h->col_num != 0 || end != -1)
+                    return set_error(WK_EINVAL, "wk_execute: constant start must be the first pattern and bind -1");
+                st = wk_const_to_unknown(ctx, h, start, (int32_t)d, (int32_t)pid);
+            } else if (ts == 0 && te == 1) {
+                if (-end - 1 != h->col_num)
+                    return set_error(WK_EINVAL, "wk_execute: pattern %d binds %lld but the next column is %d", i,
+                                     (long long)end, h->col_num);
+                st = wk_known_to_unknown(ctx, h, start, (int32_t)d, (int32_t)pid);
+            } else if (ts == 0 && te == 0) {
+                st = wk_known_to_known(ctx, h, start, (int32_t)d, (int32_t)pid, end);
+            } else if (ts == 0 && te == 2) {
+                st = wk_known_to_const(ctx, h, start, (int32_t)d, (int32_t)pid, end);
+            } else {
+                return set_error(WK_EINVAL, "wk_execute: unsupported pattern shape at step %d (start %lld, end %lld)",
+                                 i, (long long)start, (long long)end);
+            }
+        }
+        if (st == WK_OK && step_rows) step_rows[i] = h->col_num ? h->size / h->col_num : 0;
+    }
+    ctx->protect.clear();
+    return st;
+}

@@ -1,0 +1,88 @@
+// Host runtime state behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "wk_internal.h"
+#include "wk_kernels.h"
+
+namespace wk {
+
+int cuda_fail(cudaError_t e, const char *what);
+
+// growable device buffer (grows by 1.5x, never shrinks)
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t cap = 0;
+    int reserve(size_t nbytes);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// The device copy of the store: either fully resident (one bucket array and
+// one edge array) or paged per id through a fixed device pool
+// (ShardManager, core/shard_manager.hpp:44-557).
+struct DeviceStore {
+    struct Resident {
+        bool resident = false;
+        uint64_t off = 0, bytes = 0, last_use = 0;
+        cudaEvent_t ev = nullptr;   // completion of the segment's copy
+    };
+    int device = 0;
+    std::unique_ptr<HostStore> hs;
+    std::vector<PredView> views;    // per id
+    uint64_t device_bytes = 0;
+    // resident mode
+    void *d_buckets = nullptr;
+    int32_t *d_edges = nullptr;
+    // paged mode
+    void *pool = nullptr;
+    uint64_t pool_bytes = 0, clock = 0;
+    std::map<uint64_t, uint64_t> free_list;   // offset -> size
+    std::vector<Resident> res;
+    int64_t loads = 0, evictions = 0;
+    uint64_t bytes_loaded = 0;
+
+    ~DeviceStore();
+    int upload_resident();
+    int init_paged(uint64_t budget);
+    uint64_t seg_bytes(int id) const;
+    bool pool_alloc(uint64_t need, uint64_t *off);
+    void pool_free(uint64_t off, uint64_t n);
+    int ensure(int id, const std::vector<int> &protect, cudaStream_t copy_st, cudaStream_t use_st,
+               cudaEvent_t use_ready);
+};
+
+}  // namespace wk
+
+struct wk_ctx {
+    int device = 0;
+    wk_config cfg{};
+    cudaStream_t stream = nullptr;   // op stream
+    cudaStream_t side = nullptr;     // segment prefetch stream
+    cudaEvent_t use_ready = nullptr;
+    std::shared_ptr<wk::DeviceStore> store;
+
+    wk::DevBuf hbuf[2];              // ping-pong history buffers (core/rcache.hpp:87-88)
+    // scratch of the two-pass ops
+    wk::DevBuf deg, off, mask, blk_sum, blk_nz, cz_row, cz_pos, cz_off, tile_k0;
+    wk::DevBuf dscal;                // [0] error flag, [8..] totals
+    unsigned long long *h_scal = nullptr;   // pinned mirror of the totals
+
+    // timing
+    bool timing = false;
+    std::vector<cudaEvent_t> tev;
+    std::vector<int> tmain;          // index of kernel pairs that are the op's main kernel
+    int tn = 0;
+    wk_op_stats last{};
+    int64_t launches = 0;
+
+    // query-level state (segment cache protection / prefetch)
+    std::vector<int> protect;
+
+    ~wk_ctx();
+};

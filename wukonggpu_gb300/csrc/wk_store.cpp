@@ -1,0 +1,312 @@
+// Host-side build of the store image from ID-form triples.
+//
+// Content follows the reference loader and store:
+//  - triples are grouped per predicate, sorted by (s,o) for out-edges and by
+//    (o,s) for in-edges and deduplicated (core/dgraph.hpp:268-330, sort orders
+//    edge_sort_by_spo / edge_sort_by_ops at core/gstore.hpp:56-99), so every
+//    adjacency list is ascending by neighbour id;
+//  - key [s|p|OUT] -> objects, key [o|p|IN] -> subjects for p != rdf:type;
+//    key [s|1|OUT] -> the vertex's classes; no IN key for type triples
+//    (core/gstore.hpp:665-790);
+//  - index keys: [0|c|IN] -> members of class c (type index), [0|p|IN] ->
+//    subjects of p, [0|p|OUT] -> objects of p (record_index_info,
+//    core/gstore.hpp:835-870, insert_type_index_map / insert_index_map
+//    :460-524).
+// The layout is this library's own: per id, a bucket array of 8 x 16 B slots
+// (7 data slots + 1 overflow link) sized for a load of at most 1/2, followed by
+// overflow buckets, and one contiguous int32 edge segment holding the id's
+// out-lists, in-lists and index lists.
+#include "wk_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <thread>
+
+namespace wk {
+
+HostStore::~HostStore() {
+    if (pinned) {
+        if (buckets) cudaFreeHost(buckets);
+        if (edges) cudaFreeHost(edges);
+    } else {
+        free(buckets);
+        free(edges);
+    }
+}
+
+uint64_t HostStore::lookup(uint64_t vid, uint32_t pid, uint32_t dir, const int32_t **edges_out) const {
+    *edges_out = nullptr;
+    if (pid < 1 || (int32_t)pid > num_ids) return 0;
+    const PredSeg &sg = segs[pid];
+    if (sg.nmain == 0) return 0;
+    const uint64_t key = make_key(vid, pid, dir);
+    uint32_t b = bucket_of(key_mix(key), sg.nmain);
+    const uint32_t *base = buckets + sg.bucket_off * 4;
+    for (uint32_t hop = 0; hop <= sg.nover; ++hop) {
+        const uint32_t *bk = base + (uint64_t)b * WK_SLOTS_PER_BUCKET * 4;
+        for (int i = 0; i < WK_DATA_SLOTS; ++i) {
+            uint64_t k = (uint64_t)bk[i * 4] | ((uint64_t)bk[i * 4 + 1] << 32);
+            if (k == key) {
+                *edges_out = edges + sg.edge_off + bk[i * 4 + 2];
+                return bk[i * 4 + 3];
+            }
+        }
+        const uint32_t *link = bk + WK_DATA_SLOTS * 4;
+        if (!(link[1] & WK_LINK_TAG)) return 0;
+        b = link[0];
+    }
+    return 0;
+}
+
+namespace {
+
+struct KeyRec {       // one key of a segment before insertion
+    uint64_t key;
+    uint32_t off;     // offset in the segment's edge list
+    uint32_t deg;
+};
+
+struct SegBuild {
+    std::vector<KeyRec> keys;
+    std::vector<int32_t> edges;
+    int64_t triples = 0, subjects = 0, objects = 0;
+};
+
+// Sort (hi,lo) pairs packed as hi<<32|lo, dedup, and emit one key per hi
+// group with the group's lo values as the adjacency list.
+void emit_groups(std::vector<uint64_t> &pairs, uint32_t pid, uint32_t dir, SegBuild &sb,
+                 std::vector<int32_t> *distinct_hi) {
+    std::sort(pairs.begin(), pairs.end());
+    pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+    size_t i = 0, n = pairs.size();
+    while (i < n) {
+        uint32_t hi = (uint32_t)(pairs[i] >> 32);
+        size_t j = i;
+        KeyRec kr;
+        kr.key = make_key(hi, pid, dir);
+        kr.off = (uint32_t)sb.edges.size();
+        while (j < n && (uint32_t)(pairs[j] >> 32) == hi) {
+            sb.edges.push_back((int32_t)(uint32_t)pairs[j]);
+            ++j;
+        }
+        kr.deg = (uint32_t)(j - i);
+        sb.keys.push_back(kr);
+        if (distinct_hi) distinct_hi->push_back((int32_t)hi);
+        i = j;
+    }
+}
+
+void add_index(uint32_t pid, uint32_t dir, const std::vector<int32_t> &list, SegBuild &sb) {
+    if (list.empty()) return;
+    KeyRec kr;
+    kr.key = make_key(0, pid, dir);
+    kr.off = (uint32_t)sb.edges.size();
+    kr.deg = (uint32_t)list.size();
+    sb.edges.insert(sb.edges.end(), list.begin(), list.end());
+    sb.keys.push_back(kr);
+}
+
+template <class F>
+void parallel_for(size_t n, F f) {
+    int nt = (int)std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 64));
+    std::atomic<size_t> next{0};
+    auto w = [&]() {
+        for (;;) {
+            size_t i = next.fetch_add(1);
+            if (i >= n) break;
+            f(i);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int i = 1; i < nt; ++i) th.emplace_back(w);
+    w();
+    for (auto &t : th) t.join();
+}
+
+}  // namespace
+
+int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
+                     int32_t num_ids, HostStore **out) {
+    if (n < 0 || (n > 0 && (!s || !p || !o)) || num_ids < 1 || num_ids >= WK_VID_BASE)
+        return set_error(WK_EINVAL, "store build: bad arguments (n=%lld, num_ids=%d)", (long long)n, num_ids);
+    // validate and bucket triples by predicate (counting sort)
+    std::vector<int64_t> cnt((size_t)num_ids + 2, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t pi = p[i];
+        if (pi < 1 || pi > num_ids)
+            return set_error(WK_EINVAL, "store build: triple %lld has predicate %d outside [1,%d]",
+                             (long long)i, pi, num_ids);
+        if (s[i] < WK_VID_BASE)
+            return set_error(WK_EINVAL, "store build: triple %lld has subject %d below 2^17", (long long)i, s[i]);
+        if (pi == WK_TYPE_ID) {
+            if (o[i] < 2 || o[i] > num_ids)
+                return set_error(WK_EINVAL, "store build: type triple %lld has class %d outside [2,%d]",
+                                 (long long)i, o[i], num_ids);
+        } else if (o[i] < WK_VID_BASE) {
+            return set_error(WK_EINVAL, "store build: triple %lld has object %d below 2^17", (long long)i, o[i]);
+        }
+        cnt[(size_t)pi]++;
+    }
+    std::vector<int64_t> start((size_t)num_ids + 2, 0);
+    for (int32_t i = 1; i <= num_ids + 1; ++i) start[(size_t)i] = start[(size_t)i - 1] + cnt[(size_t)i - 1];
+    std::vector<uint64_t> so((size_t)n);       // packed s<<32|o, grouped by p
+    {
+        std::vector<int64_t> at(start);
+        for (int64_t i = 0; i < n; ++i)
+            so[(size_t)at[(size_t)p[i]]++] = ((uint64_t)(uint32_t)s[i] << 32) | (uint32_t)o[i];
+    }
+
+    std::vector<SegBuild> sb((size_t)num_ids + 1);
+    // type triples first: they feed both the type lists and the class indexes
+    std::vector<std::vector<int32_t>> class_members((size_t)num_ids + 1);
+    {
+        const int64_t a = start[WK_TYPE_ID], b = start[WK_TYPE_ID + 1];
+        std::vector<uint64_t> out_pairs(so.begin() + a, so.begin() + b);
+        emit_groups(out_pairs, WK_TYPE_ID, WK_DIR_OUT, sb[WK_TYPE_ID], nullptr);
+        sb[WK_TYPE_ID].triples = (int64_t)out_pairs.size();
+        sb[WK_TYPE_ID].subjects = (int64_t)sb[WK_TYPE_ID].keys.size();
+        std::vector<uint64_t> cs;
+        cs.reserve(out_pairs.size());
+        for (uint64_t x : out_pairs) cs.push_back(((x & 0xffffffffull) << 32) | (x >> 32));
+        std::sort(cs.begin(), cs.end());
+        for (uint64_t x : cs) class_members[(size_t)(x >> 32)].push_back((int32_t)(uint32_t)x);
+    }
+    // normal predicates in parallel
+    parallel_for((size_t)num_ids + 1, [&](size_t id) {
+        if (id == 0) return;
+        SegBuild &b = sb[id];
+        if (id != WK_TYPE_ID && cnt[id] > 0) {
+            std::vector<uint64_t> pairs(so.begin() + start[id], so.begin() + start[id + 1]);
+            std::vector<int32_t> subjects, objects;
+            emit_groups(pairs, (uint32_t)id, WK_DIR_OUT, b, &subjects);
+            b.triples = (int64_t)pairs.size();
+            for (auto &x : pairs) x = ((x & 0xffffffffull) << 32) | (x >> 32);
+            emit_groups(pairs, (uint32_t)id, WK_DIR_IN, b, &objects);
+            add_index((uint32_t)id, WK_DIR_IN, subjects, b);    // [0|p|IN]  subjects of p
+            add_index((uint32_t)id, WK_DIR_OUT, objects, b);    // [0|p|OUT] objects of p
+            b.subjects = (int64_t)subjects.size();
+            b.objects = (int64_t)objects.size();
+        }
+        if (!class_members[id].empty()) {                    // [0|c|IN] members of c
+            add_index((uint32_t)id, WK_DIR_IN, class_members[id], b);
+            b.subjects += (int64_t)class_members[id].size();
+            b.triples += (int64_t)class_members[id].size();
+        }
+    });
+    std::vector<uint64_t>().swap(so);
+
+    // sizes and image allocation
+    HostStore *hs = new HostStore();
+    hs->num_ids = num_ids;
+    hs->segs.resize((size_t)num_ids + 1);
+    uint64_t slot_at = 0, edge_at = 0;
+    for (size_t id = 1; id <= (size_t)num_ids; ++id) {
+        PredSeg &sg = hs->segs[id];
+        SegBuild &b = sb[id];
+        sg.nkeys = b.keys.size();
+        sg.nedges = b.edges.size();
+        sg.triples = b.triples; sg.subjects = b.subjects; sg.objects = b.objects;
+        if (sg.nedges > 0xffffffffull) {
+            delete hs;
+            return set_error(WK_EINVAL, "store build: id %zu has more than 2^32 edge entries", id);
+        }
+        // main buckets: keys / (7 * 0.5), at least one bucket when there are keys;
+        // overflow room: worst case one bucket per 7 keys beyond the first
+        uint64_t nm = sg.nkeys ? (sg.nkeys * 2 + WK_DATA_SLOTS - 1) / WK_DATA_SLOTS : 0;
+        if (nm > 0x7fffffffull) { delete hs; return set_error(WK_EINVAL, "store build: id %zu too many keys", id); }
+        sg.nmain = (uint32_t)nm;
+        sg.bucket_off = slot_at;
+        sg.edge_off = edge_at;
+        slot_at += (uint64_t)(sg.nmain + sg.nkeys / WK_DATA_SLOTS + 1) * WK_SLOTS_PER_BUCKET;
+        edge_at += sg.nedges;
+    }
+    // reserve the upper bound, compact after insertion
+    uint64_t slot_cap = slot_at ? slot_at : 8;
+    uint64_t edge_cap = edge_at ? edge_at : 1;
+    uint32_t *bk_tmp = (uint32_t *)calloc(slot_cap, 16);
+    if (!bk_tmp) { delete hs; return set_error(WK_ENOMEM, "store build: out of host memory"); }
+
+    // insertion per id in parallel: cluster chaining with a per-id overflow area
+    std::vector<uint32_t> nover((size_t)num_ids + 1, 0);
+    parallel_for((size_t)num_ids + 1, [&](size_t id) {
+        if (id == 0) return;
+        PredSeg &sg = hs->segs[id];
+        if (!sg.nkeys) return;
+        uint32_t *base = bk_tmp + sg.bucket_off * 4;
+        uint32_t used_over = 0;
+        for (const KeyRec &kr : sb[id].keys) {
+            uint32_t b = bucket_of(key_mix(kr.key), sg.nmain);
+            for (;;) {
+                uint32_t *bk = base + (uint64_t)b * WK_SLOTS_PER_BUCKET * 4;
+                int free_slot = -1;
+                for (int i = 0; i < WK_DATA_SLOTS; ++i)
+                    if (bk[i * 4] == 0 && bk[i * 4 + 1] == 0) { free_slot = i; break; }
+                if (free_slot >= 0) {
+                    uint32_t *sl = bk + free_slot * 4;
+                    sl[0] = (uint32_t)kr.key; sl[1] = (uint32_t)(kr.key >> 32);
+                    sl[2] = kr.off; sl[3] = kr.deg;
+                    break;
+                }
+                uint32_t *link = bk + WK_DATA_SLOTS * 4;
+                if (link[1] & WK_LINK_TAG) { b = link[0]; continue; }
+                uint32_t nb = sg.nmain + used_over++;
+                link[0] = nb; link[1] = WK_LINK_TAG;
+                b = nb;
+            }
+        }
+        nover[id] = used_over;
+    });
+
+    // compact: final bucket offsets and copy into the (pinned if possible) image
+    uint64_t total_slots = 0;
+    for (size_t id = 1; id <= (size_t)num_ids; ++id) {
+        PredSeg &sg = hs->segs[id];
+        sg.nover = nover[id];
+        total_slots += (uint64_t)(sg.nmain + sg.nover) * WK_SLOTS_PER_BUCKET;
+    }
+    void *bp = nullptr, *ep = nullptr;
+    bool pinned = cudaHostAlloc(&bp, (total_slots ? total_slots : 8) * 16, cudaHostAllocPortable) == cudaSuccess &&
+                  cudaHostAlloc(&ep, edge_cap * 4, cudaHostAllocPortable) == cudaSuccess;
+    if (!pinned) {
+        cudaGetLastError();
+        if (bp) cudaFreeHost(bp);
+        if (ep) cudaFreeHost(ep);
+        bp = malloc((total_slots ? total_slots : 8) * 16);
+        ep = malloc(edge_cap * 4);
+        if (!bp || !ep) { free(bp); free(ep); free(bk_tmp); delete hs;
+                          return set_error(WK_ENOMEM, "store build: out of host memory"); }
+    }
+    hs->pinned = pinned;
+    hs->buckets = (uint32_t *)bp;
+    hs->edges = (int32_t *)ep;
+    std::vector<uint64_t> new_off((size_t)num_ids + 1, 0);
+    uint64_t at = 0;
+    for (size_t id = 1; id <= (size_t)num_ids; ++id) {
+        new_off[id] = at;
+        at += (uint64_t)(hs->segs[id].nmain + hs->segs[id].nover) * WK_SLOTS_PER_BUCKET;
+    }
+    parallel_for((size_t)num_ids + 1, [&](size_t id) {
+        if (id == 0) return;
+        PredSeg &sg = hs->segs[id];
+        uint64_t nsl = (uint64_t)(sg.nmain + sg.nover) * WK_SLOTS_PER_BUCKET;
+        if (nsl) std::memcpy(hs->buckets + new_off[id] * 4, bk_tmp + sg.bucket_off * 4, nsl * 16);
+        sg.bucket_off = new_off[id];
+        if (sg.nedges) std::memcpy(hs->edges + sg.edge_off, sb[id].edges.data(), sg.nedges * 4);
+        std::vector<KeyRec>().swap(sb[id].keys);
+        std::vector<int32_t>().swap(sb[id].edges);
+    });
+    free(bk_tmp);
+    hs->total_slots = total_slots;
+    hs->total_edges = edge_at;
+    for (size_t id = 1; id <= (size_t)num_ids; ++id) {
+        hs->total_keys += hs->segs[id].nkeys;
+        hs->total_over += hs->segs[id].nover;
+    }
+    *out = hs;
+    return WK_OK;
+}
+
+}  // namespace wk
