@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Benchmark of the per-pattern operator on the single-query-scale workload.
+
+Workload: a seeded RDF graph of ~100M triples over 2M entities (8 one-to-one,
+16 one-to-many Zipf(1.1, cap 4096) and 8 many-to-one predicates onto a 1% hub
+set, rdf:type with 15 classes), and three 6-pattern star+chain BGPs starting
+from a type index (1.3e5 start rows; final tables of 1.3e7..6.2e7 rows x 6
+int32 columns).  One step = the three queries executed once.
+
+  value : queries/s with the store and every history resident in HBM (device
+          time from CUDA events on the library's stream, max over ranks).
+  e2e   : queries/s through the public C ABI with host buffers: the query goes
+          in from the host and the final table comes back to pinned host
+          memory inside the timed region.
+  roofline : the k2u op (probe + scan + compact + write kernels) -- the
+          expansion path that dominates the step -- algorithmic bytes per
+          op / its summed kernel time, against the measured HBM copy peak.
+  cpu_baseline : the CPU oracle (a C port of the reference store + engine) on
+          the same mix, all host threads.
+
+``--impl reference`` times the CPU implementation alone (the reference's
+store and engine restated in C, with the reference's strided multi-thread
+split) on the same workload and prints the same line with impl=reference.
+Under torchrun (N>1) every rank runs an independent replica (the path is
+replicated, not sharded, on this build); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "BGP queries/sec + p50/p99 latency, learned vs stats plans; op HBM GB/s"
+WORKLOAD = "single-query scale: 100M-triple RDF graph, 2M entities, 6-pattern star+chain BGPs from a type index"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="entity-count scale of the graph (1.0 = 2M)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class Dist:
+    """Rank info and the few collectives the bench needs (barrier, max, sum)."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend)
+            self.torch, self.dist = torch, dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64,
+                              device="cuda" if self.torch.cuda.is_available() else "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX if op == "max" else self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_dev{device}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic_ratio():
+    """DRAM bytes per algorithmic byte of the k2u op from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / "k2u_traffic.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_alg_byte="):
+            try:
+                return float(line.split("=", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(g, queries, nthreads: int, steps: int = 1):
+    """The oracle (C port of the reference store + CPU engine) on the mix; returns (qps, seconds, sample)."""
+    import oracle
+    s, p, o = g.arrays()
+    orc = oracle.Oracle(s, p, o, g.num_ids)
+    t0 = time.perf_counter()
+    n = 0
+    for _ in range(steps):
+        for _, q in queries:
+            orc.execute(q, nthreads=nthreads)
+            n += 1
+    dt = time.perf_counter() - t0
+    orc.close()
+    return n / dt, dt, f"{steps} pass(es) over the {len(queries)}-query mix on the full graph, {nthreads} threads"
+
+
+def run_reference(args, dist):
+    import wukonggpu_gb300 as W
+    from wukonggpu_gb300 import workloads
+    if dist.rank != 0:
+        return
+    import oracle
+    W.load_library()
+    g = W.Graph(W.spec_single_query(scale=args.scale))
+    s, p, o = g.arrays()
+    queries = workloads.scale_queries()
+    nthreads = os.cpu_count() or 1
+    orc = oracle.Oracle(s, p, o, g.num_ids)
+    for _ in range(args.warmup):
+        orc.execute(queries[0][1], nthreads=nthreads)
+    lat = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for _, q in queries:
+            a = time.perf_counter()
+            orc.execute(q, nthreads=nthreads)
+            lat.append(time.perf_counter() - a)
+    dt = time.perf_counter() - t0
+    qps = len(lat) / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator, reference id encoding)",
+        "config": {"workload": WORKLOAD, "queries": [n for n, _ in queries], "triples": int(g.n)},
+        "p50_ms": statistics.median(lat) * 1000, "p99_ms": float(np.percentile(lat, 99)) * 1000,
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{args.steps} step(s) of the {len(queries)}-query mix on the full graph"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, dist):
+    import wukonggpu_gb300 as W
+    from wukonggpu_gb300 import build as wb
+    from wukonggpu_gb300 import workloads
+    wb.build()
+    W.load_library()
+    t_setup = time.perf_counter()
+    g = W.Graph(W.spec_single_query(scale=args.scale))
+    queries = workloads.scale_queries()
+    rc = W.RCache(device=dist.local)
+    rc.build_store_graph(g)
+    info = rc.store_info()
+    t_setup = time.perf_counter() - t_setup
+    nq = len(queries)
+
+    def one_step(lat=None, stats=None):
+        for _, q in queries:
+            if lat is not None:
+                rc.timer_begin()
+            req, _ = rc.execute(q, download=False)
+            if lat is not None:
+                lat.append(rc.timer_end())
+            if stats is not None:
+                stats.append(req)
+
+    for _ in range(args.warmup):
+        one_step()
+    rc.sync()
+
+    # ---- device-resident timed region (per-op timing on: roofline from the same run)
+    rc.enable_timing(True)
+    op_log = []
+
+    def step_with_ops(lat):
+        for _, q in queries:
+            req = W.Request(q)
+            n = len(req.cmd_chains) // 4
+            rc.timer_begin()
+            # execute pattern by pattern through the ops so each op's device time is recorded
+            for i in range(n):
+                st, pid, d, en = req.cmd_chains[4 * i:4 * i + 4]
+                if i == 0 and 1 < st < W.VID_BASE:
+                    rc.index_to_unknown(req, st, d)
+                elif st >= 0:
+                    rc.const_to_unknown(req, st, d, pid)
+                elif en < 0 and -en > req.col_num:
+                    rc.known_to_unknown(req, st, d, pid)
+                elif en < 0:
+                    rc.known_to_known(req, st, d, pid, en)
+                else:
+                    rc.known_to_const(req, st, d, pid, en)
+                op_log.append(rc.last_op_stats())
+            lat.append(rc.timer_end())
+
+    launches0 = rc.kernel_launches()
+    lat = []
+    dist.barrier()
+    rc.sync()
+    wall0 = time.perf_counter()
+    with ClockSampler(dist.local) as clk:
+        for _ in range(args.steps):
+            step_with_ops(lat)
+        rc.sync()
+    wall_s = time.perf_counter() - wall0
+    dist.barrier()
+    launches = rc.kernel_launches() - launches0
+    rc.enable_timing(False)
+    total_ms = sum(lat)
+    max_ms = dist.reduce(total_ms, "max")
+    n_done = dist.reduce(float(args.steps * nq), "sum")
+    value = n_done / (max_ms / 1000.0)
+
+    # ---- roofline of the k2u op (the expansion path), from the timed region
+    k2u = [op for op in op_log if op["kind"] == 0 and op["rows_out"] > 0]
+    alg = sum(op["alg_bytes"] for op in k2u)
+    k2u_ms = sum(op["ms"] for op in k2u)
+    write_ms = sum(op["ms_main"] for op in k2u)
+    all_ms = sum(op["ms"] for op in op_log)
+    peak, peak_kind = peaks()
+    achieved = alg / (k2u_ms / 1000.0) / 1e9 if k2u_ms > 0 else 0.0
+    per_launch = alg / max(len(k2u), 1)
+    ratio = profile_traffic_ratio()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": (ratio * per_launch) if ratio else None,
+                "peak_source": peak_kind, "kernel": "k2u op (probe+scan+compact+write)",
+                "alg_bytes_per_launch": per_launch, "k2u_share_of_op_time": k2u_ms / all_ms if all_ms else None,
+                "write_kernel_gbs": (sum(4 * op["rows_out"] * (op["cols_in"] + 2) for op in k2u)
+                                     / (write_ms / 1000.0) / 1e9) if write_ms else None}
+
+    # ---- end to end through the C ABI with host buffers
+    maxrows = 0
+    for _, q in queries:
+        req, rows = rc.execute(q, download=False)
+        maxrows = max(maxrows, req.hist.size)
+    pinned = W.PinnedBuffer(maxrows)
+    d2h = 0
+    h2d = 0
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for _, q in queries:
+            cc = np.asarray(q, np.int64)
+            h2d += cc.nbytes
+            req, _ = rc.execute(cc.tolist(), download=False)
+            out = rc.download(req, into=pinned)
+            d2h += out.nbytes
+    e2e_s = time.perf_counter() - t0
+    e2e_s = dist.reduce(e2e_s, "max")
+    e2e_qps = n_done / e2e_s
+    pinned.close()
+
+    # ---- CPU baseline (rank 0 only)
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        qps, secs, sample = cpu_baseline(g, queries, nthreads)
+        cpu = {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port", "sample": sample,
+               "seconds": secs}
+
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded generator, reference id encoding)",
+            "config": {"workload": WORKLOAD, "queries": [n for n, _ in queries], "triples": int(g.n),
+                       "entities": int(g.spec.n_entities), "parallelism": f"replicas{args.gpus}",
+                       "store_device_bytes": info["device_bytes"], "l2": "inputs larger than L2 "
+                       f"(store {info['device_bytes'] / 1e9:.1f} GB, histories up to "
+                       f"{maxrows * 4 / 1e9:.2f} GB)", "plans": "given (statistics/learned planners not in this line)",
+                       "setup_s": t_setup, "timed_wall_s": wall_s},
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "per_query_ms": {n: float(np.mean(lat[i::nq])) for i, (n, _) in enumerate(queries)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    rc.close()
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_gb300(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

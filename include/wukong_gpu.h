@@ -109,6 +109,9 @@ typedef struct {
     int64_t device_bytes;    /* bytes of the store resident on the device     */
     int32_t num_ids;
     int32_t paged;           /* 1 if predicate segments are paged (cache mode)*/
+    int64_t cache_loads;     /* segment loads (H2D) so far, paged mode        */
+    int64_t cache_evictions; /* segment evictions so far, paged mode          */
+    int64_t cache_bytes_loaded;
 } wk_store_info;
 int wk_store_get_info(wk_ctx *ctx, wk_store_info *info);
 
@@ -178,6 +181,13 @@ int wk_enable_timing(wk_ctx *ctx, int enable);
 int wk_last_op_stats(wk_ctx *ctx, wk_op_stats *st);
 int64_t wk_kernel_launches(wk_ctx *ctx);   /* cumulative kernel launches */
 int wk_sync(wk_ctx *ctx);
+/* Device-side interval on the context's stream: begin records a CUDA event,
+ * end records another, synchronises and returns the elapsed milliseconds. */
+int wk_timer_begin(wk_ctx *ctx);
+int wk_timer_end(wk_ctx *ctx, double *ms);
+/* Page-locked host memory for history uploads/downloads at full link speed. */
+int wk_host_alloc(int64_t bytes, void **out);
+int wk_host_free(void *p);
 
 /* ------------------------------------------------ synthetic RDF graphs
  * Seeded generator of ID-form graphs with the id encoding of

@@ -56,6 +56,8 @@ def _load():
         lib.orc_get_edges.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.POINTER(_I32P)]
         lib.orc_num_keys.restype = C.c_int64
         lib.orc_num_keys.argtypes = [C.c_void_p]
+        lib.orc_digest.restype = C.c_uint64
+        lib.orc_digest.argtypes = [C.c_void_p, _I64P, _I64P]
         lib.orc_key_at.restype = C.c_int64
         lib.orc_key_at.argtypes = [C.c_void_p, C.c_int64, _I64P, _I32P, _I32P]
         lib.orc_step.restype = C.c_int
@@ -100,6 +102,12 @@ class Oracle:
 
     def num_keys(self) -> int:
         return _load().orc_num_keys(self._h)
+
+    def digest(self):
+        """(order-independent content digest, keys, edge entries)"""
+        k, e = C.c_int64(), C.c_int64()
+        d = _load().orc_digest(self._h, C.byref(k), C.byref(e))
+        return int(d), k.value, e.value
 
     def keys(self):
         """All stored keys as (vid, pid, dir) tuples."""
@@ -183,6 +191,8 @@ def _load_ref():
         lib.ref_execute.argtypes = [C.c_void_p, _I64P, C.c_int32, C.POINTER(_I32P), _I64P, C.POINTER(C.c_int32),
                                     _I64P]
         lib.ref_free_table.argtypes = [_I32P]
+        lib.ref_digest.restype = C.c_uint64
+        lib.ref_digest.argtypes = [C.c_void_p, _I64P, _I64P]
         _ref = lib
     return _ref
 
@@ -202,6 +212,11 @@ class RefStore:
         out = np.zeros(max(n, 1), np.int32)
         lib.ref_get_edges(self._h, vid, pid, d, out.ctypes.data_as(_I32P), n)
         return out[:n]
+
+    def digest(self):
+        k, e = C.c_int64(), C.c_int64()
+        d = _load_ref().ref_digest(self._h, C.byref(k), C.byref(e))
+        return int(d), k.value, e.value
 
     def keys(self):
         lib = _load_ref()

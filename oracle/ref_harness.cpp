@@ -16,7 +16,9 @@
 // Lookups go through GStore::get_edges_global with one server.  The CPU
 // engine's step loops (core/engine.hpp:96-255) are restated below over those
 // lookups; they are a few lines each and carry no state of their own.
+#include <fcntl.h>
 #include <pthread.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cstdlib>
@@ -81,12 +83,19 @@ void *ref_build(const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
         std::sort(ops[t].begin(), ops[t].end(), edge_sort_by_ops());
         dedup(ops[t]);
     }
+    // the reference loader reports progress on stdout; keep it out of the caller's output
+    fflush(stdout);
+    const int saved = dup(1), devnull = open("/dev/null", O_WRONLY);
+    if (saved >= 0 && devnull >= 0) dup2(devnull, 1);
     r->g->init(spo, ops);
     std::vector<std::thread> th;
     for (int t = 0; t < nthread_parallel_load; ++t)
         th.emplace_back([r, t, &spo, &ops]() { r->g->insert_normal(t, spo[t], ops[t]); });
     for (auto &x : th) x.join();
     r->g->finish_pred_metas();
+    fflush(stdout);
+    if (saved >= 0) { dup2(saved, 1); close(saved); }
+    if (devnull >= 0) close(devnull);
     return r;
 }
 
@@ -185,5 +194,33 @@ int ref_execute(void *h, const int64_t *cmd, int32_t npat, int32_t **out, int64_
 }
 
 void ref_free_table(int32_t *p) { free(p); }
+
+// Order-independent content digest, same definition as orc_digest in wk_oracle.c.
+static inline uint64_t dmix(uint64_t x) {
+    x ^= x >> 31; x *= 0x7fb5d329728ea185ull; x ^= x >> 27; x *= 0x81dadef4bc2dd44dull; x ^= x >> 33;
+    return x;
+}
+uint64_t ref_digest(void *h, int64_t *nkeys, int64_t *nedges) {
+    RefStore *r = (RefStore *)h;
+    vertex_t *v = r->g->get_vertices_ptr();
+    edge_t *e = r->g->get_edges_ptr();
+    const uint64_t ns = r->g->get_num_slots();
+    uint64_t d = 0;
+    int64_t k = 0, ne = 0;
+    for (uint64_t i = 0; i < ns; ++i) {
+        if (i % 8 == 7 || v[i].key.is_empty()) continue;
+        const uint64_t key = ((uint64_t)v[i].key.vid << 18) | ((uint64_t)v[i].key.pid << 1) | (uint64_t)v[i].key.dir;
+        const uint64_t sz = v[i].ptr.size, off = v[i].ptr.off;
+        uint64_t a = 0;
+        for (uint64_t j = 0; j < sz; ++j) a += dmix((uint64_t)e[off + j].val);
+        d += dmix(key ^ dmix(sz) ^ dmix(a + 0x9e37));
+        ++k;
+        ne += (int64_t)sz;
+    }
+    *nkeys = k;
+    *nedges = ne;
+    return d;
+}
+
 
 }  // extern "C"

@@ -328,6 +328,32 @@ int64_t orc_get_edges(const orc_store *st, int64_t vid, int32_t pid, int32_t dir
     return 0;
 }
 
+
+/* Order-independent digest of the stored content: per key, the key bits, its
+ * degree and the sum of mix64 over its neighbours; summed over keys.  Index
+ * lists are filled by racing threads in the reference, so no order enters. */
+static inline uint64_t dmix(uint64_t x) {
+    x ^= x >> 31; x *= 0x7fb5d329728ea185ull; x ^= x >> 27; x *= 0x81dadef4bc2dd44dull; x ^= x >> 33;
+    return x;
+}
+uint64_t orc_digest(const orc_store *st, int64_t *nkeys, int64_t *nedges) {
+    const uint64_t nslots = (st->num_buckets + st->num_buckets_ext) * ASSOC;
+    uint64_t d = 0;
+    int64_t k = 0, e = 0;
+    for (uint64_t i = 0; i < nslots; ++i) {
+        if ((i % ASSOC) == ASSOC - 1 || st->slots[i].key == 0) continue;
+        const uint64_t sz = st->slots[i].ptr & ((1ull << 28) - 1), off = st->slots[i].ptr >> 28;
+        uint64_t a = 0;
+        for (uint64_t j = 0; j < sz; ++j) a += dmix((uint64_t)(uint32_t)st->edges[off + j]);
+        d += dmix(st->slots[i].key ^ dmix(sz) ^ dmix(a + 0x9e37));
+        ++k;
+        e += (int64_t)sz;
+    }
+    *nkeys = k;
+    *nedges = e;
+    return d;
+}
+
 int64_t orc_num_keys(const orc_store *st) { return st->nkeys; }
 
 int64_t orc_key_at(const orc_store *st, int64_t i, int64_t *vid, int32_t *pid, int32_t *dir) {

@@ -34,6 +34,8 @@ void orc_free(orc_store *st);
 /* GStore::get_edges_local (core/gstore.hpp:471-481); returns the degree. */
 int64_t orc_get_edges(const orc_store *st, int64_t vid, int32_t pid, int32_t dir, const int32_t **out);
 int64_t orc_num_keys(const orc_store *st);
+/* order-independent content digest (keys, degrees, neighbour sets) */
+uint64_t orc_digest(const orc_store *st, int64_t *nkeys, int64_t *nedges);
 /* i-th stored key in slot order; returns its degree, -1 past the end */
 int64_t orc_key_at(const orc_store *st, int64_t i, int64_t *vid, int32_t *pid, int32_t *dir);
 

@@ -1,0 +1,66 @@
+"""The C ABI library: it loads, exports every symbol the header declares, and
+reports errors as statuses (no compute call needs a GPU here)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import wukonggpu_gb300 as W
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "wukong_gpu.h"
+
+
+def _declared():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(wk_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_op_surface():
+    names = _declared()
+    for n in ("wk_known_to_unknown", "wk_known_to_known", "wk_known_to_const", "wk_index_to_unknown",
+              "wk_const_to_unknown", "wk_execute", "wk_store_build", "wk_ctx_create"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib_built):
+    lib = C.CDLL(str(W.lib_path()))
+    missing = [n for n in _declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_mirror_covers_header(lib_built):
+    assert set(_declared()) <= set(W.exported_symbols())
+
+
+def test_status_strings(lib_built):
+    lib = W.load_library()
+    for st in (W.WK_OK, W.WK_EINVAL, W.WK_ENOMEM, W.WK_ETIMEDOUT, W.WK_EDEVICE, W.WK_ENOSTORE, W.WK_EOVERFLOW):
+        assert lib.wk_status_str(st)
+
+
+def test_null_arguments_are_rejected(lib_built):
+    lib = W.load_library()
+    assert lib.wk_ctx_create(None, None) == W.WK_EINVAL
+    assert lib.wk_execute(None, None, 0, None, None) == W.WK_EINVAL
+    assert lib.wk_known_to_unknown(None, None, -1, 1, 2) == W.WK_EINVAL
+    assert b"null" in lib.wk_last_error()
+
+
+def test_no_device_is_an_error_not_a_fallback(lib_built):
+    if W.device_count() > 0:
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(W.WkError) as ei:
+        W.RCache(device=0)
+    assert ei.value.status == W.WK_EDEVICE
+
+
+def test_graph_generator_rejects_bad_specs(lib_built):
+    bad = W.graph_spec(1, 0, 3, [dict(kind=0, count=2, zipf_s=1.2, zipf_cap=8, participation=0.1)])
+    with pytest.raises(W.WkError):
+        W.Graph(bad)
+    bad = W.graph_spec(1, 1000, 3, [dict(kind=7, count=2)])
+    with pytest.raises(W.WkError):
+        W.Graph(bad)

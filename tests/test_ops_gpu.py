@@ -1,0 +1,209 @@
+"""Parity of the CUDA path with the oracle and the reference fixtures.
+
+Every comparison is bit-exact.  Non-index queries must match the reference
+row order exactly; index-start queries match in canonical order (the
+reference fills its index lists from racing loader threads) and match the
+oracle exactly (both keep index lists ascending)."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle
+import wukonggpu_gb300 as W
+from wukonggpu_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _sha(t):
+    return hashlib.sha256(np.ascontiguousarray(t, np.int32).tobytes()).hexdigest()
+
+
+def test_store_matches_oracle_keys(gpu_small, small_oracle):
+    info = gpu_small.store_info()
+    assert info["num_keys"] == small_oracle.num_keys()
+    d, k, e = small_oracle.digest()
+    assert info["num_edges"] == e
+    assert info["overflow_buckets"] > 0          # chains are exercised
+
+
+def test_host_lookup_matches_oracle(gpu_small, small_graph, small_oracle):
+    g, s, p, o = small_graph
+    rng = np.random.default_rng(3)
+    verts = rng.choice(np.unique(np.concatenate([s, o[p != 1]])), 300, replace=False)
+    for v in verts:
+        for pid in (1, 2, 5, 9):
+            for d in (W.IN, W.OUT):
+                assert np.array_equal(gpu_small.get_edges(int(v), pid, d), small_oracle.get_edges(int(v), pid, d))
+
+
+def test_golden_queries(gpu_small, small_oracle, golden_small):
+    for q in golden_small["queries"]:
+        req, rows = gpu_small.execute(q["cmd_chains"])
+        t = req.result_table
+        assert t.shape[0] == q["rows"], q["name"]
+        assert list(rows) == q["step_rows"], q["name"]
+        assert _sha(oracle.canonical(t)) == q["canonical_sha256"], q["name"]
+        if "ordered_sha256" in q:
+            assert _sha(t) == q["ordered_sha256"], q["name"]
+        ref, _ = small_oracle.execute(q["cmd_chains"])
+        assert np.array_equal(t.reshape(ref.shape) if t.size else ref, ref), q["name"]
+
+
+def _random_history(rng, verts, R, C, miss_frac=0.3):
+    h = rng.choice(verts, size=(R, C)).astype(np.int32)
+    miss = rng.random((R, C)) < miss_frac
+    h[miss] = W.VID_BASE + 10_000_000 + rng.integers(0, 1000, size=miss.sum())
+    return h
+
+
+@pytest.mark.parametrize("R", [1, 31, 33, 1023, 1025, 4097, 70_001])
+@pytest.mark.parametrize("C", [1, 3, 8])
+def test_k2u_random_histories(gpu_small, small_graph, small_oracle, R, C):
+    g, s, p, o = small_graph
+    rng = np.random.default_rng(R * 7 + C)
+    verts = np.unique(s)
+    h = _random_history(rng, verts, R, C)
+    for pid, d in ((2, W.OUT), (3, W.IN), (1, W.OUT)):
+        scol = int(rng.integers(0, C))
+        req = W.Request([])
+        gpu_small.upload_history(req, h)
+        gpu_small.known_to_unknown(req, -scol - 1, d, pid)
+        got = gpu_small.download(req)
+        exp, _ = small_oracle.step(h, False, -scol - 1, pid, d, -C - 1)
+        assert got.shape == exp.shape and np.array_equal(got, exp), (pid, d, scol)
+
+
+@pytest.mark.parametrize("R", [1, 33, 1025, 50_000])
+@pytest.mark.parametrize("C", [2, 5])
+def test_k2k_k2c_random_histories(gpu_small, small_graph, small_oracle, R, C):
+    g, s, p, o = small_graph
+    rng = np.random.default_rng(R + 13 * C)
+    # rows that are real edges (so matches occur) mixed with random pairs
+    m = p == 2
+    es, eo = s[m], o[m]
+    idx = rng.integers(0, len(es), size=R)
+    h = _random_history(rng, np.unique(s), R, C, miss_frac=0.1)
+    real = rng.random(R) < 0.6
+    h[real, 0] = es[idx[real]]
+    h[real, 1] = eo[idx[real]]
+    for (start, d, pid, end) in ((-1, W.OUT, 2, -2), (-2, W.IN, 2, -1), (-1, W.OUT, 3, -2)):
+        req = W.Request([])
+        gpu_small.upload_history(req, h)
+        gpu_small.known_to_known(req, start, d, pid, end)
+        got = gpu_small.download(req)
+        exp, _ = small_oracle.step(h, False, start, pid, d, end)
+        assert np.array_equal(got.reshape(exp.shape), exp), (start, d, pid, end)
+    vals, counts = np.unique(eo, return_counts=True)
+    for const in (int(vals[np.argmax(counts)]), int(vals[0]), W.VID_BASE + 99_999_999):
+        req = W.Request([])
+        gpu_small.upload_history(req, h)
+        gpu_small.known_to_const(req, -1, W.OUT, 2, const)
+        got = gpu_small.download(req)
+        exp, _ = small_oracle.step(h, False, -1, 2, W.OUT, const)
+        assert np.array_equal(got.reshape(exp.shape), exp), const
+
+
+def test_index_and_const_starts(gpu_small, small_graph, small_oracle):
+    g, s, p, o = small_graph
+    for idx, d in ((17, W.IN), (20, W.IN), (2, W.IN), (2, W.OUT), (16, W.OUT)):
+        req = W.Request([])
+        gpu_small.index_to_unknown(req, idx, d)
+        got = gpu_small.download(req).reshape(-1)
+        exp, _ = small_oracle.step(None, True, idx, 0, d, -1)
+        assert np.array_equal(got, exp.reshape(-1)), (idx, d)
+    for v in np.unique(s)[:50]:
+        req = W.Request([])
+        gpu_small.const_to_unknown(req, int(v), W.OUT, 2)
+        got = gpu_small.download(req).reshape(-1)
+        assert np.array_equal(got, small_oracle.get_edges(int(v), 2, W.OUT))
+
+
+def test_empty_history_steps(gpu_small):
+    req = W.Request([])
+    gpu_small.upload_history(req, np.zeros((0, 3), np.int32))
+    gpu_small.known_to_unknown(req, -2, W.OUT, 2)
+    assert req.hist.size == 0 and req.hist.col_num == 4
+    gpu_small.known_to_known(req, -1, W.OUT, 2, -4)
+    assert req.hist.size == 0 and req.hist.col_num == 4
+
+
+def test_bad_patterns_are_errors(gpu_small):
+    req = W.Request([])
+    gpu_small.upload_history(req, np.full((4, 2), W.VID_BASE, np.int32))
+    with pytest.raises(W.WkError) as e:
+        gpu_small.known_to_unknown(req, -3, W.OUT, 2)     # column 2 is not bound
+    assert e.value.status == W.WK_EINVAL
+    with pytest.raises(W.WkError):
+        gpu_small.known_to_unknown(req, -1, W.OUT, 999)   # predicate out of range
+    with pytest.raises(W.WkError):
+        gpu_small.known_to_unknown(req, -1, 2, 2)         # direction
+    with pytest.raises(W.WkError):
+        gpu_small.execute([W.VID_BASE + 1, 2, W.OUT, -1, -1, 2, W.OUT, -3])   # skips a column
+    with pytest.raises(W.WkError):
+        gpu_small.execute([-1, 2, W.OUT, -2])               # starts from an unknown variable
+
+
+def _hub_graph():
+    """A graph with one subject of degree 5000 (k2u rows spanning many write
+    tiles), a functional chain for wide tables, and ordinary random edges."""
+    rng = np.random.default_rng(11)
+    n = 20_000
+    V = W.VID_BASE
+    hub = V
+    s = [np.full(3000, hub), V + rng.integers(0, n, 40_000), V + np.arange(n)]
+    o = [V + 1 + np.arange(3000), V + rng.integers(0, n, 40_000), V + (np.arange(n) * 7919 + 1) % n]
+    pp = [np.full(3000, 2), np.full(40_000, 2), np.full(n, 3)]
+    s = np.concatenate(s).astype(np.int32)
+    o = np.concatenate(o).astype(np.int32)
+    pp = np.concatenate(pp).astype(np.int32)
+    # type triples
+    s = np.concatenate([s, V + np.arange(n)]).astype(np.int32)
+    o = np.concatenate([o, 4 + (np.arange(n) % 3)]).astype(np.int32)
+    pp = np.concatenate([pp, np.ones(n, np.int32)]).astype(np.int32)
+    return s, pp, o, 6
+
+
+def test_high_degree_and_wide_tables(lib_built):
+    s, p, o, nid = _hub_graph()
+    rc = W.RCache(device=0)
+    rc.build_store(s, p, o, nid)
+    orc = oracle.Oracle(s, p, o, nid)
+    hubq = [W.VID_BASE, 2, W.OUT, -1, -1, 2, W.IN, -2, -2, 2, W.OUT, -3]
+    req, rows = rc.execute(hubq)
+    exp, erows = orc.execute(hubq)
+    assert list(rows) == list(erows) and np.array_equal(req.result_table, exp)
+    # 26-column table through a functional chain (the reference stops at 20 columns)
+    q = [4, W.TYPE_ID, W.IN, -1]
+    for i in range(25):
+        q += [-(i + 1), 3, W.OUT, -(i + 2)]
+    req, rows = rc.execute(q)
+    exp, erows = orc.execute(q)
+    assert req.result_table.shape == exp.shape == (exp.shape[0], 26)
+    assert np.array_equal(req.result_table, exp)
+
+
+def test_paged_segment_cache_gives_same_rows(small_graph, small_oracle, golden_small):
+    g, s, p, o = small_graph
+    rc = W.RCache(device=0, cache_budget_mb=12)
+    rc.build_store_graph(g)
+    assert rc.store_info()["paged"] == 1
+    for q in golden_small["queries"]:
+        req, rows = rc.execute(q["cmd_chains"])
+        assert _sha(oracle.canonical(req.result_table)) == q["canonical_sha256"], q["name"]
+        assert list(rows) == q["step_rows"], q["name"]
+    info = rc.store_info()
+    assert info["cache_loads"] > 0 and info["cache_evictions"] > 0
+
+
+def test_kernel_launch_count_and_timing(gpu_small, golden_small):
+    before = gpu_small.kernel_launches()
+    gpu_small.enable_timing(True)
+    q = next(x for x in golden_small["queries"] if x["name"] == "type_chain")
+    gpu_small.execute(q["cmd_chains"])
+    st = gpu_small.last_op_stats()
+    gpu_small.enable_timing(False)
+    assert gpu_small.kernel_launches() > before
+    assert st["kernels"] == 4 and st["ms"] > 0 and st["ms_main"] > 0
+    assert st["rows_out"] == q["rows"]

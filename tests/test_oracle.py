@@ -1,0 +1,107 @@
+"""The CPU oracle against the reference: golden fixtures and, where the
+reference sources are present, the reference store compiled in place."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle
+import wukonggpu_gb300 as W
+from wukonggpu_gb300 import workloads
+
+
+def _sha(t):
+    return hashlib.sha256(np.ascontiguousarray(t, np.int32).tobytes()).hexdigest()
+
+
+def test_generator_matches_fixture(small_graph, golden_small):
+    g, s, p, o = small_graph
+    h = hashlib.sha256()
+    for a in (s, p, o):
+        h.update(np.ascontiguousarray(a, np.int32).tobytes())
+    assert g.n == golden_small["num_triples"]
+    assert g.num_ids == golden_small["num_ids"]
+    assert h.hexdigest() == golden_small["graph_sha256"]
+
+
+def test_generator_thread_count_independent(lib_built):
+    spec = W.spec_small(seed=99)
+    a = W.Graph(spec, n_threads=1)
+    b = W.Graph(spec, n_threads=7)
+    for x, y in zip(a.arrays(), b.arrays()):
+        assert np.array_equal(x, y)
+
+
+def test_generator_shapes(small_graph):
+    g, s, p, o = small_graph
+    assert s.min() >= W.VID_BASE and o[p != W.TYPE_ID].min() >= W.VID_BASE
+    t = p == W.TYPE_ID
+    assert t.sum() == 200_000                       # one class per entity
+    assert o[t].min() == 17 and o[t].max() == 26    # 10 classes after the 15 predicates
+    trip = np.stack([s, p, o], 1)
+    assert len(np.unique(trip, axis=0)) == len(trip)   # no duplicate triples
+    # Zipf(1.2, cap 64) out-degree: mean near 10, cap respected
+    m = p == 2
+    _, deg = np.unique(s[m], return_counts=True)
+    assert deg.max() <= 64 and 8.0 < deg.mean() < 12.5
+
+
+def test_oracle_store_digest_matches_reference_fixture(small_oracle, golden_small):
+    d, k, e = small_oracle.digest()
+    assert (str(d), k, e) == (golden_small["store"]["digest"], golden_small["store"]["keys"],
+                              golden_small["store"]["edges"])
+
+
+def test_oracle_queries_match_reference_fixture(small_graph, small_oracle, golden_small):
+    g, s, p, o = small_graph
+    qs = dict(workloads.small_queries(s, p, o))
+    assert [q["name"] for q in golden_small["queries"]] == list(qs)
+    for q in golden_small["queries"]:
+        assert qs[q["name"]] == q["cmd_chains"], q["name"]
+        t, rows = small_oracle.execute(q["cmd_chains"])
+        assert t.shape[0] == q["rows"], q["name"]
+        assert list(rows) == q["step_rows"], q["name"]
+        assert _sha(oracle.canonical(t)) == q["canonical_sha256"], q["name"]
+        if "ordered_sha256" in q:
+            assert _sha(t) == q["ordered_sha256"], q["name"]
+
+
+def test_oracle_multithread_equals_single(small_oracle, golden_small):
+    for q in golden_small["queries"]:
+        a, _ = small_oracle.execute(q["cmd_chains"], nthreads=1)
+        b, _ = small_oracle.execute(q["cmd_chains"], nthreads=4)
+        assert np.array_equal(oracle.canonical(a), oracle.canonical(b)), q["name"]
+
+
+def test_oracle_adjacency_ascending(small_graph, small_oracle):
+    g, s, p, o = small_graph
+    rng = np.random.default_rng(1)
+    for v in rng.choice(np.unique(s), 200, replace=False):
+        for pid in (1, 2, 3):
+            e = small_oracle.get_edges(int(v), pid, W.OUT)
+            assert np.all(np.diff(e) > 0)
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference sources not present on this machine")
+def test_oracle_equals_live_reference(small_graph, small_oracle):
+    g, s, p, o = small_graph
+    ref = oracle.RefStore(s, p, o, g.num_ids, keys_million=16, memstore_mb=1024)
+    assert ref.digest() == small_oracle.digest()
+    for name, cmd in workloads.small_queries(s, p, o):
+        a, ra = ref.execute(cmd)
+        b, rb = small_oracle.execute(cmd)
+        assert np.array_equal(oracle.canonical(a), oracle.canonical(b)), name
+        assert list(ra) == list(rb), name
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference sources not present on this machine")
+def test_reference_harness_edge_graph(lib_built):
+    """A second seeded graph with a different shape (oracle vs live reference)."""
+    spec = W.graph_spec(5, 60_000, 4, [dict(kind=0, count=5, zipf_s=1.1, zipf_cap=300, participation=0.2),
+                                       dict(kind=1, count=2, participation=0.9),
+                                       dict(kind=2, count=2, participation=0.8, hub_frac=0.01)])
+    g = W.Graph(spec)
+    s, p, o = (np.array(a) for a in g.arrays())
+    orc = oracle.Oracle(s, p, o, g.num_ids)
+    ref = oracle.RefStore(s, p, o, g.num_ids, keys_million=16, memstore_mb=1024)
+    assert ref.digest() == orc.digest()

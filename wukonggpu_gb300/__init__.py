@@ -48,7 +48,8 @@ class wk_history(C.Structure):
 class wk_store_info(C.Structure):
     _fields_ = [("num_keys", C.c_int64), ("num_edges", C.c_int64), ("key_bytes", C.c_int64),
                 ("edge_bytes", C.c_int64), ("overflow_buckets", C.c_int64), ("device_bytes", C.c_int64),
-                ("num_ids", C.c_int32), ("paged", C.c_int32)]
+                ("num_ids", C.c_int32), ("paged", C.c_int32), ("cache_loads", C.c_int64),
+                ("cache_evictions", C.c_int64), ("cache_bytes_loaded", C.c_int64)]
 
 
 class wk_op_stats(C.Structure):
@@ -95,6 +96,10 @@ _SIGS = {
     "wk_last_op_stats": (C.c_int, [_P, C.POINTER(wk_op_stats)]),
     "wk_kernel_launches": (C.c_int64, [_P]),
     "wk_sync": (C.c_int, [_P]),
+    "wk_timer_begin": (C.c_int, [_P]),
+    "wk_timer_end": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "wk_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_P)]),
+    "wk_host_free": (C.c_int, [_P]),
     "wk_graph_generate": (C.c_int, [C.POINTER(wk_graph_spec), C.c_int32, C.POINTER(_P)]),
     "wk_graph_size": (C.c_int64, [_P]),
     "wk_graph_num_ids": (C.c_int32, [_P]),
@@ -305,8 +310,11 @@ class RCache:
         cols = t.shape[1] if t.ndim == 2 else 1
         _check(load_library().wk_history_upload(self._h, C.byref(req.hist), _i32(t.reshape(-1)), t.size, cols))
 
-    def download(self, req: Request) -> np.ndarray:
+    def download(self, req: Request, into: "PinnedBuffer | None" = None) -> np.ndarray:
         h = req.hist
+        if into is not None and into.n >= h.size:
+            _check(load_library().wk_history_download(self._h, C.byref(h), _i32(into.array), into.n))
+            return into.array[:h.size].reshape(-1, max(h.col_num, 1))
         out = np.zeros(max(h.size, 1), np.int32)
         _check(load_library().wk_history_download(self._h, C.byref(h), _i32(out), out.size))
         cols = max(h.col_num, 1)
@@ -337,10 +345,43 @@ class RCache:
     def sync(self):
         _check(load_library().wk_sync(self._h))
 
+    def timer_begin(self):
+        """Record a CUDA event on the context's stream."""
+        _check(load_library().wk_timer_begin(self._h))
+
+    def timer_end(self) -> float:
+        """Device milliseconds since timer_begin (synchronises the stream)."""
+        ms = C.c_double()
+        _check(load_library().wk_timer_end(self._h, C.byref(ms)))
+        return ms.value
+
     def close(self):
         if getattr(self, "_h", None):
             load_library().wk_ctx_destroy(self._h)
             self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PinnedBuffer:
+    """Page-locked host int32 buffer (for host<->device history transfers)."""
+
+    def __init__(self, n_int32: int):
+        p = _P()
+        _check(load_library().wk_host_alloc(max(n_int32, 1) * 4, C.byref(p)))
+        self._p = p
+        self.n = max(n_int32, 1)
+        self.array = np.ctypeslib.as_array(C.cast(p, _I32P), shape=(self.n,))
+
+    def close(self):
+        if getattr(self, "_p", None):
+            self.array = None
+            load_library().wk_host_free(self._p)
+            self._p = None
 
     def __del__(self):
         try:

@@ -225,6 +225,8 @@ wk_ctx::~wk_ctx() {
     if (h_scal) cudaFreeHost(h_scal);
     for (auto &e : tev) cudaEventDestroy(e);
     if (use_ready) cudaEventDestroy(use_ready);
+    if (tm0) cudaEventDestroy(tm0);
+    if (tm1) cudaEventDestroy(tm1);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
 }
@@ -344,6 +346,9 @@ extern "C" int wk_store_get_info(wk_ctx *ctx, wk_store_info *info) {
     info->device_bytes = (int64_t)ctx->store->device_bytes;
     info->num_ids = hs->num_ids;
     info->paged = ctx->store->pool ? 1 : 0;
+    info->cache_loads = ctx->store->loads;
+    info->cache_evictions = ctx->store->evictions;
+    info->cache_bytes_loaded = (int64_t)ctx->store->bytes_loaded;
     return WK_OK;
 }
 
@@ -384,6 +389,40 @@ extern "C" int wk_last_op_stats(wk_ctx *ctx, wk_op_stats *st) {
 }
 
 extern "C" int64_t wk_kernel_launches(wk_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" int wk_host_alloc(int64_t bytes, void **out) {
+    if (!out || bytes < 0) return set_error(WK_EINVAL, "wk_host_alloc: bad arguments");
+    *out = nullptr;
+    cudaError_t e = cudaHostAlloc(out, (size_t)(bytes ? bytes : 1), cudaHostAllocPortable);
+    if (e != cudaSuccess) { *out = nullptr; return cuda_fail(e, "wk_host_alloc"); }
+    return WK_OK;
+}
+
+extern "C" int wk_host_free(void *p) {
+    if (!p) return WK_OK;
+    cudaError_t e = cudaFreeHost(p);
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "wk_host_free");
+}
+
+extern "C" int wk_timer_begin(wk_ctx *ctx) {
+    if (!ctx) return set_error(WK_EINVAL, "wk_timer_begin: null");
+    cudaError_t e;
+    for (auto *ev : {&ctx->tm0, &ctx->tm1})
+        if (!*ev && (e = cudaEventCreate(ev)) != cudaSuccess) { *ev = nullptr; return cuda_fail(e, "timer event"); }
+    e = cudaEventRecord(ctx->tm0, ctx->stream);
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "timer record");
+}
+
+extern "C" int wk_timer_end(wk_ctx *ctx, double *ms) {
+    if (!ctx || !ms || !ctx->tm0) return set_error(WK_EINVAL, "wk_timer_end: no interval begun");
+    cudaError_t e = cudaEventRecord(ctx->tm1, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ctx->tm1);
+    float f = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&f, ctx->tm0, ctx->tm1);
+    if (e != cudaSuccess) return cuda_fail(e, "timer");
+    *ms = f;
+    return WK_OK;
+}
 
 extern "C" void wk_history_init(wk_history *h) {
     if (h) std::memset(h, 0, sizeof(*h));

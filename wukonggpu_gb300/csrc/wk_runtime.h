@@ -80,6 +80,7 @@ struct wk_ctx {
     int tn = 0;
     wk_op_stats last{};
     int64_t launches = 0;
+    cudaEvent_t tm0 = nullptr, tm1 = nullptr;   // wk_timer_begin / wk_timer_end
 
     // query-level state (segment cache protection / prefetch)
     std::vector<int> protect;

@@ -1,0 +1,109 @@
+"""Synthetic workloads: graph specs and seeded query sets of the benchmark configurations.
+
+Queries are ``cmd_chains`` lists (4 ints per pattern: start, predicate,
+direction, end; core/query.hpp:68) in the reference's variable encoding
+(negative = variable -v-1, >= 0 = constant).  Index-start patterns put a
+class id (type index) or a predicate id (predicate index) first with
+predicate TYPE_ID / PREDICATE_ID, as the reference planner emits them
+(core/query.hpp:177-195).
+
+Constants are chosen deterministically from the graph so that each query's
+result is non-empty; the choice uses sparse matrix products over the triples
+(no engine involved).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import IN, OUT, PREDICATE_ID, TYPE_ID, VID_BASE, graph_spec
+
+# --------------------------------------------------------------- layouts
+# spec_small: pid 1 = type, 2..16 one-to-many Zipf(1.2, 64), classes 17..26
+SMALL_PREDS = list(range(2, 17))
+SMALL_FIRST_CLASS = 17
+
+
+def _adj(s, p, o, pid, n_ent):
+    """Sparse 0/1 adjacency (entity index space) of predicate pid, subject -> object."""
+    from scipy.sparse import csr_matrix
+    m = p == pid
+    r = s[m].astype(np.int64) - VID_BASE
+    c = o[m].astype(np.int64) - VID_BASE
+    return csr_matrix((np.ones(len(r), np.float64), (r, c)), shape=(n_ent, n_ent))
+
+
+def _pick(cands: np.ndarray, ok: np.ndarray, seed: int) -> int:
+    """First candidate (in a seeded order) whose flag is set."""
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(len(cands))
+    for i in order:
+        if ok[i]:
+            return int(cands[i])
+    return int(cands[order[0]])
+
+
+def small_queries(s, p, o, n_ent: int = 200_000, seed: int = 7):
+    """Parity query set on the small graph: every pattern kind, both directions.
+
+    Returns a list of (name, cmd_chains)."""
+    A = {pid: _adj(s, p, o, pid, n_ent) for pid in (2, 3, 4, 5, 6, 7, 8, 9)}
+    ones = np.ones(n_ent)
+    # headline: <c> p2 ?y . ?y p5 ?z . ?z p7 ?w with c among p2 subjects
+    v = A[5] @ (A[7] @ ones)
+    cnt = A[2] @ v
+    subj2 = np.unique(s[p == 2]).astype(np.int64)
+    c = _pick(subj2, cnt[subj2 - VID_BASE] > 0, seed)
+    # const start, IN direction: <o> p4^-1 ?x . ?x p3 ?y
+    obj4 = np.unique(o[p == 4]).astype(np.int64)
+    in_cnt = A[4].T @ (A[3] @ ones)
+    c_in = _pick(obj4, in_cnt[obj4 - VID_BASE] > 0, seed + 1)
+    # a popular object of p2 for known_to_const
+    vals, counts = np.unique(o[p == 2], return_counts=True)
+    pop = int(vals[np.argmax(counts)])
+    C0, C1, C2 = SMALL_FIRST_CLASS, SMALL_FIRST_CLASS + 1, SMALL_FIRST_CLASS + 2
+    return [
+        ("chain3_const", [c, 2, OUT, -1, -1, 5, OUT, -2, -2, 7, OUT, -3]),
+        ("const_in", [c_in, 4, IN, -1, -1, 3, OUT, -2]),
+        ("type_chain", [C0, TYPE_ID, IN, -1, -1, 2, OUT, -2, -2, 5, OUT, -3]),
+        ("type_star", [C1, TYPE_ID, IN, -1, -1, 3, OUT, -2, -1, 4, OUT, -3, -1, 6, IN, -4]),
+        ("type_in_chain", [C2, TYPE_ID, IN, -1, -1, 6, IN, -2, -2, 8, OUT, -3]),
+        ("pindex_out", [9, PREDICATE_ID, OUT, -1, -1, 9, IN, -2]),
+        ("pindex_in_k2k_back", [2, PREDICATE_ID, IN, -1, -1, 2, OUT, -2, -2, 2, IN, -1]),
+        ("k2k_cycle", [3, PREDICATE_ID, IN, -1, -1, 3, OUT, -2, -2, 5, OUT, -3, -1, 4, OUT, -3]),
+        ("k2k_wide", [C0, TYPE_ID, IN, -1, -1, 2, OUT, -2, -1, 3, OUT, -3, -2, 3, IN, -4, -4, 2, OUT, -2]),
+        ("k2c_type", [4, PREDICATE_ID, IN, -1, -1, 4, OUT, -2, -1, TYPE_ID, OUT, C1]),
+        ("k2c_obj", [2, PREDICATE_ID, IN, -1, -1, 2, OUT, pop]),
+        ("k2k_same_type", [2, PREDICATE_ID, IN, -1, -1, 2, OUT, -2, -2, TYPE_ID, OUT, -3, -1, TYPE_ID, OUT, -3]),
+        ("type_of", [c, 2, OUT, -1, -1, TYPE_ID, OUT, -2]),
+        ("empty_const", [VID_BASE + n_ent + 5, 2, OUT, -1, -1, 5, OUT, -2]),
+        ("empty_mid", [c, 2, OUT, -1, -1, 2, OUT, -2, -2, 2, OUT, -3, -3, 2, OUT, -4, -4, 2, OUT, -5,
+                       -5, 2, OUT, -6, -6, 2, OUT, -7]),
+    ]
+
+
+# ------------------------------------------- single-query scale (100M triples)
+# spec_single_query layout: 2..9 functional, 10..25 Zipf(1.1, 4096), 26..33 many-to-one, classes 34..48
+SQ_FUNC = list(range(2, 10))
+SQ_ZIPF = list(range(10, 26))
+SQ_M2O = list(range(26, 34))
+SQ_FIRST_CLASS = 34
+
+
+def scale_queries(n_classes: int = 15):
+    """Six-pattern star+chain BGPs from a type index (the single-query-scale workload).
+
+    With 2M entities each class holds ~1.3e5 members; hub fan-in makes the
+    history reach 1e7..1e8 rows over up to 6 columns."""
+    C = SQ_FIRST_CLASS
+    f, z, m = SQ_FUNC, SQ_ZIPF, SQ_M2O
+    return [
+        # ?x type C . ?x m1 ?h . ?h m2^-1 ?y . ?y f1 ?a . ?y m3 ?g . ?x f2 ?b
+        ("star_chain_hub", [C + 0, TYPE_ID, IN, -1, -1, m[0], OUT, -2, -2, m[1], IN, -3,
+                            -3, f[0], OUT, -4, -3, m[2], OUT, -5, -1, f[1], OUT, -6]),
+        # ?x type C . ?x z1^-1 ?y . ?y m1 ?h . ?h m2^-1 ?w . ?w f1 ?a . ?w z2 ?c
+        ("chain_zipf_hub", [C + 1, TYPE_ID, IN, -1, -1, z[0], IN, -2, -2, m[3], OUT, -3,
+                            -3, m[4], IN, -4, -4, f[2], OUT, -5, -4, z[1], OUT, -6]),
+        # ?x type C . ?x f1 ?a . ?a m1 ?h . ?h m1^-1 ?y . ?y f1 ?b . ?x z3 ?c
+        ("star_fan_in", [C + 2, TYPE_ID, IN, -1, -1, f[3], OUT, -2, -2, m[5], OUT, -3,
+                         -3, m[5], IN, -4, -4, f[4], OUT, -5, -1, z[2], OUT, -6]),
+    ]
