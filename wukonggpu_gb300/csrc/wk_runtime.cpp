@@ -164,9 +164,15 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
             if (std::find(protect.begin(), protect.end(), v) != protect.end()) continue;
             if (x.last_use < oldest) { oldest = x.last_use; victim = v; }
         }
-        if (victim < 0)
-            return set_error(WK_ENOMEM, "segment cache: cannot fit id %d (%llu bytes) beside protected segments",
-                             id, (unsigned long long)need);
+        if (victim < 0) {
+            uint64_t free_total = 0;
+            for (auto &f : free_list) free_total += f.second;
+            return set_error(WK_ENOMEM,
+                             "segment cache: cannot fit id %d (%llu bytes) beside the protected segments "
+                             "(%llu bytes free in %zu ranges; the budget must hold the largest segments a "
+                             "query step and its prefetch use at once)",
+                             id, (unsigned long long)need, (unsigned long long)free_total, free_list.size());
+        }
         Resident &x = res[(size_t)victim];
         pool_free(x.off, x.bytes);
         x.resident = false;
