@@ -92,7 +92,7 @@ class Dist:
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -121,27 +121,34 @@ class ClockSampler:
                 self.proc.kill()
             self.fh.close()
 
-    def summary(self):
+    def summary(self, t0: float, t1: float):
+        """Median SM clock and active throttle reasons of the samples taken in [t0, t1] (epoch s).
+
+        When the window holds fewer than three samples, the three nearest are used."""
         if self.proc is None or not self.path.exists():
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm, smax, reasons = [], [], set()
+        import datetime
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.path.read_text().splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                smax.append(float(f[2]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(f[2]), float(f[3]),
+                             [n for n, v in zip(names, f[6:10]) if v.lower().startswith("active")]))
             except ValueError:
                 continue
-            for n, v in zip(names, f[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(n)
-        if not sm:
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = [r for r in rows if t0 <= r[0] <= t1]
+        if len(inside) < 3:
+            mid = 0.5 * (t0 + t1)
+            inside = sorted(rows, key=lambda r: abs(r[0] - mid))[:3]
+        reasons = sorted({n for r in inside for n in r[3]})
+        return {"sm_mhz": statistics.median(r[1] for r in inside), "sm_max_mhz": max(r[2] for r in inside),
+                "reasons": reasons, "samples": len(inside)}
 
 
 def peaks():
@@ -210,7 +217,7 @@ def run_reference(args, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator, reference id encoding)",
-        "config": {"workload": WORKLOAD, "queries": [n for n, _ in queries], "triples": int(g.n)},
+        "config": {"workload": WORKLOAD, "queries_per_step": len(queries), "triples": int(g.n)},
         "p50_ms": statistics.median(lat) * 1000, "p99_ms": float(np.percentile(lat, 99)) * 1000,
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port",
                          "sample": f"{args.steps} step(s) of the {len(queries)}-query mix on the full graph"},
@@ -244,6 +251,7 @@ def run_gb300(args, dist):
             if stats is not None:
                 stats.append(req)
 
+    clk = ClockSampler(dist.local).__enter__()
     for _ in range(args.warmup):
         one_step()
     rc.sync()
@@ -277,12 +285,14 @@ def run_gb300(args, dist):
     lat = []
     dist.barrier()
     rc.sync()
-    wall0 = time.perf_counter()
-    with ClockSampler(dist.local) as clk:
-        for _ in range(args.steps):
-            step_with_ops(lat)
-        rc.sync()
-    wall_s = time.perf_counter() - wall0
+    wall0, ep0 = time.perf_counter(), time.time()
+    for _ in range(args.steps):
+        step_with_ops(lat)
+    rc.sync()
+    wall_s, ep1 = time.perf_counter() - wall0, time.time()
+    time.sleep(0.3)
+    clk.__exit__(None, None, None)
+    clocks = clk.summary(ep0, ep1)
     dist.barrier()
     launches = rc.kernel_launches() - launches0
     rc.enable_timing(False)
@@ -344,20 +354,21 @@ def run_gb300(args, dist):
             "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded generator, reference id encoding)",
-            "config": {"workload": WORKLOAD, "queries": [n for n, _ in queries], "triples": int(g.n),
+            "config": {"workload": WORKLOAD, "queries_per_step": nq, "triples": int(g.n),
                        "entities": int(g.spec.n_entities), "parallelism": f"replicas{args.gpus}",
                        "store_device_bytes": info["device_bytes"], "l2": "inputs larger than L2 "
                        f"(store {info['device_bytes'] / 1e9:.1f} GB, histories up to "
                        f"{maxrows * 4 / 1e9:.2f} GB)", "plans": "given (statistics/learned planners not in this line)",
                        "setup_s": t_setup, "timed_wall_s": wall_s},
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "per_query_ms": {n: float(np.mean(lat[i::nq])) for i, (n, _) in enumerate(queries)},
+            "per_shape_ms": {sh: float(np.mean([x for i, x in enumerate(lat) if queries[i % nq][0].startswith(sh)]))
+                             for sh in sorted({n.split("/")[0] for n, _ in queries})},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d // args.steps,
                     "d2h_bytes_per_step": d2h // args.steps},
             "gpu_launches": launches,
-            "clocks": clk.summary(),
+            "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
     rc.close()

@@ -89,21 +89,23 @@ SQ_M2O = list(range(26, 34))
 SQ_FIRST_CLASS = 34
 
 
-def scale_queries(n_classes: int = 15):
+def scale_queries(per_shape: int = 5):
     """Six-pattern star+chain BGPs from a type index (the single-query-scale workload).
 
-    With 2M entities each class holds ~1.3e5 members; hub fan-in makes the
-    history reach 1e7..1e8 rows over up to 6 columns."""
+    Three query shapes, each instantiated on ``per_shape`` different classes
+    (15 classes in all).  With 2M entities a class holds ~1.3e5 members; hub
+    fan-in makes the history reach 1e7..1e8 rows over up to 6 columns."""
     C = SQ_FIRST_CLASS
     f, z, m = SQ_FUNC, SQ_ZIPF, SQ_M2O
-    return [
+    out = []
+    for k in range(per_shape):
         # ?x type C . ?x m1 ?h . ?h m2^-1 ?y . ?y f1 ?a . ?y m3 ?g . ?x f2 ?b
-        ("star_chain_hub", [C + 0, TYPE_ID, IN, -1, -1, m[0], OUT, -2, -2, m[1], IN, -3,
-                            -3, f[0], OUT, -4, -3, m[2], OUT, -5, -1, f[1], OUT, -6]),
+        out.append((f"star_chain_hub/{k}", [C + k, TYPE_ID, IN, -1, -1, m[0], OUT, -2, -2, m[1], IN, -3,
+                                            -3, f[0], OUT, -4, -3, m[2], OUT, -5, -1, f[1], OUT, -6]))
         # ?x type C . ?x z1^-1 ?y . ?y m1 ?h . ?h m2^-1 ?w . ?w f1 ?a . ?w z2 ?c
-        ("chain_zipf_hub", [C + 1, TYPE_ID, IN, -1, -1, z[0], IN, -2, -2, m[3], OUT, -3,
-                            -3, m[4], IN, -4, -4, f[2], OUT, -5, -4, z[1], OUT, -6]),
+        out.append((f"chain_zipf_hub/{k}", [C + 5 + k, TYPE_ID, IN, -1, -1, z[0], IN, -2, -2, m[3], OUT, -3,
+                                            -3, m[4], IN, -4, -4, f[2], OUT, -5, -4, z[1], OUT, -6]))
         # ?x type C . ?x f1 ?a . ?a m1 ?h . ?h m1^-1 ?y . ?y f1 ?b . ?x z3 ?c
-        ("star_fan_in", [C + 2, TYPE_ID, IN, -1, -1, f[3], OUT, -2, -2, m[5], OUT, -3,
-                         -3, m[5], IN, -4, -4, f[4], OUT, -5, -1, z[2], OUT, -6]),
-    ]
+        out.append((f"star_fan_in/{k}", [C + 10 + k, TYPE_ID, IN, -1, -1, f[3], OUT, -2, -2, m[5], OUT, -3,
+                                         -3, m[5], IN, -4, -4, f[4], OUT, -5, -1, z[2], OUT, -6]))
+    return out
