@@ -88,6 +88,8 @@ _SIGS = {
     "wk_known_to_const": (C.c_int, [_P, C.POINTER(wk_history), C.c_int64, C.c_int32, C.c_int32, C.c_int64]),
     "wk_index_to_unknown": (C.c_int, [_P, C.POINTER(wk_history), C.c_int32, C.c_int32]),
     "wk_const_to_unknown": (C.c_int, [_P, C.POINTER(wk_history), C.c_int64, C.c_int32, C.c_int32]),
+    "wk_known_to_unknown_noalloc": (C.c_int, [_P, _P, C.c_int64, C.c_int32, C.c_int64, C.c_int32, C.c_int32, _P,
+                                             C.c_int64, _I64P]),
     "wk_history_upload": (C.c_int, [_P, C.POINTER(wk_history), _I32P, C.c_int64, C.c_int32]),
     "wk_history_download": (C.c_int, [_P, C.POINTER(wk_history), _I32P, C.c_int64]),
     "wk_history_init": (None, [C.POINTER(wk_history)]),

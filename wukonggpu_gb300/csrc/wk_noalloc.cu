@@ -1,0 +1,142 @@
+// known_to_unknown without any allocation.
+//
+// Some callers cannot allocate device memory at the moment they expand a
+// pattern: a host that runs this operator inside its own memory-pool
+// callback or under a fixed device-memory budget, or a real-time serving
+// thread that must never enter cudaMalloc/cudaFree (both can synchronise the
+// whole device and stall every other stream).  This entry point serves them:
+// the caller passes the input history and an output buffer it already owns,
+// and every scratch array of the two-pass expansion lives in one file-scope
+// device array of fixed size, so the call allocates nothing.
+//
+// Limits and sharing rules:
+//   - at most kMaxRows input rows and kMaxTiles * tile_rows output rows per
+//     call (262,144 input rows, 16,777,216 output rows); larger calls are
+//     rejected with WK_EINVAL / WK_EOVERFLOW before any device work;
+//   - the array (about 6.4 MB) is held by every GPU that loads the library
+//     until the process exits;
+//   - every call shares it and it keeps the last call's contents: the only
+//     field that must start at zero (the probe's error flag) is cleared at
+//     the start of each call, everything else is fully written before it is
+//     read.  Calls that overlap on the GPU (from several host threads or
+//     several contexts' streams at once) race on the array and must not be
+//     issued;
+//   - the device address of the array is looked up once per device, on the
+//     first call made with that device current (cudaGetSymbolAddress); make
+//     that first call before any stream capture begins.
+#include <mutex>
+
+#include "wk_runtime.h"
+
+namespace {
+
+constexpr int64_t kMaxRows = 1 << 18;                 // input rows per call
+constexpr int64_t kMaxBlocks = kMaxRows / wk::dev::kRowsPerBlock;
+constexpr int64_t kMaxTiles = 1 << 14;                // output tiles per call
+
+constexpr size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+// byte layout of the scratch array
+constexpr size_t kOffFlags = 0;                                         // err (int) + totals (3 x u64)
+constexpr size_t kOffDeg = al(kOffFlags + 64);
+constexpr size_t kOffOff = al(kOffDeg + 4 * kMaxRows);
+constexpr size_t kOffBlkSum = al(kOffOff + 4 * kMaxRows);
+constexpr size_t kOffBlkNz = al(kOffBlkSum + 8 * kMaxBlocks);
+constexpr size_t kOffCzRow = al(kOffBlkNz + 4 * kMaxBlocks);
+constexpr size_t kOffCzPos = al(kOffCzRow + 4 * kMaxRows);
+constexpr size_t kOffCzOff = al(kOffCzPos + 8 * (kMaxRows + 1));
+constexpr size_t kOffTiles = al(kOffCzOff + 4 * kMaxRows);
+constexpr size_t kScratchBytes = al(kOffTiles + 4 * kMaxTiles);
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+std::mutex g_mu;
+void *g_addr[256] = {nullptr};   // per device ordinal
+
+// the array's device address for `device` (which must be current)
+int scratch_address(int device, unsigned char **out) {
+    if (device < 0 || device >= 256) return wk::set_error(WK_EINVAL, "noalloc: device ordinal %d", device);
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_addr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return wk::cuda_fail(e == cudaSuccess ? cudaErrorInvalidSymbol : e,
+                                                         "noalloc: cudaGetSymbolAddress");
+        g_addr[device] = p;
+    }
+    *out = static_cast<unsigned char *>(g_addr[device]);
+    return WK_OK;
+}
+
+}  // namespace
+
+using namespace wk;
+
+extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int64_t rows, int32_t cols,
+                                           int64_t start, int32_t direction, int32_t predict, int32_t *out,
+                                           int64_t out_capacity, int64_t *out_rows) {
+    if (!ctx || !out_rows || rows < 0 || cols < 1 || (rows > 0 && !hist) || out_capacity < 0 ||
+        (out_capacity > 0 && !out))
+        return set_error(WK_EINVAL, "known_to_unknown_noalloc: bad arguments");
+    *out_rows = 0;
+    if (!ctx->store) return set_error(WK_ENOSTORE, "known_to_unknown_noalloc: no store built");
+    if (ctx->store->pool)
+        return set_error(WK_EINVAL, "known_to_unknown_noalloc: needs a resident store (paging loads segments)");
+    if (predict < 1 || predict > ctx->store->hs->num_ids || (direction != WK_DIR_IN && direction != WK_DIR_OUT))
+        return set_error(WK_EINVAL, "known_to_unknown_noalloc: bad predicate %d / direction %d", predict, direction);
+    if (start >= 0 || -start > cols)
+        return set_error(WK_EINVAL, "known_to_unknown_noalloc: start %lld is not a bound column", (long long)start);
+    if (rows > kMaxRows)
+        return set_error(WK_EINVAL, "known_to_unknown_noalloc: %lld input rows exceed the maximum of %lld",
+                         (long long)rows, (long long)kMaxRows);
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    if (rows == 0) return WK_OK;
+    unsigned char *sc = nullptr;
+    int st = scratch_address(ctx->device, &sc);
+    if (st) return st;
+    int *err = reinterpret_cast<int *>(sc + kOffFlags);
+    unsigned long long *tot = reinterpret_cast<unsigned long long *>(sc + kOffFlags) + 1;
+    uint32_t *deg = reinterpret_cast<uint32_t *>(sc + kOffDeg);
+    uint32_t *off = reinterpret_cast<uint32_t *>(sc + kOffOff);
+    unsigned long long *blk_sum = reinterpret_cast<unsigned long long *>(sc + kOffBlkSum);
+    unsigned int *blk_nz = reinterpret_cast<unsigned int *>(sc + kOffBlkNz);
+    int32_t *cz_row = reinterpret_cast<int32_t *>(sc + kOffCzRow);
+    unsigned long long *cz_pos = reinterpret_cast<unsigned long long *>(sc + kOffCzPos);
+    uint32_t *cz_off = reinterpret_cast<uint32_t *>(sc + kOffCzOff);
+    int32_t *tile_k0 = reinterpret_cast<int32_t *>(sc + kOffTiles);
+
+    const PredView pv = ctx->store->views[(size_t)predict];
+    const int scol = (int)(-start - 1);
+    const int64_t nblk = (rows + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
+    cudaStream_t s = ctx->stream;
+    if ((e = cudaMemsetAsync(err, 0, sizeof(int), s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flag");
+    dev::launch_k2u_probe(hist, rows, cols, scol, (uint32_t)predict, (uint32_t)direction, pv, deg, off, blk_sum,
+                          blk_nz, err, s);
+    dev::launch_scan_blocks(blk_sum, blk_nz, nblk, tot, cz_pos, s);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: probe/scan launch");
+    ctx->launches += 2;
+    if ((e = cudaMemcpyAsync(ctx->h_scal, sc + kOffFlags, 32, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "noalloc: totals");
+    if (ctx->h_scal[0] & 0xffffffffull)
+        return set_error(WK_EDEVICE, "known_to_unknown_noalloc: corrupt overflow chain in the store");
+    const int64_t R_out = (int64_t)ctx->h_scal[1], nz = (int64_t)ctx->h_scal[2];
+    *out_rows = R_out;
+    if (R_out == 0) return WK_OK;
+    const int T = dev::k2u_tile_rows(cols + 1);
+    const int64_t ntiles = (R_out + T - 1) / T;
+    if (ntiles > kMaxTiles)
+        return set_error(WK_EOVERFLOW, "known_to_unknown_noalloc: %lld output rows exceed the maximum of %lld",
+                         (long long)R_out, (long long)(kMaxTiles * T));
+    if (R_out * (cols + 1) > out_capacity)
+        return set_error(WK_EOVERFLOW,
+                         "known_to_unknown_noalloc: output needs %lld int32 elements, capacity is %lld "
+                         "(*out_rows holds the row count)",
+                         (long long)(R_out * (cols + 1)), (long long)out_capacity);
+    dev::launch_k2u_compact(deg, off, rows, blk_sum, blk_nz, cz_row, cz_pos, cz_off, tile_k0, T, s);
+    dev::launch_k2u_write(hist, cols, pv.edges, cz_row, cz_pos, cz_off, nz, tile_k0, ntiles, T, R_out, out, s);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: compact/write launch");
+    ctx->launches += 2;
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "noalloc: sync");
+    return WK_OK;
+}
