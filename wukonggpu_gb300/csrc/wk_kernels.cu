@@ -45,33 +45,46 @@ __device__ __forceinline__ uint4 ld_slot(const uint4 *p) {
     return r;
 }
 
-// Warp-cooperative probe of 32 keys (one per lane).  The warp is split into
-// four 8-lane groups; a group reads one 128 B bucket with one 16 B load per
-// lane, and __ballot_sync over the warp tells each group which slot matched.
-// All eight buckets a lane needs are loaded before any is resolved, so every
-// lane has eight independent 16 B loads in flight.  On return lane L holds
-// (off, deg) of its own key; deg = 0 when the key is absent (the CPU engine's
-// size-0 result, core/gstore.hpp:389-409).
+// Warp-cooperative probe of the 32 keys held one per lane.  Equal keys in
+// the warp (the same start vertex on consecutive rows, common after an
+// expansion) are probed once: __match_any_sync groups them and only the
+// distinct keys are looked up.  The warp is split into four 8-lane groups; a
+// group reads one 128 B bucket with one 16 B load per lane, and
+// __ballot_sync tells each group which slot matched.  All buckets a lane
+// needs are loaded before any is resolved, so up to eight independent 16 B
+// loads per lane are in flight.  On return lane L holds (off, deg) of its
+// own key; deg = 0 when the key is absent (the CPU engine's size-0 result,
+// core/gstore.hpp:389-409).  Overflow hops are bounded by the segment's
+// overflow-bucket count.
 __device__ __forceinline__ void warp_probe32(const PredView &pv, uint64_t mykey, bool valid,
                                              uint32_t &r_off, uint32_t &r_deg, int *err) {
     const int lane = threadIdx.x & 31;
     const int sub = lane & 7, g = lane >> 3, gbase = lane & ~7;
+    // distinct keys of the warp, compacted to lanes 0..nu-1
+    const unsigned same = __match_any_sync(FULL, valid ? mykey : ~0ull);
+    const int lead = __ffs(same) - 1;
+    const unsigned L = __ballot_sync(FULL, valid && lead == lane);
+    const int nu = __popc(L);
+    const int src = lane < nu ? (int)__fns(L, 0, lane + 1) : 0;
+    const uint64_t ukey = __shfl_sync(FULL, mykey, src);
+    const int nit = (nu + 3) >> 2;
+
     uint4 w[8];
     uint64_t k[8];
     bool act[8];
 #pragma unroll
     for (int it = 0; it < 8; ++it) {
-        const int src = it * 4 + g;
-        k[it] = __shfl_sync(FULL, mykey, src);
-        act[it] = __shfl_sync(FULL, (int)valid, src) != 0 && pv.nmain > 0;
+        const int j = it * 4 + g;
+        k[it] = __shfl_sync(FULL, ukey, j);
+        act[it] = j < nu && pv.nmain > 0;
         const uint32_t b = act[it] ? d_bucket(d_mix(k[it]), pv.nmain) : 0u;
         w[it] = act[it] ? ld_slot(pv.buckets + (size_t)b * WK_SLOTS_PER_BUCKET + sub)
                         : make_uint4(0u, 0u, 0u, 0u);
     }
-    r_off = 0u;
-    r_deg = 0u;
+    uint32_t u_off = 0u, u_deg = 0u;   // result of distinct key `lane`
 #pragma unroll
     for (int it = 0; it < 8; ++it) {
+        if (it >= nit) break;           // warp-uniform
         uint32_t off_g = 0u, deg_g = 0u;
         bool pend = act[it];
         uint4 cw = w[it];
@@ -107,13 +120,19 @@ __device__ __forceinline__ void warp_probe32(const PredView &pv, uint64_t mykey,
             cw = pend ? ld_slot(pv.buckets + (size_t)nb * WK_SLOTS_PER_BUCKET + sub)
                       : make_uint4(0u, 0u, 0u, 0u);
         }
+        // distinct key it*4+g' is delivered to lane it*4+g'
         const uint32_t vo = __shfl_sync(FULL, off_g, (lane & 3) * 8);
         const uint32_t vd = __shfl_sync(FULL, deg_g, (lane & 3) * 8);
         if ((lane >> 2) == it) {
-            r_off = vo;
-            r_deg = vd;
+            u_off = vo;
+            u_deg = vd;
         }
     }
+    const int u = __popc(L & ((1u << lead) - 1u));
+    const uint32_t o = __shfl_sync(FULL, u_off, u);
+    const uint32_t d = __shfl_sync(FULL, u_deg, u);
+    r_off = valid ? o : 0u;
+    r_deg = valid ? d : 0u;
 }
 
 template <typename T>
@@ -343,8 +362,10 @@ k2u_compact_kernel(const uint32_t *__restrict__ deg, const uint32_t *__restrict_
 // covering the tile are staged in shared memory; each output row finds its
 // source by binary search, then the tile is written as a contiguous run of
 // 16 B stores (the tile start is a multiple of 32 rows, so 16 B aligned).
+// WC = output width (C + 1) when known at compile time, 0 for the generic case.
+template <int WC>
 __global__ void __launch_bounds__(kThreads)
-k2u_write_kernel(const int32_t *__restrict__ hist, int C, const int32_t *__restrict__ edges,
+k2u_write_kernel(const int32_t *__restrict__ hist, int C_rt, const int32_t *__restrict__ edges,
                  const int32_t *__restrict__ cz_row, const unsigned long long *__restrict__ cz_pos,
                  const uint32_t *__restrict__ cz_off, int64_t nz, const int32_t *__restrict__ tile_k0,
                  int64_t ntiles, int tile_rows, int64_t R_out, int32_t *__restrict__ out) {
@@ -353,6 +374,8 @@ k2u_write_kernel(const int32_t *__restrict__ hist, int C, const int32_t *__restr
     int *srow = pos_rel + tile_rows + 2;         // tile_rows + 1
     uint32_t *soff = (uint32_t *)(srow + tile_rows + 1);   // tile_rows + 1
     int *rsrc = (int *)(soff + tile_rows + 1);   // tile_rows
+    const int W = WC > 0 ? WC : C_rt + 1;
+    const int C = W - 1;
 
     const int64_t t = blockIdx.x;
     const int64_t o0 = t * (int64_t)tile_rows;
@@ -376,13 +399,12 @@ k2u_write_kernel(const int32_t *__restrict__ hist, int C, const int32_t *__restr
         rsrc[j] = lo;
     }
     __syncthreads();
-    const int W = C + 1;
-    const int64_t nwords = (int64_t)nrows * W;
+    const int nwords = nrows * W;
     int32_t *gout = out + o0 * W;
-    const int64_t nvec = (nwords + 3) >> 2;
-    for (int64_t v = threadIdx.x; v < nvec; v += blockDim.x) {
-        const int64_t w0 = v << 2;
-        int j = (int)(w0 / W), c = (int)(w0 - (int64_t)j * W);
+    const int nvec = (nwords + 3) >> 2;
+    for (int v = threadIdx.x; v < nvec; v += blockDim.x) {
+        const int w0 = v << 2;
+        int j = w0 / W, c = w0 - j * W;
         int vals[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -494,8 +516,22 @@ void launch_k2u_write(const int32_t *hist, int C, const int32_t *edges, const in
                       const unsigned long long *cz_pos, const uint32_t *cz_off, int64_t nz,
                       const int32_t *tile_k0, int64_t ntiles, int tile_rows, int64_t R_out,
                       int32_t *out, cudaStream_t st) {
-    k2u_write_kernel<<<(unsigned int)ntiles, kThreads, k2u_write_smem(tile_rows), st>>>(
-        hist, C, edges, cz_row, cz_pos, cz_off, nz, tile_k0, ntiles, tile_rows, R_out, out);
+    const unsigned int g = (unsigned int)ntiles;
+    const size_t sm = k2u_write_smem(tile_rows);
+#define WK_WRITE(WC)                                                                                   \
+    k2u_write_kernel<WC><<<g, kThreads, sm, st>>>(hist, C, edges, cz_row, cz_pos, cz_off, nz, tile_k0, \
+                                                  ntiles, tile_rows, R_out, out)
+    switch (C + 1) {
+        case 2: WK_WRITE(2); break;
+        case 3: WK_WRITE(3); break;
+        case 4: WK_WRITE(4); break;
+        case 5: WK_WRITE(5); break;
+        case 6: WK_WRITE(6); break;
+        case 7: WK_WRITE(7); break;
+        case 8: WK_WRITE(8); break;
+        default: WK_WRITE(0); break;
+    }
+#undef WK_WRITE
 }
 
 void launch_filter_write(const int32_t *hist, int64_t R, int C, const uint32_t *mask,
