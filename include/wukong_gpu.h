@@ -65,7 +65,8 @@ typedef struct {
 
 /* Context configuration (the global_gpu_* knobs of core/config.hpp:66-78). */
 typedef struct {
-    int32_t  device;                 /* CUDA device ordinal                          */
+    int32_t  device;                 /* CUDA device ordinal; -1 = host-only context
+                                        (store image, statistics, planner)          */
     int32_t  cache_budget_mb;        /* 0 = whole store resident; > 0 = page
                                         predicate segments from pinned host memory
                                         into a device pool of this many MiB
@@ -198,6 +199,28 @@ int wk_enable_timing(wk_ctx *ctx, int enable);
 int wk_last_op_stats(wk_ctx *ctx, wk_op_stats *st);
 int64_t wk_kernel_launches(wk_ctx *ctx);   /* cumulative kernel launches */
 int wk_sync(wk_ctx *ctx);
+/* ------------------------------------------------------- the planner
+ * Statistics-based plan of a BGP: Planner::generate_plan
+ * (core/planner.hpp:927-1028) over the statistics of
+ * GStore::generate_statistic (core/gstore.hpp:1010-1127).  The input is a
+ * BGP in cmd_chains form (any variable numbering, 1..10 patterns); the output
+ * is the executable order (possibly starting with an inserted index pattern)
+ * with variables renumbered -1, -2, ... in plan order.  *n_out holds the room
+ * of cmd_out in patterns on entry and the plan's patterns on return.  When
+ * the correlation statistics prove the result empty, *proved_empty is set
+ * and no plan is returned (the reference's "identified empty result
+ * query").  When the search finds no complete order, *n_out is 0 and the
+ * cost is +inf, as the reference returns an empty plan (it happens when every
+ * pattern starts from one constant); callers then run the query as written.
+ * Statistics are built on first use.  Works on host-only contexts. */
+int wk_plan(wk_ctx *ctx, const int64_t *cmd_in, int32_t n, int64_t *cmd_out, int32_t *n_out,
+            double *est_cost, int32_t *proved_empty);
+/* One statistic: which = 0 triples, 1 subjects, 2 objects, 3 type members
+ * (of id a; out4[0]), 4 correlation of the pair (a, b) as {out_out, out_in,
+ * in_in, in_out} in out4[0..3].  Same counts as the reference's global_*
+ * maps after its gather. */
+int wk_stat_get(wk_ctx *ctx, int32_t which, int32_t a, int32_t b, int64_t *out4);
+
 /* Device-side interval on the context's stream: begin records a CUDA event,
  * end records another, synchronises and returns the elapsed milliseconds. */
 int wk_timer_begin(wk_ctx *ctx);

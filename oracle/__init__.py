@@ -193,6 +193,13 @@ def _load_ref():
         lib.ref_free_table.argtypes = [_I32P]
         lib.ref_digest.restype = C.c_uint64
         lib.ref_digest.argtypes = [C.c_void_p, _I64P, _I64P]
+        lib.ref_stats.restype = C.c_void_p
+        lib.ref_stats.argtypes = [C.c_void_p]
+        lib.ref_stats_free.argtypes = [C.c_void_p]
+        lib.ref_stat_get.restype = C.c_int
+        lib.ref_stat_get.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _I64P]
+        lib.ref_plan.restype = C.c_int
+        lib.ref_plan.argtypes = [C.c_void_p, _I64P, C.c_int32, _I64P, C.POINTER(C.c_int32)]
         _ref = lib
     return _ref
 
@@ -245,7 +252,35 @@ class RefStore:
         lib.ref_free_table(ptr)
         return out, step_rows
 
+    def stats(self):
+        """The reference statistics (generate_statistic + one-server gather)."""
+        if getattr(self, "_st", None) is None:
+            self._st = _load_ref().ref_stats(self._h)
+        return self._st
+
+    def stat(self, which: int, a: int, b: int = 0):
+        out = np.zeros(4, np.int64)
+        _load_ref().ref_stat_get(self.stats(), which, a, b, out.ctypes.data_as(_I64P))
+        return [int(x) for x in out] if which == 4 else int(out[0])
+
+    def plan(self, cmd_chains):
+        """Planner::generate_plan of the reference: (plan or None when empty)."""
+        cc = np.asarray(cmd_chains, np.int64)
+        n = len(cc) // 4
+        out = np.zeros(4 * (n + 2), np.int64)
+        n_out = C.c_int32(n + 2)
+        rc = _load_ref().ref_plan(self.stats(), cc.ctypes.data_as(_I64P), n, out.ctypes.data_as(_I64P),
+                                  C.byref(n_out))
+        if rc == 1:
+            return None
+        if rc != 0:
+            raise ValueError("reference planner: output too long")
+        return [int(x) for x in out[:4 * n_out.value]]
+
     def close(self):
+        if getattr(self, "_st", None):
+            _load_ref().ref_stats_free(self._st)
+            self._st = None
         if getattr(self, "_h", None):
             _load_ref().ref_free(self._h)
             self._h = None

@@ -1,5 +1,11 @@
 // Reference harness -- TEST INFRASTRUCTURE ONLY.
 //
+// Besides the store, the harness exposes the reference's statistics and
+// planner: GStore::generate_statistic fills a data_statistic, the one-server
+// part of data_statistic::gather_data (core/data_statistic.hpp:66-157:
+// global maps = local maps, then the two type fix-ups) is restated, and
+// Planner::generate_plan runs on it unchanged.
+//
 // Compiles the reference's own store, core/gstore.hpp, from the reference
 // sources in place (see the `ref` target of oracle/Makefile: the reference
 // headers are reached through symlinks, the missing network/RDMA headers and
@@ -28,6 +34,7 @@
 #include <vector>
 
 #include "gstore.hpp"   // the reference store, compiled from its own sources
+#include "planner.hpp"  // the reference statistics planner
 
 namespace {
 
@@ -222,5 +229,90 @@ uint64_t ref_digest(void *h, int64_t *nkeys, int64_t *nedges) {
     return d;
 }
 
+
+}  // extern "C"
+
+namespace {
+struct RefStats {
+    data_statistic st;
+    boost::mpi::communicator world;
+};
+}  // namespace
+
+extern "C" {
+
+void *ref_stats(void *h) {
+    RefStore *r = (RefStore *)h;
+    RefStats *rs = new RefStats();
+    rs->st.world = &rs->world;
+    rs->st.tcp_adaptor = nullptr;
+    fflush(stdout);
+    const int saved = dup(1), devnull = open("/dev/null", O_WRONLY);
+    if (saved >= 0 && devnull >= 0) dup2(devnull, 1);
+    r->g->generate_statistic(rs->st);
+    fflush(stdout);
+    if (saved >= 0) { dup2(saved, 1); close(saved); }
+    if (devnull >= 0) close(devnull);
+    data_statistic &d = rs->st;
+    // one server: the gathered maps are the local ones (core/data_statistic.hpp:83-142)
+    d.global_ptcount = d.predicate_to_triple;
+    d.global_pscount = d.predicate_to_subject;
+    d.global_pocount = d.predicate_to_object;
+    d.global_ppcount = d.correlation;
+    d.global_tyscount = d.type_to_subject;
+    // type predicate fix-ups (core/data_statistic.hpp:150-156)
+    d.global_pocount[1] = d.global_tyscount.size();
+    int triple = 0;
+    for (auto &kv : d.global_tyscount) triple += kv.second;
+    d.global_ptcount[1] = triple;
+    return rs;
+}
+
+void ref_stats_free(void *p) { delete (RefStats *)p; }
+
+// which: 0 triples, 1 subjects, 2 objects, 3 type members, 4 correlation pair
+int ref_stat_get(void *p, int which, int a, int b, int64_t *out4) {
+    data_statistic &d = ((RefStats *)p)->st;
+    out4[0] = out4[1] = out4[2] = out4[3] = 0;
+    auto get = [](unordered_map<int, int> &m, int k) -> int64_t { auto it = m.find(k); return it == m.end() ? 0 : it->second; };
+    switch (which) {
+        case 0: out4[0] = get(d.global_ptcount, a); break;
+        case 1: out4[0] = get(d.global_pscount, a); break;
+        case 2: out4[0] = get(d.global_pocount, a); break;
+        case 3: out4[0] = get(d.global_tyscount, a); break;
+        case 4: {
+            auto it = d.global_ppcount.find(make_pair(a, b));
+            if (it != d.global_ppcount.end()) {
+                out4[0] = it->second.out_out; out4[1] = it->second.out_in;
+                out4[2] = it->second.in_in; out4[3] = it->second.in_out;
+            }
+            break;
+        }
+        default: return -1;
+    }
+    return 0;
+}
+
+// Planner::generate_plan on the reference statistics.  Returns 0 with a plan,
+// 1 when the planner reports an empty result.  *n_out in: room (patterns).
+int ref_plan(void *p, const int64_t *cmd, int32_t n, int64_t *out, int32_t *n_out) {
+    RefStats *rs = (RefStats *)p;
+    request_or_reply req;
+    req.cmd_chains.assign(cmd, cmd + (size_t)n * 4);
+    Planner planner;
+    fflush(stdout);
+    const int saved = dup(1), devnull = open("/dev/null", O_WRONLY);
+    if (saved >= 0 && devnull >= 0) dup2(devnull, 1);
+    const bool ok = planner.generate_plan(req, &rs->st);
+    fflush(stdout);
+    if (saved >= 0) { dup2(saved, 1); close(saved); }
+    if (devnull >= 0) close(devnull);
+    if (!ok) { *n_out = 0; return 1; }
+    const int32_t m = (int32_t)(req.cmd_chains.size() / 4);
+    if (m > *n_out) return -1;
+    for (size_t i = 0; i < req.cmd_chains.size(); ++i) out[i] = req.cmd_chains[i];
+    *n_out = m;
+    return 0;
+}
 
 }  // extern "C"

@@ -76,6 +76,11 @@ def main() -> None:
             entry["ordered_sha256"] = table_digest(t)
         out["queries"].append(entry)
         print(f"{name:22s} rows={t.shape[0]:8d} steps={list(step_rows)}")
+    # the reference planner on seeded random BGPs (core/planner.hpp generate_plan)
+    out["plans"] = []
+    for q in workloads.random_bgps(s, p, o, 120, seed=77, first_class=g.first_class, n_classes=10):
+        plan = ref.plan(q)
+        out["plans"].append({"bgp": [int(x) for x in q], "plan": plan})
     (OUT / "small.json").write_text(json.dumps(out, indent=1) + "\n")
     print(f"wrote {OUT / 'small.json'}")
 

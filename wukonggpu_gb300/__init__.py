@@ -98,6 +98,9 @@ _SIGS = {
     "wk_last_op_stats": (C.c_int, [_P, C.POINTER(wk_op_stats)]),
     "wk_kernel_launches": (C.c_int64, [_P]),
     "wk_sync": (C.c_int, [_P]),
+    "wk_plan": (C.c_int, [_P, _I64P, C.c_int32, _I64P, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                          C.POINTER(C.c_int32)]),
+    "wk_stat_get": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, _I64P]),
     "wk_timer_begin": (C.c_int, [_P]),
     "wk_timer_end": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "wk_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_P)]),
@@ -332,6 +335,28 @@ class RCache:
                                          rows.ctypes.data_as(_I64P)))
         req.result_table = self.download(req) if download else None
         return req, rows
+
+    def plan(self, cmd_chains):
+        """Statistics-based plan: (planned cmd_chains, estimated cost).
+
+        None when the statistics prove the result empty; [] (cost inf) when the
+        planner finds no order, as the reference does."""
+        cc = np.asarray(cmd_chains, np.int64)
+        n = len(cc) // 4
+        out = np.zeros(4 * (n + 2), np.int64)
+        n_out = C.c_int32(n + 2)
+        cost = C.c_double()
+        empty = C.c_int32()
+        _check(load_library().wk_plan(self._h, cc.ctypes.data_as(_I64P), n, out.ctypes.data_as(_I64P),
+                                      C.byref(n_out), C.byref(cost), C.byref(empty)))
+        if empty.value:
+            return None, 0.0
+        return [int(x) for x in out[:4 * n_out.value]], cost.value
+
+    def stat(self, which: int, a: int, b: int = 0):
+        out = np.zeros(4, np.int64)
+        _check(load_library().wk_stat_get(self._h, which, a, b, out.ctypes.data_as(_I64P)))
+        return [int(x) for x in out] if which == 4 else int(out[0])
 
     def enable_timing(self, on: bool = True):
         _check(load_library().wk_enable_timing(self._h, 1 if on else 0))

@@ -69,6 +69,10 @@ struct HostStore {
     uint64_t lookup(uint64_t vid, uint32_t pid, uint32_t dir, const int32_t **edges_out) const;
 };
 
+struct Stats;   // planner statistics (wk_planner.cpp)
+Stats *build_stats(const HostStore &hs);
+void free_stats(Stats *s);
+
 int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
                      int32_t num_ids, HostStore **out);
 

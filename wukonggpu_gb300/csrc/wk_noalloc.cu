@@ -79,6 +79,7 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
         return set_error(WK_EINVAL, "known_to_unknown_noalloc: bad arguments");
     *out_rows = 0;
     if (!ctx->store) return set_error(WK_ENOSTORE, "known_to_unknown_noalloc: no store built");
+    if (ctx->device < 0) return set_error(WK_EDEVICE, "known_to_unknown_noalloc: host-only context");
     if (ctx->store->pool)
         return set_error(WK_EINVAL, "known_to_unknown_noalloc: needs a resident store (paging loads segments)");
     if (predict < 1 || predict > ctx->store->hs->num_ids || (direction != WK_DIR_IN && direction != WK_DIR_OUT))

@@ -30,6 +30,7 @@ inline bool is_tpid(int64_t id) { return id > 1 && id < WK_VID_BASE; }   // core
 int check_ctx(wk_ctx *ctx, wk_history *h, const char *what) {
     if (!ctx || !h) return set_error(WK_EINVAL, "%s: null argument", what);
     if (!ctx->store) return set_error(WK_ENOSTORE, "%s: no store built", what);
+    if (ctx->device < 0) return set_error(WK_EDEVICE, "%s: host-only context", what);
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     return WK_OK;
@@ -350,6 +351,7 @@ static int vtype(int64_t v, int col_num) {   // 0 known, 1 unknown, 2 const
 extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history *h, int64_t *step_rows) {
     if (!ctx || !cmd || !h || n <= 0) return set_error(WK_EINVAL, "wk_execute: bad arguments");
     if (!ctx->store) return set_error(WK_ENOSTORE, "wk_execute: no store");
+    if (ctx->device < 0) return set_error(WK_EDEVICE, "wk_execute: host-only context");
     wk_history_init(h);
     ctx->protect.clear();
     DeviceStore &ds = *ctx->store;

@@ -218,11 +218,13 @@ using namespace wk;
 
 // ================================================================ context
 static int make_current(wk_ctx *ctx) {
+    if (ctx->device < 0) return set_error(WK_EDEVICE, "host-only context: no device work");
     cudaError_t e = cudaSetDevice(ctx->device);
     return e == cudaSuccess ? WK_OK : cuda_fail(e, "cudaSetDevice");
 }
 
 wk_ctx::~wk_ctx() {
+    if (device < 0) return;
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
     for (auto &b : hbuf) b.release();
@@ -273,6 +275,13 @@ extern "C" int wk_ctx_create(const wk_config *cfg_in, wk_ctx **out) {
     wk_config cfg;
     if (cfg_in) cfg = *cfg_in;
     else wk_config_default(&cfg);
+    if (cfg.device < 0) {   // host-only: store image, statistics and planner, no device work
+        wk_ctx *hctx = new wk_ctx();
+        hctx->device = -1;
+        hctx->cfg = cfg;
+        *out = hctx;
+        return WK_OK;
+    }
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
     if (e != cudaSuccess || n <= 0) return cuda_fail(e == cudaSuccess ? cudaErrorNoDevice : e, "wk_ctx_create: no CUDA device");
@@ -306,6 +315,7 @@ extern "C" int wk_ctx_destroy(wk_ctx *ctx) {
 
 extern "C" int wk_sync(wk_ctx *ctx) {
     if (!ctx) return set_error(WK_EINVAL, "wk_sync: null ctx");
+    if (ctx->device < 0) return WK_OK;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     return e == cudaSuccess ? WK_OK : cuda_fail(e, "wk_sync");
 }
@@ -313,13 +323,17 @@ extern "C" int wk_sync(wk_ctx *ctx) {
 extern "C" int wk_store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o,
                               int64_t n, int32_t num_ids) {
     if (!ctx) return set_error(WK_EINVAL, "wk_store_build: null ctx");
-    int st = make_current(ctx);
-    if (st) return st;
+    int st;
+    if (ctx->device >= 0 && (st = make_current(ctx))) return st;
     HostStore *hs = nullptr;
     if ((st = build_host_store(s, p, o, n, num_ids, &hs)) != WK_OK) return st;
     auto ds = std::make_shared<DeviceStore>();
     ds->hs.reset(hs);
     ds->device = ctx->device;
+    if (ctx->device < 0) {   // host-only: no device copy
+        ctx->store = ds;
+        return WK_OK;
+    }
     if (ctx->cfg.cache_budget_mb > 0) st = ds->init_paged((uint64_t)ctx->cfg.cache_budget_mb << 20);
     else st = ds->upload_resident();
     if (st != WK_OK) return st;

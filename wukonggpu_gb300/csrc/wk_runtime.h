@@ -34,6 +34,7 @@ struct DeviceStore {
     };
     int device = 0;
     std::unique_ptr<HostStore> hs;
+    std::shared_ptr<Stats> stats;   // built on first use by the planner
     std::vector<PredView> views;    // per id
     uint64_t device_bytes = 0;
     // resident mode
@@ -60,7 +61,7 @@ struct DeviceStore {
 }  // namespace wk
 
 struct wk_ctx {
-    int device = 0;
+    int device = 0;                  // -1: host-only context (store image, statistics, planner)
     wk_config cfg{};
     cudaStream_t stream = nullptr;   // op stream
     cudaStream_t side = nullptr;     // segment prefetch stream

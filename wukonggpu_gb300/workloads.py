@@ -109,3 +109,61 @@ def scale_queries(per_shape: int = 5):
         out.append((f"star_fan_in/{k}", [C + 10 + k, TYPE_ID, IN, -1, -1, f[3], OUT, -2, -2, m[5], OUT, -3,
                                          -3, m[5], IN, -4, -4, f[4], OUT, -5, -1, z[2], OUT, -6]))
     return out
+
+
+# ---------------------------------------------------------- random BGPs
+def random_bgps(s, p, o, n: int, seed: int, min_pat: int = 2, max_pat: int = 6, first_class: int | None = None,
+                n_classes: int = 0, const_frac: float = 0.4):
+    """Seeded random connected BGPs in SPARQL triple form (start, pid, OUT, end),
+    as a parser emits them (variables -1, -2, ... in order of appearance).
+
+    Shapes: chains, stars and single cycles (a chain closed by one edge back to
+    its first variable).  A query is anchored either on a type constraint
+    (``?x rdf:type C``) or on a constant vertex drawn from the subjects of its
+    first predicate.  Predicates are drawn among those present in the graph."""
+    rng = np.random.default_rng(seed)
+    preds = [int(x) for x in np.unique(p) if x != TYPE_ID]
+    subj_by_pred = {}
+    out = []
+    for q in range(n):
+        k = int(rng.integers(min_pat, max_pat + 1))
+        shape = ("chain", "star", "cycle")[int(rng.integers(0, 3))]
+        pats = []
+        nv = 1
+        anchor_type = first_class is not None and n_classes > 0 and rng.random() >= const_frac
+        body = k - (1 if anchor_type else 0)
+        if shape == "cycle" and body < 3:
+            shape = "chain"
+        cur = -1
+        for i in range(body):
+            pid = preds[int(rng.integers(0, len(preds)))]
+            if shape == "star":
+                nv += 1
+                pats.append([-1, pid, OUT, -nv])
+            elif shape == "cycle" and i == body - 1:
+                pats.append([cur, pid, OUT, -1])
+            else:
+                nv += 1
+                pats.append([cur, pid, OUT, -nv])
+                cur = -nv
+        if anchor_type:
+            c = first_class + int(rng.integers(0, n_classes))
+            pats.insert(int(rng.integers(0, len(pats) + 1)), [-1, TYPE_ID, OUT, c])
+        else:
+            pid0 = pats[0][1]
+            if pid0 not in subj_by_pred:
+                subj_by_pred[pid0] = np.unique(s[p == pid0])
+            cands = subj_by_pred[pid0]
+            c = int(cands[int(rng.integers(0, len(cands)))])
+            # replace variable -1 by the constant everywhere
+            pats = [[c if x == -1 else x for x in pat[:1]] + pat[1:3] + [c if pat[3] == -1 else pat[3]]
+                    for pat in pats]
+            # renumber variables in order of appearance
+            conv = {}
+            for pat in pats:
+                for j in (0, 3):
+                    if pat[j] < 0:
+                        conv.setdefault(pat[j], -1 - len(conv))
+                        pat[j] = conv[pat[j]]
+        out.append([x for pat in pats for x in pat])
+    return out
