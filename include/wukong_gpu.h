@@ -183,6 +183,36 @@ void wk_history_init(wk_history *h);
 int wk_execute(wk_ctx *ctx, const int64_t *cmd_chains, int32_t n_patterns, wk_history *h,
                int64_t *step_rows);
 
+/* -------------------------------------------------- batched light queries
+ * Many concurrent constant-start queries executed together: one persistent
+ * launch per plan step over a packed multi-query history with per-query
+ * offsets, captured once as a CUDA graph and replayed for every batch (the
+ * batched counterpart of running GPU_Engine::execute_request once per query,
+ * core/gpu_engine.hpp:471-526).  Every query's rows are exactly those it
+ * produces alone.  Queries: 1..max_steps patterns, the first one
+ * `<const> p d -1`, the others k2u / k2k / k2c; packed back to back in
+ * cmd_chains with n_patterns[q] patterns each.  capacity_ints bounds every
+ * step's packed table; a larger step returns WK_EOVERFLOW. */
+typedef struct wk_batch wk_batch;
+int wk_batch_create(wk_ctx *ctx, int32_t max_queries, int32_t max_steps, int64_t capacity_ints,
+                    wk_batch **out);
+int wk_batch_destroy(wk_batch *b);
+int wk_batch_run(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
+                 int32_t use_graph);
+/* Result of query q of the last run: rows, columns and its int32 offset in the packed result. */
+int wk_batch_result(wk_batch *b, int32_t q, int64_t *rows, int32_t *cols, int64_t *int_offset);
+/* Copy the packed results of the last run to host memory (host may be NULL to get the size). */
+int wk_batch_download(wk_batch *b, int32_t *host, int64_t cap, int64_t *total_ints);
+/* Launch shape of the step kernels: persistent blocks per SM, input rows per
+ * warp per tile, and the output size (ints) above which a row is written by a
+ * whole warp instead of one thread. */
+int wk_batch_set_tuning(wk_batch *b, int32_t blocks_per_sm, int32_t rows_per_warp, int32_t split_ints);
+int wk_batch_get_tuning(wk_batch *b, int32_t *blocks_per_sm, int32_t *rows_per_warp, int32_t *split_ints);
+/* Autotuner: time every candidate launch shape on these queries and keep the fastest. */
+int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
+                      int32_t reps, double *best_ms);
+int64_t wk_batch_kernel_launches(wk_batch *b);
+
 /* Per-op timing of the last op (device time from CUDA events, ms) and its
  * algorithmic bytes (input rows/cols, output rows, adjacency entries read). */
 typedef struct {

@@ -1,0 +1,81 @@
+"""Batched execution: every query's table equals the one it produces alone
+(same rows, same order) -- against the oracle and against the single-query
+GPU path -- through graph replays of different batches, tuning changes and
+capacity limits."""
+import numpy as np
+import pytest
+
+import oracle
+import wukonggpu_gb300 as W
+from wukonggpu_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def light(small_graph):
+    g, s, p, o = small_graph
+    return workloads.light_queries(s, p, o, 600, seed=3)
+
+
+def _check(tables, queries, orc):
+    for t, q in zip(tables, queries):
+        exp, _ = orc.execute(q)
+        got = t.reshape(exp.shape) if t.size == 0 else t
+        assert got.shape == exp.shape and np.array_equal(got, exp), q
+
+
+def test_batch_matches_oracle_graph_and_plain(gpu_small, small_oracle, light):
+    b = W.Batch(gpu_small, max_queries=1024, max_steps=4, capacity_ints=1 << 24)
+    for use_graph in (False, True):
+        nq = b.run(light, use_graph=use_graph)
+        _check(b.download(nq), light, small_oracle)
+
+
+def test_graph_replay_with_new_batches(gpu_small, small_oracle, small_graph):
+    g, s, p, o = small_graph
+    b = W.Batch(gpu_small, max_queries=1024, max_steps=4, capacity_ints=1 << 24)
+    for seed in (11, 12, 13):
+        qs = workloads.light_queries(s, p, o, 512, seed=seed)
+        nq = b.run(qs)
+        _check(b.download(nq), qs, small_oracle)
+
+
+def test_alone_equals_in_the_mix(gpu_small, light):
+    b = W.Batch(gpu_small, max_queries=1024, max_steps=4, capacity_ints=1 << 24)
+    nq = b.run(light)
+    mixed = [t.copy() for t in b.download(nq)]
+    for i in (0, 7, 100, 599):
+        b1 = W.Batch(gpu_small, max_queries=1, max_steps=4, capacity_ints=1 << 22)
+        b1.run([light[i]])
+        alone = b1.download(1)[0]
+        assert np.array_equal(alone, mixed[i])
+        req, _ = gpu_small.execute(light[i])              # the single-query path
+        assert np.array_equal(req.result_table.reshape(alone.shape) if alone.size == 0 else req.result_table, alone)
+
+
+def test_tuning_and_autotune_keep_results(gpu_small, small_oracle, light):
+    b = W.Batch(gpu_small, max_queries=1024, max_steps=4, capacity_ints=1 << 24)
+    for bps, rows, split in ((2, 32, 16), (8, 128, 256), (4, 64, 1)):
+        b.set_tuning(bps, rows, split)
+        nq = b.run(light[:300])
+        _check(b.download(nq), light[:300], small_oracle)
+    ms = b.autotune(light, reps=2)
+    assert ms > 0 and b.tuning()[0] in (2, 4, 8)
+    nq = b.run(light)
+    _check(b.download(nq), light, small_oracle)
+
+
+def test_capacity_overflow_is_reported(gpu_small, light):
+    b = W.Batch(gpu_small, max_queries=1024, max_steps=4, capacity_ints=4096)
+    with pytest.raises(W.WkError) as e:
+        b.run(light)
+    assert e.value.status == W.WK_EOVERFLOW
+
+
+def test_bad_batch_queries_rejected(gpu_small):
+    b = W.Batch(gpu_small, max_queries=8, max_steps=2, capacity_ints=1 << 16)
+    with pytest.raises(W.WkError):
+        b.run([[W.VID_BASE, 2, W.OUT, -1, -1, 2, W.OUT, -2, -2, 2, W.OUT, -3]])   # 3 patterns > 2
+    with pytest.raises(W.WkError):
+        b.run([[-1, 2, W.OUT, -2]])                                               # no constant start

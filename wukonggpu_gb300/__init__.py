@@ -101,6 +101,15 @@ _SIGS = {
     "wk_plan": (C.c_int, [_P, _I64P, C.c_int32, _I64P, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                           C.POINTER(C.c_int32)]),
     "wk_stat_get": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32, _I64P]),
+    "wk_batch_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64, C.POINTER(_P)]),
+    "wk_batch_destroy": (C.c_int, [_P]),
+    "wk_batch_run": (C.c_int, [_P, _I64P, _I32P, C.c_int32, C.c_int32]),
+    "wk_batch_result": (C.c_int, [_P, C.c_int32, _I64P, _I32P, _I64P]),
+    "wk_batch_download": (C.c_int, [_P, _I32P, C.c_int64, _I64P]),
+    "wk_batch_set_tuning": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "wk_batch_get_tuning": (C.c_int, [_P, _I32P, _I32P, _I32P]),
+    "wk_batch_autotune": (C.c_int, [_P, _I64P, _I32P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
+    "wk_batch_kernel_launches": (C.c_int64, [_P]),
     "wk_timer_begin": (C.c_int, [_P]),
     "wk_timer_end": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "wk_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_P)]),
@@ -385,6 +394,75 @@ class RCache:
     def close(self):
         if getattr(self, "_h", None):
             load_library().wk_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Batched execution of constant-start queries (one CUDA graph per batch shape)."""
+
+    def __init__(self, rc: "RCache", max_queries: int = 4096, max_steps: int = 4, capacity_ints: int = 1 << 26):
+        h = _P()
+        _check(load_library().wk_batch_create(rc._h, max_queries, max_steps, capacity_ints, C.byref(h)))
+        self._h = h
+        self.rc = rc
+        self.max_steps = max_steps
+
+    @staticmethod
+    def pack(queries):
+        cmd = np.asarray([x for q in queries for x in q], np.int64)
+        npat = np.asarray([len(q) // 4 for q in queries], np.int32)
+        return cmd, npat
+
+    def run(self, queries, use_graph: bool = True, packed=None):
+        cmd, npat = packed if packed is not None else self.pack(queries)
+        _check(load_library().wk_batch_run(self._h, cmd.ctypes.data_as(_I64P), npat.ctypes.data_as(_I32P),
+                                           len(npat), 1 if use_graph else 0))
+        return len(npat)
+
+    def download(self, nq: int, into: "PinnedBuffer | None" = None):
+        """Per-query result tables of the last run (numpy views into one packed array)."""
+        lib = load_library()
+        tot = C.c_int64()
+        _check(lib.wk_batch_download(self._h, None, 0, C.byref(tot)))
+        if into is not None and into.n >= tot.value:
+            buf = into.array
+        else:
+            buf = np.zeros(max(tot.value, 1), np.int32)
+        _check(lib.wk_batch_download(self._h, buf.ctypes.data_as(_I32P), buf.size, C.byref(tot)))
+        out = []
+        rows, cols, off = C.c_int64(), C.c_int32(), C.c_int64()
+        for q in range(nq):
+            _check(lib.wk_batch_result(self._h, q, C.byref(rows), C.byref(cols), C.byref(off)))
+            out.append(buf[off.value:off.value + rows.value * cols.value].reshape(rows.value, max(cols.value, 1)))
+        return out
+
+    def set_tuning(self, blocks_per_sm: int, rows_per_warp: int, split_ints: int):
+        _check(load_library().wk_batch_set_tuning(self._h, blocks_per_sm, rows_per_warp, split_ints))
+
+    def tuning(self):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(load_library().wk_batch_get_tuning(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def autotune(self, queries, reps: int = 3) -> float:
+        cmd, npat = self.pack(queries)
+        ms = C.c_double()
+        _check(load_library().wk_batch_autotune(self._h, cmd.ctypes.data_as(_I64P), npat.ctypes.data_as(_I32P),
+                                                len(npat), reps, C.byref(ms)))
+        return ms.value
+
+    def kernel_launches(self) -> int:
+        return load_library().wk_batch_kernel_launches(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().wk_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -167,3 +167,57 @@ def random_bgps(s, p, o, n: int, seed: int, min_pat: int = 2, max_pat: int = 6, 
                         pat[j] = conv[pat[j]]
         out.append([x for pat in pats for x in pat])
     return out
+
+
+# ------------------------------------------------ light constant-start queries
+def light_queries(s, p, o, n: int, seed: int, max_pat: int = 4, filters: bool = True):
+    """Seeded light queries for batching: a constant start vertex drawn uniformly
+    among subjects, then 1..max_pat patterns, each predicate drawn among those
+    present on the vertex the walk reached (so results are non-empty and their
+    sizes heavy-tailed).  With ``filters`` some later steps are known_to_known /
+    known_to_const checks.  Executable as written (start bound, end new)."""
+    rng = np.random.default_rng(seed)
+    order = np.argsort(s, kind="stable")
+    ss, pp, oo = s[order], p[order], o[order]
+    starts = np.searchsorted(ss, np.arange(VID_BASE, VID_BASE + int(s.max()) - VID_BASE + 2))
+
+    def out_edges(v):
+        i = v - VID_BASE
+        if i < 0 or i + 1 >= len(starts):
+            return pp[:0], oo[:0]
+        a, b = starts[i], starts[i + 1]
+        m = pp[a:b] != TYPE_ID
+        return pp[a:b][m], oo[a:b][m]
+
+    subj = np.unique(s[p != TYPE_ID])
+    out = []
+    while len(out) < n:
+        c = int(subj[int(rng.integers(0, len(subj)))])
+        k = int(rng.integers(1, max_pat + 1))
+        q = []
+        cur_v, col = c, 0
+        ok = True
+        for step in range(k):
+            ps_, os_ = out_edges(cur_v)
+            if len(ps_) == 0:
+                ok = step > 0
+                break
+            j = int(rng.integers(0, len(ps_)))
+            pid, nxt = int(ps_[j]), int(os_[j])
+            if step == 0:
+                q += [c, pid, OUT, -1]
+                col = 1
+            elif filters and step >= 2 and rng.random() < 0.25:
+                # a check on an existing binding: ?x p <const> or ?x p ?y
+                if rng.random() < 0.5:
+                    q += [-col, pid, OUT, nxt]
+                else:
+                    q += [-col, pid, OUT, -max(1, col - 1)]
+                continue
+            else:
+                q += [-col, pid, OUT, -(col + 1)]
+                col += 1
+            cur_v = nxt
+        if ok and q:
+            out.append(q)
+    return out
