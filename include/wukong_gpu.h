@@ -199,6 +199,13 @@ int wk_batch_create(wk_ctx *ctx, int32_t max_queries, int32_t max_steps, int64_t
 int wk_batch_destroy(wk_batch *b);
 int wk_batch_run(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
                  int32_t use_graph);
+/* Asynchronous form: launch on the batch's own stream, poll, wait (wait
+ * reports WK_EOVERFLOW / WK_EDEVICE like wk_batch_run).  Two batches overlap
+ * on the device. */
+int wk_batch_launch(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
+                    int32_t use_graph);
+int wk_batch_ready(wk_batch *b);
+int wk_batch_wait(wk_batch *b);
 /* Result of query q of the last run: rows, columns and its int32 offset in the packed result. */
 int wk_batch_result(wk_batch *b, int32_t q, int64_t *rows, int32_t *cols, int64_t *int_offset);
 /* Copy the packed results of the last run to host memory (host may be NULL to get the size). */
@@ -212,6 +219,48 @@ int wk_batch_get_tuning(wk_batch *b, int32_t *blocks_per_sm, int32_t *rows_per_w
 int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
                       int32_t reps, double *best_ms);
 int64_t wk_batch_kernel_launches(wk_batch *b);
+
+/* ------------------------------------------------------- request loop
+ * Open-loop serving: requests carry a scheduled arrival time (seconds after
+ * wk_server_start) and become visible when the server clock passes it.
+ * mode 0: one query at a time through wk_execute, in arrival order.
+ * mode 1: light requests (constant start, <= max_steps patterns) are packed
+ * into continuous batches on two alternating batch objects; heavy requests
+ * run on worker contexts sharing the store, overlapping on the device.
+ * Admission: a batch takes arrived requests while their projected history
+ * bytes fit light_budget_bytes.  plan = 1 plans each request with wk_plan at
+ * submission (statistically empty requests complete without device work).
+ * The latency of a request is its completion time minus its arrival time. */
+typedef struct {
+    int32_t mode;                 /* 0 query-at-a-time, 1 batched serving        */
+    int32_t max_batch;            /* queries per batch (<= 4096)                  */
+    int32_t max_steps;            /* patterns of a batched (light) request        */
+    int32_t heavy_workers;        /* worker contexts for heavy requests (mode 1) */
+    int64_t batch_capacity_ints;  /* int32 capacity of each batch step table      */
+    int64_t light_budget_bytes;   /* admission budget of one batch                */
+    int32_t plan;                 /* 0 run as given, 1 statistics planner          */
+    int32_t keep_results;         /* 1 keep every result table on the host         */
+} wk_server_config;
+
+typedef struct {
+    int64_t completed, light, heavy, failed, batches;
+    double  mean_batch;           /* requests per batch                           */
+    double  span_s;               /* first arrival .. last completion             */
+    double  qps;                  /* completed / span                             */
+    double  p50_ms, p99_ms, light_p50_ms, light_p99_ms, heavy_p50_ms, heavy_p99_ms;
+} wk_server_stats;
+
+typedef struct wk_server wk_server;
+void    wk_server_config_default(wk_server_config *cfg);
+int     wk_server_create(wk_ctx *ctx, const wk_server_config *cfg, wk_server **out);
+/* returns the request id (>= 0) or a negative status */
+int64_t wk_server_submit(wk_server *s, const int64_t *cmd_chains, int32_t n_patterns, double arrival_s);
+int     wk_server_start(wk_server *s);
+int     wk_server_drain(wk_server *s, double timeout_s);
+int     wk_server_result(wk_server *s, int64_t id, int64_t *rows, int32_t *cols, int32_t *host, int64_t cap,
+                         double *latency_s, int32_t *status);
+int     wk_server_get_stats(wk_server *s, wk_server_stats *out);
+int     wk_server_destroy(wk_server *s);
 
 /* Per-op timing of the last op (device time from CUDA events, ms) and its
  * algorithmic bytes (input rows/cols, output rows, adjacency entries read). */

@@ -57,6 +57,19 @@ class wk_op_stats(C.Structure):
                 ("cols_in", C.c_int32), ("kind", C.c_int32), ("alg_bytes", C.c_int64), ("kernels", C.c_int64)]
 
 
+class wk_server_config(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("max_batch", C.c_int32), ("max_steps", C.c_int32), ("heavy_workers", C.c_int32),
+                ("batch_capacity_ints", C.c_int64), ("light_budget_bytes", C.c_int64), ("plan", C.c_int32),
+                ("keep_results", C.c_int32)]
+
+
+class wk_server_stats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("light", C.c_int64), ("heavy", C.c_int64), ("failed", C.c_int64),
+                ("batches", C.c_int64), ("mean_batch", C.c_double), ("span_s", C.c_double), ("qps", C.c_double),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("light_p50_ms", C.c_double),
+                ("light_p99_ms", C.c_double), ("heavy_p50_ms", C.c_double), ("heavy_p99_ms", C.c_double)]
+
+
 class wk_pred_group(C.Structure):
     _fields_ = [("kind", C.c_int32), ("count", C.c_int32), ("zipf_s", C.c_double), ("zipf_cap", C.c_int32),
                 ("pad", C.c_int32), ("participation", C.c_double), ("hub_frac", C.c_double)]
@@ -104,12 +117,24 @@ _SIGS = {
     "wk_batch_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64, C.POINTER(_P)]),
     "wk_batch_destroy": (C.c_int, [_P]),
     "wk_batch_run": (C.c_int, [_P, _I64P, _I32P, C.c_int32, C.c_int32]),
+    "wk_batch_launch": (C.c_int, [_P, _I64P, _I32P, C.c_int32, C.c_int32]),
+    "wk_batch_ready": (C.c_int, [_P]),
+    "wk_batch_wait": (C.c_int, [_P]),
     "wk_batch_result": (C.c_int, [_P, C.c_int32, _I64P, _I32P, _I64P]),
     "wk_batch_download": (C.c_int, [_P, _I32P, C.c_int64, _I64P]),
     "wk_batch_set_tuning": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "wk_batch_get_tuning": (C.c_int, [_P, _I32P, _I32P, _I32P]),
     "wk_batch_autotune": (C.c_int, [_P, _I64P, _I32P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "wk_batch_kernel_launches": (C.c_int64, [_P]),
+    "wk_server_config_default": (None, [C.POINTER(wk_server_config)]),
+    "wk_server_create": (C.c_int, [_P, C.POINTER(wk_server_config), C.POINTER(_P)]),
+    "wk_server_submit": (C.c_int64, [_P, _I64P, C.c_int32, C.c_double]),
+    "wk_server_start": (C.c_int, [_P]),
+    "wk_server_drain": (C.c_int, [_P, C.c_double]),
+    "wk_server_result": (C.c_int, [_P, C.c_int64, _I64P, _I32P, _I32P, C.c_int64, C.POINTER(C.c_double),
+                                   _I32P]),
+    "wk_server_get_stats": (C.c_int, [_P, C.POINTER(wk_server_stats)]),
+    "wk_server_destroy": (C.c_int, [_P]),
     "wk_timer_begin": (C.c_int, [_P]),
     "wk_timer_end": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "wk_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_P)]),
@@ -470,6 +495,68 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """The request loop (open-loop arrivals, continuous batching, overlap)."""
+
+    def __init__(self, rc: "RCache", **kw):
+        lib = load_library()
+        cfg = wk_server_config()
+        lib.wk_server_config_default(C.byref(cfg))
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        h = _P()
+        _check(lib.wk_server_create(rc._h, C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.cfg = cfg
+
+    def submit(self, cmd_chains, arrival_s: float = 0.0) -> int:
+        cc = np.asarray(cmd_chains, np.int64)
+        rid = load_library().wk_server_submit(self._h, cc.ctypes.data_as(_I64P), len(cc) // 4, arrival_s)
+        if rid < 0:
+            _check(int(rid))
+        return rid
+
+    def start(self):
+        _check(load_library().wk_server_start(self._h))
+
+    def drain(self, timeout_s: float = 600.0):
+        _check(load_library().wk_server_drain(self._h, timeout_s))
+
+    def result(self, rid: int, fetch: bool = True):
+        """(table or None, latency seconds, status)."""
+        lib = load_library()
+        rows, cols, lat, st = C.c_int64(), C.c_int32(), C.c_double(), C.c_int32()
+        _check(lib.wk_server_result(self._h, rid, C.byref(rows), C.byref(cols), None, 0, C.byref(lat), C.byref(st)))
+        if not fetch:
+            return None, lat.value, st.value
+        out = np.zeros(max(rows.value * cols.value, 1), np.int32)
+        _check(lib.wk_server_result(self._h, rid, C.byref(rows), C.byref(cols), out.ctypes.data_as(_I32P), out.size,
+                                    C.byref(lat), C.byref(st)))
+        return out[:rows.value * cols.value].reshape(rows.value, max(cols.value, 1)), lat.value, st.value
+
+    def stats(self) -> dict:
+        st = wk_server_stats()
+        _check(load_library().wk_server_get_stats(self._h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().wk_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def poisson_arrivals(n: int, rate_qps: float, seed: int = 0) -> np.ndarray:
+    """Open-loop Poisson arrival times (seconds) of n requests at the given rate."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate_qps, size=n))
 
 
 class PinnedBuffer:

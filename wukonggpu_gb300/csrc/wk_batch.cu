@@ -412,6 +412,8 @@ using namespace wk::dev;
 
 struct wk_batch {
     wk_ctx *ctx = nullptr;
+    cudaStream_t stream = nullptr;          // the batch's own stream (batches overlap)
+    cudaEvent_t done = nullptr;
     int32_t max_q = 0, max_steps = 0;
     int64_t cap_ints = 0, cap_rows = 0;
     int sms = 0;
@@ -447,7 +449,10 @@ int64_t max_tiles(const wk_batch *b, int rounds) {
 
 void free_batch(wk_batch *b) {
     cudaSetDevice(b->ctx->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->stream) cudaStreamDestroy(b->stream);
     cudaFree(b->d_pvs); cudaFree(b->d_desc);
     for (int i = 0; i < 2; ++i) { cudaFree(b->d_row_off[i]); cudaFree(b->d_int_off[i]); cudaFree(b->d_cols[i]); cudaFree(b->d_hist[i]); }
     cudaFree(b->d_cnt); cudaFree(b->d_off); cudaFree(b->d_tile); cudaFree(b->d_qrows); cudaFree(b->d_flags);
@@ -532,7 +537,9 @@ extern "C" int wk_batch_create(wk_ctx *ctx, int32_t max_queries, int32_t max_ste
               cudaMalloc(&b->d_flags, 64) == cudaSuccess &&
               cudaHostAlloc((void **)&b->h_desc, sizeof(StepDesc) * (size_t)max_queries * max_steps, 0) == cudaSuccess &&
               cudaHostAlloc((void **)&b->h_layout, 8 * (size_t)(3 * max_queries + 1), 0) == cudaSuccess &&
-              cudaHostAlloc((void **)&b->h_flags, 64, 0) == cudaSuccess;
+              cudaHostAlloc((void **)&b->h_flags, 64, 0) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; ok && i < 2; ++i)
         ok = cudaMalloc(&b->d_row_off[i], 8 * (size_t)(max_queries + 1)) == cudaSuccess &&
              cudaMalloc(&b->d_int_off[i], 8 * (size_t)max_queries) == cudaSuccess &&
@@ -609,24 +616,26 @@ static int fill_desc(wk_batch *b, const int64_t *cmd, const int32_t *npat, int32
     return WK_OK;
 }
 
-extern "C" int wk_batch_run(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
-                            int32_t use_graph) {
+extern "C" int wk_batch_launch(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
+                               int32_t use_graph) {
     if (!b || !cmd_chains || !n_patterns || nq < 1 || nq > b->max_q)
-        return set_error(WK_EINVAL, "wk_batch_run: bad arguments (1..%d queries)", b ? b->max_q : 0);
+        return set_error(WK_EINVAL, "wk_batch_launch: bad arguments (1..%d queries)", b ? b->max_q : 0);
     wk_ctx *ctx = b->ctx;
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    // the pinned descriptors may still be read by a previous launch
+    if ((e = cudaEventSynchronize(b->done)) != cudaSuccess) return cuda_fail(e, "batch previous launch");
     int st = fill_desc(b, cmd_chains, n_patterns, nq);
     if (st) return st;
-    if (max_tiles(b, b->tune.rounds) > max_tiles(b, 1)) return set_error(WK_EINVAL, "wk_batch_run: tuning");
+    cudaStream_t s = b->stream;
     if (use_graph) {
         if (!b->gexec || b->graph_q != nq || std::memcmp(&b->graph_tune, &b->tune, sizeof(BatchTune)) != 0) {
             if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
             cudaGraph_t g;
-            if ((e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+            if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
                 return cuda_fail(e, "batch capture");
-            st = enqueue(b, nq, b->tune, ctx->stream);
-            e = cudaStreamEndCapture(ctx->stream, &g);
+            st = enqueue(b, nq, b->tune, s);
+            e = cudaStreamEndCapture(s, &g);
             if (st) { if (e == cudaSuccess) cudaGraphDestroy(g); return st; }
             if (e != cudaSuccess) return cuda_fail(e, "batch capture end");
             e = cudaGraphInstantiate(&b->gexec, g, 0);
@@ -636,27 +645,46 @@ extern "C" int wk_batch_run(wk_batch *b, const int64_t *cmd_chains, const int32_
             b->graph_tune = b->tune;
             b->kernels -= 1 + 3 * (int64_t)b->max_steps;   // capture does not launch
         }
-        if ((e = cudaGraphLaunch(b->gexec, ctx->stream)) != cudaSuccess) return cuda_fail(e, "batch graph launch");
+        if ((e = cudaGraphLaunch(b->gexec, s)) != cudaSuccess) return cuda_fail(e, "batch graph launch");
         b->kernels += 1 + 3 * (int64_t)b->max_steps;
     } else {
-        if ((st = enqueue(b, nq, b->tune, ctx->stream))) return st;
+        if ((st = enqueue(b, nq, b->tune, s))) return st;
     }
     ctx->launches += 1 + 3 * (int64_t)b->max_steps;
     b->last_q = nq;
     b->final_buf = b->max_steps & 1;
-    // layout of the final tables + flags
+    // layout of the final tables + flags, then the completion event
     const int fb = b->final_buf;
-    if ((e = cudaMemcpyAsync(b->h_flags, b->d_flags, 8, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(b->h_layout, b->d_row_off[fb], 8 * (size_t)(nq + 1), cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(b->h_layout + nq + 1, b->d_int_off[fb], 8 * (size_t)nq, cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
+    if ((e = cudaMemcpyAsync(b->h_flags, b->d_flags, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b->h_layout, b->d_row_off[fb], 8 * (size_t)(nq + 1), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b->h_layout + nq + 1, b->d_int_off[fb], 8 * (size_t)nq, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(reinterpret_cast<int32_t *>(b->h_layout + 2 * nq + 1), b->d_cols[fb], 4 * (size_t)nq,
-                             cudaMemcpyDeviceToHost, ctx->stream)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+                             cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaEventRecord(b->done, s)) != cudaSuccess)
         return cuda_fail(e, "batch layout readback");
-    if (b->h_flags[1]) return set_error(WK_EOVERFLOW, "wk_batch_run: a step exceeded the batch capacity of %lld ints",
-                                        (long long)b->cap_ints);
-    if (b->h_flags[0]) return set_error(WK_EDEVICE, "wk_batch_run: corrupt overflow chain in the store");
     return WK_OK;
+}
+
+// 1 when the last launch has finished, 0 while it runs
+extern "C" int wk_batch_ready(wk_batch *b) {
+    if (!b) return 1;
+    return cudaEventQuery(b->done) == cudaSuccess ? 1 : 0;
+}
+
+extern "C" int wk_batch_wait(wk_batch *b) {
+    if (!b) return set_error(WK_EINVAL, "wk_batch_wait: null");
+    cudaError_t e = cudaEventSynchronize(b->done);
+    if (e != cudaSuccess) return cuda_fail(e, "batch wait");
+    if (b->h_flags[1]) return set_error(WK_EOVERFLOW, "wk_batch: a step exceeded the batch capacity of %lld ints",
+                                        (long long)b->cap_ints);
+    if (b->h_flags[0]) return set_error(WK_EDEVICE, "wk_batch: corrupt overflow chain in the store");
+    return WK_OK;
+}
+
+extern "C" int wk_batch_run(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
+                            int32_t use_graph) {
+    int st = wk_batch_launch(b, cmd_chains, n_patterns, nq, use_graph);
+    return st ? st : wk_batch_wait(b);
 }
 
 extern "C" int wk_batch_result(wk_batch *b, int32_t q, int64_t *rows, int32_t *cols, int64_t *int_offset) {
@@ -679,9 +707,9 @@ extern "C" int wk_batch_download(wk_batch *b, int32_t *host, int64_t cap, int64_
     if (cap < tot) return set_error(WK_EOVERFLOW, "wk_batch_download: %lld ints, room for %lld", (long long)tot, (long long)cap);
     cudaError_t e;
     if (tot && (e = cudaMemcpyAsync(host, b->d_hist[b->final_buf], 4 * (size_t)tot, cudaMemcpyDeviceToHost,
-                                    b->ctx->stream)) != cudaSuccess)
+                                    b->stream)) != cudaSuccess)
         return cuda_fail(e, "wk_batch_download");
-    if ((e = cudaStreamSynchronize(b->ctx->stream)) != cudaSuccess) return cuda_fail(e, "wk_batch_download sync");
+    if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return cuda_fail(e, "wk_batch_download sync");
     return WK_OK;
 }
 
@@ -707,9 +735,9 @@ extern "C" int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const i
                 if (st) { cudaEventDestroy(e0); cudaEventDestroy(e1); b->tune = keep; return st; }
                 double tbest = 1e30;
                 for (int r = 0; r < reps; ++r) {
-                    cudaEventRecord(e0, b->ctx->stream);
-                    cudaGraphLaunch(b->gexec, b->ctx->stream);
-                    cudaEventRecord(e1, b->ctx->stream);
+                    cudaEventRecord(e0, b->stream);
+                    cudaGraphLaunch(b->gexec, b->stream);
+                    cudaEventRecord(e1, b->stream);
                     cudaEventSynchronize(e1);
                     float ms = 0.f;
                     cudaEventElapsedTime(&ms, e0, e1);
