@@ -220,6 +220,35 @@ int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_p
                       int32_t reps, double *best_ms);
 int64_t wk_batch_kernel_launches(wk_batch *b);
 
+/* ------------------------------------------- learned cardinality estimator
+ * An MLP (48 features + 32-d predicate embedding -> 3 x 256 GELU -> 1) that
+ * predicts log(1 + rows) after a plan step, trained and run by BF16
+ * tensor-core kernels (FP32 accumulation, FP32 Adam over FP32 master
+ * weights).  Parameters in one block: W1[256x80], W2[256x256], W3[256x256],
+ * W4[1x256], b1[256], b2[256], b3[256], b4[64] (first used),
+ * emb[(n_ids+1) x 32]. */
+typedef struct wk_mlp wk_mlp;
+int     wk_mlp_create(wk_ctx *ctx, int32_t n_ids, int32_t max_batch, uint64_t seed, wk_mlp **out);
+int     wk_mlp_destroy(wk_mlp *m);
+int64_t wk_mlp_num_params(wk_mlp *m);
+int     wk_mlp_get_params(wk_mlp *m, float *host, int64_t n);
+int     wk_mlp_set_params(wk_mlp *m, const float *host, int64_t n);
+/* one forward + backward without an update: loss and every gradient */
+int     wk_mlp_gradients(wk_mlp *m, const float *feats, const int32_t *pids, const float *target, int32_t n,
+                         float *grads, float *loss);
+int     wk_mlp_train(wk_mlp *m, const float *feats, const int32_t *pids, const float *target, int64_t n,
+                     int32_t epochs, int32_t batch, float lr, uint64_t seed, float *last_loss);
+int     wk_mlp_predict(wk_mlp *m, const float *feats, const int32_t *pids, int64_t n, float *out);
+/* Features (n x 48) and embedding ids of every step of an executable plan;
+ * true_rows (optional) = rows after each step, stats_est (optional) receives
+ * the chained statistics estimate of the rows after each step. */
+int     wk_featurize(wk_ctx *ctx, const int64_t *cmd_chains, int32_t n, const int64_t *true_rows, float *feats,
+                     int32_t *pids, double *stats_est);
+/* Greedy plan by the model's predicted cardinalities; same output format as
+ * wk_plan (*n_out = 0 when no executable order exists). */
+int     wk_plan_learned(wk_ctx *ctx, wk_mlp *m, const int64_t *cmd_in, int32_t n, int64_t *cmd_out,
+                        int32_t *n_out, double *est_log_rows);
+
 /* ------------------------------------------------------- request loop
  * Open-loop serving: requests carry a scheduled arrival time (seconds after
  * wk_server_start) and become visible when the server clock passes it.

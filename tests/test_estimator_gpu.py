@@ -1,0 +1,90 @@
+"""The learned estimator: GPU gradients against the numpy oracle, training,
+and the trained model against the statistics estimate on engine-recorded
+cardinalities; learned plans give the same bindings as statistics plans."""
+import numpy as np
+import pytest
+
+import oracle
+import wukonggpu_gb300 as W
+from oracle import mlp_ref
+from wukonggpu_gb300 import estimator, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _rand_batch(rng, M, n_ids):
+    feats = rng.normal(0, 1, size=(M, 48)).astype(np.float32)
+    pids = rng.integers(0, n_ids + 1, size=M).astype(np.int32)
+    tgt = rng.normal(2, 1, size=M).astype(np.float32)
+    return feats, pids, tgt
+
+
+@pytest.mark.parametrize("M", [1, 77, 300])
+def test_gradients_match_cpu_oracle(gpu_small, M):
+    n_ids = 26
+    est = W.Estimator(gpu_small, n_ids, max_batch=512, seed=5)
+    rng = np.random.default_rng(M)
+    params = est.get_params()
+    params += rng.normal(0, 0.01, size=params.shape).astype(np.float32)   # non-zero biases too
+    est.set_params(params)
+    feats, pids, tgt = _rand_batch(rng, M, n_ids)
+    g_gpu, loss_gpu = est.gradients(feats, pids, tgt)
+    loss_ref, g_ref = mlp_ref.forward_backward(params, n_ids, feats, pids, tgt)
+    # tolerance: BF16 products with FP32 accumulation against the same BF16 roundings
+    assert abs(loss_gpu - loss_ref) <= 1e-2 * max(1.0, abs(loss_ref))
+    W1 = 256 * 80
+    blocks = {"W1": (0, W1), "W2": (W1, W1 + 65536), "W3": (W1 + 65536, W1 + 131072),
+              "W4": (W1 + 131072, W1 + 131328), "biases": (W1 + 131328, W1 + 131328 + 832),
+              "emb": (W1 + 131328 + 832, len(g_ref))}
+    for name, (a, b) in blocks.items():
+        x, y = g_gpu[a:b].astype(np.float64), g_ref[a:b].astype(np.float64)
+        ny = np.linalg.norm(y)
+        if ny == 0:
+            assert np.linalg.norm(x) <= 1e-6, name
+            continue
+        cos = float(x @ y / (np.linalg.norm(x) * ny + 1e-30))
+        rel = float(np.linalg.norm(x - y) / ny)
+        assert cos > 0.999 and rel < 0.05, (name, cos, rel)
+
+
+def test_training_fits_a_function(gpu_small):
+    est = W.Estimator(gpu_small, 26, max_batch=1024, seed=3)
+    rng = np.random.default_rng(0)
+    feats, pids, _ = _rand_batch(rng, 4000, 26)
+    tgt = (feats[:, :4].sum(1) * 0.7 + 0.3 * pids + np.sin(feats[:, 5])).astype(np.float32)
+    first = est.train(feats, pids, tgt, epochs=1, batch=256, lr=1e-3)
+    last = est.train(feats, pids, tgt, epochs=30, batch=256, lr=1e-3)
+    assert last < 0.1 * first, (first, last)
+
+
+def test_learned_beats_statistics_and_plans_keep_bindings(gpu_small, small_graph, small_oracle):
+    g, s, p, o = small_graph
+    bgps = workloads.random_bgps(s, p, o, 1500, seed=31, first_class=g.first_class, n_classes=10)
+    ds = estimator.build_dataset(gpu_small, bgps)
+    tr, te = estimator.split(ds, 0.9, seed=1)
+    est = W.Estimator(gpu_small, g.num_ids, max_batch=2048, seed=7)
+    est.train(tr["feats"], tr["pids"], tr["target"], epochs=40, batch=512, lr=2e-3)
+    ev = estimator.evaluate(est, te)
+    assert ev["samples"] > 100
+    assert ev["learned_median"] <= ev["stats_median"], ev
+    assert ev["learned_p95"] <= ev["stats_p95"], ev
+    # learned plans execute to the same bindings as the statistics plans
+    from test_planner import _match
+    checked = 0
+    for q in bgps[:150]:
+        sp, _ = gpu_small.plan(q)
+        lp, _ = est.plan(q)
+        if not sp or not lp:
+            continue
+        ms, ml = _match(q, sp), _match(q, lp)
+        assert ms is not None and ml is not None, (q, sp, lp)
+        a, _ = small_oracle.execute(sp)
+        b, _ = small_oracle.execute(lp)
+        nv = max(-x for x in q if x < 0)
+        ca = [-ms[-(k + 1)] - 1 for k in range(nv)]
+        cb = [-ml[-(k + 1)] - 1 for k in range(nv)]
+        A = oracle.canonical(a[:, ca]) if a.size else np.zeros((0, nv), np.int32)
+        B = oracle.canonical(b[:, cb]) if b.size else np.zeros((0, nv), np.int32)
+        assert np.array_equal(A, B), (q, sp, lp)
+        checked += 1
+    assert checked >= 50

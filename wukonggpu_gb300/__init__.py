@@ -135,6 +135,18 @@ _SIGS = {
                                    _I32P]),
     "wk_server_get_stats": (C.c_int, [_P, C.POINTER(wk_server_stats)]),
     "wk_server_destroy": (C.c_int, [_P]),
+    "wk_mlp_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P)]),
+    "wk_mlp_destroy": (C.c_int, [_P]),
+    "wk_mlp_num_params": (C.c_int64, [_P]),
+    "wk_mlp_get_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_int64]),
+    "wk_mlp_set_params": (C.c_int, [_P, C.POINTER(C.c_float), C.c_int64]),
+    "wk_mlp_gradients": (C.c_int, [_P, C.POINTER(C.c_float), _I32P, C.POINTER(C.c_float), C.c_int32,
+                                   C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "wk_mlp_train": (C.c_int, [_P, C.POINTER(C.c_float), _I32P, C.POINTER(C.c_float), C.c_int64, C.c_int32,
+                               C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
+    "wk_mlp_predict": (C.c_int, [_P, C.POINTER(C.c_float), _I32P, C.c_int64, C.POINTER(C.c_float)]),
+    "wk_featurize": (C.c_int, [_P, _I64P, C.c_int32, _I64P, C.POINTER(C.c_float), _I32P, C.POINTER(C.c_double)]),
+    "wk_plan_learned": (C.c_int, [_P, _P, _I64P, C.c_int32, _I64P, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "wk_timer_begin": (C.c_int, [_P]),
     "wk_timer_end": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "wk_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_P)]),
@@ -495,6 +507,99 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+_F32P = C.POINTER(C.c_float)
+
+N_FEATURES = 48
+
+
+class Estimator:
+    """The learned cardinality estimator (BF16 tensor-core MLP) of a store."""
+
+    def __init__(self, rc: "RCache", n_ids: int, max_batch: int = 4096, seed: int = 1):
+        h = _P()
+        _check(load_library().wk_mlp_create(rc._h, n_ids, max_batch, seed, C.byref(h)))
+        self._h = h
+        self.rc = rc
+        self.n_ids = n_ids
+        self.max_batch = max_batch
+
+    def num_params(self) -> int:
+        return load_library().wk_mlp_num_params(self._h)
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.num_params(), np.float32)
+        _check(load_library().wk_mlp_get_params(self._h, out.ctypes.data_as(_F32P), out.size))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        _check(load_library().wk_mlp_set_params(self._h, p.ctypes.data_as(_F32P), p.size))
+
+    def gradients(self, feats, pids, target):
+        f = np.ascontiguousarray(feats, np.float32)
+        pp = np.ascontiguousarray(pids, np.int32)
+        t = np.ascontiguousarray(target, np.float32)
+        g = np.zeros(self.num_params(), np.float32)
+        loss = C.c_float()
+        _check(load_library().wk_mlp_gradients(self._h, f.ctypes.data_as(_F32P), pp.ctypes.data_as(_I32P),
+                                               t.ctypes.data_as(_F32P), len(t), g.ctypes.data_as(_F32P),
+                                               C.byref(loss)))
+        return g, loss.value
+
+    def train(self, feats, pids, target, epochs: int = 10, batch: int = 1024, lr: float = 1e-3, seed: int = 0):
+        f = np.ascontiguousarray(feats, np.float32)
+        pp = np.ascontiguousarray(pids, np.int32)
+        t = np.ascontiguousarray(target, np.float32)
+        loss = C.c_float()
+        _check(load_library().wk_mlp_train(self._h, f.ctypes.data_as(_F32P), pp.ctypes.data_as(_I32P),
+                                           t.ctypes.data_as(_F32P), len(t), epochs, batch, lr, seed, C.byref(loss)))
+        return loss.value
+
+    def predict(self, feats, pids) -> np.ndarray:
+        f = np.ascontiguousarray(feats, np.float32)
+        pp = np.ascontiguousarray(pids, np.int32)
+        out = np.zeros(len(pp), np.float32)
+        _check(load_library().wk_mlp_predict(self._h, f.ctypes.data_as(_F32P), pp.ctypes.data_as(_I32P), len(pp),
+                                             out.ctypes.data_as(_F32P)))
+        return out
+
+    def plan(self, cmd_chains):
+        cc = np.asarray(cmd_chains, np.int64)
+        n = len(cc) // 4
+        out = np.zeros(4 * (n + 2), np.int64)
+        n_out = C.c_int32(n + 2)
+        est = C.c_double()
+        _check(load_library().wk_plan_learned(self.rc._h, self._h, cc.ctypes.data_as(_I64P), n,
+                                              out.ctypes.data_as(_I64P), C.byref(n_out), C.byref(est)))
+        return [int(x) for x in out[:4 * n_out.value]], est.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().wk_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def featurize(rc: "RCache", plan, true_rows=None):
+    """(features [n x 48] float32, embedding ids [n], chained statistics estimates [n])."""
+    cc = np.asarray(plan, np.int64)
+    n = len(cc) // 4
+    f = np.zeros((n, N_FEATURES), np.float32)
+    p = np.zeros(n, np.int32)
+    est = np.zeros(n, np.float64)
+    tr = None if true_rows is None else np.ascontiguousarray(true_rows, np.int64)
+    _check(load_library().wk_featurize(rc._h, cc.ctypes.data_as(_I64P), n,
+                                       tr.ctypes.data_as(_I64P) if tr is not None else None,
+                                       f.ctypes.data_as(_F32P), p.ctypes.data_as(_I32P),
+                                       est.ctypes.data_as(C.POINTER(C.c_double))))
+    return f, p, est
 
 
 class Server:

@@ -1,0 +1,569 @@
+// The learned cardinality estimator: an MLP trained and evaluated by
+// hand-written BF16 tensor-core kernels.
+//
+// Model: x = [48 pattern features | 32-d embedding of the predicate] (80)
+//        -> 256 -> 256 -> 256 (GELU after each) -> 1
+// It predicts log(1 + rows) of the table after a pattern is applied.  Weights
+// and activations are BF16, every product accumulates in FP32 on the tensor
+// cores (mma.sync m16n8k16 bf16), and the optimiser is FP32 Adam over FP32
+// master weights whose BF16 copies are refreshed after each step.
+//
+// One GEMM kernel does all products: C[M x N] = A[M x K] . B[N x K]^T with A
+// and B row-major (K contiguous), which is the natural form for the forward
+// product (X . W^T), for the input gradient (dZ . W, with W^T kept as a BF16
+// copy) and for the weight gradient (dZ^T . X, with the transposed
+// activations written by the forward pass).  Dimensions are padded: M and N
+// to multiples of 64, K to multiples of 16; padding is zero.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "wk_runtime.h"
+
+namespace wk {
+namespace mlp {
+
+constexpr int kIn = 48;       // pattern features
+constexpr int kEmb = 32;      // predicate embedding
+constexpr int kX = kIn + kEmb;   // 80
+constexpr int kH = 256;
+constexpr int kOutPad = 64;   // output layer padded to one GEMM tile
+constexpr int kXPadN = 128;   // W1^T rows padded (dX GEMM has N = 80 -> 128)
+
+// ------------------------------------------------------------------ GEMM
+constexpr int BM = 64, BN = 64, BK = 16, SK = 24;   // smem row stride (bf16) avoids bank conflicts
+
+__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
+
+// C = A . B^T (+ bias[n]); A [M x K] lda, B [N x K] ldb, C fp32 [M x N] ldc.
+// M, N multiples of 64; K multiple of 16.  128 threads, 64 x 64 tile, each
+// warp a 32 x 32 sub-tile of 2 x 4 m16n8k16 products.
+__global__ void __launch_bounds__(128)
+gemm_tn_kernel(const __nv_bfloat16 *__restrict__ A, int lda, const __nv_bfloat16 *__restrict__ B, int ldb,
+               float *__restrict__ C, int ldc, int K, const float *__restrict__ bias) {
+    __shared__ __align__(16) __nv_bfloat16 As[BM * SK];
+    __shared__ __align__(16) __nv_bfloat16 Bs[BN * SK];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+    const int lr = tid >> 1, lc = (tid & 1) * 8;   // one 16 B load per thread per operand
+    for (int k0 = 0; k0 < K; k0 += BK) {
+        *reinterpret_cast<uint4 *>(&As[lr * SK + lc]) =
+            *reinterpret_cast<const uint4 *>(A + (size_t)(m0 + lr) * lda + k0 + lc);
+        *reinterpret_cast<uint4 *>(&Bs[lr * SK + lc]) =
+            *reinterpret_cast<const uint4 *>(B + (size_t)(n0 + lr) * ldb + k0 + lc);
+        __syncthreads();
+        uint32_t a[2][4], b[4][2];
+#pragma unroll
+        for (int mi = 0; mi < 2; ++mi) {
+            const int r = wm + mi * 16 + g;
+            a[mi][0] = ld32(&As[r * SK + 2 * t]);
+            a[mi][1] = ld32(&As[(r + 8) * SK + 2 * t]);
+            a[mi][2] = ld32(&As[r * SK + 2 * t + 8]);
+            a[mi][3] = ld32(&As[(r + 8) * SK + 2 * t + 8]);
+        }
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni) {
+            const int c = wn + ni * 8 + g;
+            b[ni][0] = ld32(&Bs[c * SK + 2 * t]);
+            b[ni][1] = ld32(&Bs[c * SK + 2 * t + 8]);
+        }
+#pragma unroll
+        for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+            for (int ni = 0; ni < 4; ++ni)
+                asm volatile(
+                    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                    "{%8,%9}, {%0,%1,%2,%3};"
+                    : "+f"(acc[mi][ni][0]), "+f"(acc[mi][ni][1]), "+f"(acc[mi][ni][2]), "+f"(acc[mi][ni][3])
+                    : "r"(a[mi][0]), "r"(a[mi][1]), "r"(a[mi][2]), "r"(a[mi][3]), "r"(b[ni][0]), "r"(b[ni][1]));
+        __syncthreads();
+    }
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni) {
+            const int r = m0 + wm + mi * 16 + g, c = n0 + wn + ni * 8 + 2 * t;
+            const float b0 = bias ? bias[c] : 0.f, b1 = bias ? bias[c + 1] : 0.f;
+            C[(size_t)r * ldc + c] = acc[mi][ni][0] + b0;
+            C[(size_t)r * ldc + c + 1] = acc[mi][ni][1] + b1;
+            C[(size_t)(r + 8) * ldc + c] = acc[mi][ni][2] + b0;
+            C[(size_t)(r + 8) * ldc + c + 1] = acc[mi][ni][3] + b1;
+        }
+}
+
+// ------------------------------------------------------------ elementwise
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+// X0 [Mp x 80] bf16 = [feats | emb[pid]] for real rows, 0 for padding
+__global__ void build_input_kernel(const float *__restrict__ feats, const int32_t *__restrict__ pids, int M, int Mp,
+                                   const float *__restrict__ emb, int n_ids, __nv_bfloat16 *__restrict__ X0,
+                                   __nv_bfloat16 *__restrict__ X0t) {
+    const int64_t n = (int64_t)Mp * kX;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / kX), c = (int)(i % kX);
+        float v = 0.f;
+        if (r < M) {
+            if (c < kIn) v = feats[(size_t)r * kIn + c];
+            else {
+                int p = pids[r];
+                p = p < 0 ? 0 : (p > n_ids ? n_ids : p);
+                v = emb[(size_t)p * kEmb + (c - kIn)];
+            }
+        }
+        const __nv_bfloat16 bv = __float2bfloat16(v);
+        X0[i] = bv;
+        X0t[(size_t)c * Mp + r] = bv;
+    }
+}
+
+// H = GELU(Z) as bf16, row-major and transposed; rows >= M are zero
+__global__ void gelu_fwd_kernel(const float *__restrict__ Z, int M, int Mp, int N, __nv_bfloat16 *__restrict__ H,
+                                __nv_bfloat16 *__restrict__ Ht) {
+    const int64_t n = (int64_t)Mp * N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / N), c = (int)(i % N);
+        const __nv_bfloat16 h = __float2bfloat16(r < M ? gelu(Z[i]) : 0.f);
+        H[i] = h;
+        Ht[(size_t)c * Mp + r] = h;
+    }
+}
+
+// dZ = dH * GELU'(Z) as bf16 (row-major and transposed), and db = column sums
+__global__ void gelu_bwd_kernel(const float *__restrict__ dH, const float *__restrict__ Z, int M, int Mp, int N,
+                                __nv_bfloat16 *__restrict__ dZ, __nv_bfloat16 *__restrict__ dZt) {
+    const int64_t n = (int64_t)Mp * N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / N), c = (int)(i % N);
+        const float v = r < M ? dH[i] * gelu_grad(Z[i]) : 0.f;
+        const __nv_bfloat16 b = __float2bfloat16(v);
+        dZ[i] = b;
+        dZt[(size_t)c * Mp + r] = b;
+    }
+}
+
+// column sums of a bf16 [Mp x N] matrix into fp32 db[N] (one block per column)
+__global__ void colsum_kernel(const __nv_bfloat16 *__restrict__ Dt, int Mp, float *__restrict__ db) {
+    const int c = blockIdx.x;
+    float s = 0.f;
+    for (int r = threadIdx.x; r < Mp; r += blockDim.x) s += __bfloat162float(Dt[(size_t)c * Mp + r]);
+    __shared__ float sh[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) db[c] = s;
+    }
+}
+
+// loss = mean((y - t)^2) over real rows; dY (bf16, col 0, row-major and
+// transposed) = 2 (y - t) / M.  One block.
+__global__ void loss_kernel(const float *__restrict__ Y, const float *__restrict__ tgt, int M, int Mp,
+                            __nv_bfloat16 *__restrict__ dY, __nv_bfloat16 *__restrict__ dYt, float *__restrict__ loss) {
+    float s = 0.f;
+    for (int r = threadIdx.x; r < Mp; r += blockDim.x) {
+        float g = 0.f;
+        if (r < M) {
+            const float d = Y[(size_t)r * kOutPad] - tgt[r];
+            s += d * d;
+            g = 2.f * d / (float)M;
+        }
+        const __nv_bfloat16 b = __float2bfloat16(g);
+        dY[(size_t)r * kOutPad] = b;
+        dYt[r] = b;   // row 0 of dY^T
+    }
+    __shared__ float sh[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) *loss = s / (float)(M > 0 ? M : 1);
+    }
+}
+
+// embedding gradient: demb[pid] += dX[r, 48..79]
+__global__ void emb_grad_kernel(const float *__restrict__ dX, int ldx, const int32_t *__restrict__ pids, int M,
+                                int n_ids, float *__restrict__ demb) {
+    const int64_t n = (int64_t)M * kEmb;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / kEmb), c = (int)(i % kEmb);
+        int p = pids[r];
+        p = p < 0 ? 0 : (p > n_ids ? n_ids : p);
+        atomicAdd(&demb[(size_t)p * kEmb + c], dX[(size_t)r * ldx + kIn + c]);
+    }
+}
+
+// Adam over fp32 master weights; g, m, v, w all of length n
+__global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
+                            float *__restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float c1,
+                            float c2) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+// bf16 copies of a weight matrix W [rows x cols] (fp32): row-major into Wb
+// (ld = ldb, zero padded) and transposed into Wt (ld = ldt)
+__global__ void weight_copy_kernel(const float *__restrict__ W, int rows, int cols, __nv_bfloat16 *__restrict__ Wb,
+                                   int ldb, int rows_pad, __nv_bfloat16 *__restrict__ Wt, int ldt, int cols_pad) {
+    const int64_t n = (int64_t)rows_pad * ldb;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / ldb), c = (int)(i % ldb);
+        const float v = (r < rows && c < cols) ? W[(size_t)r * cols + c] : 0.f;
+        Wb[i] = __float2bfloat16(v);
+        if (c < cols_pad && r < ldt) Wt[(size_t)c * ldt + r] = __float2bfloat16(v);
+    }
+}
+
+}  // namespace mlp
+}  // namespace wk
+
+using namespace wk;
+using namespace wk::mlp;
+
+struct wk_mlp {
+    wk_ctx *ctx = nullptr;
+    int n_ids = 0;
+    int cap_m = 0;               // padded batch capacity
+    // fp32 master parameters, gradients, Adam moments (one contiguous block)
+    float *params = nullptr, *grads = nullptr, *m1 = nullptr, *m2 = nullptr;
+    int64_t n_params = 0;
+    // views into params/grads
+    int64_t off_w[4] = {}, off_b[4] = {}, off_emb = 0;
+    // bf16 weights (row-major, padded) and transposes
+    __nv_bfloat16 *wb[4] = {}, *wt[4] = {};
+    // activations (capacity cap_m)
+    __nv_bfloat16 *x0 = nullptr, *x0t = nullptr, *h[3] = {}, *ht[3] = {}, *dz = nullptr, *dzt = nullptr, *dy = nullptr,
+                  *dyt = nullptr;
+    float *z[4] = {}, *dh = nullptr, *dx = nullptr, *feats = nullptr, *tgt = nullptr, *loss = nullptr;
+    int32_t *pids = nullptr;
+    int64_t step = 0;
+    int64_t kernels = 0;
+};
+
+namespace {
+
+const int kRows[4] = {kH, kH, kH, 1};        // output dim of each layer
+const int kCols[4] = {kX, kH, kH, kH};       // input dim of each layer
+const int kRowsPad[4] = {kH, kH, kH, kOutPad};
+
+inline int pad64(int x) { return (x + 63) / 64 * 64; }
+unsigned int nblk(int64_t n) { int64_t b = (n + 255) / 256; return (unsigned int)(b > 2048 ? 2048 : (b < 1 ? 1 : b)); }
+
+void refresh_bf16(wk_mlp *m, cudaStream_t s) {
+    for (int l = 0; l < 4; ++l) {
+        // W^T of layer l is [cols x rows_pad]: the dX product takes it as B
+        // with N = cols (layer 0 pads 80 -> 128; the extra rows stay zero)
+        const int tcols = (l == 0) ? kXPadN : kH;
+        weight_copy_kernel<<<nblk((int64_t)kRowsPad[l] * kCols[l]), 256, 0, s>>>(
+            m->params + m->off_w[l], kRows[l], kCols[l], m->wb[l], kCols[l], kRowsPad[l], m->wt[l], kRowsPad[l], tcols);
+    }
+    m->kernels += 4;
+}
+
+void gemm(wk_mlp *m, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N,
+          int K, const float *bias, cudaStream_t s) {
+    dim3 grid((unsigned)(N / BN), (unsigned)(M / BM));
+    gemm_tn_kernel<<<grid, 128, 0, s>>>(A, lda, B, ldb, C, ldc, K, bias);
+    m->kernels++;
+}
+
+// forward over M rows already uploaded (feats, pids); Y in z[3] col 0
+void forward(wk_mlp *m, int M, cudaStream_t s) {
+    const int Mp = pad64(M);
+    build_input_kernel<<<nblk((int64_t)Mp * kX), 256, 0, s>>>(m->feats, m->pids, M, Mp, m->params + m->off_emb,
+                                                              m->n_ids, m->x0, m->x0t);
+    const __nv_bfloat16 *in = m->x0;
+    int kin = kX;
+    for (int l = 0; l < 3; ++l) {
+        gemm(m, in, kin, m->wb[l], kin, m->z[l], kH, Mp, kH, kin, m->params + m->off_b[l], s);
+        gelu_fwd_kernel<<<nblk((int64_t)Mp * kH), 256, 0, s>>>(m->z[l], M, Mp, kH, m->h[l], m->ht[l]);
+        in = m->h[l];
+        kin = kH;
+    }
+    gemm(m, in, kH, m->wb[3], kH, m->z[3], kOutPad, Mp, kOutPad, kH, nullptr, s);
+    // output bias (layer 4 has one real output): added in the loss / predict read
+    m->kernels += 4;
+}
+
+// loss + backward + Adam on M rows (targets uploaded)
+void backward_step(wk_mlp *m, int M, float lr, bool update, cudaStream_t s) {
+    const int Mp = pad64(M);
+    float *g = m->grads;
+    cudaMemsetAsync(g, 0, sizeof(float) * (size_t)m->n_params, s);
+    // dY: y includes the output bias
+    loss_kernel<<<1, 1024, 0, s>>>(m->z[3], m->tgt, M, Mp, m->dy, m->dyt, m->loss);
+    // layer 4: dW4 = dY^T . H3 (B = H3^T [256 x Mp]); db4 = sum dY; dH3 = dY . W4 (B = W4^T [256 x 64])
+    {
+        float *dw4 = g + m->off_w[3];   // [1 x 256] real, GEMM writes [64 x 256]
+        gemm(m, m->dyt, Mp, m->ht[2], Mp, m->dx /*scratch [64 x 256]*/, kH, kOutPad, kH, Mp, nullptr, s);
+        cudaMemcpyAsync(dw4, m->dx, sizeof(float) * kH, cudaMemcpyDeviceToDevice, s);   // row 0
+        colsum_kernel<<<1, 256, 0, s>>>(m->dyt, Mp, g + m->off_b[3]);
+        gemm(m, m->dy, kOutPad, m->wt[3], kOutPad, m->dh, kH, Mp, kH, kOutPad, nullptr, s);
+    }
+    for (int l = 2; l >= 0; --l) {
+        gelu_bwd_kernel<<<nblk((int64_t)Mp * kH), 256, 0, s>>>(m->dh, m->z[l], M, Mp, kH, m->dz, m->dzt);
+        const __nv_bfloat16 *inT = (l == 0) ? m->x0t : m->ht[l - 1];
+        const int kin = (l == 0) ? kX : kH;
+        // dW_l [256 x kin] = dZ^T [256 x Mp] . (X^T [kin x Mp])^T ; N = kin must be a multiple of 64
+        if (kin % 64 == 0) {
+            gemm(m, m->dzt, Mp, inT, Mp, g + m->off_w[l], kin, kH, kin, Mp, nullptr, s);
+        } else {
+            // layer 0: kin = 80 -> compute into scratch [256 x 128] then copy the first 80 columns
+            gemm(m, m->dzt, Mp, inT, Mp, m->dx, kXPadN, kH, kXPadN, Mp, nullptr, s);
+            cudaMemcpy2DAsync(g + m->off_w[0], sizeof(float) * kX, m->dx, sizeof(float) * kXPadN, sizeof(float) * kX,
+                              kH, cudaMemcpyDeviceToDevice, s);
+        }
+        colsum_kernel<<<kH, 256, 0, s>>>(m->dzt, Mp, g + m->off_b[l]);
+        // dH_{l-1} = dZ . W_l  (B = W_l^T [kin(pad) x 256])
+        if (l > 0) gemm(m, m->dz, kH, m->wt[l], kH, m->dh, kH, Mp, kH, kH, nullptr, s);
+        else gemm(m, m->dz, kH, m->wt[0], kH, m->dx, kXPadN, Mp, kXPadN, kH, nullptr, s);
+        m->kernels += 2;
+    }
+    emb_grad_kernel<<<nblk((int64_t)M * kEmb), 256, 0, s>>>(m->dx, kXPadN, m->pids, M, m->n_ids, g + m->off_emb);
+    m->kernels += 3;
+    if (update) {
+        ++m->step;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.f - std::pow(b1, (float)m->step), c2 = 1.f - std::pow(b2, (float)m->step);
+        adam_kernel<<<nblk(m->n_params), 256, 0, s>>>(m->params, g, m->m1, m->m2, m->n_params, lr, b1, b2, 1e-8f, c1, c2);
+        refresh_bf16(m, s);
+        m->kernels++;
+    }
+}
+
+__global__ void add_bias_read_kernel(const float *Y, const float *b4, int M, float *out) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < M; r += gridDim.x * blockDim.x) out[r] = Y[(size_t)r * kOutPad] + b4[0];
+}
+
+// add the output bias to column 0 of Y in place (so loss and predict see y = H3 . w4 + b4)
+__global__ void add_out_bias_kernel(float *Y, const float *b4, int M) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < M; r += gridDim.x * blockDim.x) Y[(size_t)r * kOutPad] += b4[0];
+}
+
+int upload(wk_mlp *m, const float *feats, const int32_t *pids, const float *tgt, int M, cudaStream_t s) {
+    cudaError_t e = cudaMemcpyAsync(m->feats, feats, sizeof(float) * (size_t)M * kIn, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m->pids, pids, sizeof(int32_t) * (size_t)M, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && tgt) e = cudaMemcpyAsync(m->tgt, tgt, sizeof(float) * (size_t)M, cudaMemcpyHostToDevice, s);
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "mlp upload");
+}
+
+void free_mlp(wk_mlp *m) {
+    if (m->ctx && m->ctx->device >= 0) cudaSetDevice(m->ctx->device);
+    cudaFree(m->params);
+    cudaFree(m->grads);
+    cudaFree(m->m1);
+    cudaFree(m->m2);
+    for (int l = 0; l < 4; ++l) { cudaFree(m->wb[l]); cudaFree(m->wt[l]); cudaFree(m->z[l]); }
+    for (int l = 0; l < 3; ++l) { cudaFree(m->h[l]); cudaFree(m->ht[l]); }
+    cudaFree(m->x0); cudaFree(m->x0t); cudaFree(m->dz); cudaFree(m->dzt); cudaFree(m->dy); cudaFree(m->dyt);
+    cudaFree(m->dh); cudaFree(m->dx); cudaFree(m->feats); cudaFree(m->tgt); cudaFree(m->loss); cudaFree(m->pids);
+    delete m;
+}
+
+}  // namespace
+
+extern "C" int wk_mlp_create(wk_ctx *ctx, int32_t n_ids, int32_t max_batch, uint64_t seed, wk_mlp **out) {
+    if (!ctx || !out || n_ids < 1 || max_batch < 1 || max_batch > (1 << 20))
+        return set_error(WK_EINVAL, "wk_mlp_create: bad arguments");
+    if (ctx->device < 0) return set_error(WK_EDEVICE, "wk_mlp_create: host-only context");
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    wk_mlp *m = new wk_mlp();
+    m->ctx = ctx;
+    m->n_ids = n_ids;
+    m->cap_m = pad64(max_batch);
+    int64_t at = 0;
+    for (int l = 0; l < 4; ++l) { m->off_w[l] = at; at += (int64_t)kRows[l] * kCols[l]; }
+    for (int l = 0; l < 4; ++l) { m->off_b[l] = at; at += kRowsPad[l]; }
+    m->off_emb = at;
+    at += (int64_t)(n_ids + 1) * kEmb;
+    m->n_params = at;
+    const size_t P = sizeof(float) * (size_t)at, Mp = (size_t)m->cap_m;
+    bool ok = cudaMalloc(&m->params, P) == cudaSuccess && cudaMalloc(&m->grads, P) == cudaSuccess &&
+              cudaMalloc(&m->m1, P) == cudaSuccess && cudaMalloc(&m->m2, P) == cudaSuccess;
+    for (int l = 0; ok && l < 4; ++l) {
+        const int tcols = (l == 0) ? kXPadN : kH;
+        ok = cudaMalloc(&m->wb[l], 2 * (size_t)kRowsPad[l] * kCols[l]) == cudaSuccess &&
+             cudaMalloc(&m->wt[l], 2 * (size_t)tcols * kRowsPad[l]) == cudaSuccess &&
+             cudaMalloc(&m->z[l], 4 * Mp * (size_t)(l < 3 ? kH : kOutPad)) == cudaSuccess;
+    }
+    for (int l = 0; ok && l < 3; ++l)
+        ok = cudaMalloc(&m->h[l], 2 * Mp * kH) == cudaSuccess && cudaMalloc(&m->ht[l], 2 * Mp * kH) == cudaSuccess;
+    // X0^T has kXPadN rows: the layer-0 weight-gradient product pads N = 80 to 128 and reads rows 80..127 (zero)
+    ok = ok && cudaMalloc(&m->x0, 2 * Mp * kX) == cudaSuccess && cudaMalloc(&m->x0t, 2 * Mp * kXPadN) == cudaSuccess &&
+         cudaMalloc(&m->dz, 2 * Mp * kH) == cudaSuccess && cudaMalloc(&m->dzt, 2 * Mp * kH) == cudaSuccess &&
+         cudaMalloc(&m->dy, 2 * Mp * kOutPad) == cudaSuccess && cudaMalloc(&m->dyt, 2 * Mp * kOutPad) == cudaSuccess &&
+         cudaMalloc(&m->dh, 4 * Mp * kH) == cudaSuccess &&
+         cudaMalloc(&m->dx, 4 * std::max(Mp * (size_t)kXPadN, (size_t)kH * kXPadN)) == cudaSuccess &&
+         cudaMalloc(&m->feats, 4 * Mp * kIn) == cudaSuccess && cudaMalloc(&m->tgt, 4 * Mp) == cudaSuccess &&
+         cudaMalloc(&m->loss, 16) == cudaSuccess && cudaMalloc(&m->pids, 4 * Mp) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        free_mlp(m);
+        return set_error(WK_ENOMEM, "wk_mlp_create: allocation failed");
+    }
+    // He-style initialisation (uniform with the fan-in bound), zero biases, small embeddings
+    std::vector<float> h((size_t)at, 0.f);
+    std::mt19937_64 rng(seed);
+    for (int l = 0; l < 4; ++l) {
+        const float bound = std::sqrt(6.f / (float)kCols[l]) * (l == 3 ? 0.5f : 1.f);
+        std::uniform_real_distribution<float> U(-bound, bound);
+        for (int64_t i = 0; i < (int64_t)kRows[l] * kCols[l]; ++i) h[(size_t)(m->off_w[l] + i)] = U(rng);
+    }
+    std::normal_distribution<float> Nrm(0.f, 0.1f);
+    for (int64_t i = 0; i < (int64_t)(n_ids + 1) * kEmb; ++i) h[(size_t)(m->off_emb + i)] = Nrm(rng);
+    cudaStream_t s = ctx->stream;
+    e = cudaMemcpyAsync(m->params, h.data(), P, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->m1, 0, P, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->m2, 0, P, s);
+    for (int l = 0; e == cudaSuccess && l < 4; ++l) {
+        const int tcols = (l == 0) ? kXPadN : kH;
+        e = cudaMemsetAsync(m->wt[l], 0, 2 * (size_t)tcols * kRowsPad[l], s);
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->x0t, 0, 2 * Mp * kXPadN, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->dy, 0, 2 * Mp * kOutPad, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->dyt, 0, 2 * Mp * kOutPad, s);
+    if (e != cudaSuccess) { int r = cuda_fail(e, "wk_mlp_create init"); free_mlp(m); return r; }
+    refresh_bf16(m, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) { int r = cuda_fail(e, "wk_mlp_create sync"); free_mlp(m); return r; }
+    *out = m;
+    return WK_OK;
+}
+
+extern "C" int wk_mlp_destroy(wk_mlp *m) {
+    if (m) free_mlp(m);
+    return WK_OK;
+}
+
+extern "C" int64_t wk_mlp_num_params(wk_mlp *m) { return m ? m->n_params : 0; }
+
+// parameter block layout: W1 [256x80], W2, W3 [256x256], W4 [1x256], b1, b2, b3 [256], b4 [64, first used], emb [(n_ids+1) x 32]
+extern "C" int wk_mlp_get_params(wk_mlp *m, float *host, int64_t n) {
+    if (!m || !host || n < m->n_params) return set_error(WK_EINVAL, "wk_mlp_get_params");
+    cudaError_t e = cudaMemcpy(host, m->params, sizeof(float) * (size_t)m->n_params, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "wk_mlp_get_params");
+}
+
+extern "C" int wk_mlp_set_params(wk_mlp *m, const float *host, int64_t n) {
+    if (!m || !host || n < m->n_params) return set_error(WK_EINVAL, "wk_mlp_set_params");
+    cudaSetDevice(m->ctx->device);
+    cudaError_t e = cudaMemcpy(m->params, host, sizeof(float) * (size_t)m->n_params, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "wk_mlp_set_params");
+    refresh_bf16(m, m->ctx->stream);
+    e = cudaStreamSynchronize(m->ctx->stream);
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "wk_mlp_set_params sync");
+}
+
+// One forward + backward on rows 0..M-1 without an update: loss and the
+// gradients of every parameter (same layout as the parameters).
+extern "C" int wk_mlp_gradients(wk_mlp *m, const float *feats, const int32_t *pids, const float *tgt, int32_t M,
+                                float *grads_host, float *loss_host) {
+    if (!m || !feats || !pids || !tgt || M < 1 || M > m->cap_m) return set_error(WK_EINVAL, "wk_mlp_gradients");
+    cudaSetDevice(m->ctx->device);
+    cudaStream_t s = m->ctx->stream;
+    int st = upload(m, feats, pids, tgt, M, s);
+    if (st) return st;
+    forward(m, M, s);
+    add_out_bias_kernel<<<nblk(M), 256, 0, s>>>(m->z[3], m->params + m->off_b[3], M);
+    backward_step(m, M, 0.f, false, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && grads_host)
+        e = cudaMemcpyAsync(grads_host, m->grads, sizeof(float) * (size_t)m->n_params, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && loss_host) e = cudaMemcpyAsync(loss_host, m->loss, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "wk_mlp_gradients");
+}
+
+// Mini-batch training: `epochs` passes over n samples in batches of `batch`
+// (sample order shuffled with `seed`), Adam with learning rate lr.  Returns
+// the mean loss of the last epoch.
+extern "C" int wk_mlp_train(wk_mlp *m, const float *feats, const int32_t *pids, const float *tgt, int64_t n,
+                            int32_t epochs, int32_t batch, float lr, uint64_t seed, float *last_loss) {
+    if (!m || !feats || !pids || !tgt || n < 1 || epochs < 1 || batch < 1 || batch > m->cap_m)
+        return set_error(WK_EINVAL, "wk_mlp_train: bad arguments");
+    cudaSetDevice(m->ctx->device);
+    cudaStream_t s = m->ctx->stream;
+    std::vector<int64_t> order((size_t)n);
+    for (int64_t i = 0; i < n; ++i) order[(size_t)i] = i;
+    std::mt19937_64 rng(seed);
+    std::vector<float> bf((size_t)batch * kIn), bt((size_t)batch);
+    std::vector<int32_t> bp((size_t)batch);
+    float *h_loss = nullptr;
+    if (cudaHostAlloc((void **)&h_loss, 4, 0) != cudaSuccess) return set_error(WK_ENOMEM, "wk_mlp_train: pinned");
+    double ep_loss = 0.0;
+    for (int ep = 0; ep < epochs; ++ep) {
+        std::shuffle(order.begin(), order.end(), rng);
+        double tot = 0.0;
+        int64_t nb = 0;
+        for (int64_t b0 = 0; b0 < n; b0 += batch) {
+            const int M = (int)std::min<int64_t>(batch, n - b0);
+            for (int i = 0; i < M; ++i) {
+                const int64_t j = order[(size_t)(b0 + i)];
+                std::memcpy(&bf[(size_t)i * kIn], feats + j * kIn, sizeof(float) * kIn);
+                bp[(size_t)i] = pids[j];
+                bt[(size_t)i] = tgt[j];
+            }
+            int st = upload(m, bf.data(), bp.data(), bt.data(), M, s);
+            if (st) { cudaFreeHost(h_loss); return st; }
+            forward(m, M, s);
+            add_out_bias_kernel<<<nblk(M), 256, 0, s>>>(m->z[3], m->params + m->off_b[3], M);
+            backward_step(m, M, lr, true, s);
+            cudaMemcpyAsync(h_loss, m->loss, 4, cudaMemcpyDeviceToHost, s);
+            cudaError_t e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) { cudaFreeHost(h_loss); return cuda_fail(e, "wk_mlp_train"); }
+            tot += *h_loss;
+            ++nb;
+        }
+        ep_loss = tot / (double)(nb ? nb : 1);
+    }
+    cudaFreeHost(h_loss);
+    m->ctx->launches += m->kernels;
+    m->kernels = 0;
+    if (last_loss) *last_loss = (float)ep_loss;
+    return WK_OK;
+}
+
+// Predictions (log(1 + rows)) for n samples, in chunks of the batch capacity.
+extern "C" int wk_mlp_predict(wk_mlp *m, const float *feats, const int32_t *pids, int64_t n, float *out) {
+    if (!m || (n > 0 && (!feats || !pids || !out)) || n < 0) return set_error(WK_EINVAL, "wk_mlp_predict");
+    cudaSetDevice(m->ctx->device);
+    cudaStream_t s = m->ctx->stream;
+    for (int64_t b0 = 0; b0 < n; b0 += m->cap_m) {
+        const int M = (int)std::min<int64_t>(m->cap_m, n - b0);
+        int st = upload(m, feats + b0 * kIn, pids + b0, nullptr, M, s);
+        if (st) return st;
+        forward(m, M, s);
+        add_bias_read_kernel<<<nblk(M), 256, 0, s>>>(m->z[3], m->params + m->off_b[3], M, m->tgt);
+        cudaError_t e = cudaMemcpyAsync(out + b0, m->tgt, sizeof(float) * (size_t)M, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_fail(e, "wk_mlp_predict");
+    }
+    m->ctx->launches += m->kernels;
+    m->kernels = 0;
+    return WK_OK;
+}

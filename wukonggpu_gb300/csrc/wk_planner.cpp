@@ -21,6 +21,7 @@
 // renumbered in plan order.  Ties and floating-point order follow the
 // reference so that the same statistics give the same plan.
 #include "wk_runtime.h"
+#include "wk_stats.h"
 
 #include <algorithm>
 #include <cstring>
@@ -31,21 +32,6 @@
 #include <vector>
 
 namespace wk {
-
-struct FourNum {
-    int64_t out_out = 0, out_in = 0, in_in = 0, in_out = 0;
-};
-
-struct Stats {
-    int32_t num_ids = 0;
-    std::unordered_map<int, int64_t> pt, ps, po, tys;   // global_* after the gather
-    std::vector<FourNum> pp;                             // (num_ids+1)^2, index p1*(n+1)+p2
-    FourNum &pair(int a, int b) { return pp[(size_t)a * (size_t)(num_ids + 1) + (size_t)b]; }
-    const FourNum *pair_c(int a, int b) const {
-        if (a < 0 || b < 0 || a > num_ids || b > num_ids) return nullptr;
-        return &pp[(size_t)a * (size_t)(num_ids + 1) + (size_t)b];
-    }
-};
 
 namespace {
 
@@ -439,6 +425,11 @@ void free_stats(Stats *s) { delete s; }
 }  // namespace wk
 
 using namespace wk;
+
+Stats &wk::stats_of(wk_ctx *ctx) {
+    if (!ctx->store->stats) ctx->store->stats.reset(build_stats(*ctx->store->hs), free_stats);
+    return *ctx->store->stats;
+}
 
 extern "C" int wk_plan(wk_ctx *ctx, const int64_t *cmd_in, int32_t n, int64_t *cmd_out, int32_t *n_out,
                        double *est_cost, int32_t *proved_empty) {
