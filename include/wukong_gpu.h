@@ -249,6 +249,15 @@ int     wk_featurize(wk_ctx *ctx, const int64_t *cmd_chains, int32_t n, const in
 int     wk_plan_learned(wk_ctx *ctx, wk_mlp *m, const int64_t *cmd_in, int32_t n, int64_t *cmd_out,
                         int32_t *n_out, double *est_log_rows);
 
+/* Learned plans of nq BGPs at once (lockstep greedy, one model call per
+ * step for all queries).  cmd_in packs the queries (n_in[q] patterns each);
+ * cmd_out must hold sum(n_in[q] + 1) patterns; n_out[q] = plan length. */
+int     wk_plan_learned_batch(wk_ctx *ctx, wk_mlp *m, const int64_t *cmd_in, const int32_t *n_in, int32_t nq,
+                              int64_t *cmd_out, int32_t *n_out);
+/* Cap on the rows of any k2u output of this context (0 = none); a larger
+ * step returns WK_EOVERFLOW before writing. */
+int     wk_set_row_limit(wk_ctx *ctx, int64_t max_rows);
+
 /* ------------------------------------------------------- request loop
  * Open-loop serving: requests carry a scheduled arrival time (seconds after
  * wk_server_start) and become visible when the server clock passes it.

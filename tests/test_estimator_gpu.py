@@ -69,7 +69,7 @@ def test_learned_beats_statistics_and_plans_keep_bindings(gpu_small, small_graph
     assert ev["learned_median"] <= ev["stats_median"], ev
     assert ev["learned_p95"] <= ev["stats_p95"], ev
     # learned plans execute to the same bindings as the statistics plans
-    from test_planner import _match
+    from wukonggpu_gb300.plans import match_plan as _match
     checked = 0
     for q in bgps[:150]:
         sp, _ = gpu_small.plan(q)
@@ -88,3 +88,26 @@ def test_learned_beats_statistics_and_plans_keep_bindings(gpu_small, small_graph
         assert np.array_equal(A, B), (q, sp, lp)
         checked += 1
     assert checked >= 50
+
+
+def test_batched_learned_planning_equals_single(gpu_small, small_graph):
+    g, s, p, o = small_graph
+    bgps = workloads.random_bgps(s, p, o, 200, seed=41, first_class=g.first_class, n_classes=10)
+    est = W.Estimator(gpu_small, g.num_ids, max_batch=4096, seed=9)
+    many = est.plan_many(bgps)
+    for q, pm in zip(bgps, many):
+        single, _ = est.plan(q)
+        assert pm == single
+
+
+def test_row_limit_is_an_error_not_a_truncation(gpu_small, golden_small):
+    q = next(x for x in golden_small["queries"] if x["name"] == "pindex_out")
+    gpu_small.set_row_limit(1000)
+    try:
+        with pytest.raises(W.WkError) as e:
+            gpu_small.execute(q["cmd_chains"])
+        assert e.value.status == W.WK_EOVERFLOW
+    finally:
+        gpu_small.set_row_limit(0)
+    req, _ = gpu_small.execute(q["cmd_chains"])
+    assert req.result_table.shape[0] == q["rows"]

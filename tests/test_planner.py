@@ -51,51 +51,7 @@ def test_plans_match_reference(host_ctx, ref_store, small_graph):
         assert mine == ref, (q, mine, ref)
 
 
-def _match(q, plan):
-    """Original variable -> planned variable, by matching every planned pattern
-    to a distinct original pattern (backtracking; an inserted index pattern
-    binds the subjects (IN) or objects (OUT) of a pattern with that predicate)."""
-    orig = [q[i:i + 4] for i in range(0, len(q), 4)]
-    pl = [plan[i:i + 4] for i in range(0, len(plan), 4)]
-    index = None
-    if pl and pl[0][1] in (W.PREDICATE_ID, W.TYPE_ID) and 1 < pl[0][0] < W.VID_BASE and pl[0][1] == W.PREDICATE_ID:
-        index = pl.pop(0)
-
-    def bind(vmap, x, y):
-        if x >= 0 or y >= 0:
-            return vmap if x == y else None
-        if vmap.get(x, y) != y or (y in vmap.values() and vmap.get(x) != y):
-            return None
-        v = dict(vmap)
-        v[x] = y
-        return v
-
-    def rec(k, used, vmap):
-        if k == len(pl):
-            return vmap if all(used) else None
-        st, pid, d, en = pl[k]
-        for j, (a, pp, dd, b) in enumerate(orig):
-            if used[j] or pp != pid:
-                continue
-            ca, cb = (a, b) if d == W.OUT else (b, a)
-            v = bind(vmap, ca, st)
-            v = bind(v, cb, en) if v is not None else None
-            if v is None:
-                continue
-            u = list(used)
-            u[j] = True
-            r = rec(k + 1, u, v)
-            if r is not None:
-                if index is not None:
-                    ip, _, idir, ivar = index
-                    ok = any(pp == ip and ((idir == W.IN and r.get(a) == ivar) or (idir == W.OUT and r.get(b) == ivar))
-                             for (a, pp, dd, b) in orig)
-                    if not ok:
-                        continue
-                return r
-        return None
-
-    return rec(0, [False] * len(orig), {})
+from wukonggpu_gb300.plans import match_plan as _match  # noqa: E402
 
 
 def test_plans_give_the_same_rows(host_ctx, small_graph, small_oracle):

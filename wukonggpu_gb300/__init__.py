@@ -147,6 +147,8 @@ _SIGS = {
     "wk_mlp_predict": (C.c_int, [_P, C.POINTER(C.c_float), _I32P, C.c_int64, C.POINTER(C.c_float)]),
     "wk_featurize": (C.c_int, [_P, _I64P, C.c_int32, _I64P, C.POINTER(C.c_float), _I32P, C.POINTER(C.c_double)]),
     "wk_plan_learned": (C.c_int, [_P, _P, _I64P, C.c_int32, _I64P, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "wk_plan_learned_batch": (C.c_int, [_P, _P, _I64P, _I32P, C.c_int32, _I64P, _I32P]),
+    "wk_set_row_limit": (C.c_int, [_P, C.c_int64]),
     "wk_timer_begin": (C.c_int, [_P]),
     "wk_timer_end": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "wk_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_P)]),
@@ -404,6 +406,10 @@ class RCache:
         _check(load_library().wk_stat_get(self._h, which, a, b, out.ctypes.data_as(_I64P)))
         return [int(x) for x in out] if which == 4 else int(out[0])
 
+    def set_row_limit(self, max_rows: int):
+        """Cap on k2u output rows (0 = none); larger steps fail with WK_EOVERFLOW."""
+        _check(load_library().wk_set_row_limit(self._h, max_rows))
+
     def enable_timing(self, on: bool = True):
         _check(load_library().wk_enable_timing(self._h, 1 if on else 0))
 
@@ -574,6 +580,21 @@ class Estimator:
         _check(load_library().wk_plan_learned(self.rc._h, self._h, cc.ctypes.data_as(_I64P), n,
                                               out.ctypes.data_as(_I64P), C.byref(n_out), C.byref(est)))
         return [int(x) for x in out[:4 * n_out.value]], est.value
+
+    def plan_many(self, queries):
+        """Learned plans of many BGPs at once ([] where no executable order exists)."""
+        cmd = np.asarray([x for q in queries for x in q], np.int64)
+        n_in = np.asarray([len(q) // 4 for q in queries], np.int32)
+        out = np.zeros(int(4 * (n_in.sum() + len(queries))), np.int64)
+        n_out = np.zeros(len(queries), np.int32)
+        _check(load_library().wk_plan_learned_batch(self.rc._h, self._h, cmd.ctypes.data_as(_I64P),
+                                                    n_in.ctypes.data_as(_I32P), len(queries),
+                                                    out.ctypes.data_as(_I64P), n_out.ctypes.data_as(_I32P)))
+        res, at = [], 0
+        for k in n_out:
+            res.append([int(x) for x in out[at:at + 4 * k]])
+            at += 4 * int(k)
+        return res
 
     def close(self):
         if getattr(self, "_h", None):

@@ -311,3 +311,130 @@ extern "C" int wk_plan_learned(wk_ctx *ctx, wk_mlp *mlp, const int64_t *cmd_in, 
     if (est_log_rows) *est_log_rows = std::log1p(total_est);
     return WK_OK;
 }
+
+// Learned plans of many BGPs at once: the greedy steps of all queries run in
+// lockstep, so each step is one model call over every query's candidates.
+// cmd_in packs the queries back to back (n_in[q] patterns each); cmd_out must
+// hold sum(n_in[q] + 1) patterns; n_out[q] receives each plan's length (0:
+// no executable order).
+extern "C" int wk_plan_learned_batch(wk_ctx *ctx, wk_mlp *mlp, const int64_t *cmd_in, const int32_t *n_in, int32_t nq,
+                                     int64_t *cmd_out, int32_t *n_out) {
+    if (!ctx || !mlp || !cmd_in || !n_in || nq < 1 || !cmd_out || !n_out)
+        return set_error(WK_EINVAL, "wk_plan_learned_batch: bad arguments");
+    if (!ctx->store) return set_error(WK_ENOSTORE, "wk_plan_learned_batch: no store");
+    Stats &st = stats_of(ctx);
+    struct Cand { Step s; int pat; bool consumes; };
+    struct QState {
+        const int64_t *cmd;
+        int n;
+        std::vector<int> used;
+        std::unordered_map<int64_t, VarInfo> vars;
+        std::vector<int64_t> plan;
+        double rows = 0.0;
+        int cols = 0, step = 0;
+        bool done = false, failed = false;
+        std::vector<Cand> cands;
+    };
+    std::vector<QState> qs((size_t)nq);
+    int64_t at = 0;
+    for (int q = 0; q < nq; ++q) {
+        if (n_in[q] < 1 || n_in[q] > 10) return set_error(WK_EINVAL, "wk_plan_learned_batch: query %d has %d patterns", q, n_in[q]);
+        qs[(size_t)q].cmd = cmd_in + at;
+        qs[(size_t)q].n = n_in[q];
+        qs[(size_t)q].used.assign((size_t)n_in[q], 0);
+        at += 4 * (int64_t)n_in[q];
+    }
+    std::vector<float> fb, pred;
+    std::vector<int32_t> pb;
+    for (int round = 0; round < 11; ++round) {
+        fb.clear();
+        pb.clear();
+        for (auto &Q : qs) {
+            Q.cands.clear();
+            if (Q.done) continue;
+            const int n = Q.n;
+            if (Q.step == 0) {
+                for (int i = 0; i < n; ++i) {
+                    const int64_t a = Q.cmd[4 * i], p = Q.cmd[4 * i + 1], b = Q.cmd[4 * i + 3];
+                    if (a >= WK_VID_BASE) Q.cands.push_back(Cand{Step{K_C2U, a, p, WK_DIR_OUT, b, (int)p}, i, true});
+                    if (b >= WK_VID_BASE) Q.cands.push_back(Cand{Step{K_C2U, b, p, WK_DIR_IN, a, (int)p}, i, true});
+                    if (p == WK_TYPE_ID && a < 0 && b > 1 && b < WK_VID_BASE)
+                        Q.cands.push_back(Cand{Step{K_I2U, b, WK_TYPE_ID, WK_DIR_IN, a, (int)b}, i, true});
+                    if (a < 0 && b < 0 && p != WK_TYPE_ID) {
+                        Q.cands.push_back(Cand{Step{K_I2U, p, WK_PREDICATE_ID, WK_DIR_IN, a, (int)p}, i, false});
+                        Q.cands.push_back(Cand{Step{K_I2U, p, WK_PREDICATE_ID, WK_DIR_OUT, b, (int)p}, i, false});
+                    }
+                }
+            } else {
+                bool all = true;
+                for (int i = 0; i < n; ++i) {
+                    if (Q.used[(size_t)i]) continue;
+                    all = false;
+                    const int64_t a = Q.cmd[4 * i], p = Q.cmd[4 * i + 1], b = Q.cmd[4 * i + 3];
+                    const bool ka = a < 0 && Q.vars.count(a), kb = b < 0 && Q.vars.count(b);
+                    auto kind_for = [&](int64_t other) {
+                        if (other >= 0) return (int)K_K2C;
+                        return Q.vars.count(other) ? (int)K_K2K : (int)K_K2U;
+                    };
+                    if (ka) Q.cands.push_back(Cand{Step{kind_for(b), a, p, WK_DIR_OUT, b, (int)p}, i, true});
+                    if (kb) Q.cands.push_back(Cand{Step{kind_for(a), b, p, WK_DIR_IN, a, (int)p}, i, true});
+                }
+                if (all) { Q.done = true; continue; }
+            }
+            if (Q.cands.empty()) { Q.done = true; Q.failed = true; continue; }
+            for (const Cand &c : Q.cands) {
+                const Step &s = c.s;
+                const VarInfo *bind = (s.kind != K_I2U && s.kind != K_C2U) ? &Q.vars[s.start] : nullptr;
+                fb.resize(fb.size() + kF);
+                features(ctx, st, s, Q.step == 0 ? 0.0 : Q.rows, Q.step, Q.cols, bind, fb.data() + fb.size() - kF);
+                pb.push_back(s.feat_pid);
+            }
+        }
+        if (pb.empty()) break;
+        pred.assign(pb.size(), 0.f);
+        int rc = wk_mlp_predict(mlp, fb.data(), pb.data(), (int64_t)pb.size(), pred.data());
+        if (rc) return rc;
+        size_t k = 0;
+        for (auto &Q : qs) {
+            if (Q.cands.empty()) continue;
+            size_t best = 0;
+            for (size_t c = 1; c < Q.cands.size(); ++c)
+                if (pred[k + c] < pred[k + best]) best = c;
+            const Cand &ch = Q.cands[best];
+            const Step &s = ch.s;
+            Q.plan.insert(Q.plan.end(), {s.start, s.pid, s.dir, s.end});
+            if (ch.consumes) Q.used[(size_t)ch.pat] = 1;
+            if (s.kind == K_I2U || s.kind == K_C2U || s.kind == K_K2U) {
+                VarInfo v;
+                v.col = Q.cols++;
+                v.pred = s.kind == K_I2U ? (int)s.start : (int)s.pid;
+                v.dir = (int)s.dir;
+                Q.vars[s.end] = v;
+            }
+            Q.rows = std::expm1((double)std::max(0.f, pred[k + best]));
+            Q.step++;
+            k += Q.cands.size();
+        }
+    }
+    int64_t out_at = 0;
+    for (int q = 0; q < nq; ++q) {
+        QState &Q = qs[(size_t)q];
+        if (Q.failed) { n_out[q] = 0; continue; }
+        std::unordered_map<int64_t, int64_t> conv;
+        for (auto &x : Q.plan)
+            if (x < 0) {
+                auto it = conv.find(x);
+                if (it == conv.end()) {
+                    const int64_t v = -1 - (int64_t)conv.size();
+                    conv.emplace(x, v);
+                    x = v;
+                } else {
+                    x = it->second;
+                }
+            }
+        std::memcpy(cmd_out + out_at, Q.plan.data(), Q.plan.size() * sizeof(int64_t));
+        n_out[q] = (int32_t)(Q.plan.size() / 4);
+        out_at += (int64_t)Q.plan.size();
+    }
+    return WK_OK;
+}

@@ -160,6 +160,9 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     if (errf) return fail_corrupt(ctx);
     const int64_t R_out = (int64_t)ctx->h_scal[1];
     const int64_t nz = (int64_t)ctx->h_scal[2];
+    if (R_out > ctx->row_limit)
+        return set_error(WK_EOVERFLOW, "k2u: %lld output rows exceed the context's row limit %lld", (long long)R_out,
+                         (long long)ctx->row_limit);
     ctx->last.rows_out = R_out;
     ctx->last.alg_bytes = 4 * R * C + 16 * R + 4 * R_out + 4 * R_out * (C + 1);
     if (R_out == 0) {
@@ -396,4 +399,10 @@ extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history
     }
     ctx->protect.clear();
     return st;
+}
+
+extern "C" int wk_set_row_limit(wk_ctx *ctx, int64_t max_rows) {
+    if (!ctx || max_rows < 0) return set_error(WK_EINVAL, "wk_set_row_limit: bad arguments");
+    ctx->row_limit = max_rows ? max_rows : INT64_MAX;
+    return WK_OK;
 }

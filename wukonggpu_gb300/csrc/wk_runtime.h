@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <map>
 #include <memory>
 #include <vector>
@@ -81,6 +82,7 @@ struct wk_ctx {
     int tn = 0;
     wk_op_stats last{};
     int64_t launches = 0;
+    int64_t row_limit = INT64_MAX;   // wk_set_row_limit
     cudaEvent_t tm0 = nullptr, tm1 = nullptr;   // wk_timer_begin / wk_timer_end
 
     // query-level state (segment cache protection / prefetch)

@@ -221,3 +221,55 @@ def light_queries(s, p, o, n: int, seed: int, max_pat: int = 4, filters: bool = 
         if ok and q:
             out.append(q)
     return out
+
+
+def light_queries_store(rc, n_entities: int, preds, n: int, seed: int, max_pat: int = 4, max_tries: int = 8):
+    """Light constant-start queries by random walks over the store (both
+    directions), for graphs too large to index in numpy: start at a uniform
+    entity, then 1..max_pat steps, each a (predicate, direction) drawn among
+    those present on the vertex reached (rejection over random draws)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n:
+        c = VID_BASE + int(rng.integers(0, n_entities))
+        k = int(rng.integers(1, max_pat + 1))
+        q, cur, col = [], c, 0
+        for step in range(k):
+            nxt = None
+            for _ in range(max_tries):
+                pid = int(preds[int(rng.integers(0, len(preds)))])
+                d = OUT if rng.random() < 0.6 else IN
+                e = rc.get_edges(cur, pid, d)
+                if len(e):
+                    nxt = (pid, d, int(e[int(rng.integers(0, len(e)))]))
+                    break
+            if nxt is None:
+                break
+            pid, d, v = nxt
+            if step == 0:
+                q += [c, pid, d, -1]
+                col = 1
+            else:
+                q += [-col, pid, d, -(col + 1)]
+                col += 1
+            cur = v
+        if q:
+            out.append(q)
+    return out
+
+
+def serving_heavy_queries(n_classes: int = 15):
+    """Heavy requests of the serving mix: 4..6 patterns from a type index,
+    widening through one-to-one and many-to-one predicates (~1.3e5 rows)."""
+    C = SQ_FIRST_CLASS
+    f, m = SQ_FUNC, SQ_M2O
+    out = []
+    for k in range(n_classes):
+        c = C + k
+        base = [c, TYPE_ID, IN, -1, -1, f[k % 8], OUT, -2, -1, m[k % 8], OUT, -3, -2, f[(k + 1) % 8], OUT, -4]
+        if k % 3 == 1:
+            base += [-3, f[(k + 2) % 8], OUT, -5]
+        if k % 3 == 2:
+            base += [-3, f[(k + 2) % 8], OUT, -5, -4, m[(k + 3) % 8], OUT, -6]
+        out.append(base)
+    return out
