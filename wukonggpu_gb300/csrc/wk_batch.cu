@@ -30,6 +30,7 @@
 #include <cstring>
 #include <vector>
 
+#include "wk_probe.cuh"
 #include "wk_runtime.h"
 
 namespace wk {
@@ -51,76 +52,6 @@ struct BatchTune {
 
 constexpr int kBT = 256;                    // threads per block
 constexpr int kMaxQ = 4096;                 // queries per batch (shared-memory row offsets)
-
-__device__ __forceinline__ uint64_t b_key(uint32_t vid, uint32_t pid, uint32_t dir) {
-    return ((uint64_t)vid << 18) | ((uint64_t)pid << 1) | (uint64_t)dir;
-}
-__device__ __forceinline__ uint64_t b_mix(uint64_t k) {
-    k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
-    return k;
-}
-__device__ __forceinline__ uint4 b_ld(const uint4 *p) {
-    uint4 r;
-    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
-        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
-    return r;
-}
-
-// The warp-cooperative probe with a per-lane segment: lane L's key lives in
-// segment pv (its query's predicate).  Keys encode the predicate, so equal
-// keys share a segment and are probed once.  Same bucket protocol as the
-// single-query probe: one 16 B load per lane of an 8-lane group, ballot.
-__device__ __forceinline__ void warp_probe32_multi(const PredView &pv, uint64_t mykey, bool valid,
-                                                   uint32_t &r_off, uint32_t &r_deg, int *err) {
-    const int lane = threadIdx.x & 31;
-    const int sub = lane & 7, g = lane >> 3, gbase = lane & ~7;
-    const unsigned same = __match_any_sync(FULL, valid ? mykey : ~0ull);
-    const int lead = __ffs(same) - 1;
-    const unsigned L = __ballot_sync(FULL, valid && lead == lane);
-    const int nu = __popc(L);
-    const int src = lane < nu ? (int)__fns(L, 0, lane + 1) : 0;
-    const uint64_t ukey = __shfl_sync(FULL, mykey, src);
-    const unsigned long long ubk = __shfl_sync(FULL, (unsigned long long)pv.buckets, src);
-    const uint32_t unm = __shfl_sync(FULL, pv.nmain, src);
-    const uint32_t uno = __shfl_sync(FULL, pv.nover, src);
-    uint32_t u_off = 0u, u_deg = 0u;
-    for (int it = 0; it * 4 < nu; ++it) {
-        const int j = it * 4 + g;
-        const uint64_t k = __shfl_sync(FULL, ukey, j);
-        const uint4 *bk = (const uint4 *)__shfl_sync(FULL, ubk, j);
-        const uint32_t nm = __shfl_sync(FULL, unm, j), no = __shfl_sync(FULL, uno, j);
-        bool pend = j < nu && nm > 0u;
-        uint32_t b = pend ? (uint32_t)__umul64hi(b_mix(k), (uint64_t)nm) : 0u;
-        uint32_t off_g = 0u, deg_g = 0u, hops = 0u;
-        for (;;) {
-            const uint4 cw = pend ? b_ld(bk + (size_t)b * WK_SLOTS_PER_BUCKET + sub) : make_uint4(0u, 0u, 0u, 0u);
-            const uint64_t sk = ((uint64_t)cw.y << 32) | cw.x;
-            const bool hit = pend && sub < WK_DATA_SLOTS && sk == k;
-            const uint32_t m = __ballot_sync(FULL, hit);
-            const uint32_t gm = (m >> gbase) & 0xffu;
-            const int sl = gbase + (gm ? (__ffs(gm) - 1) : WK_DATA_SLOTS);
-            const uint32_t sx = __shfl_sync(FULL, cw.x, sl), sy = __shfl_sync(FULL, cw.y, sl);
-            const uint32_t sz = __shfl_sync(FULL, cw.z, sl), sw = __shfl_sync(FULL, cw.w, sl);
-            bool more = false;
-            if (pend) {
-                if (gm) { off_g = sz; deg_g = sw; }
-                else if (sy & WK_LINK_TAG) {
-                    if (hops < no && sx < nm + no) { b = sx; ++hops; more = true; }
-                    else if (sub == 0) atomicOr(err, 1);
-                }
-            }
-            pend = more;
-            if (!__any_sync(FULL, pend)) break;
-        }
-        const uint32_t vo = __shfl_sync(FULL, off_g, (lane & 3) * 8);
-        const uint32_t vd = __shfl_sync(FULL, deg_g, (lane & 3) * 8);
-        if ((lane >> 2) == it) { u_off = vo; u_deg = vd; }
-    }
-    const int u = __popc(L & ((1u << lead) - 1u));
-    const uint32_t o = __shfl_sync(FULL, u_off, u), d = __shfl_sync(FULL, u_deg, u);
-    r_off = valid ? o : 0u;
-    r_deg = valid ? d : 0u;
-}
 
 __device__ __forceinline__ int find_query(const int64_t *s_off, int Q, int64_t g) {
     int lo = 0, hi = Q - 1;   // largest q with s_off[q] <= g
@@ -179,24 +110,23 @@ batch_count_kernel(StepIO io, int rounds) {
             StepDesc d{BK_NOP, 0, 0, 0, 0, 0};
             if (valid) { q = find_query(s_off, io.Q, g); d = io.desc[q]; }
             PredView pv{nullptr, nullptr, 0u, 0u};
-            uint64_t key = 0;
+            int32_t vid = -1;
             bool probe = valid && d.kind != BK_NOP;
             int32_t target = 0;
             if (probe) {
                 pv = io.pvs[d.pid];
-                uint32_t vid;
                 if (d.kind == BK_C2U) {
-                    vid = (uint32_t)d.cst;
+                    vid = d.cst;
                 } else {
                     const int64_t r = g - s_off[q];
                     const int32_t *row = io.hist + io.in_int_off[q] + r * io.in_cols[q];
-                    vid = (uint32_t)__ldg(row + d.scol);
+                    vid = __ldg(row + d.scol);
                     target = d.kind == BK_K2K ? __ldg(row + d.ecol) : d.cst;
                 }
-                key = b_key(vid, (uint32_t)d.pid, (uint32_t)d.dir);
             }
             uint32_t o = 0u, deg = 0u;
-            if (__any_sync(FULL, probe)) warp_probe32_multi(pv, key, probe, o, deg, io.flags);
+            if (__any_sync(FULL, probe))
+                probe_warp_multi(pv, (uint32_t)d.pid, probe, vid, (uint32_t)d.dir, o, deg, io.flags);
             uint32_t c = 0u;
             if (valid) {
                 if (d.kind == BK_NOP) c = 1u;

@@ -1,6 +1,6 @@
 // Expansion kernels of the per-pattern operator (sm_103a).
 //
-// Every op is integer work bounded by HBM: random 128 B bucket reads for the
+// Every op is integer work bounded by HBM: random 64 B bucket reads for the
 // probe, then streaming reads of history/adjacency and streaming writes of the
 // new table.  No tensor cores are involved.
 //
@@ -11,129 +11,12 @@
 // output rows follow input row order, and for k2u each input row's block of
 // output rows follows adjacency order.
 #include "wk_kernels.h"
+#include "wk_probe.cuh"
 
 namespace wk {
 namespace dev {
 
 #define FULL 0xffffffffu
-
-__device__ __forceinline__ uint64_t d_make_key(uint32_t vid, uint32_t pid, uint32_t dir) {
-    return ((uint64_t)vid << 18) | ((uint64_t)pid << 1) | (uint64_t)dir;
-}
-
-// MurmurHash3 fmix64, identical to key_mix() in the host builder.
-__device__ __forceinline__ uint64_t d_mix(uint64_t k) {
-    k ^= k >> 33;
-    k *= 0xff51afd7ed558ccdull;
-    k ^= k >> 33;
-    k *= 0xc4ceb9fe1a85ec53ull;
-    k ^= k >> 33;
-    return k;
-}
-
-__device__ __forceinline__ uint32_t d_bucket(uint64_t h, uint32_t n) {
-    return (uint32_t)__umul64hi(h, (uint64_t)n);
-}
-
-// 16 B bucket-slot load through the non-coherent path without L1 allocation:
-// bucket reads are random and have no reuse inside an SM.
-__device__ __forceinline__ uint4 ld_slot(const uint4 *p) {
-    uint4 r;
-    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
-        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
-        : "l"(p));
-    return r;
-}
-
-// Warp-cooperative probe of the 32 keys held one per lane.  Equal keys in
-// the warp (the same start vertex on consecutive rows, common after an
-// expansion) are probed once: __match_any_sync groups them and only the
-// distinct keys are looked up.  The warp is split into four 8-lane groups; a
-// group reads one 128 B bucket with one 16 B load per lane, and
-// __ballot_sync tells each group which slot matched.  All buckets a lane
-// needs are loaded before any is resolved, so up to eight independent 16 B
-// loads per lane are in flight.  On return lane L holds (off, deg) of its
-// own key; deg = 0 when the key is absent (the CPU engine's size-0 result,
-// core/gstore.hpp:389-409).  Overflow hops are bounded by the segment's
-// overflow-bucket count.
-__device__ __forceinline__ void warp_probe32(const PredView &pv, uint64_t mykey, bool valid,
-                                             uint32_t &r_off, uint32_t &r_deg, int *err) {
-    const int lane = threadIdx.x & 31;
-    const int sub = lane & 7, g = lane >> 3, gbase = lane & ~7;
-    // distinct keys of the warp, compacted to lanes 0..nu-1
-    const unsigned same = __match_any_sync(FULL, valid ? mykey : ~0ull);
-    const int lead = __ffs(same) - 1;
-    const unsigned L = __ballot_sync(FULL, valid && lead == lane);
-    const int nu = __popc(L);
-    const int src = lane < nu ? (int)__fns(L, 0, lane + 1) : 0;
-    const uint64_t ukey = __shfl_sync(FULL, mykey, src);
-    const int nit = (nu + 3) >> 2;
-
-    uint4 w[8];
-    uint64_t k[8];
-    bool act[8];
-#pragma unroll
-    for (int it = 0; it < 8; ++it) {
-        const int j = it * 4 + g;
-        k[it] = __shfl_sync(FULL, ukey, j);
-        act[it] = j < nu && pv.nmain > 0;
-        const uint32_t b = act[it] ? d_bucket(d_mix(k[it]), pv.nmain) : 0u;
-        w[it] = act[it] ? ld_slot(pv.buckets + (size_t)b * WK_SLOTS_PER_BUCKET + sub)
-                        : make_uint4(0u, 0u, 0u, 0u);
-    }
-    uint32_t u_off = 0u, u_deg = 0u;   // result of distinct key `lane`
-#pragma unroll
-    for (int it = 0; it < 8; ++it) {
-        if (it >= nit) break;           // warp-uniform
-        uint32_t off_g = 0u, deg_g = 0u;
-        bool pend = act[it];
-        uint4 cw = w[it];
-        uint32_t hops = 0;
-        for (;;) {
-            const uint64_t sk = ((uint64_t)cw.y << 32) | cw.x;
-            const bool hit = pend && sub < WK_DATA_SLOTS && sk == k[it];
-            const uint32_t m = __ballot_sync(FULL, hit);
-            const uint32_t gm = (m >> gbase) & 0xffu;
-            const int sl = gbase + (gm ? (__ffs(gm) - 1) : WK_DATA_SLOTS);
-            const uint32_t sx = __shfl_sync(FULL, cw.x, sl);
-            const uint32_t sy = __shfl_sync(FULL, cw.y, sl);
-            const uint32_t sz = __shfl_sync(FULL, cw.z, sl);
-            const uint32_t sw = __shfl_sync(FULL, cw.w, sl);
-            bool more = false;
-            uint32_t nb = 0;
-            if (pend) {
-                if (gm) {
-                    off_g = sz;
-                    deg_g = sw;
-                } else if (sy & WK_LINK_TAG) {
-                    if (hops < pv.nover && sx < pv.nmain + pv.nover) {
-                        nb = sx;
-                        ++hops;
-                        more = true;
-                    } else if (sub == 0) {
-                        atomicOr(err, 1);   // chain longer than the overflow area
-                    }
-                }
-            }
-            pend = more;
-            if (!__any_sync(FULL, pend)) break;
-            cw = pend ? ld_slot(pv.buckets + (size_t)nb * WK_SLOTS_PER_BUCKET + sub)
-                      : make_uint4(0u, 0u, 0u, 0u);
-        }
-        // distinct key it*4+g' is delivered to lane it*4+g'
-        const uint32_t vo = __shfl_sync(FULL, off_g, (lane & 3) * 8);
-        const uint32_t vd = __shfl_sync(FULL, deg_g, (lane & 3) * 8);
-        if ((lane >> 2) == it) {
-            u_off = vo;
-            u_deg = vd;
-        }
-    }
-    const int u = __popc(L & ((1u << lead) - 1u));
-    const uint32_t o = __shfl_sync(FULL, u_off, u);
-    const uint32_t d = __shfl_sync(FULL, u_deg, u);
-    r_off = valid ? o : 0u;
-    r_deg = valid ? d : 0u;
-}
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
@@ -161,26 +44,33 @@ __device__ __forceinline__ void block_sum2(unsigned long long &a, unsigned int &
 }
 
 // ----------------------------------------------------------------- k2u probe
+// A warp owns kRounds * 32 consecutive rows.  Their start vertices are loaded
+// first (kRounds independent coalesced loads), then each round of 32 rows is
+// probed, so the history read does not sit in front of every bucket read.
+constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
+
 __global__ void __launch_bounds__(kThreads)
-k2u_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t pid,
-                 uint32_t dir, PredView pv, uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
+k2u_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
+                 uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
                  unsigned long long *__restrict__ blk_sum, unsigned int *__restrict__ blk_nz, int *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t blk0 = (int64_t)blockIdx.x * kRowsPerBlock;
+    const int64_t wrow0 = (int64_t)blockIdx.x * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
+    int32_t v[kRounds];
+#pragma unroll
+    for (int rd = 0; rd < kRounds; ++rd) {
+        const int64_t r = wrow0 + rd * 32 + lane;
+        v[rd] = r < R ? __ldg(hist + r * C + scol) : -1;
+    }
     unsigned long long my_sum = 0;
     unsigned int my_nz = 0;
-    constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
-#pragma unroll 1
-    for (int round = 0; round < kRounds; ++round) {
-        const int64_t row0 = blk0 + (int64_t)warp * (kRounds * 32) + round * 32;
-        if (row0 >= R) break;
+#pragma unroll
+    for (int rd = 0; rd < kRounds; ++rd) {
+        const int64_t row0 = wrow0 + rd * 32;
+        if (row0 >= R) break;   // warp-uniform
         const int64_t r = row0 + lane;
-        const bool valid = r < R;
-        uint64_t key = 0;
-        if (valid) key = d_make_key((uint32_t)__ldg(hist + r * C + scol), pid, dir);
         uint32_t o, d;
-        warp_probe32(pv, key, valid, o, d, err);
-        if (valid) {
+        probe_warp(pv, v[rd], dir, o, d, err);
+        if (r < R) {
             deg[r] = d;
             off[r] = o;
             my_sum += d;
@@ -214,32 +104,31 @@ __device__ __forceinline__ bool list_contains(const int32_t *__restrict__ e, uin
 
 __global__ void __launch_bounds__(kThreads)
 filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, int ecol,
-                    int32_t end_const, uint32_t pid, uint32_t dir, PredView pv,
+                    int32_t end_const, uint32_t dir, PredView pv,
                     uint32_t *__restrict__ mask, unsigned long long *__restrict__ blk_sum,
                     unsigned int *__restrict__ blk_nz, int *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t blk0 = (int64_t)blockIdx.x * kRowsPerBlock;
+    const int64_t wrow0 = (int64_t)blockIdx.x * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
+    int32_t v[kRounds], tg[kRounds];
+#pragma unroll
+    for (int rd = 0; rd < kRounds; ++rd) {
+        const int64_t r = wrow0 + rd * 32 + lane;
+        v[rd] = r < R ? __ldg(hist + r * C + scol) : -1;
+        tg[rd] = (r < R && ecol >= 0) ? __ldg(hist + r * C + ecol) : end_const;
+    }
     unsigned int my_nz = 0;
     unsigned long long my_scan = 0;   // adjacency entries a linear scan would touch
-    constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
-#pragma unroll 1
-    for (int round = 0; round < kRounds; ++round) {
-        const int64_t row0 = blk0 + (int64_t)warp * (kRounds * 32) + round * 32;
-        if (row0 >= R) break;
+#pragma unroll
+    for (int rd = 0; rd < kRounds; ++rd) {
+        const int64_t row0 = wrow0 + rd * 32;
+        if (row0 >= R) break;   // warp-uniform
         const int64_t r = row0 + lane;
-        const bool valid = r < R;
-        uint64_t key = 0;
-        int32_t target = end_const;
-        if (valid) {
-            key = d_make_key((uint32_t)__ldg(hist + r * C + scol), pid, dir);
-            if (ecol >= 0) target = __ldg(hist + r * C + ecol);
-        }
         uint32_t o, d;
-        warp_probe32(pv, key, valid, o, d, err);
+        probe_warp(pv, v[rd], dir, o, d, err);
         bool found = false;
-        if (valid && d > 0u) {
+        if (r < R && d > 0u) {
             uint32_t sc = 0;
-            found = list_contains(pv.edges + o, d, target, &sc);
+            found = list_contains(pv.edges + o, d, tg[rd], &sc);
             my_scan += sc;
         }
         const uint32_t m = __ballot_sync(FULL, found);
@@ -485,17 +374,17 @@ int k2u_tile_rows(int out_cols) {
 
 static size_t k2u_write_smem(int tile_rows) { return (size_t)(4 * tile_rows + 4) * sizeof(int); }
 
-void launch_k2u_probe(const int32_t *hist, int64_t R, int C, int scol, uint32_t pid, uint32_t dir,
-                      PredView pv, uint32_t *deg, uint32_t *off, unsigned long long *blk_sum,
-                      unsigned int *blk_nz, int *err, cudaStream_t st) {
-    k2u_probe_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, pid, dir, pv, deg, off,
-                                                           blk_sum, blk_nz, err);
+void launch_k2u_probe(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
+                      uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned int *blk_nz,
+                      int *err, cudaStream_t st) {
+    k2u_probe_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum,
+                                                           blk_nz, err);
 }
 
 void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ecol, int32_t end_const,
-                         uint32_t pid, uint32_t dir, PredView pv, uint32_t *mask,
-                         unsigned long long *blk_sum, unsigned int *blk_nz, int *err, cudaStream_t st) {
-    filter_probe_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, pid, dir, pv,
+                         uint32_t dir, PredView pv, uint32_t *mask, unsigned long long *blk_sum,
+                         unsigned int *blk_nz, int *err, cudaStream_t st) {
+    filter_probe_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv,
                                                               mask, blk_sum, blk_nz, err);
 }
 

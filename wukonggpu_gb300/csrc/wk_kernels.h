@@ -15,15 +15,15 @@ constexpr int kThreads = 256;
 int k2u_tile_rows(int out_cols);
 
 // Pass 1 of k2u: probe key hist[r][scol] -> deg[r], off[r]; per-block sums.
-void launch_k2u_probe(const int32_t *hist, int64_t R, int C, int scol, uint32_t pid, uint32_t dir,
-                      PredView pv, uint32_t *deg, uint32_t *off, unsigned long long *blk_sum,
-                      unsigned int *blk_nz, int *err, cudaStream_t st);
+void launch_k2u_probe(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
+                      uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned int *blk_nz,
+                      int *err, cudaStream_t st);
 
 // Pass 1 of k2k/k2c: probe + membership of the end value; ballot masks and per-block counts.
 // ecol >= 0: end is column ecol (k2k); ecol < 0: end is the constant `end_const` (k2c).
 void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ecol, int32_t end_const,
-                         uint32_t pid, uint32_t dir, PredView pv, uint32_t *mask,
-                         unsigned long long *blk_sum, unsigned int *blk_nz, int *err, cudaStream_t st);
+                         uint32_t dir, PredView pv, uint32_t *mask, unsigned long long *blk_sum,
+                         unsigned int *blk_nz, int *err, cudaStream_t st);
 
 // Exclusive scan of the per-block sums in place; totals[0] = sum, totals[1] = nz;
 // if cz_pos != nullptr also writes cz_pos[nz] = sum (sentinel).

@@ -111,8 +111,7 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     const int64_t nblk = (rows + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
     cudaStream_t s = ctx->stream;
     if ((e = cudaMemsetAsync(err, 0, sizeof(int), s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flag");
-    dev::launch_k2u_probe(hist, rows, cols, scol, (uint32_t)predict, (uint32_t)direction, pv, deg, off, blk_sum,
-                          blk_nz, err, s);
+    dev::launch_k2u_probe(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, blk_nz, err, s);
     dev::launch_scan_blocks(blk_sum, blk_nz, nblk, tot, cz_pos, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: probe/scan launch");
     ctx->launches += 2;

@@ -149,7 +149,7 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
     int *err = ctx->dscal.as<int>();
     if ((st = clk.begin())) return st;
-    dev::launch_k2u_probe(h->data, R, C, scol, pid, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
+    dev::launch_k2u_probe(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
                           ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), err, ctx->stream);
     if ((st = launch_check("k2u probe")) || (st = clk.end(false)) || (st = clk.begin())) return st;
     dev::launch_scan_blocks(ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), nblk, tot,
@@ -223,7 +223,7 @@ int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const,
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
     int *err = ctx->dscal.as<int>();
     if ((st = clk.begin())) return st;
-    dev::launch_filter_probe(h->data, R, C, scol, ecol, end_const, pid, dir, pv, ctx->mask.as<uint32_t>(),
+    dev::launch_filter_probe(h->data, R, C, scol, ecol, end_const, dir, pv, ctx->mask.as<uint32_t>(),
                              ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), err, ctx->stream);
     if ((st = launch_check("filter probe")) || (st = clk.end(true)) || (st = clk.begin())) return st;
     dev::launch_scan_blocks(ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), nblk, tot,

@@ -54,15 +54,15 @@ Stats *build_stats(const HostStore &hs) {
     for (int id = 1; id <= hs.num_ids; ++id) {
         const PredSeg &sg = hs.segs[(size_t)id];
         const uint64_t nb = (uint64_t)sg.nmain + sg.nover;
-        const uint32_t *base = hs.buckets + sg.bucket_off * 4;
+        const Bucket *base = hs.buckets + sg.bucket_off;
+        const uint32_t pid = (uint32_t)id;   // every key of a segment has the segment's id
         for (uint64_t b = 0; b < nb; ++b) {
+            const uint32_t *w = base[b].w;
             for (int i = 0; i < WK_DATA_SLOTS; ++i) {
-                const uint32_t *sl = base + (b * WK_SLOTS_PER_BUCKET + (uint64_t)i) * 4;
-                const uint64_t key = (uint64_t)sl[0] | ((uint64_t)sl[1] << 32);
-                if (!key) continue;
-                const uint32_t vid = (uint32_t)(key >> 18), pid = (uint32_t)((key >> 1) & 0x1ffff),
-                               dir = (uint32_t)(key & 1);
-                const uint32_t deg = sl[3];
+                const uint32_t key = w[i];
+                if (key == WK_EMPTY_KEY) continue;
+                const uint32_t vid = key >> 1, dir = key & 1u;
+                const uint32_t deg = w[WK_DEG_WORD + i];
                 if (dir == WK_DIR_IN) {
                     pt[(int)pid] += deg;
                     po[(int)pid] += 1;
@@ -71,7 +71,7 @@ Stats *build_stats(const HostStore &hs) {
                     ps[(int)pid] += 1;
                     lists.push_back(DirP{vid, (pid << 1) | (uint32_t)WK_DIR_OUT});
                     if (pid == WK_TYPE_ID) {
-                        const int32_t *e = hs.edges + sg.edge_off + sl[2];
+                        const int32_t *e = hs.edges + sg.edge_off + w[WK_OFF_WORD + i];
                         for (uint32_t k = 0; k < deg; ++k) {
                             tys[e[k]] += 1;
                             ps[e[k]] += 1;

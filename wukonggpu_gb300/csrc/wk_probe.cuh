@@ -1,0 +1,90 @@
+// Device-side segment probe, shared by the single-query and batched kernels.
+//
+// One lane looks up one key.  A 64 B bucket is fetched as two independent
+// 32 B loads, so a lane has the whole bucket after one memory round trip and
+// resolves the slot in registers: no cross-lane traffic on the hit path.
+// The reference's lookup is GStore::get_edges_global / get_edges_local
+// (core/gstore.hpp:389-409): a key that is absent yields an empty list.
+#pragma once
+
+#include "wk_internal.h"
+
+namespace wk {
+namespace dev {
+
+#ifndef WK_FULL_MASK
+#define WK_FULL_MASK 0xffffffffu
+#endif
+
+// 32 B load through the non-coherent path without L1 allocation: bucket reads
+// are random and have no reuse inside an SM.  p must be 32 B aligned (buckets
+// are 64 B aligned in every image: cudaMalloc and the segment pool give 256 B).
+__device__ __forceinline__ void ld_bucket_half(const uint32_t *p, uint32_t (&v)[8]) {
+    asm("ld.global.nc.L1::no_allocate.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+        : "l"(p));
+}
+
+// Look up `key` in a segment of nmain main and nover overflow buckets.
+// Returns the degree (0 when the key is absent) and the edge offset in *off.
+// Overflow hops are bounded by nover; a longer chain, or a link outside the
+// segment, sets bit 0 of *err and reports the key absent.
+__device__ __forceinline__ uint32_t probe_seg(const Bucket *bk, uint32_t nmain, uint32_t nover, uint32_t key,
+                                              uint32_t *off, int *err) {
+    *off = 0u;
+    if (nmain == 0u) return 0u;
+    uint32_t b = seg_bucket(key, nmain);
+    for (uint32_t hop = 0;; ++hop) {
+        uint32_t a[8], c[8];
+        ld_bucket_half(bk[b].w, a);       // keys 0-4, link, off 0-1
+        ld_bucket_half(bk[b].w + 8, c);   // off 2-4, deg 0-4
+        if (a[0] == key) { *off = a[6]; return c[3]; }
+        if (a[1] == key) { *off = a[7]; return c[4]; }
+        if (a[2] == key) { *off = c[0]; return c[5]; }
+        if (a[3] == key) { *off = c[1]; return c[6]; }
+        if (a[4] == key) { *off = c[2]; return c[7]; }
+        const uint32_t link = a[5];
+        if (link == WK_NO_LINK) return 0u;
+        if (hop >= nover || link >= nmain + nover) {
+            atomicOr(err, 1);
+            return 0u;
+        }
+        b = link;
+    }
+}
+
+// Probe the 32 keys (vid, dir) of a warp in one segment.  Equal keys (the same
+// start vertex on nearby rows, common after an expansion) are looked up once:
+// __match_any_sync groups them, the lowest lane of a group probes and the
+// others read its result.  vid < 0 is not a vertex and is reported absent.
+__device__ __forceinline__ void probe_warp(const PredView &pv, int32_t vid, uint32_t dir, uint32_t &r_off,
+                                           uint32_t &r_deg, int *err) {
+    const int lane = threadIdx.x & 31;
+    const bool ok = vid >= 0;
+    const uint32_t key = seg_key((uint32_t)vid, dir);
+    // a lane without a key groups with WK_EMPTY_KEY, which is never stored
+    const unsigned same = __match_any_sync(WK_FULL_MASK, ok ? key : WK_EMPTY_KEY);
+    const int lead = __ffs(same) - 1;
+    uint32_t o = 0u, d = 0u;
+    if (ok && lead == lane) d = probe_seg(pv.buckets, pv.nmain, pv.nover, key, &o, err);
+    r_off = __shfl_sync(WK_FULL_MASK, o, lead);
+    r_deg = __shfl_sync(WK_FULL_MASK, d, lead);
+}
+
+// As probe_warp, with a segment per lane (rows of different queries).  Equal
+// (segment, key) pairs are probed once.
+__device__ __forceinline__ void probe_warp_multi(const PredView &pv, uint32_t seg, bool valid, int32_t vid,
+                                                 uint32_t dir, uint32_t &r_off, uint32_t &r_deg, int *err) {
+    const int lane = threadIdx.x & 31;
+    const bool ok = valid && vid >= 0;
+    const uint32_t key = seg_key((uint32_t)vid, dir);
+    const unsigned same = __match_any_sync(WK_FULL_MASK, ok ? (((uint64_t)seg << 32) | key) : ~0ull);
+    const int lead = __ffs(same) - 1;
+    uint32_t o = 0u, d = 0u;
+    if (ok && lead == lane) d = probe_seg(pv.buckets, pv.nmain, pv.nover, key, &o, err);
+    r_off = __shfl_sync(WK_FULL_MASK, o, lead);
+    r_deg = __shfl_sync(WK_FULL_MASK, d, lead);
+}
+
+}  // namespace dev
+}  // namespace wk

@@ -65,7 +65,7 @@ DeviceStore::~DeviceStore() {
 static inline uint64_t align256(uint64_t x) { return (x + 255) & ~(uint64_t)255; }
 
 int DeviceStore::upload_resident() {
-    const uint64_t bbytes = hs->total_slots * 16, ebytes = hs->total_edges * 4;
+    const uint64_t bbytes = hs->total_buckets * sizeof(Bucket), ebytes = hs->total_edges * 4;
     cudaError_t e;
     if ((e = cudaMalloc(&d_buckets, bbytes ? bbytes : 16)) != cudaSuccess) { d_buckets = nullptr; return cuda_fail(e, "store upload (buckets)"); }
     if ((e = cudaMalloc(&d_edges, ebytes ? ebytes : 16)) != cudaSuccess) { d_edges = nullptr; return cuda_fail(e, "store upload (edges)"); }
@@ -76,7 +76,7 @@ int DeviceStore::upload_resident() {
     views.assign((size_t)hs->num_ids + 1, PredView{nullptr, nullptr, 0, 0});
     for (int id = 1; id <= hs->num_ids; ++id) {
         const PredSeg &sg = hs->segs[(size_t)id];
-        views[(size_t)id] = PredView{reinterpret_cast<const uint4 *>(d_buckets) + sg.bucket_off,
+        views[(size_t)id] = PredView{static_cast<const Bucket *>(d_buckets) + sg.bucket_off,
                                      d_edges + sg.edge_off, sg.nmain, sg.nover};
     }
     device_bytes = bbytes + ebytes;
@@ -189,7 +189,7 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
     }
     char *base = static_cast<char *>(pool) + off;
     const uint64_t bb = sg.bucket_bytes(), eb = sg.edge_bytes();
-    if (bb && (e = cudaMemcpyAsync(base, hs->buckets + sg.bucket_off * 4, bb, cudaMemcpyHostToDevice, copy_st)) != cudaSuccess)
+    if (bb && (e = cudaMemcpyAsync(base, hs->buckets + sg.bucket_off, bb, cudaMemcpyHostToDevice, copy_st)) != cudaSuccess)
         return cuda_fail(e, "segment cache copy (buckets)");
     char *ebase = base + align256(bb);
     if (eb && (e = cudaMemcpyAsync(ebase, hs->edges + sg.edge_off, eb, cudaMemcpyHostToDevice, copy_st)) != cudaSuccess)
@@ -205,7 +205,7 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
     r.off = off;
     r.bytes = need;
     r.last_use = clock;
-    views[(size_t)id] = PredView{reinterpret_cast<const uint4 *>(base), reinterpret_cast<const int32_t *>(ebase),
+    views[(size_t)id] = PredView{reinterpret_cast<const Bucket *>(base), reinterpret_cast<const int32_t *>(ebase),
                                  sg.nmain, sg.nover};
     ++loads;
     bytes_loaded += bb + eb;
@@ -360,7 +360,7 @@ extern "C" int wk_store_get_info(wk_ctx *ctx, wk_store_info *info) {
     const HostStore *hs = ctx->store->hs.get();
     info->num_keys = (int64_t)hs->total_keys;
     info->num_edges = (int64_t)hs->total_edges;
-    info->key_bytes = (int64_t)hs->total_slots * 16;
+    info->key_bytes = (int64_t)(hs->total_buckets * sizeof(Bucket));
     info->edge_bytes = (int64_t)hs->total_edges * 4;
     info->overflow_buckets = (int64_t)hs->total_over;
     info->device_bytes = (int64_t)ctx->store->device_bytes;

@@ -12,15 +12,17 @@
 //    subjects of p, [0|p|OUT] -> objects of p (record_index_info,
 //    core/gstore.hpp:835-870, insert_type_index_map / insert_index_map
 //    :460-524).
-// The layout is this library's own: per id, a bucket array of 8 x 16 B slots
-// (7 data slots + 1 overflow link) sized for a load of at most 1/2, followed by
-// overflow buckets, and one contiguous int32 edge segment holding the id's
-// out-lists, in-lists and index lists.
+// The layout is this library's own: per id, a hash table of 64 B buckets
+// (5 slots of 32-bit segment-local keys + 1 overflow link) sized for a load of
+// at most 1/2, followed by overflow buckets, and one contiguous int32 edge
+// segment holding the id's out-lists, in-lists and index lists.
 #include "wk_internal.h"
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
+#include <cstdlib>
 #include <atomic>
 #include <cstring>
 #include <thread>
@@ -39,24 +41,22 @@ HostStore::~HostStore() {
 
 uint64_t HostStore::lookup(uint64_t vid, uint32_t pid, uint32_t dir, const int32_t **edges_out) const {
     *edges_out = nullptr;
-    if (pid < 1 || (int32_t)pid > num_ids) return 0;
+    if (pid < 1 || (int32_t)pid > num_ids || vid >= 0x7fffffffull || dir > 1u) return 0;
     const PredSeg &sg = segs[pid];
     if (sg.nmain == 0) return 0;
-    const uint64_t key = make_key(vid, pid, dir);
-    uint32_t b = bucket_of(key_mix(key), sg.nmain);
-    const uint32_t *base = buckets + sg.bucket_off * 4;
+    const uint32_t key = seg_key((uint32_t)vid, dir);
+    uint32_t b = seg_bucket(key, sg.nmain);
+    const Bucket *base = buckets + sg.bucket_off;
     for (uint32_t hop = 0; hop <= sg.nover; ++hop) {
-        const uint32_t *bk = base + (uint64_t)b * WK_SLOTS_PER_BUCKET * 4;
+        const uint32_t *w = base[b].w;
         for (int i = 0; i < WK_DATA_SLOTS; ++i) {
-            uint64_t k = (uint64_t)bk[i * 4] | ((uint64_t)bk[i * 4 + 1] << 32);
-            if (k == key) {
-                *edges_out = edges + sg.edge_off + bk[i * 4 + 2];
-                return bk[i * 4 + 3];
+            if (w[i] == key) {
+                *edges_out = edges + sg.edge_off + w[WK_OFF_WORD + i];
+                return w[WK_DEG_WORD + i];
             }
         }
-        const uint32_t *link = bk + WK_DATA_SLOTS * 4;
-        if (!(link[1] & WK_LINK_TAG)) return 0;
-        b = link[0];
+        if (w[WK_LINK_WORD] == WK_NO_LINK || w[WK_LINK_WORD] >= sg.nmain + sg.nover) return 0;
+        b = w[WK_LINK_WORD];
     }
     return 0;
 }
@@ -64,7 +64,7 @@ uint64_t HostStore::lookup(uint64_t vid, uint32_t pid, uint32_t dir, const int32
 namespace {
 
 struct KeyRec {       // one key of a segment before insertion
-    uint64_t key;
+    uint32_t key;     // seg_key(vid, dir)
     uint32_t off;     // offset in the segment's edge list
     uint32_t deg;
 };
@@ -77,7 +77,7 @@ struct SegBuild {
 
 // Sort (hi,lo) pairs packed as hi<<32|lo, dedup, and emit one key per hi
 // group with the group's lo values as the adjacency list.
-void emit_groups(std::vector<uint64_t> &pairs, uint32_t pid, uint32_t dir, SegBuild &sb,
+void emit_groups(std::vector<uint64_t> &pairs, uint32_t dir, SegBuild &sb,
                  std::vector<int32_t> *distinct_hi) {
     std::sort(pairs.begin(), pairs.end());
     pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
@@ -86,7 +86,7 @@ void emit_groups(std::vector<uint64_t> &pairs, uint32_t pid, uint32_t dir, SegBu
         uint32_t hi = (uint32_t)(pairs[i] >> 32);
         size_t j = i;
         KeyRec kr;
-        kr.key = make_key(hi, pid, dir);
+        kr.key = seg_key(hi, dir);
         kr.off = (uint32_t)sb.edges.size();
         while (j < n && (uint32_t)(pairs[j] >> 32) == hi) {
             sb.edges.push_back((int32_t)(uint32_t)pairs[j]);
@@ -99,10 +99,10 @@ void emit_groups(std::vector<uint64_t> &pairs, uint32_t pid, uint32_t dir, SegBu
     }
 }
 
-void add_index(uint32_t pid, uint32_t dir, const std::vector<int32_t> &list, SegBuild &sb) {
+void add_index(uint32_t dir, const std::vector<int32_t> &list, SegBuild &sb) {
     if (list.empty()) return;
     KeyRec kr;
-    kr.key = make_key(0, pid, dir);
+    kr.key = seg_key(0, dir);
     kr.off = (uint32_t)sb.edges.size();
     kr.deg = (uint32_t)list.size();
     sb.edges.insert(sb.edges.end(), list.begin(), list.end());
@@ -139,14 +139,16 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         if (pi < 1 || pi > num_ids)
             return set_error(WK_EINVAL, "store build: triple %lld has predicate %d outside [1,%d]",
                              (long long)i, pi, num_ids);
-        if (s[i] < WK_VID_BASE)
-            return set_error(WK_EINVAL, "store build: triple %lld has subject %d below 2^17", (long long)i, s[i]);
+        if (s[i] < WK_VID_BASE || s[i] == INT32_MAX)
+            return set_error(WK_EINVAL, "store build: triple %lld has subject %d outside [2^17, 2^31-1)",
+                             (long long)i, s[i]);
         if (pi == WK_TYPE_ID) {
             if (o[i] < 2 || o[i] > num_ids)
                 return set_error(WK_EINVAL, "store build: type triple %lld has class %d outside [2,%d]",
                                  (long long)i, o[i], num_ids);
-        } else if (o[i] < WK_VID_BASE) {
-            return set_error(WK_EINVAL, "store build: triple %lld has object %d below 2^17", (long long)i, o[i]);
+        } else if (o[i] < WK_VID_BASE || o[i] == INT32_MAX) {
+            return set_error(WK_EINVAL, "store build: triple %lld has object %d outside [2^17, 2^31-1)",
+                             (long long)i, o[i]);
         }
         cnt[(size_t)pi]++;
     }
@@ -165,7 +167,7 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
     {
         const int64_t a = start[WK_TYPE_ID], b = start[WK_TYPE_ID + 1];
         std::vector<uint64_t> out_pairs(so.begin() + a, so.begin() + b);
-        emit_groups(out_pairs, WK_TYPE_ID, WK_DIR_OUT, sb[WK_TYPE_ID], nullptr);
+        emit_groups(out_pairs, WK_DIR_OUT, sb[WK_TYPE_ID], nullptr);
         sb[WK_TYPE_ID].triples = (int64_t)out_pairs.size();
         sb[WK_TYPE_ID].subjects = (int64_t)sb[WK_TYPE_ID].keys.size();
         std::vector<uint64_t> cs;
@@ -181,17 +183,17 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         if (id != WK_TYPE_ID && cnt[id] > 0) {
             std::vector<uint64_t> pairs(so.begin() + start[id], so.begin() + start[id + 1]);
             std::vector<int32_t> subjects, objects;
-            emit_groups(pairs, (uint32_t)id, WK_DIR_OUT, b, &subjects);
+            emit_groups(pairs, WK_DIR_OUT, b, &subjects);
             b.triples = (int64_t)pairs.size();
             for (auto &x : pairs) x = ((x & 0xffffffffull) << 32) | (x >> 32);
-            emit_groups(pairs, (uint32_t)id, WK_DIR_IN, b, &objects);
-            add_index((uint32_t)id, WK_DIR_IN, subjects, b);    // [0|p|IN]  subjects of p
-            add_index((uint32_t)id, WK_DIR_OUT, objects, b);    // [0|p|OUT] objects of p
+            emit_groups(pairs, WK_DIR_IN, b, &objects);
+            add_index(WK_DIR_IN, subjects, b);    // [0|p|IN]  subjects of p
+            add_index(WK_DIR_OUT, objects, b);    // [0|p|OUT] objects of p
             b.subjects = (int64_t)subjects.size();
             b.objects = (int64_t)objects.size();
         }
         if (!class_members[id].empty()) {                    // [0|c|IN] members of c
-            add_index((uint32_t)id, WK_DIR_IN, class_members[id], b);
+            add_index(WK_DIR_IN, class_members[id], b);
             b.subjects += (int64_t)class_members[id].size();
             b.triples += (int64_t)class_members[id].size();
         }
@@ -202,7 +204,7 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
     HostStore *hs = new HostStore();
     hs->num_ids = num_ids;
     hs->segs.resize((size_t)num_ids + 1);
-    uint64_t slot_at = 0, edge_at = 0;
+    uint64_t bucket_at = 0, edge_at = 0;
     for (size_t id = 1; id <= (size_t)num_ids; ++id) {
         PredSeg &sg = hs->segs[id];
         SegBuild &b = sb[id];
@@ -213,20 +215,23 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
             delete hs;
             return set_error(WK_EINVAL, "store build: id %zu has more than 2^32 edge entries", id);
         }
-        // main buckets: keys / (7 * 0.5), at least one bucket when there are keys;
-        // overflow room: worst case one bucket per 7 keys beyond the first
-        uint64_t nm = sg.nkeys ? (sg.nkeys * 2 + WK_DATA_SLOTS - 1) / WK_DATA_SLOTS : 0;
-        if (nm > 0x7fffffffull) { delete hs; return set_error(WK_EINVAL, "store build: id %zu too many keys", id); }
+        // main buckets: keys / (5 * 0.5), at least one bucket when there are keys;
+        // overflow room: worst case one bucket per 5 keys beyond the first
+        const uint64_t nm = sg.nkeys ? (sg.nkeys * 2 + WK_DATA_SLOTS - 1) / WK_DATA_SLOTS : 0;
+        if (nm + sg.nkeys / WK_DATA_SLOTS + 1 >= 0xffffffffull) {
+            delete hs;
+            return set_error(WK_EINVAL, "store build: id %zu has too many keys", id);
+        }
         sg.nmain = (uint32_t)nm;
-        sg.bucket_off = slot_at;
+        sg.bucket_off = bucket_at;
         sg.edge_off = edge_at;
-        slot_at += (uint64_t)(sg.nmain + sg.nkeys / WK_DATA_SLOTS + 1) * WK_SLOTS_PER_BUCKET;
+        if (sg.nkeys) bucket_at += nm + sg.nkeys / WK_DATA_SLOTS + 1;
         edge_at += sg.nedges;
     }
     // reserve the upper bound, compact after insertion
-    uint64_t slot_cap = slot_at ? slot_at : 8;
-    uint64_t edge_cap = edge_at ? edge_at : 1;
-    uint32_t *bk_tmp = (uint32_t *)calloc(slot_cap, 16);
+    const uint64_t bucket_cap = bucket_at ? bucket_at : 1;
+    const uint64_t edge_cap = edge_at ? edge_at : 1;
+    Bucket *bk_tmp = static_cast<Bucket *>(malloc(bucket_cap * sizeof(Bucket)));
     if (!bk_tmp) { delete hs; return set_error(WK_ENOMEM, "store build: out of host memory"); }
 
     // insertion per id in parallel: cluster chaining with a per-id overflow area
@@ -235,25 +240,34 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         if (id == 0) return;
         PredSeg &sg = hs->segs[id];
         if (!sg.nkeys) return;
-        uint32_t *base = bk_tmp + sg.bucket_off * 4;
+        Bucket *base = bk_tmp + sg.bucket_off;
+        const uint64_t cap = (uint64_t)sg.nmain + sg.nkeys / WK_DATA_SLOTS + 1;
+        for (uint64_t i = 0; i < cap; ++i) {
+            uint32_t *w = base[i].w;
+            for (int j = 0; j < WK_DATA_SLOTS; ++j) {
+                w[j] = WK_EMPTY_KEY;
+                w[WK_OFF_WORD + j] = 0u;
+                w[WK_DEG_WORD + j] = 0u;
+            }
+            w[WK_LINK_WORD] = WK_NO_LINK;
+        }
         uint32_t used_over = 0;
         for (const KeyRec &kr : sb[id].keys) {
-            uint32_t b = bucket_of(key_mix(kr.key), sg.nmain);
+            uint32_t b = seg_bucket(kr.key, sg.nmain);
             for (;;) {
-                uint32_t *bk = base + (uint64_t)b * WK_SLOTS_PER_BUCKET * 4;
+                uint32_t *w = base[b].w;
                 int free_slot = -1;
                 for (int i = 0; i < WK_DATA_SLOTS; ++i)
-                    if (bk[i * 4] == 0 && bk[i * 4 + 1] == 0) { free_slot = i; break; }
+                    if (w[i] == WK_EMPTY_KEY) { free_slot = i; break; }
                 if (free_slot >= 0) {
-                    uint32_t *sl = bk + free_slot * 4;
-                    sl[0] = (uint32_t)kr.key; sl[1] = (uint32_t)(kr.key >> 32);
-                    sl[2] = kr.off; sl[3] = kr.deg;
+                    w[free_slot] = kr.key;
+                    w[WK_OFF_WORD + free_slot] = kr.off;
+                    w[WK_DEG_WORD + free_slot] = kr.deg;
                     break;
                 }
-                uint32_t *link = bk + WK_DATA_SLOTS * 4;
-                if (link[1] & WK_LINK_TAG) { b = link[0]; continue; }
-                uint32_t nb = sg.nmain + used_over++;
-                link[0] = nb; link[1] = WK_LINK_TAG;
+                if (w[WK_LINK_WORD] != WK_NO_LINK) { b = w[WK_LINK_WORD]; continue; }
+                const uint32_t nb = sg.nmain + used_over++;
+                w[WK_LINK_WORD] = nb;
                 b = nb;
             }
         }
@@ -261,45 +275,46 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
     });
 
     // compact: final bucket offsets and copy into the (pinned if possible) image
-    uint64_t total_slots = 0;
+    uint64_t total_buckets = 0;
     for (size_t id = 1; id <= (size_t)num_ids; ++id) {
         PredSeg &sg = hs->segs[id];
         sg.nover = nover[id];
-        total_slots += (uint64_t)(sg.nmain + sg.nover) * WK_SLOTS_PER_BUCKET;
+        total_buckets += (uint64_t)sg.nmain + sg.nover;
     }
+    const uint64_t bbytes = (total_buckets ? total_buckets : 1) * sizeof(Bucket);
     void *bp = nullptr, *ep = nullptr;
-    bool pinned = cudaHostAlloc(&bp, (total_slots ? total_slots : 8) * 16, cudaHostAllocPortable) == cudaSuccess &&
+    bool pinned = cudaHostAlloc(&bp, bbytes, cudaHostAllocPortable) == cudaSuccess &&
                   cudaHostAlloc(&ep, edge_cap * 4, cudaHostAllocPortable) == cudaSuccess;
     if (!pinned) {
         cudaGetLastError();
         if (bp) cudaFreeHost(bp);
         if (ep) cudaFreeHost(ep);
-        bp = malloc((total_slots ? total_slots : 8) * 16);
+        bp = aligned_alloc(WK_BUCKET_BYTES, bbytes);
         ep = malloc(edge_cap * 4);
         if (!bp || !ep) { free(bp); free(ep); free(bk_tmp); delete hs;
                           return set_error(WK_ENOMEM, "store build: out of host memory"); }
     }
     hs->pinned = pinned;
-    hs->buckets = (uint32_t *)bp;
+    hs->buckets = static_cast<Bucket *>(bp);
     hs->edges = (int32_t *)ep;
     std::vector<uint64_t> new_off((size_t)num_ids + 1, 0);
     uint64_t at = 0;
     for (size_t id = 1; id <= (size_t)num_ids; ++id) {
         new_off[id] = at;
-        at += (uint64_t)(hs->segs[id].nmain + hs->segs[id].nover) * WK_SLOTS_PER_BUCKET;
+        at += (uint64_t)hs->segs[id].nmain + hs->segs[id].nover;
     }
     parallel_for((size_t)num_ids + 1, [&](size_t id) {
         if (id == 0) return;
         PredSeg &sg = hs->segs[id];
-        uint64_t nsl = (uint64_t)(sg.nmain + sg.nover) * WK_SLOTS_PER_BUCKET;
-        if (nsl) std::memcpy(hs->buckets + new_off[id] * 4, bk_tmp + sg.bucket_off * 4, nsl * 16);
+        const uint64_t nb = (uint64_t)sg.nmain + sg.nover;
+        if (nb) std::memcpy(hs->buckets + new_off[id], bk_tmp + sg.bucket_off, nb * sizeof(Bucket));
         sg.bucket_off = new_off[id];
         if (sg.nedges) std::memcpy(hs->edges + sg.edge_off, sb[id].edges.data(), sg.nedges * 4);
         std::vector<KeyRec>().swap(sb[id].keys);
         std::vector<int32_t>().swap(sb[id].edges);
     });
     free(bk_tmp);
-    hs->total_slots = total_slots;
+    hs->total_buckets = total_buckets;
     hs->total_edges = edge_at;
     for (size_t id = 1; id <= (size_t)num_ids; ++id) {
         hs->total_keys += hs->segs[id].nkeys;
