@@ -153,14 +153,16 @@ int wk_const_to_unknown(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direc
  * or under a fixed device budget, a serving thread that must never enter
  * cudaMalloc/cudaFree).  No counterpart in the reference.  The caller passes
  * the input history (device, rows x cols int32) and an output buffer it owns
- * (out_capacity int32 elements); *out_rows receives the output row count
+ * (out_capacity int32 elements, 16 B aligned; hist 4 B aligned, else
+ * WK_EINVAL); *out_rows receives the output row count
  * (also when the output does not fit: WK_EOVERFLOW).  The call allocates
  * nothing: its scratch is one fixed device array inside the library (about
- * 6.4 MB, held by every GPU that loads the library until exit).  Limits: at
- * most 262,144 input rows and 16,777,216 output rows per call; needs a
- * resident (unpaged) store.  Every call shares that array, so calls that
- * overlap on the GPU race; the first call on a device looks the array up and
- * should precede any stream capture.  Returns after the output is written. */
+ * 2.1 MB, held by every GPU that loads the library until exit).  Limits: at
+ * most 262,144 input rows per call; the output is bounded by out_capacity;
+ * needs a resident (unpaged) store.  Every call shares that array, so calls
+ * that overlap on the GPU race; the first call on a device looks the array up
+ * and should precede any stream capture.  Returns after the output is
+ * written. */
 int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int64_t rows, int32_t cols,
                                 int64_t start, int32_t direction, int32_t predict,
                                 int32_t *out, int64_t out_capacity, int64_t *out_rows);

@@ -59,7 +59,7 @@ def _random_history(rng, verts, R, C, miss_frac=0.3):
 
 
 @pytest.mark.parametrize("R", [1, 31, 33, 1023, 1025, 4097, 70_001])
-@pytest.mark.parametrize("C", [1, 3, 8])
+@pytest.mark.parametrize("C", [1, 2, 3, 4, 5, 6, 7, 8])   # every specialised output width, and one above
 def test_k2u_random_histories(gpu_small, small_graph, small_oracle, R, C):
     g, s, p, o = small_graph
     rng = np.random.default_rng(R * 7 + C)
@@ -186,7 +186,7 @@ def test_high_degree_and_wide_tables(lib_built):
 
 def test_paged_segment_cache_gives_same_rows(small_graph, small_oracle, golden_small):
     g, s, p, o = small_graph
-    rc = W.RCache(device=0, cache_budget_mb=20)   # the store is ~47 MB: evictions happen
+    rc = W.RCache(device=0, cache_budget_mb=20)   # the store is ~37 MB: evictions happen
     rc.build_store_graph(g)
     assert rc.store_info()["paged"] == 1
     for q in golden_small["queries"]:
@@ -205,5 +205,5 @@ def test_kernel_launch_count_and_timing(gpu_small, golden_small):
     st = gpu_small.last_op_stats()
     gpu_small.enable_timing(False)
     assert gpu_small.kernel_launches() > before
-    assert st["kernels"] == 4 and st["ms"] > 0 and st["ms_main"] > 0
+    assert st["kernels"] == 2 and st["ms"] > 0 and st["ms_main"] > 0   # k2u: count + expand
     assert st["rows_out"] == q["rows"]

@@ -84,3 +84,20 @@ def test_noalloc_rejects_oversize_and_small_output(setup):
     out_owner.upload_history(small, np.zeros((8, 1), np.int32))
     st, nrows = _noalloc(rc, req.hist.data, 1000, 2, -1, W.OUT, 2, small.hist.data, 8)
     assert st == W.WK_EOVERFLOW and nrows > 2
+
+
+def test_noalloc_rejects_unaligned_buffers(setup):
+    """Output rows are written as 16 B vectors: an output pointer off a 16 B
+    boundary (and a history pointer off a 4 B boundary) is refused on the host,
+    before any kernel runs."""
+    g, s, rc, out_owner = setup
+    req = W.Request([])
+    rc.upload_history(req, _history(s, 100, 2, 5))
+    dst = W.Request([])
+    out_owner.upload_history(dst, np.zeros((4096, 1), np.int32))
+    base = C.cast(dst.hist.data, C.c_void_p).value
+    hbase = C.cast(req.hist.data, C.c_void_p).value
+    st, _ = _noalloc(rc, req.hist.data, 100, 2, -1, W.OUT, 2, C.cast(C.c_void_p(base + 4), W._I32P), 4000)
+    assert st == W.WK_EINVAL and b"aligned" in W.load_library().wk_last_error()
+    st, _ = _noalloc(rc, C.cast(C.c_void_p(hbase + 2), W._I32P), 99, 2, -1, W.OUT, 2, dst.hist.data, 4096)
+    assert st == W.WK_EINVAL and b"aligned" in W.load_library().wk_last_error()

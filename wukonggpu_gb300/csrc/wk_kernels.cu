@@ -4,8 +4,18 @@
 // probe, then streaming reads of history/adjacency and streaming writes of the
 // new table.  No tensor cores are involved.
 //
-//   k2u : probe (+ per-block sums) -> block scan -> compact -> tiled write
-//   k2k/k2c : probe + membership (ballot masks) -> block scan -> filtered copy
+//   k2u     : count (probe; per-row degree and edge offset; per-block output
+//             count; op total) -> the host reads the total and sizes the
+//             output -> expand (per input block: local scan, output prefix by
+//             look-back, rows written)
+//   k2k/k2c : probe + membership (per-row ballot masks; per-block count; op
+//             total) -> filtered copy (per input block: output prefix by
+//             look-back, selected rows copied)
+//
+// The look-back never waits: the first kernel of an op has written every
+// block's count before the second kernel starts, so a block finds its output
+// prefix by adding its predecessors' counts back to the nearest predecessor
+// that has already published its inclusive prefix (or back to block 0).
 //
 // Result order equals the reference CPU engine's (core/engine.hpp:126-225):
 // output rows follow input row order, and for k2u each input row's block of
@@ -43,16 +53,61 @@ __device__ __forceinline__ void block_sum2(unsigned long long &a, unsigned int &
     }
 }
 
-// ----------------------------------------------------------------- k2u probe
+// ------------------------------------------------------------- look-back
+constexpr unsigned long long kPrefixReady = 1ull << 63;
+
+__device__ __forceinline__ unsigned long long ld_flag(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_flag(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Exclusive output prefix of block b: the sum of agg[0..b).  flags[k] is
+// kPrefixReady | (inclusive prefix of block k) once block k has published it,
+// else 0 (cleared by the op's first kernel).  Called by one full warp, which
+// reads 32 predecessors per step and stops at the nearest published one.  It
+// never waits on another block, so it ends after at most b / 32 steps.
+template <typename A>
+__device__ __forceinline__ unsigned long long lookback_prefix(const A *__restrict__ agg,
+                                                              const unsigned long long *flags, int64_t b) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long acc = 0;
+    for (int64_t i = b - 1; i >= 0; i -= 32) {
+        const int64_t k = i - lane;
+        unsigned long long f = 0ull, a = 0ull;
+        if (k >= 0) {
+            f = ld_flag(flags + k);
+            a = (unsigned long long)agg[k];
+        }
+        const unsigned ready = __ballot_sync(FULL, (f & kPrefixReady) != 0ull);
+        if (ready) {
+            const int L = __ffs(ready) - 1;   // nearest published predecessor
+            acc += warp_sum(lane < L ? a : (lane == L ? (f & ~kPrefixReady) : 0ull));
+            return acc;
+        }
+        acc += warp_sum(a);
+    }
+    return acc;
+}
+
+// --------------------------------------------------------------- k2u count
 // A warp owns kRounds * 32 consecutive rows.  Their start vertices are loaded
 // first (kRounds independent coalesced loads), then each round of 32 rows is
 // probed, so the history read does not sit in front of every bucket read.
 constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
 
+// totals[0] += output rows, totals[1] += rows with a match; err bit 1 when a
+// block's output count reaches 2^32 (the expansion keeps block-local
+// positions in 32 bits).
 __global__ void __launch_bounds__(kThreads)
-k2u_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
+k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
                  uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
-                 unsigned long long *__restrict__ blk_sum, unsigned int *__restrict__ blk_nz, int *err) {
+                 unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ flags,
+                 unsigned long long *__restrict__ totals, int *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t wrow0 = (int64_t)blockIdx.x * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
     int32_t v[kRounds];
@@ -80,7 +135,184 @@ k2u_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
     block_sum2(my_sum, my_nz);
     if (threadIdx.x == 0) {
         blk_sum[blockIdx.x] = my_sum;
-        blk_nz[blockIdx.x] = my_nz;
+        flags[blockIdx.x] = 0ull;
+        if (my_sum) atomicAdd(totals, my_sum);
+        if (my_nz) atomicAdd(totals + 1, (unsigned long long)my_nz);
+        if (my_sum >> 32) atomicOr(err, 2);
+    }
+}
+
+// -------------------------------------------------------------- k2u expand
+// last row i in [0, n) with pos[i] <= j; pos is non-decreasing with pos[0] = 0,
+// so for j below the block's total that row has a non-empty list
+__device__ __forceinline__ int row_of(const uint32_t *pos, int n, uint32_t j) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pos[mid] <= j) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Output rows gb..gb+3 (gb a multiple of 4) of those in [P, gend): row
+// g = P + j copies input row i (the one whose list covers j) and appends
+// entry j - pos[i] of its list.  A whole group is W 16 B stores (4 rows of W
+// words); the first and last group of a block may be partial.
+template <int W, bool STAGED>
+__device__ __forceinline__ void k2u_write_group(unsigned long long gb, unsigned long long P,
+                                                unsigned long long gend, const uint32_t *pos,
+                                                const uint32_t *eoff, int n, const int32_t *rows,
+                                                const int32_t *__restrict__ edges, int32_t *__restrict__ out) {
+    constexpr int C = W - 1;
+    int i = row_of(pos, n, gb >= P ? (uint32_t)(gb - P) : 0u);
+    uint32_t nxt = pos[i + 1];
+    int32_t v[4 * W];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const unsigned long long g = gb + q;
+        if (g >= P && g < gend) {
+            const uint32_t j = (uint32_t)(g - P);
+            while (j >= nxt) nxt = pos[++i + 1];
+            const int32_t *src = rows + i * C;
+#pragma unroll
+            for (int c = 0; c < C; ++c) v[q * W + c] = STAGED ? src[c] : __ldg(src + c);
+            v[q * W + C] = __ldg(edges + (eoff[i] + (j - pos[i])));
+        } else {
+#pragma unroll
+            for (int c = 0; c < W; ++c) v[q * W + c] = 0;
+        }
+    }
+    int32_t *g = out + gb * W;
+    if (gb >= P && gb + 4 <= gend) {
+#pragma unroll
+        for (int k = 0; k < W; ++k)
+            reinterpret_cast<int4 *>(g)[k] = make_int4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (gb + q >= P && gb + q < gend) {
+#pragma unroll
+                for (int c = 0; c < W; ++c) g[q * W + c] = v[q * W + c];
+            }
+    }
+}
+
+// One CTA per block of kRowsPerBlock input rows; it writes that block's output
+// rows.  W = C + 1 output columns for 2 <= W <= 8; W = 0 for any width (rows
+// read from global memory, one output row per thread and step).  When at least
+// a quarter of the block's rows expand, their history rows are first copied
+// to shared memory with 16 B loads.
+template <int W>
+__global__ void __launch_bounds__(kThreads)
+k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const int32_t *__restrict__ edges,
+                  const uint32_t *__restrict__ deg, const uint32_t *__restrict__ off,
+                  const unsigned long long *__restrict__ blk_sum, unsigned long long *flags,
+                  int32_t *__restrict__ out) {
+    constexpr int kRPT = kRowsPerBlock / kThreads;
+    static_assert(kRPT == 4, "4 input rows per thread");
+    constexpr int kSC = W >= 2 ? W - 1 : 1;
+    __shared__ uint32_t pos[kRowsPerBlock + 1];
+    __shared__ uint32_t eoff[kRowsPerBlock];
+    __shared__ __align__(16) int32_t hrow[W >= 2 ? kRowsPerBlock * kSC : 4];
+    __shared__ uint32_t s_w[kThreads / 32], s_z[kThreads / 32];
+    __shared__ unsigned long long s_P;
+    const int C = W >= 2 ? W - 1 : C_rt;
+    const int64_t b = blockIdx.x;
+    const unsigned long long Tb = blk_sum[b];
+    if (Tb == 0ull) return;   // no output; successors add this block's count (0) as they walk past
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const int64_t r0 = b * kRowsPerBlock;
+    const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
+
+    // 1. the block's degrees and edge offsets, 4 rows per thread; local exclusive scan
+    const int q0 = t * kRPT;
+    uint32_t d[kRPT], o[kRPT];
+    if (q0 + kRPT <= n) {
+        const uint4 dv = *reinterpret_cast<const uint4 *>(deg + r0 + q0);
+        const uint4 ov = *reinterpret_cast<const uint4 *>(off + r0 + q0);
+        d[0] = dv.x; d[1] = dv.y; d[2] = dv.z; d[3] = dv.w;
+        o[0] = ov.x; o[1] = ov.y; o[2] = ov.z; o[3] = ov.w;
+    } else {
+#pragma unroll
+        for (int q = 0; q < kRPT; ++q) {
+            d[q] = q0 + q < n ? deg[r0 + q0 + q] : 0u;
+            o[q] = q0 + q < n ? off[r0 + q0 + q] : 0u;
+        }
+    }
+    uint32_t ls = 0, lz = 0;
+#pragma unroll
+    for (int q = 0; q < kRPT; ++q) {
+        ls += d[q];
+        lz += d[q] != 0u;
+    }
+    uint32_t is = ls;
+#pragma unroll
+    for (int sh = 1; sh < 32; sh <<= 1) {
+        const uint32_t x = __shfl_up_sync(FULL, is, sh);
+        if (lane >= sh) is += x;
+    }
+    const uint32_t wz = warp_sum(lz);
+    if (lane == 31) s_w[wid] = is;
+    if (lane == 0) s_z[wid] = wz;
+    __syncthreads();
+    uint32_t base = 0, nzb = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+        if (w < wid) base += s_w[w];
+        nzb += s_z[w];
+    }
+    uint32_t e = base + is - ls;
+#pragma unroll
+    for (int q = 0; q < kRPT; ++q) {
+        pos[q0 + q] = e;
+        eoff[q0 + q] = o[q];
+        e += d[q];
+    }
+    if (t == kThreads - 1) pos[kRowsPerBlock] = e;   // the block's total; rows >= n have no list
+
+    // 2. history rows of the block, when enough of them expand
+    const bool staged = W >= 2 && nzb * 4u >= (uint32_t)n;
+    const int32_t *hblk = hist + r0 * C;
+    if (W >= 2 && staged) {
+        const int nw = n * C;
+        if ((reinterpret_cast<uintptr_t>(hblk) & 15u) == 0) {
+            const int nv = nw >> 2;
+            for (int x = t; x < nv; x += kThreads)
+                reinterpret_cast<int4 *>(hrow)[x] = __ldg(reinterpret_cast<const int4 *>(hblk) + x);
+            for (int x = (nv << 2) + t; x < nw; x += kThreads) hrow[x] = __ldg(hblk + x);
+        } else {
+            for (int x = t; x < nw; x += kThreads) hrow[x] = __ldg(hblk + x);
+        }
+    }
+
+    // 3. output prefix of the block (warp 0), published for the blocks after it
+    if (wid == 0) {
+        const unsigned long long P = lookback_prefix(blk_sum, flags, b);
+        if (lane == 0) {
+            st_flag(flags + b, kPrefixReady | (P + Tb));
+            s_P = P;
+        }
+    }
+    __syncthreads();
+    const unsigned long long P = s_P, gend = P + Tb;
+
+    // 4. output rows [P, P + Tb)
+    if constexpr (W >= 2) {
+        for (unsigned long long gb = (P & ~3ull) + 4ull * t; gb < gend; gb += 4ull * kThreads) {
+            if (staged) k2u_write_group<W, true>(gb, P, gend, pos, eoff, n, hrow, edges, out);
+            else k2u_write_group<W, false>(gb, P, gend, pos, eoff, n, hblk, edges, out);
+        }
+    } else {
+        const int Wd = C + 1;
+        for (unsigned long long g = P + t; g < gend; g += kThreads) {
+            const uint32_t j = (uint32_t)(g - P);
+            const int i = row_of(pos, n, j);
+            int32_t *dst = out + g * Wd;
+            const int32_t *src = hblk + (int64_t)i * C;
+            for (int c = 0; c < C; ++c) dst[c] = __ldg(src + c);
+            dst[C] = __ldg(edges + (eoff[i] + (j - pos[i])));
+        }
     }
 }
 
@@ -102,11 +334,12 @@ __device__ __forceinline__ bool list_contains(const int32_t *__restrict__ e, uin
     return f;
 }
 
+// totals[0] += adjacency entries a linear scan would touch, totals[1] += rows kept
 __global__ void __launch_bounds__(kThreads)
 filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, int ecol,
                     int32_t end_const, uint32_t dir, PredView pv,
-                    uint32_t *__restrict__ mask, unsigned long long *__restrict__ blk_sum,
-                    unsigned int *__restrict__ blk_nz, int *err) {
+                    uint32_t *__restrict__ mask, unsigned int *__restrict__ blk_nz,
+                    unsigned long long *__restrict__ flags, unsigned long long *__restrict__ totals, int *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t wrow0 = (int64_t)blockIdx.x * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
     int32_t v[kRounds], tg[kRounds];
@@ -117,7 +350,7 @@ filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol
         tg[rd] = (r < R && ecol >= 0) ? __ldg(hist + r * C + ecol) : end_const;
     }
     unsigned int my_nz = 0;
-    unsigned long long my_scan = 0;   // adjacency entries a linear scan would touch
+    unsigned long long my_scan = 0;
 #pragma unroll
     for (int rd = 0; rd < kRounds; ++rd) {
         const int64_t row0 = wrow0 + rd * 32;
@@ -139,189 +372,28 @@ filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol
     }
     block_sum2(my_scan, my_nz);
     if (threadIdx.x == 0) {
-        blk_sum[blockIdx.x] = my_scan;
         blk_nz[blockIdx.x] = my_nz;
-    }
-}
-
-// ------------------------------------------------------------ block scan
-// One block: exclusive scan of n (u64, u32) pairs in place.
-__global__ void __launch_bounds__(1024)
-scan_blocks_kernel(unsigned long long *__restrict__ s, unsigned int *__restrict__ z, int64_t n,
-                   unsigned long long *__restrict__ totals, unsigned long long *__restrict__ cz_pos) {
-    __shared__ unsigned long long ws[32];
-    __shared__ unsigned int wz[32];
-    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    const int64_t per = (n + 1023) / 1024;
-    const int64_t a = (int64_t)t * per, b = a + per < n ? a + per : n;
-    unsigned long long ls = 0;
-    unsigned int lz = 0;
-    for (int64_t i = a; i < b; ++i) { ls += s[i]; lz += z[i]; }
-    // inclusive warp scan
-    unsigned long long is = ls;
-    unsigned int iz = lz;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long vs = __shfl_up_sync(FULL, is, o);
-        const unsigned int vz = __shfl_up_sync(FULL, iz, o);
-        if (lane >= o) { is += vs; iz += vz; }
-    }
-    if (lane == 31) { ws[wid] = is; wz[wid] = iz; }
-    __syncthreads();
-    if (wid == 0) {
-        unsigned long long x = ws[lane];
-        unsigned int y = wz[lane];
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long vs = __shfl_up_sync(FULL, x, o);
-            const unsigned int vz = __shfl_up_sync(FULL, y, o);
-            if (lane >= o) { x += vs; y += vz; }
-        }
-        ws[lane] = x;   // inclusive over warps
-        wz[lane] = y;
-    }
-    __syncthreads();
-    unsigned long long es = is - ls + (wid ? ws[wid - 1] : 0ull);
-    unsigned int ez = iz - lz + (wid ? wz[wid - 1] : 0u);
-    for (int64_t i = a; i < b; ++i) {
-        const unsigned long long vs = s[i];
-        const unsigned int vz = z[i];
-        s[i] = es;
-        z[i] = ez;
-        es += vs;
-        ez += vz;
-    }
-    if (t == 1023) {
-        totals[0] = es;
-        totals[1] = ez;
-        if (cz_pos) cz_pos[ez] = es;
-    }
-}
-
-// ------------------------------------------------------------ k2u compact
-__global__ void __launch_bounds__(kThreads)
-k2u_compact_kernel(const uint32_t *__restrict__ deg, const uint32_t *__restrict__ off, int64_t R,
-                   const unsigned long long *__restrict__ blk_sum, const unsigned int *__restrict__ blk_nz,
-                   int32_t *__restrict__ cz_row, unsigned long long *__restrict__ cz_pos,
-                   uint32_t *__restrict__ cz_off, int32_t *__restrict__ tile_k0, int tile_rows) {
-    __shared__ unsigned long long ws[kThreads / 32];
-    __shared__ unsigned int wz[kThreads / 32];
-    constexpr int kPer = kRowsPerBlock / kThreads;   // 4 rows per thread
-    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock + (int64_t)t * kPer;
-    uint32_t d[kPer];
-    unsigned long long ls = 0;
-    unsigned int lz = 0;
-#pragma unroll
-    for (int q = 0; q < kPer; ++q) {
-        d[q] = (r0 + q < R) ? deg[r0 + q] : 0u;
-        ls += d[q];
-        lz += d[q] > 0u;
-    }
-    unsigned long long is = ls;
-    unsigned int iz = lz;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long vs = __shfl_up_sync(FULL, is, o);
-        const unsigned int vz = __shfl_up_sync(FULL, iz, o);
-        if (lane >= o) { is += vs; iz += vz; }
-    }
-    if (lane == 31) { ws[wid] = is; wz[wid] = iz; }
-    __syncthreads();
-    unsigned long long es = blk_sum[blockIdx.x] + is - ls;
-    unsigned int ez = blk_nz[blockIdx.x] + iz - lz;
-    for (int w = 0; w < wid; ++w) { es += ws[w]; ez += wz[w]; }
-#pragma unroll
-    for (int q = 0; q < kPer; ++q) {
-        if (d[q] == 0u) continue;
-        const int64_t r = r0 + q;
-        cz_row[ez] = (int32_t)r;
-        cz_pos[ez] = es;
-        cz_off[ez] = off[r];
-        // every tile whose first output row falls in [es, es + d) starts at this row
-        const unsigned long long T = (unsigned long long)tile_rows;
-        for (unsigned long long tt = (es + T - 1) / T; tt * T < es + d[q]; ++tt) tile_k0[tt] = (int32_t)ez;
-        es += d[q];
-        ++ez;
-    }
-}
-
-// -------------------------------------------------------------- k2u write
-// One block per output tile of `tile_rows` rows.  The compacted source rows
-// covering the tile are staged in shared memory; each output row finds its
-// source by binary search, then the tile is written as a contiguous run of
-// 16 B stores (the tile start is a multiple of 32 rows, so 16 B aligned).
-// WC = output width (C + 1) when known at compile time, 0 for the generic case.
-template <int WC>
-__global__ void __launch_bounds__(kThreads)
-k2u_write_kernel(const int32_t *__restrict__ hist, int C_rt, const int32_t *__restrict__ edges,
-                 const int32_t *__restrict__ cz_row, const unsigned long long *__restrict__ cz_pos,
-                 const uint32_t *__restrict__ cz_off, int64_t nz, const int32_t *__restrict__ tile_k0,
-                 int64_t ntiles, int tile_rows, int64_t R_out, int32_t *__restrict__ out) {
-    extern __shared__ int smem[];
-    int *pos_rel = smem;                         // tile_rows + 2
-    int *srow = pos_rel + tile_rows + 2;         // tile_rows + 1
-    uint32_t *soff = (uint32_t *)(srow + tile_rows + 1);   // tile_rows + 1
-    int *rsrc = (int *)(soff + tile_rows + 1);   // tile_rows
-    const int W = WC > 0 ? WC : C_rt + 1;
-    const int C = W - 1;
-
-    const int64_t t = blockIdx.x;
-    const int64_t o0 = t * (int64_t)tile_rows;
-    const int nrows = (int)((R_out - o0) < tile_rows ? (R_out - o0) : tile_rows);
-    const int64_t k0 = tile_k0[t];
-    const int64_t k1 = (t + 1 < ntiles) ? (int64_t)tile_k0[t + 1] : nz - 1;
-    const int nk = (int)(k1 - k0 + 1);
-    for (int i = threadIdx.x; i < nk; i += blockDim.x) {
-        pos_rel[i] = (int)((long long)cz_pos[k0 + i] - (long long)o0);
-        srow[i] = cz_row[k0 + i];
-        soff[i] = cz_off[k0 + i];
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < nrows; j += blockDim.x) {
-        int lo = 0, hi = nk - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (pos_rel[mid] <= j) lo = mid;
-            else hi = mid - 1;
-        }
-        rsrc[j] = lo;
-    }
-    __syncthreads();
-    const int nwords = nrows * W;
-    int32_t *gout = out + o0 * W;
-    const int nvec = (nwords + 3) >> 2;
-    for (int v = threadIdx.x; v < nvec; v += blockDim.x) {
-        const int w0 = v << 2;
-        int j = w0 / W, c = w0 - j * W;
-        int vals[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            int x = 0;
-            if (w0 + q < nwords) {
-                const int i = rsrc[j];
-                if (c < C) x = __ldg(hist + (int64_t)srow[i] * C + c);
-                else x = __ldg(edges + soff[i] + (uint32_t)(j - pos_rel[i]));
-            }
-            vals[q] = x;
-            if (++c == W) { c = 0; ++j; }
-        }
-        if (w0 + 4 <= nwords) {
-            reinterpret_cast<int4 *>(gout)[v] = make_int4(vals[0], vals[1], vals[2], vals[3]);
-        } else {
-            for (int q = 0; q < 4 && w0 + q < nwords; ++q) gout[w0 + q] = vals[q];
-        }
+        flags[blockIdx.x] = 0ull;
+        if (my_scan) atomicAdd(totals, my_scan);
+        if (my_nz) atomicAdd(totals + 1, (unsigned long long)my_nz);
     }
 }
 
 // ----------------------------------------------------------- filter write
+// One CTA per block of input rows: the kept rows, in order, go to the output
+// rows that start at the block's look-back prefix.
 __global__ void __launch_bounds__(kThreads)
 filter_write_kernel(const int32_t *__restrict__ hist, int64_t R, int C, const uint32_t *__restrict__ mask,
-                    const unsigned int *__restrict__ blk_nz, int32_t *__restrict__ out) {
+                    const unsigned int *__restrict__ blk_nz, unsigned long long *flags,
+                    int32_t *__restrict__ out) {
     __shared__ int sel[kRowsPerBlock];
     __shared__ unsigned int wbase[kRowsPerBlock / 32 + 1];
+    __shared__ unsigned long long s_P;
     constexpr int kPer = kRowsPerBlock / kThreads;   // 4 rows per thread
-    const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
+    const int64_t b = blockIdx.x;
+    const unsigned int nb = blk_nz[b];
+    if (nb == 0u) return;   // successors add this block's count (0) as they walk past
+    const int64_t r0 = b * kRowsPerBlock;
     const int64_t nwords_mask = (R + 31) >> 5;
     const int t = threadIdx.x;
     if (t < 32) {
@@ -335,6 +407,11 @@ filter_write_kernel(const int32_t *__restrict__ hist, int64_t R, int C, const ui
         }
         wbase[t] = inc - c;
         if (t == 31) wbase[32] = inc;
+        const unsigned long long P = lookback_prefix(blk_nz, flags, b);
+        if (t == 0) {
+            st_flag(flags + b, kPrefixReady | (P + nb));
+            s_P = P;
+        }
     }
     __syncthreads();
     {
@@ -347,12 +424,11 @@ filter_write_kernel(const int32_t *__restrict__ hist, int64_t R, int C, const ui
             if (m & (1u << (bit0 + q))) sel[pos++] = t * kPer + q;
     }
     __syncthreads();
-    const int nsel = (int)wbase[32];
-    const int64_t base = (int64_t)blk_nz[blockIdx.x] * C;
-    const int64_t nwords = (int64_t)nsel * C;
-    for (int64_t w = t; w < nwords; w += blockDim.x) {
-        const int j = (int)(w / C), c = (int)(w - (int64_t)j * C);
-        out[base + w] = __ldg(hist + (r0 + sel[j]) * C + c);
+    int32_t *dst = out + (int64_t)s_P * C;
+    for (int j = t; j < (int)nb; j += kThreads) {
+        const int32_t *src = hist + (r0 + sel[j]) * C;
+        int32_t *d = dst + (int64_t)j * C;
+        for (int c = 0; c < C; ++c) d[c] = __ldg(src + c);
     }
 }
 
@@ -367,65 +443,42 @@ static inline unsigned int nblocks_rows(int64_t R) {
     return (unsigned int)((R + kRowsPerBlock - 1) / kRowsPerBlock);
 }
 
-int k2u_tile_rows(int out_cols) {
-    (void)out_cols;
-    return 1024;
+void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg,
+                      uint32_t *off, unsigned long long *blk_sum, unsigned long long *flags,
+                      unsigned long long *totals, int *err, cudaStream_t st) {
+    k2u_count_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, flags,
+                                                           totals, err);
 }
 
-static size_t k2u_write_smem(int tile_rows) { return (size_t)(4 * tile_rows + 4) * sizeof(int); }
-
-void launch_k2u_probe(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
-                      uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned int *blk_nz,
-                      int *err, cudaStream_t st) {
-    k2u_probe_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum,
-                                                           blk_nz, err);
+void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edges, const uint32_t *deg,
+                       const uint32_t *off, const unsigned long long *blk_sum, unsigned long long *flags,
+                       int32_t *out, cudaStream_t st) {
+    const unsigned int g = nblocks_rows(R);
+#define WK_EXPAND(WC) \
+    k2u_expand_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, C, edges, deg, off, blk_sum, flags, out)
+    switch (C + 1) {
+        case 2: WK_EXPAND(2); break;
+        case 3: WK_EXPAND(3); break;
+        case 4: WK_EXPAND(4); break;
+        case 5: WK_EXPAND(5); break;
+        case 6: WK_EXPAND(6); break;
+        case 7: WK_EXPAND(7); break;
+        case 8: WK_EXPAND(8); break;
+        default: WK_EXPAND(0); break;
+    }
+#undef WK_EXPAND
 }
 
 void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ecol, int32_t end_const,
-                         uint32_t dir, PredView pv, uint32_t *mask, unsigned long long *blk_sum,
-                         unsigned int *blk_nz, int *err, cudaStream_t st) {
-    filter_probe_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv,
-                                                              mask, blk_sum, blk_nz, err);
+                         uint32_t dir, PredView pv, uint32_t *mask, unsigned int *blk_nz,
+                         unsigned long long *flags, unsigned long long *totals, int *err, cudaStream_t st) {
+    filter_probe_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv, mask,
+                                                              blk_nz, flags, totals, err);
 }
 
-void launch_scan_blocks(unsigned long long *blk_sum, unsigned int *blk_nz, int64_t nblk,
-                        unsigned long long *totals, unsigned long long *cz_pos, cudaStream_t st) {
-    scan_blocks_kernel<<<1, 1024, 0, st>>>(blk_sum, blk_nz, nblk, totals, cz_pos);
-}
-
-void launch_k2u_compact(const uint32_t *deg, const uint32_t *off, int64_t R,
-                        const unsigned long long *blk_sum, const unsigned int *blk_nz,
-                        int32_t *cz_row, unsigned long long *cz_pos, uint32_t *cz_off,
-                        int32_t *tile_k0, int tile_rows, cudaStream_t st) {
-    k2u_compact_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(deg, off, R, blk_sum, blk_nz, cz_row, cz_pos,
-                                                             cz_off, tile_k0, tile_rows);
-}
-
-void launch_k2u_write(const int32_t *hist, int C, const int32_t *edges, const int32_t *cz_row,
-                      const unsigned long long *cz_pos, const uint32_t *cz_off, int64_t nz,
-                      const int32_t *tile_k0, int64_t ntiles, int tile_rows, int64_t R_out,
-                      int32_t *out, cudaStream_t st) {
-    const unsigned int g = (unsigned int)ntiles;
-    const size_t sm = k2u_write_smem(tile_rows);
-#define WK_WRITE(WC)                                                                                   \
-    k2u_write_kernel<WC><<<g, kThreads, sm, st>>>(hist, C, edges, cz_row, cz_pos, cz_off, nz, tile_k0, \
-                                                  ntiles, tile_rows, R_out, out)
-    switch (C + 1) {
-        case 2: WK_WRITE(2); break;
-        case 3: WK_WRITE(3); break;
-        case 4: WK_WRITE(4); break;
-        case 5: WK_WRITE(5); break;
-        case 6: WK_WRITE(6); break;
-        case 7: WK_WRITE(7); break;
-        case 8: WK_WRITE(8); break;
-        default: WK_WRITE(0); break;
-    }
-#undef WK_WRITE
-}
-
-void launch_filter_write(const int32_t *hist, int64_t R, int C, const uint32_t *mask,
-                         const unsigned int *blk_nz, int32_t *out, cudaStream_t st) {
-    filter_write_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, mask, blk_nz, out);
+void launch_filter_write(const int32_t *hist, int64_t R, int C, const uint32_t *mask, const unsigned int *blk_nz,
+                         unsigned long long *flags, int32_t *out, cudaStream_t st) {
+    filter_write_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, mask, blk_nz, flags, out);
 }
 
 void launch_copy_list(const int32_t *src, int64_t n, int32_t *dst, cudaStream_t st) {

@@ -10,20 +10,20 @@
 // device array of fixed size, so the call allocates nothing.
 //
 // Limits and sharing rules:
-//   - at most kMaxRows input rows and kMaxTiles * tile_rows output rows per
-//     call (262,144 input rows, 16,777,216 output rows); larger calls are
-//     rejected with WK_EINVAL / WK_EOVERFLOW before any device work;
-//   - the array (about 6.4 MB) is held by every GPU that loads the library
+//   - at most kMaxRows input rows per call (262,144); a larger call is
+//     rejected with WK_EINVAL before any device work; the output is bounded
+//     only by the caller's capacity (WK_EOVERFLOW, with the row count);
+//   - the array (about 2.1 MB) is held by every GPU that loads the library
 //     until the process exits;
-//   - every call shares it and it keeps the last call's contents: the only
-//     field that must start at zero (the probe's error flag) is cleared at
-//     the start of each call, everything else is fully written before it is
-//     read.  Calls that overlap on the GPU (from several host threads or
-//     several contexts' streams at once) race on the array and must not be
-//     issued;
+//   - every call shares it and it keeps the last call's contents: the fields
+//     that must start at zero (error flags and totals) are cleared at the
+//     start of each call, everything else is fully written before it is read.
+//     Calls that overlap on the GPU (from several host threads or several
+//     contexts' streams at once) race on the array and must not be issued;
 //   - the device address of the array is looked up once per device, on the
 //     first call made with that device current (cudaGetSymbolAddress); make
 //     that first call before any stream capture begins.
+#include <cstdint>
 #include <mutex>
 
 #include "wk_runtime.h"
@@ -32,7 +32,6 @@ namespace {
 
 constexpr int64_t kMaxRows = 1 << 18;                 // input rows per call
 constexpr int64_t kMaxBlocks = kMaxRows / wk::dev::kRowsPerBlock;
-constexpr int64_t kMaxTiles = 1 << 14;                // output tiles per call
 
 constexpr size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // byte layout of the scratch array
@@ -40,12 +39,8 @@ constexpr size_t kOffFlags = 0;                                         // err (
 constexpr size_t kOffDeg = al(kOffFlags + 64);
 constexpr size_t kOffOff = al(kOffDeg + 4 * kMaxRows);
 constexpr size_t kOffBlkSum = al(kOffOff + 4 * kMaxRows);
-constexpr size_t kOffBlkNz = al(kOffBlkSum + 8 * kMaxBlocks);
-constexpr size_t kOffCzRow = al(kOffBlkNz + 4 * kMaxBlocks);
-constexpr size_t kOffCzPos = al(kOffCzRow + 4 * kMaxRows);
-constexpr size_t kOffCzOff = al(kOffCzPos + 8 * (kMaxRows + 1));
-constexpr size_t kOffTiles = al(kOffCzOff + 4 * kMaxRows);
-constexpr size_t kScratchBytes = al(kOffTiles + 4 * kMaxTiles);
+constexpr size_t kOffLookback = al(kOffBlkSum + 8 * kMaxBlocks);
+constexpr size_t kScratchBytes = al(kOffLookback + 8 * kMaxBlocks);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -89,6 +84,9 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     if (rows > kMaxRows)
         return set_error(WK_EINVAL, "known_to_unknown_noalloc: %lld input rows exceed the maximum of %lld",
                          (long long)rows, (long long)kMaxRows);
+    // the expansion kernel writes whole output rows as 16 B vectors
+    if (((uintptr_t)out & 15u) != 0 || ((uintptr_t)hist & 3u) != 0)
+        return set_error(WK_EINVAL, "known_to_unknown_noalloc: out must be 16 B aligned and hist 4 B aligned");
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     if (rows == 0) return WK_OK;
@@ -100,43 +98,33 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     uint32_t *deg = reinterpret_cast<uint32_t *>(sc + kOffDeg);
     uint32_t *off = reinterpret_cast<uint32_t *>(sc + kOffOff);
     unsigned long long *blk_sum = reinterpret_cast<unsigned long long *>(sc + kOffBlkSum);
-    unsigned int *blk_nz = reinterpret_cast<unsigned int *>(sc + kOffBlkNz);
-    int32_t *cz_row = reinterpret_cast<int32_t *>(sc + kOffCzRow);
-    unsigned long long *cz_pos = reinterpret_cast<unsigned long long *>(sc + kOffCzPos);
-    uint32_t *cz_off = reinterpret_cast<uint32_t *>(sc + kOffCzOff);
-    int32_t *tile_k0 = reinterpret_cast<int32_t *>(sc + kOffTiles);
+    unsigned long long *flags = reinterpret_cast<unsigned long long *>(sc + kOffLookback);
 
     const PredView pv = ctx->store->views[(size_t)predict];
     const int scol = (int)(-start - 1);
-    const int64_t nblk = (rows + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
     cudaStream_t s = ctx->stream;
-    if ((e = cudaMemsetAsync(err, 0, sizeof(int), s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flag");
-    dev::launch_k2u_probe(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, blk_nz, err, s);
-    dev::launch_scan_blocks(blk_sum, blk_nz, nblk, tot, cz_pos, s);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: probe/scan launch");
-    ctx->launches += 2;
+    if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 32, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
+    dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, flags, tot, err, s);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: count launch");
+    ctx->launches += 1;
     if ((e = cudaMemcpyAsync(ctx->h_scal, sc + kOffFlags, 32, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "noalloc: totals");
-    if (ctx->h_scal[0] & 0xffffffffull)
+    if (ctx->h_scal[0] & 1ull)
         return set_error(WK_EDEVICE, "known_to_unknown_noalloc: corrupt overflow chain in the store");
-    const int64_t R_out = (int64_t)ctx->h_scal[1], nz = (int64_t)ctx->h_scal[2];
+    const int64_t R_out = (int64_t)ctx->h_scal[1];
     *out_rows = R_out;
+    if (ctx->h_scal[0] & 2ull)
+        return set_error(WK_EOVERFLOW, "known_to_unknown_noalloc: 1024 consecutive input rows expand to 2^32 rows or more");
     if (R_out == 0) return WK_OK;
-    const int T = dev::k2u_tile_rows(cols + 1);
-    const int64_t ntiles = (R_out + T - 1) / T;
-    if (ntiles > kMaxTiles)
-        return set_error(WK_EOVERFLOW, "known_to_unknown_noalloc: %lld output rows exceed the maximum of %lld",
-                         (long long)R_out, (long long)(kMaxTiles * T));
     if (R_out * (cols + 1) > out_capacity)
         return set_error(WK_EOVERFLOW,
                          "known_to_unknown_noalloc: output needs %lld int32 elements, capacity is %lld "
                          "(*out_rows holds the row count)",
                          (long long)(R_out * (cols + 1)), (long long)out_capacity);
-    dev::launch_k2u_compact(deg, off, rows, blk_sum, blk_nz, cz_row, cz_pos, cz_off, tile_k0, T, s);
-    dev::launch_k2u_write(hist, cols, pv.edges, cz_row, cz_pos, cz_off, nz, tile_k0, ntiles, T, R_out, out, s);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: compact/write launch");
-    ctx->launches += 2;
+    dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, flags, out, s);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: expand launch");
+    ctx->launches += 1;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "noalloc: sync");
     return WK_OK;
 }

@@ -121,7 +121,13 @@ int fail_corrupt(wk_ctx *ctx) {
     return set_error(WK_EDEVICE, "probe found an overflow chain longer than the segment's overflow area (corrupt store)");
 }
 
-// two-pass k2u (count -> scan -> write)
+// zero the op totals (dscal[1..3]) before a first pass accumulates into them
+int clear_totals(wk_ctx *ctx) {
+    cudaError_t e = cudaMemsetAsync(ctx->dscal.as<unsigned long long>() + 1, 0, 24, ctx->stream);
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "clear totals");
+}
+
+// two-pass k2u (count -> host reads the total -> expand)
 int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     const int C = h->col_num;
     const int64_t R = h->size / C;
@@ -143,23 +149,24 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     }
     const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
     if ((st = ctx->deg.reserve((size_t)R * 4)) || (st = ctx->off.reserve((size_t)R * 4)) ||
-        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->blk_nz.reserve((size_t)nblk * 4)) ||
-        (st = ctx->cz_pos.reserve((size_t)(R + 1) * 8)))
+        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->lb_flags.reserve((size_t)nblk * 8)) ||
+        (st = clear_totals(ctx)))
         return st;
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
     int *err = ctx->dscal.as<int>();
     if ((st = clk.begin())) return st;
-    dev::launch_k2u_probe(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
-                          ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), err, ctx->stream);
-    if ((st = launch_check("k2u probe")) || (st = clk.end(false)) || (st = clk.begin())) return st;
-    dev::launch_scan_blocks(ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), nblk, tot,
-                            ctx->cz_pos.as<unsigned long long>(), ctx->stream);
-    if ((st = launch_check("k2u scan")) || (st = clk.end(false))) return st;
+    dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
+                          ctx->blk_sum.as<unsigned long long>(), ctx->lb_flags.as<unsigned long long>(), tot, err,
+                          ctx->stream);
+    if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;
     int errf = 0;
     if ((st = read_totals(ctx, &errf))) return st;
-    if (errf) return fail_corrupt(ctx);
+    if (errf & 1) return fail_corrupt(ctx);
+    if (errf & 2) {
+        cudaMemsetAsync(ctx->dscal.ptr, 0, 8, ctx->stream);
+        return set_error(WK_EOVERFLOW, "k2u: 1024 consecutive input rows expand to 2^32 rows or more");
+    }
     const int64_t R_out = (int64_t)ctx->h_scal[1];
-    const int64_t nz = (int64_t)ctx->h_scal[2];
     if (R_out > ctx->row_limit)
         return set_error(WK_EOVERFLOW, "k2u: %lld output rows exceed the context's row limit %lld", (long long)R_out,
                          (long long)ctx->row_limit);
@@ -168,22 +175,12 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     if (R_out == 0) {
         if ((st = ob.reserve(16))) return st;
     } else {
-        const int T = dev::k2u_tile_rows(C + 1);
-        const int64_t ntiles = (R_out + T - 1) / T;
-        if (ntiles > 0x7fffffffll) return set_error(WK_EOVERFLOW, "k2u: %lld output tiles", (long long)ntiles);
-        if ((st = ob.reserve((size_t)R_out * (C + 1) * 4)) || (st = ctx->cz_row.reserve((size_t)nz * 4)) ||
-            (st = ctx->cz_off.reserve((size_t)nz * 4)) || (st = ctx->tile_k0.reserve((size_t)ntiles * 4)))
-            return st;
+        if ((st = ob.reserve((size_t)R_out * (C + 1) * 4))) return st;
         if ((st = clk.begin())) return st;
-        dev::launch_k2u_compact(ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(), R,
-                                ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(),
-                                ctx->cz_row.as<int32_t>(), ctx->cz_pos.as<unsigned long long>(),
-                                ctx->cz_off.as<uint32_t>(), ctx->tile_k0.as<int32_t>(), T, ctx->stream);
-        if ((st = launch_check("k2u compact")) || (st = clk.end(false)) || (st = clk.begin())) return st;
-        dev::launch_k2u_write(h->data, C, pv.edges, ctx->cz_row.as<int32_t>(), ctx->cz_pos.as<unsigned long long>(),
-                              ctx->cz_off.as<uint32_t>(), nz, ctx->tile_k0.as<int32_t>(), ntiles, T, R_out,
-                              ob.as<int32_t>(), ctx->stream);
-        if ((st = launch_check("k2u write")) || (st = clk.end(true))) return st;
+        dev::launch_k2u_expand(h->data, R, C, pv.edges, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
+                               ctx->blk_sum.as<unsigned long long>(), ctx->lb_flags.as<unsigned long long>(),
+                               ob.as<int32_t>(), ctx->stream);
+        if ((st = launch_check("k2u expand")) || (st = clk.end(true))) return st;
         if (ctx->timing) {
             cudaError_t e = cudaStreamSynchronize(ctx->stream);
             if (e != cudaSuccess) return cuda_fail(e, "k2u sync");
@@ -197,7 +194,8 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     return WK_OK;
 }
 
-// two-pass k2k / k2c (probe + membership -> scan -> filtered copy)
+// two-pass k2k / k2c (probe + membership -> filtered copy); the output is
+// sized by the input, so the host reads the totals only at the end
 int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const, uint32_t pid, uint32_t dir) {
     const int C = h->col_num;
     const int64_t R = h->size / C;
@@ -217,20 +215,19 @@ int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const,
         return WK_OK;
     }
     const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
-    if ((st = ctx->mask.reserve((size_t)((R + 31) / 32) * 4)) || (st = ctx->blk_sum.reserve((size_t)nblk * 8)) ||
-        (st = ctx->blk_nz.reserve((size_t)nblk * 4)) || (st = ob.reserve((size_t)R * C * 4)))
+    if ((st = ctx->mask.reserve((size_t)((R + 31) / 32) * 4)) || (st = ctx->blk_nz.reserve((size_t)nblk * 4)) ||
+        (st = ctx->lb_flags.reserve((size_t)nblk * 8)) || (st = ob.reserve((size_t)R * C * 4)) ||
+        (st = clear_totals(ctx)))
         return st;
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
     int *err = ctx->dscal.as<int>();
     if ((st = clk.begin())) return st;
     dev::launch_filter_probe(h->data, R, C, scol, ecol, end_const, dir, pv, ctx->mask.as<uint32_t>(),
-                             ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), err, ctx->stream);
+                             ctx->blk_nz.as<unsigned int>(), ctx->lb_flags.as<unsigned long long>(), tot, err,
+                             ctx->stream);
     if ((st = launch_check("filter probe")) || (st = clk.end(true)) || (st = clk.begin())) return st;
-    dev::launch_scan_blocks(ctx->blk_sum.as<unsigned long long>(), ctx->blk_nz.as<unsigned int>(), nblk, tot,
-                            nullptr, ctx->stream);
-    if ((st = launch_check("filter scan")) || (st = clk.end(false)) || (st = clk.begin())) return st;
     dev::launch_filter_write(h->data, R, C, ctx->mask.as<uint32_t>(), ctx->blk_nz.as<unsigned int>(),
-                             ob.as<int32_t>(), ctx->stream);
+                             ctx->lb_flags.as<unsigned long long>(), ob.as<int32_t>(), ctx->stream);
     if ((st = launch_check("filter write")) || (st = clk.end(false))) return st;
     int errf = 0;
     if ((st = read_totals(ctx, &errf))) return st;

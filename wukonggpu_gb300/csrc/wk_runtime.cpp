@@ -229,7 +229,7 @@ wk_ctx::~wk_ctx() {
     if (stream) cudaStreamSynchronize(stream);
     for (auto &b : hbuf) b.release();
     deg.release(); off.release(); mask.release(); blk_sum.release(); blk_nz.release();
-    cz_row.release(); cz_pos.release(); cz_off.release(); tile_k0.release(); dscal.release();
+    lb_flags.release(); dscal.release();
     if (h_scal) cudaFreeHost(h_scal);
     for (auto &e : tev) cudaEventDestroy(e);
     if (use_ready) cudaEventDestroy(use_ready);

@@ -71,8 +71,9 @@ struct wk_ctx {
 
     wk::DevBuf hbuf[2];              // ping-pong history buffers (core/rcache.hpp:87-88)
     // scratch of the two-pass ops
-    wk::DevBuf deg, off, mask, blk_sum, blk_nz, cz_row, cz_pos, cz_off, tile_k0;
-    wk::DevBuf dscal;                // [0] error flag, [8..] totals
+    wk::DevBuf deg, off, mask, blk_sum, blk_nz;
+    wk::DevBuf lb_flags;             // per-block look-back prefixes of the second pass
+    wk::DevBuf dscal;                // [0] error flags, [8..] totals
     unsigned long long *h_scal = nullptr;   // pinned mirror of the totals
 
     // timing
