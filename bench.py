@@ -3,18 +3,22 @@
 
 Workload: a seeded RDF graph of ~100M triples over 2M entities (8 one-to-one,
 16 one-to-many Zipf(1.1, cap 4096) and 8 many-to-one predicates onto a 1% hub
-set, rdf:type with 15 classes), and three 6-pattern star+chain BGPs starting
-from a type index (1.3e5 start rows; final tables of 1.3e7..6.2e7 rows x 6
-int32 columns).  One step = the three queries executed once.
+set, rdf:type with 15 classes), and 15 six-pattern star+chain BGPs (three
+shapes, each on five classes) starting from a type index (1.3e5 start rows;
+final tables of 1e7..6e7 rows x 6 int32 columns).  One step = the 15 queries
+executed once.
 
-  value : queries/s with the store and every history resident in HBM (device
-          time from CUDA events on the library's stream, max over ranks).
-  e2e   : queries/s through the public C ABI with host buffers: the query goes
-          in from the host and the final table comes back to pinned host
-          memory inside the timed region.
-  roofline : the k2u op (probe + scan + compact + write kernels) -- the
-          expansion path that dominates the step -- algorithmic bytes per
-          op / its summed kernel time, against the measured HBM copy peak.
+  value : queries/s, each query run whole through wk_execute with the store
+          and every history resident in HBM (device time from CUDA events on
+          the library's stream around each query, max over ranks).
+  e2e   : queries/s through the public C ABI with host buffers: each query
+          goes in from the host and its final table comes back to pinned host
+          memory inside the timed region (two contexts sharing the store, one
+          host thread each, so copies overlap the next query's kernels).
+  roofline : the k2u op (count + expand kernels) -- the expansion path that
+          dominates the step -- algorithmic bytes per op / its summed kernel
+          time (per-kernel CUDA events, a second pass over the same steps),
+          against the measured HBM copy peak.
   cpu_baseline : the CPU oracle (a C port of the reference store + engine) on
           the same mix, all host threads.
 
@@ -55,6 +59,8 @@ def parse():
     ap.add_argument("--sections", default="batched,estimator,serving",
                     help="extra sections after the headline: batched, estimator, serving (comma list, or none)")
     ap.add_argument("--est-queries", type=int, default=4000, help="random BGPs executed to train the estimator")
+    ap.add_argument("--e2e-contexts", type=int, default=2,
+                    help="contexts (one host thread each) that share the store in the end-to-end pass")
     return ap.parse_args()
 
 
@@ -176,6 +182,18 @@ def profile_traffic_ratio():
     return None
 
 
+def d2h_bandwidth(rc, pinned, n_int32: int, reps: int = 3) -> float:
+    """Device -> pinned host copy bandwidth (GB/s) of one result-sized history."""
+    import wukonggpu_gb300 as W
+    req = W.Request([])
+    rc.upload_history(req, np.zeros((max(n_int32, 1), 1), np.int32))
+    rc.download(req, into=pinned)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        rc.download(req, into=pinned)
+    return reps * 4.0 * max(n_int32, 1) / (time.perf_counter() - t0) / 1e9
+
+
 def cpu_baseline(g, queries, nthreads: int, steps: int = 1):
     """The oracle (C port of the reference store + CPU engine) on the mix; returns (qps, seconds, sample)."""
     import oracle
@@ -259,10 +277,6 @@ def run_gb300(args, dist):
         one_step()
     rc.sync()
 
-    # ---- device-resident timed region (per-op timing on: roofline from the same run)
-    rc.enable_timing(True)
-    op_log = []
-
     def step_with_ops(lat):
         for _, q in queries:
             req = W.Request(q)
@@ -284,13 +298,15 @@ def run_gb300(args, dist):
                 op_log.append(rc.last_op_stats())
             lat.append(rc.timer_end())
 
+    # ---- headline: whole queries through wk_execute, device time from query-level events
+    rc.enable_timing(False)
     launches0 = rc.kernel_launches()
     lat = []
     dist.barrier()
     rc.sync()
     wall0, ep0 = time.perf_counter(), time.time()
     for _ in range(args.steps):
-        step_with_ops(lat)
+        one_step(lat)
     rc.sync()
     wall_s, ep1 = time.perf_counter() - wall0, time.time()
     time.sleep(0.3)
@@ -298,13 +314,22 @@ def run_gb300(args, dist):
     clocks = clk.summary(ep0, ep1)
     dist.barrier()
     launches = rc.kernel_launches() - launches0
-    rc.enable_timing(False)
     total_ms = sum(lat)
     max_ms = dist.reduce(total_ms, "max")
     n_done = dist.reduce(float(args.steps * nq), "sum")
     value = n_done / (max_ms / 1000.0)
 
-    # ---- roofline of the k2u op (the expansion path), from the timed region
+    # ---- the same steps again, op by op with per-kernel CUDA events (for the roofline)
+    rc.enable_timing(True)
+    op_log = []
+    lat_ops = []
+    rc.sync()
+    for _ in range(args.steps):
+        step_with_ops(lat_ops)
+    rc.sync()
+    rc.enable_timing(False)
+
+    # ---- roofline of the k2u op (the expansion path), from the per-kernel pass
     k2u = [op for op in op_log if op["kind"] == 0 and op["rows_out"] > 0]
     alg = sum(op["alg_bytes"] for op in k2u)
     k2u_ms = sum(op["ms"] for op in k2u)
@@ -316,32 +341,60 @@ def run_gb300(args, dist):
     ratio = profile_traffic_ratio()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": (ratio * per_launch) if ratio else None,
-                "peak_source": peak_kind, "kernel": "k2u op (probe+scan+compact+write)",
+                "peak_source": peak_kind, "kernel": "k2u op (count + expand kernels)",
+                "timing": "per-kernel CUDA events on the op stream, a second pass over the timed steps",
                 "alg_bytes_per_launch": per_launch, "k2u_share_of_op_time": k2u_ms / all_ms if all_ms else None,
-                "write_kernel_gbs": (sum(4 * op["rows_out"] * (op["cols_in"] + 2) for op in k2u)
-                                     / (write_ms / 1000.0) / 1e9) if write_ms else None}
+                "expand_kernel_gbs": (sum(4 * op["rows_out"] * (op["cols_in"] + 2) for op in k2u)
+                                      / (write_ms / 1000.0) / 1e9) if write_ms else None,
+                "expand_share_of_k2u_time": write_ms / k2u_ms if k2u_ms else None}
 
-    # ---- end to end through the C ABI with host buffers
+    # ---- end to end through the C ABI with host buffers: the query goes in from
+    # the host and its final table comes back to pinned host memory.  Two
+    # contexts (--e2e-contexts) share the store and run alternate queries from
+    # one host thread each, so one query's device->host copy overlaps the next
+    # query's kernels.
     maxrows = 0
     for _, q in queries:
         req, rows = rc.execute(q, download=False)
         maxrows = max(maxrows, req.hist.size)
-    pinned = W.PinnedBuffer(maxrows)
-    d2h = 0
-    h2d = 0
+    nctx = max(1, args.e2e_contexts)
+    ctxs = [rc]
+    for _ in range(nctx - 1):
+        x = W.RCache(device=dist.local)
+        x.share_store(rc)
+        for _, q in queries[:2]:
+            x.execute(q, download=False)
+        ctxs.append(x)
+    pins = [W.PinnedBuffer(maxrows) for _ in range(nctx)]
+    d2h_gbs = d2h_bandwidth(rc, pins[0], maxrows)
+    work = [q for _ in range(args.steps) for _, q in queries]
+    moved = [[0, 0] for _ in range(nctx)]
+
+    def worker(k):
+        for i in range(k, len(work), nctx):
+            cc = np.asarray(work[i], np.int64)
+            moved[k][0] += cc.nbytes
+            req, _ = ctxs[k].execute(cc.tolist(), download=False)
+            out = ctxs[k].download(req, into=pins[k])
+            moved[k][1] += out.nbytes
+
+    import threading
     dist.barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        for _, q in queries:
-            cc = np.asarray(q, np.int64)
-            h2d += cc.nbytes
-            req, _ = rc.execute(cc.tolist(), download=False)
-            out = rc.download(req, into=pinned)
-            d2h += out.nbytes
+    th = [threading.Thread(target=worker, args=(k,)) for k in range(nctx)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
     e2e_s = time.perf_counter() - t0
     e2e_s = dist.reduce(e2e_s, "max")
     e2e_qps = n_done / e2e_s
-    pinned.close()
+    h2d = sum(m[0] for m in moved)
+    d2h = sum(m[1] for m in moved)
+    for x in pins:
+        x.close()
+    for x in ctxs[1:]:
+        x.close()
 
     # ---- CPU baseline (rank 0 only)
     cpu = None
@@ -383,7 +436,8 @@ def run_gb300(args, dist):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d // args.steps,
-                    "d2h_bytes_per_step": d2h // args.steps},
+                    "d2h_bytes_per_step": d2h // args.steps, "contexts": nctx,
+                    "d2h_pinned_gbs": d2h_gbs},
             "gpu_launches": launches,
             "clocks": clocks,
             **sections,

@@ -159,10 +159,10 @@ __device__ __forceinline__ int row_of(const uint32_t *pos, int n, uint32_t j) {
 // g = P + j copies input row i (the one whose list covers j) and appends
 // entry j - pos[i] of its list.  A whole group is W 16 B stores (4 rows of W
 // words); the first and last group of a block may be partial.
-template <int W, bool STAGED>
+template <int W>
 __device__ __forceinline__ void k2u_write_group(unsigned long long gb, unsigned long long P,
                                                 unsigned long long gend, const uint32_t *pos,
-                                                const uint32_t *eoff, int n, const int32_t *rows,
+                                                const uint32_t *eoff, int n, const int32_t *__restrict__ rows,
                                                 const int32_t *__restrict__ edges, int32_t *__restrict__ out) {
     constexpr int C = W - 1;
     int i = row_of(pos, n, gb >= P ? (uint32_t)(gb - P) : 0u);
@@ -176,7 +176,7 @@ __device__ __forceinline__ void k2u_write_group(unsigned long long gb, unsigned 
             while (j >= nxt) nxt = pos[++i + 1];
             const int32_t *src = rows + i * C;
 #pragma unroll
-            for (int c = 0; c < C; ++c) v[q * W + c] = STAGED ? src[c] : __ldg(src + c);
+            for (int c = 0; c < C; ++c) v[q * W + c] = __ldg(src + c);
             v[q * W + C] = __ldg(edges + (eoff[i] + (j - pos[i])));
         } else {
 #pragma unroll
@@ -199,10 +199,12 @@ __device__ __forceinline__ void k2u_write_group(unsigned long long gb, unsigned 
 }
 
 // One CTA per block of kRowsPerBlock input rows; it writes that block's output
-// rows.  W = C + 1 output columns for 2 <= W <= 8; W = 0 for any width (rows
-// read from global memory, one output row per thread and step).  When at least
-// a quarter of the block's rows expand, their history rows are first copied
-// to shared memory with 16 B loads.
+// rows.  W = C + 1 output columns for 2 <= W <= 8; W = 0 for any width (one
+// output row per thread and step, scalar stores).  Warp 0 first finds and
+// publishes the block's output prefix, so the look-back's latency overlaps
+// the other warps' loads of the block's degrees, and later blocks find a
+// published prefix sooner.  History rows are read through L1 (consecutive
+// output rows of one input row reuse it).
 template <int W>
 __global__ void __launch_bounds__(kThreads)
 k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const int32_t *__restrict__ edges,
@@ -211,11 +213,9 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
                   int32_t *__restrict__ out) {
     constexpr int kRPT = kRowsPerBlock / kThreads;
     static_assert(kRPT == 4, "4 input rows per thread");
-    constexpr int kSC = W >= 2 ? W - 1 : 1;
     __shared__ uint32_t pos[kRowsPerBlock + 1];
     __shared__ uint32_t eoff[kRowsPerBlock];
-    __shared__ __align__(16) int32_t hrow[W >= 2 ? kRowsPerBlock * kSC : 4];
-    __shared__ uint32_t s_w[kThreads / 32], s_z[kThreads / 32];
+    __shared__ uint32_t s_w[kThreads / 32];
     __shared__ unsigned long long s_P;
     const int C = W >= 2 ? W - 1 : C_rt;
     const int64_t b = blockIdx.x;
@@ -225,7 +225,16 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
     const int64_t r0 = b * kRowsPerBlock;
     const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
 
-    // 1. the block's degrees and edge offsets, 4 rows per thread; local exclusive scan
+    // 1. output prefix of the block (warp 0), published for the blocks after it
+    if (wid == 0) {
+        const unsigned long long P = lookback_prefix(blk_sum, flags, b);
+        if (lane == 0) {
+            st_flag(flags + b, kPrefixReady | (P + Tb));
+            s_P = P;
+        }
+    }
+
+    // 2. the block's degrees and edge offsets, 4 rows per thread; local exclusive scan
     const int q0 = t * kRPT;
     uint32_t d[kRPT], o[kRPT];
     if (q0 + kRPT <= n) {
@@ -240,29 +249,19 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
             o[q] = q0 + q < n ? off[r0 + q0 + q] : 0u;
         }
     }
-    uint32_t ls = 0, lz = 0;
-#pragma unroll
-    for (int q = 0; q < kRPT; ++q) {
-        ls += d[q];
-        lz += d[q] != 0u;
-    }
+    const uint32_t ls = d[0] + d[1] + d[2] + d[3];
     uint32_t is = ls;
 #pragma unroll
     for (int sh = 1; sh < 32; sh <<= 1) {
         const uint32_t x = __shfl_up_sync(FULL, is, sh);
         if (lane >= sh) is += x;
     }
-    const uint32_t wz = warp_sum(lz);
     if (lane == 31) s_w[wid] = is;
-    if (lane == 0) s_z[wid] = wz;
     __syncthreads();
-    uint32_t base = 0, nzb = 0;
+    uint32_t e = is - ls;
 #pragma unroll
-    for (int w = 0; w < kThreads / 32; ++w) {
-        if (w < wid) base += s_w[w];
-        nzb += s_z[w];
-    }
-    uint32_t e = base + is - ls;
+    for (int w = 0; w < kThreads / 32; ++w)
+        if (w < wid) e += s_w[w];
 #pragma unroll
     for (int q = 0; q < kRPT; ++q) {
         pos[q0 + q] = e;
@@ -270,39 +269,14 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
         e += d[q];
     }
     if (t == kThreads - 1) pos[kRowsPerBlock] = e;   // the block's total; rows >= n have no list
-
-    // 2. history rows of the block, when enough of them expand
-    const bool staged = W >= 2 && nzb * 4u >= (uint32_t)n;
-    const int32_t *hblk = hist + r0 * C;
-    if (W >= 2 && staged) {
-        const int nw = n * C;
-        if ((reinterpret_cast<uintptr_t>(hblk) & 15u) == 0) {
-            const int nv = nw >> 2;
-            for (int x = t; x < nv; x += kThreads)
-                reinterpret_cast<int4 *>(hrow)[x] = __ldg(reinterpret_cast<const int4 *>(hblk) + x);
-            for (int x = (nv << 2) + t; x < nw; x += kThreads) hrow[x] = __ldg(hblk + x);
-        } else {
-            for (int x = t; x < nw; x += kThreads) hrow[x] = __ldg(hblk + x);
-        }
-    }
-
-    // 3. output prefix of the block (warp 0), published for the blocks after it
-    if (wid == 0) {
-        const unsigned long long P = lookback_prefix(blk_sum, flags, b);
-        if (lane == 0) {
-            st_flag(flags + b, kPrefixReady | (P + Tb));
-            s_P = P;
-        }
-    }
     __syncthreads();
     const unsigned long long P = s_P, gend = P + Tb;
+    const int32_t *hblk = hist + r0 * C;
 
-    // 4. output rows [P, P + Tb)
+    // 3. output rows [P, P + Tb)
     if constexpr (W >= 2) {
-        for (unsigned long long gb = (P & ~3ull) + 4ull * t; gb < gend; gb += 4ull * kThreads) {
-            if (staged) k2u_write_group<W, true>(gb, P, gend, pos, eoff, n, hrow, edges, out);
-            else k2u_write_group<W, false>(gb, P, gend, pos, eoff, n, hblk, edges, out);
-        }
+        for (unsigned long long gb = (P & ~3ull) + 4ull * t; gb < gend; gb += 4ull * kThreads)
+            k2u_write_group<W>(gb, P, gend, pos, eoff, n, hblk, edges, out);
     } else {
         const int Wd = C + 1;
         for (unsigned long long g = P + t; g < gend; g += kThreads) {

@@ -53,18 +53,22 @@ __device__ __forceinline__ uint32_t probe_seg(const Bucket *bk, uint32_t nmain, 
     }
 }
 
-// Probe the 32 keys (vid, dir) of a warp in one segment.  Equal keys (the same
-// start vertex on nearby rows, common after an expansion) are looked up once:
-// __match_any_sync groups them, the lowest lane of a group probes and the
-// others read its result.  vid < 0 is not a vertex and is reported absent.
+// Probe the 32 keys (vid, dir) of a warp in one segment.  A run of equal keys
+// on consecutive lanes (the same start vertex on consecutive rows, as an
+// expansion leaves them) is looked up once, by the run's first lane; the
+// others read its result.  This keeps a column that repeats one vertex
+// millions of times from sending every lane to the same bucket.  vid < 0 is
+// not a vertex and is reported absent.
 __device__ __forceinline__ void probe_warp(const PredView &pv, int32_t vid, uint32_t dir, uint32_t &r_off,
                                            uint32_t &r_deg, int *err) {
     const int lane = threadIdx.x & 31;
     const bool ok = vid >= 0;
     const uint32_t key = seg_key((uint32_t)vid, dir);
-    // a lane without a key groups with WK_EMPTY_KEY, which is never stored
-    const unsigned same = __match_any_sync(WK_FULL_MASK, ok ? key : WK_EMPTY_KEY);
-    const int lead = __ffs(same) - 1;
+    // a lane without a key carries WK_EMPTY_KEY, which is never stored
+    const uint32_t kk = ok ? key : WK_EMPTY_KEY;
+    const uint32_t prev = __shfl_up_sync(WK_FULL_MASK, kk, 1);
+    const unsigned heads = __ballot_sync(WK_FULL_MASK, lane == 0 || prev != kk);
+    const int lead = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));   // run head at or below this lane
     uint32_t o = 0u, d = 0u;
     if (ok && lead == lane) d = probe_seg(pv.buckets, pv.nmain, pv.nover, key, &o, err);
     r_off = __shfl_sync(WK_FULL_MASK, o, lead);
