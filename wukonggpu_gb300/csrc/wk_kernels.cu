@@ -101,7 +101,7 @@ __device__ __forceinline__ unsigned long long lookback_prefix(const A *__restric
 constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
 
 // totals[0] += output rows, totals[1] += rows with a match; err bit 1 when a
-// block's output count reaches 2^32 (the expansion keeps block-local
+// block's output count reaches 2^31 (the expansion keeps block-local
 // positions in 32 bits).
 __global__ void __launch_bounds__(kThreads)
 k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
@@ -138,7 +138,7 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
         flags[blockIdx.x] = 0ull;
         if (my_sum) atomicAdd(totals, my_sum);
         if (my_nz) atomicAdd(totals + 1, (unsigned long long)my_nz);
-        if (my_sum >> 32) atomicOr(err, 2);
+        if (my_sum >> 31) atomicOr(err, 2);
     }
 }
 
@@ -155,24 +155,26 @@ __device__ __forceinline__ int row_of(const uint32_t *pos, int n, uint32_t j) {
     return lo;
 }
 
-// Output rows gb..gb+3 (gb a multiple of 4) of those in [P, gend): row
-// g = P + j copies input row i (the one whose list covers j) and appends
-// entry j - pos[i] of its list.  A whole group is W 16 B stores (4 rows of W
-// words); the first and last group of a block may be partial.
+// One group of 4 output rows.  Rows are counted locally from P - lead, the
+// 16 B-aligned row at or before the block's first output row P (lead =
+// P mod 4); local row u is block row j = u - lead, valid for lead <= u < span
+// (span = lead + the block's count, below 2^31 + 4).  Block row j copies
+// input row i (the one whose list covers j) and appends entry j - pos[i] of
+// its list.  A whole group is W 16 B stores (4 rows of W words); the first and
+// last group of a block may be partial.
 template <int W>
-__device__ __forceinline__ void k2u_write_group(unsigned long long gb, unsigned long long P,
-                                                unsigned long long gend, const uint32_t *pos,
+__device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint32_t span, const uint32_t *pos,
                                                 const uint32_t *eoff, int n, const int32_t *__restrict__ rows,
-                                                const int32_t *__restrict__ edges, int32_t *__restrict__ out) {
+                                                const int32_t *__restrict__ edges, int32_t *__restrict__ obase) {
     constexpr int C = W - 1;
-    int i = row_of(pos, n, gb >= P ? (uint32_t)(gb - P) : 0u);
+    int i = row_of(pos, n, u >= lead ? u - lead : 0u);
     uint32_t nxt = pos[i + 1];
     int32_t v[4 * W];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const unsigned long long g = gb + q;
-        if (g >= P && g < gend) {
-            const uint32_t j = (uint32_t)(g - P);
+        const uint32_t uq = u + (uint32_t)q;
+        if (uq >= lead && uq < span) {
+            const uint32_t j = uq - lead;
             while (j >= nxt) nxt = pos[++i + 1];
             const int32_t *src = rows + i * C;
 #pragma unroll
@@ -183,18 +185,20 @@ __device__ __forceinline__ void k2u_write_group(unsigned long long gb, unsigned 
             for (int c = 0; c < W; ++c) v[q * W + c] = 0;
         }
     }
-    int32_t *g = out + gb * W;
-    if (gb >= P && gb + 4 <= gend) {
+    int32_t *g = obase + (size_t)u * W;
+    if (u >= lead && u + 4u <= span) {
 #pragma unroll
         for (int k = 0; k < W; ++k)
             reinterpret_cast<int4 *>(g)[k] = make_int4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
     } else {
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (gb + q >= P && gb + q < gend) {
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t uq = u + (uint32_t)q;
+            if (uq >= lead && uq < span) {
 #pragma unroll
                 for (int c = 0; c < W; ++c) g[q * W + c] = v[q * W + c];
             }
+        }
     }
 }
 
@@ -270,19 +274,22 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
     }
     if (t == kThreads - 1) pos[kRowsPerBlock] = e;   // the block's total; rows >= n have no list
     __syncthreads();
-    const unsigned long long P = s_P, gend = P + Tb;
+    const unsigned long long P = s_P;
+    const uint32_t T = (uint32_t)Tb;   // below 2^31 (the count kernel flags larger blocks)
     const int32_t *hblk = hist + r0 * C;
 
-    // 3. output rows [P, P + Tb)
+    // 3. output rows [P, P + T)
     if constexpr (W >= 2) {
-        for (unsigned long long gb = (P & ~3ull) + 4ull * t; gb < gend; gb += 4ull * kThreads)
-            k2u_write_group<W>(gb, P, gend, pos, eoff, n, hblk, edges, out);
+        const uint32_t lead = (uint32_t)(P & 3ull), span = T + lead;
+        int32_t *obase = out + (P - lead) * W;
+        for (uint32_t u = 4u * (uint32_t)t; u < span; u += 4u * kThreads)
+            k2u_write_group<W>(u, lead, span, pos, eoff, n, hblk, edges, obase);
     } else {
         const int Wd = C + 1;
-        for (unsigned long long g = P + t; g < gend; g += kThreads) {
-            const uint32_t j = (uint32_t)(g - P);
+        int32_t *oblk = out + P * Wd;
+        for (uint32_t j = (uint32_t)t; j < T; j += kThreads) {
             const int i = row_of(pos, n, j);
-            int32_t *dst = out + g * Wd;
+            int32_t *dst = oblk + (size_t)j * Wd;
             const int32_t *src = hblk + (int64_t)i * C;
             for (int c = 0; c < C; ++c) dst[c] = __ldg(src + c);
             dst[C] = __ldg(edges + (eoff[i] + (j - pos[i])));

@@ -14,7 +14,7 @@ constexpr int kThreads = 256;
 // k2u pass 1: probe hist[r][scol] -> deg[r], off[r]; per-block output counts
 // blk_sum[b]; clears the look-back flags; totals[0] += output rows,
 // totals[1] += rows with a match; err bit 0: overflow chain longer than the
-// segment's overflow area, bit 1: a block's count reached 2^32.
+// segment's overflow area, bit 1: a block's count reached 2^31.
 void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg,
                       uint32_t *off, unsigned long long *blk_sum, unsigned long long *flags,
                       unsigned long long *totals, int *err, cudaStream_t st);

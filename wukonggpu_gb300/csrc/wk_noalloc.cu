@@ -115,7 +115,7 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     const int64_t R_out = (int64_t)ctx->h_scal[1];
     *out_rows = R_out;
     if (ctx->h_scal[0] & 2ull)
-        return set_error(WK_EOVERFLOW, "known_to_unknown_noalloc: 1024 consecutive input rows expand to 2^32 rows or more");
+        return set_error(WK_EOVERFLOW, "known_to_unknown_noalloc: 1024 consecutive input rows expand to 2^31 rows or more");
     if (R_out == 0) return WK_OK;
     if (R_out * (cols + 1) > out_capacity)
         return set_error(WK_EOVERFLOW,

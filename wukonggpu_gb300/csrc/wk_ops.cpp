@@ -164,7 +164,7 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     if (errf & 1) return fail_corrupt(ctx);
     if (errf & 2) {
         cudaMemsetAsync(ctx->dscal.ptr, 0, 8, ctx->stream);
-        return set_error(WK_EOVERFLOW, "k2u: 1024 consecutive input rows expand to 2^32 rows or more");
+        return set_error(WK_EOVERFLOW, "k2u: 1024 consecutive input rows expand to 2^31 rows or more");
     }
     const int64_t R_out = (int64_t)ctx->h_scal[1];
     if (R_out > ctx->row_limit)
