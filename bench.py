@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--sections", default="batched,estimator,serving",
                     help="extra sections after the headline: batched, estimator, serving (comma list, or none)")
     ap.add_argument("--est-queries", type=int, default=4000, help="random BGPs executed to train the estimator")
+    ap.add_argument("--one-query", type=int, default=-1,
+                    help="run query N of the mix once, op by op, print each op's stats and exit "
+                         "(a fixed launch sequence for ncu captures)")
     ap.add_argument("--e2e-contexts", type=int, default=2,
                     help="contexts (one host thread each) that share the store in the end-to-end pass")
     return ap.parse_args()
@@ -245,6 +248,38 @@ def run_reference(args, dist):
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def run_one_query(args):
+    """Query `args.one_query` of the mix, once, op by op with per-kernel timing.
+    Kernel launches: the start op's copy, then two per k2u op (count, expand)
+    and two per filter op (probe, write), in pattern order."""
+    import wukonggpu_gb300 as W
+    from wukonggpu_gb300 import build as wb
+    from wukonggpu_gb300 import workloads
+    wb.build()
+    g = W.Graph(W.spec_single_query(scale=args.scale))
+    rc = W.RCache(device=0)
+    rc.build_store_graph(g)
+    name, q = workloads.scale_queries()[args.one_query]
+    rc.enable_timing(True)
+    req = W.Request(q)
+    for i in range(len(q) // 4):
+        st, pid, d, en = q[4 * i:4 * i + 4]
+        if i == 0 and 1 < st < W.VID_BASE:
+            rc.index_to_unknown(req, st, d)
+        elif st >= 0:
+            rc.const_to_unknown(req, st, d, pid)
+        elif en < 0 and -en > req.col_num:
+            rc.known_to_unknown(req, st, d, pid)
+        elif en < 0:
+            rc.known_to_known(req, st, d, pid, en)
+        else:
+            rc.known_to_const(req, st, d, pid, en)
+        s = rc.last_op_stats()
+        print(json.dumps({"query": name, "op": i, **{k: s[k] for k in
+                          ("kind", "rows_in", "cols_in", "rows_out", "kernels", "ms", "ms_main")}}), flush=True)
+    rc.close()
 
 
 def run_gb300(args, dist):
@@ -617,6 +652,9 @@ def section_serving(rc, g, est, n_req: int = 20000):
 
 def main():
     args = parse()
+    if args.one_query >= 0:
+        run_one_query(args)
+        return
     dist = Dist()
     try:
         if args.impl == "reference":
