@@ -545,6 +545,9 @@ def _bindings_equal(oq, pa, ta, pb, tb):
     return bool(np.array_equal(A, B))
 
 
+QERROR_BOUND_P95 = 10.0   # the learned planner is used only below this held-out p95 q-error
+
+
 def section_estimator(rc, g, n_queries: int):
     """Random BGPs (chains, stars, cycles; 2..6 patterns) executed by the engine
     to record true per-step rows; 90/10 split; BF16 MLP trained on the GPU;
@@ -563,6 +566,9 @@ def section_estimator(rc, g, n_queries: int):
     loss = est.train(tr["feats"], tr["pids"], tr["target"], epochs=30, batch=1024, lr=2e-3)
     t_train = time.perf_counter() - t0
     ev = estimator.evaluate(est, te)
+    # the statistics planner stays the fallback: the model is used only while its
+    # held-out 95th-percentile q-error is within the stated bound
+    p95_val, trusted = est.validate(te["feats"], te["pids"], te["target"], QERROR_BOUND_P95)
     # learned vs statistics plans on held-out BGPs: latency and identical bindings
     held = sorted(set(int(x) for x in te["query"]))[:300]
     qs = [bgps[i] for i in held]
@@ -585,6 +591,8 @@ def section_estimator(rc, g, n_queries: int):
     return {"config": f"{n_queries} random BGPs (2..6 patterns: chains, stars, cycles) on the 100M-triple graph, "
                       "90/10 split by query", "samples_train": int(len(tr["target"])), "samples_test": ev["samples"],
             "qerror": ev, "train_loss": loss, "train_s": t_train, "data_s": t_data,
+            "fallback": {"qerror_p95_bound": QERROR_BOUND_P95, "held_out_qerror_p95": p95_val,
+                         "learned_plans_used": trusted},
             "plan_latency_ms": {"learned_mean": float(np.mean(ls)) if ls else None,
                                 "stats_mean": float(np.mean(ss)) if ss else None,
                                 "learned_p99": float(np.percentile(ls, 99)) if ls else None,

@@ -246,14 +246,25 @@ int     wk_mlp_predict(wk_mlp *m, const float *feats, const int32_t *pids, int64
  * the chained statistics estimate of the rows after each step. */
 int     wk_featurize(wk_ctx *ctx, const int64_t *cmd_chains, int32_t n, const int64_t *true_rows, float *feats,
                      int32_t *pids, double *stats_est);
-/* Greedy plan by the model's predicted cardinalities; same output format as
- * wk_plan (*n_out = 0 when no executable order exists). */
+/* Held-out check: q-error = exp(|predicted - true|) in log(1 + rows) per
+ * sample; the model is trusted while the 95th percentile is within
+ * qerror_bound (>= 1).  A model starts trusted; an untrusted one makes the
+ * learned planners fall back to the statistics planner (wk_plan). */
+int     wk_mlp_validate(wk_mlp *m, const float *feats, const int32_t *pids, const float *target, int64_t n,
+                        double qerror_bound, double *p95_qerror, int32_t *trusted);
+int     wk_mlp_is_trusted(wk_mlp *m);
+/* Plan by the model's predicted cardinalities: beam search over join orders,
+ * cost = the sum of the predicted rows of every table the plan builds.  Same
+ * output format as wk_plan (*n_out = 0 when no executable order exists).
+ * With an untrusted model the statistics plan is returned (when wk_plan finds
+ * one); *est_log_rows = log1p of the plan's cost. */
 int     wk_plan_learned(wk_ctx *ctx, wk_mlp *m, const int64_t *cmd_in, int32_t n, int64_t *cmd_out,
                         int32_t *n_out, double *est_log_rows);
 
-/* Learned plans of nq BGPs at once (lockstep greedy, one model call per
- * step for all queries).  cmd_in packs the queries (n_in[q] patterns each);
- * cmd_out must hold sum(n_in[q] + 1) patterns; n_out[q] = plan length. */
+/* Learned plans of nq BGPs at once (every level of every query's search is
+ * one model call).  cmd_in packs the queries (n_in[q] patterns each);
+ * cmd_out must hold sum(n_in[q] + 1) patterns; n_out[q] = plan length.  Same
+ * statistics fallback as wk_plan_learned. */
 int     wk_plan_learned_batch(wk_ctx *ctx, wk_mlp *m, const int64_t *cmd_in, const int32_t *n_in, int32_t nq,
                               int64_t *cmd_out, int32_t *n_out);
 /* Cap on the rows of any k2u output of this context (0 = none); a larger

@@ -111,3 +111,28 @@ def test_row_limit_is_an_error_not_a_truncation(gpu_small, golden_small):
         gpu_small.set_row_limit(0)
     req, _ = gpu_small.execute(q["cmd_chains"])
     assert req.result_table.shape[0] == q["rows"]
+
+
+def test_untrusted_model_falls_back_to_statistics_plans(gpu_small, small_graph):
+    """A model whose held-out q-error exceeds the stated bound is not used: the
+    learned planners return exactly the statistics planner's plans."""
+    g, s, p, o = small_graph
+    bgps = workloads.random_bgps(s, p, o, 300, seed=53, first_class=g.first_class, n_classes=10)
+    ds = estimator.build_dataset(gpu_small, bgps[:150])
+    est = W.Estimator(gpu_small, g.num_ids, max_batch=4096, seed=13)   # untrained
+    assert est.trusted
+    p95, ok = est.validate(ds["feats"], ds["pids"], ds["target"], qerror_bound=2.0)
+    assert not ok and p95 > 2.0 and not est.trusted
+    many = est.plan_many(bgps)
+    n_stats = 0
+    for q, pm in zip(bgps, many):
+        sp, _ = gpu_small.plan(q)
+        single, _ = est.plan(q)
+        assert single == pm
+        if sp:
+            assert single == sp
+            n_stats += 1
+    assert n_stats > 200
+    # a bound the model meets restores it
+    p95b, okb = est.validate(ds["feats"], ds["pids"], ds["target"], qerror_bound=p95 * 2 + 1.0)
+    assert okb and est.trusted

@@ -145,6 +145,9 @@ _SIGS = {
     "wk_mlp_train": (C.c_int, [_P, C.POINTER(C.c_float), _I32P, C.POINTER(C.c_float), C.c_int64, C.c_int32,
                                C.c_int32, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
     "wk_mlp_predict": (C.c_int, [_P, C.POINTER(C.c_float), _I32P, C.c_int64, C.POINTER(C.c_float)]),
+    "wk_mlp_validate": (C.c_int, [_P, C.POINTER(C.c_float), _I32P, C.POINTER(C.c_float), C.c_int64, C.c_double,
+                                  C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+    "wk_mlp_is_trusted": (C.c_int, [_P]),
     "wk_featurize": (C.c_int, [_P, _I64P, C.c_int32, _I64P, C.POINTER(C.c_float), _I32P, C.POINTER(C.c_double)]),
     "wk_plan_learned": (C.c_int, [_P, _P, _I64P, C.c_int32, _I64P, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "wk_plan_learned_batch": (C.c_int, [_P, _P, _I64P, _I32P, C.c_int32, _I64P, _I32P]),
@@ -570,6 +573,23 @@ class Estimator:
         _check(load_library().wk_mlp_predict(self._h, f.ctypes.data_as(_F32P), pp.ctypes.data_as(_I32P), len(pp),
                                              out.ctypes.data_as(_F32P)))
         return out
+
+    def validate(self, feats, pids, target, qerror_bound: float):
+        """Held-out check: (p95 q-error, trusted).  An untrusted model makes the
+        learned planners return the statistics planner's plans."""
+        f = np.ascontiguousarray(feats, np.float32)
+        pp = np.ascontiguousarray(pids, np.int32)
+        t = np.ascontiguousarray(target, np.float32)
+        p95 = C.c_double()
+        ok = C.c_int32()
+        _check(load_library().wk_mlp_validate(self._h, f.ctypes.data_as(_F32P), pp.ctypes.data_as(_I32P),
+                                              t.ctypes.data_as(_F32P), len(t), float(qerror_bound), C.byref(p95),
+                                              C.byref(ok)))
+        return p95.value, bool(ok.value)
+
+    @property
+    def trusted(self) -> bool:
+        return bool(load_library().wk_mlp_is_trusted(self._h))
 
     def plan(self, cmd_chains):
         cc = np.asarray(cmd_chains, np.int64)

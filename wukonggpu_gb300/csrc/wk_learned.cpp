@@ -29,13 +29,15 @@
 //                  is further divided by the objects of p, as the reference
 //                  does
 //
-// Learned planner: greedy.  At every step each executable pattern -- oriented
-// from a bound end, or for the first step from a constant, a type index or a
-// predicate index -- is scored by the model's predicted log rows after it,
-// and the smallest is taken (ties: lower pattern index, then OUT before IN).
-// The result has the statistics planner's output format: executable order,
-// variables renumbered in binding order, an inserted index pattern when the
-// first pattern joins two variables.
+// Learned planner: beam search over join orders.  A partial plan is extended
+// by every executable pattern -- oriented from a bound end, or for the first
+// step from a constant, a type index or a predicate index -- and the model
+// predicts the rows after each extension.  A plan's cost is the sum of the
+// predicted rows of every table it builds; each level keeps the cheapest few
+// partial plans (ties: lower pattern index, then OUT before IN).  The result
+// has the statistics planner's output format: executable order, variables
+// renumbered in binding order, an inserted index pattern when the first
+// pattern joins two variables.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -48,6 +50,7 @@
 extern "C" {
 struct wk_mlp;
 int wk_mlp_predict(wk_mlp *m, const float *feats, const int32_t *pids, int64_t n, float *out);
+int wk_mlp_is_trusted(wk_mlp *m);
 }
 
 namespace wk {
@@ -210,88 +213,176 @@ extern "C" int wk_featurize(wk_ctx *ctx, const int64_t *cmd, int32_t n, const in
     return WK_OK;
 }
 
-// Greedy learned plan of a BGP (SPARQL triple form, any variable numbering).
-extern "C" int wk_plan_learned(wk_ctx *ctx, wk_mlp *mlp, const int64_t *cmd_in, int32_t n, int64_t *cmd_out,
-                               int32_t *n_out, double *est_log_rows) {
-    if (!ctx || !mlp || !cmd_in || !cmd_out || !n_out || n < 1 || n > 10)
-        return set_error(WK_EINVAL, "wk_plan_learned: bad arguments");
-    if (!ctx->store) return set_error(WK_ENOSTORE, "wk_plan_learned: no store");
-    Stats &st = stats_of(ctx);
-    std::vector<int> used((size_t)n, 0);
+namespace wk {
+namespace {
+
+struct Cand {
+    Step s;
+    int pat;
+    bool consumes;   // false for a predicate-index start, which leaves its pattern to run
+};
+
+// A partial plan: the patterns used so far, the variables they bound, the
+// executable steps, the predicted rows of the current table and the plan's
+// cost so far (the sum of the predicted rows of every table it builds).
+struct PState {
+    std::vector<int> used;
     std::unordered_map<int64_t, VarInfo> vars;
     std::vector<int64_t> plan;
-    double rows = 0.0, total_est = 0.0;
-    int cols = 0;
-    std::vector<float> fb;
+    double rows = 0.0, cost = 0.0;
+    int cols = 0, step = 0;
+    bool complete = false;
+};
+
+struct QPlan {
+    const int64_t *cmd = nullptr;
+    int n = 0;
+    std::vector<PState> beam;
+    bool failed = false;
+};
+
+// Executable oriented steps from state S: at the first step a constant, a type
+// index or a predicate index; later, every unused pattern from a bound end.
+// Returns false when every pattern is used.
+bool candidates(const QPlan &Q, const PState &S, std::vector<Cand> &out) {
+    out.clear();
+    const int n = Q.n;
+    if (S.step == 0) {
+        for (int i = 0; i < n; ++i) {
+            const int64_t a = Q.cmd[4 * i], p = Q.cmd[4 * i + 1], b = Q.cmd[4 * i + 3];
+            if (a >= WK_VID_BASE) out.push_back(Cand{Step{K_C2U, a, p, WK_DIR_OUT, b, (int)p}, i, true});
+            if (b >= WK_VID_BASE) out.push_back(Cand{Step{K_C2U, b, p, WK_DIR_IN, a, (int)p}, i, true});
+            if (p == WK_TYPE_ID && a < 0 && b > 1 && b < WK_VID_BASE)
+                out.push_back(Cand{Step{K_I2U, b, WK_TYPE_ID, WK_DIR_IN, a, (int)b}, i, true});
+            if (a < 0 && b < 0 && p != WK_TYPE_ID) {
+                out.push_back(Cand{Step{K_I2U, p, WK_PREDICATE_ID, WK_DIR_IN, a, (int)p}, i, false});
+                out.push_back(Cand{Step{K_I2U, p, WK_PREDICATE_ID, WK_DIR_OUT, b, (int)p}, i, false});
+            }
+        }
+        return true;
+    }
+    bool any = false;
+    for (int i = 0; i < n; ++i) {
+        if (S.used[(size_t)i]) continue;
+        any = true;
+        const int64_t a = Q.cmd[4 * i], p = Q.cmd[4 * i + 1], b = Q.cmd[4 * i + 3];
+        const bool ka = a < 0 && S.vars.count(a), kb = b < 0 && S.vars.count(b);
+        auto kind_for = [&](int64_t other) {
+            if (other >= 0) return (int)K_K2C;
+            return S.vars.count(other) ? (int)K_K2K : (int)K_K2U;
+        };
+        if (ka) out.push_back(Cand{Step{kind_for(b), a, p, WK_DIR_OUT, b, (int)p}, i, true});
+        if (kb) out.push_back(Cand{Step{kind_for(a), b, p, WK_DIR_IN, a, (int)p}, i, true});
+    }
+    return any;
+}
+
+PState apply(const PState &S, const Cand &c, double rows_after) {
+    PState t = S;
+    const Step &s = c.s;
+    t.plan.insert(t.plan.end(), {s.start, s.pid, s.dir, s.end});
+    if (c.consumes) t.used[(size_t)c.pat] = 1;
+    if (s.kind == K_I2U || s.kind == K_C2U || s.kind == K_K2U) {
+        VarInfo v;
+        v.col = t.cols++;
+        v.pred = s.kind == K_I2U ? (int)s.start : (int)s.pid;
+        v.dir = (int)s.dir;
+        t.vars[s.end] = v;
+    }
+    t.rows = rows_after;
+    t.cost += rows_after;
+    t.step++;
+    return t;
+}
+
+// Beam search over join orders for every query at once.  Each level expands
+// every partial plan in every query's beam by each executable step; one model
+// call predicts the rows after all of them; each query keeps its `beam`
+// cheapest partial plans (cost = the sum of predicted rows of the tables
+// built so far -- the quantity the statistics planner's search minimises).
+// A beam of 1 is the greedy planner.  On return qs[q].beam[0] is the cheapest
+// complete plan, or qs[q].failed is set (no executable order).
+int plan_beam(wk_ctx *ctx, wk_mlp *mlp, std::vector<QPlan> &qs, int beam) {
+    Stats &st = stats_of(ctx);
+    for (auto &Q : qs) {
+        PState s0;
+        s0.used.assign((size_t)Q.n, 0);
+        Q.beam.assign(1, s0);
+    }
+    struct Kid {
+        int q, parent;
+        Cand c;
+    };
+    std::vector<float> fb, pred;
     std::vector<int32_t> pb;
-    std::vector<float> pred;
-    struct Cand { Step s; int pat; bool consumes; };
-    for (int step = 0; step < n + 1; ++step) {
-        std::vector<Cand> cands;
-        if (step == 0) {
-            for (int i = 0; i < n; ++i) {
-                const int64_t a = cmd_in[4 * i], p = cmd_in[4 * i + 1], b = cmd_in[4 * i + 3];
-                if (a >= WK_VID_BASE) cands.push_back(Cand{Step{K_C2U, a, p, WK_DIR_OUT, b, (int)p}, i, true});
-                if (b >= WK_VID_BASE) cands.push_back(Cand{Step{K_C2U, b, p, WK_DIR_IN, a, (int)p}, i, true});
-                if (p == WK_TYPE_ID && a < 0 && b > 1 && b < WK_VID_BASE)
-                    cands.push_back(Cand{Step{K_I2U, b, WK_TYPE_ID, WK_DIR_IN, a, (int)b}, i, true});
-                if (a < 0 && b < 0 && p != WK_TYPE_ID) {
-                    cands.push_back(Cand{Step{K_I2U, p, WK_PREDICATE_ID, WK_DIR_IN, a, (int)p}, i, false});
-                    cands.push_back(Cand{Step{K_I2U, p, WK_PREDICATE_ID, WK_DIR_OUT, b, (int)p}, i, false});
+    std::vector<Kid> kids;
+    std::vector<Cand> cands;
+    for (int level = 0; level < 12; ++level) {
+        fb.clear();
+        pb.clear();
+        kids.clear();
+        for (int q = 0; q < (int)qs.size(); ++q) {
+            QPlan &Q = qs[(size_t)q];
+            if (Q.failed) continue;
+            for (int si = 0; si < (int)Q.beam.size(); ++si) {
+                PState &S = Q.beam[(size_t)si];
+                if (S.complete) continue;
+                if (!candidates(Q, S, cands)) {
+                    S.complete = true;
+                    continue;
+                }
+                for (const Cand &c : cands) {
+                    const Step &s = c.s;
+                    const VarInfo *bind = nullptr;
+                    if (s.kind != K_I2U && s.kind != K_C2U) bind = &S.vars.at(s.start);
+                    fb.resize(fb.size() + kF);
+                    features(ctx, st, s, S.step == 0 ? 0.0 : S.rows, S.step, S.cols, bind,
+                             fb.data() + fb.size() - kF);
+                    pb.push_back(s.feat_pid);
+                    kids.push_back(Kid{q, si, c});
                 }
             }
-        } else {
-            bool all = true;
-            for (int i = 0; i < n; ++i) {
-                if (used[(size_t)i]) continue;
-                all = false;
-                const int64_t a = cmd_in[4 * i], p = cmd_in[4 * i + 1], b = cmd_in[4 * i + 3];
-                const bool ka = a < 0 && vars.count(a), kb = b < 0 && vars.count(b);
-                auto kind_for = [&](int64_t other) {
-                    if (other >= 0) return (int)K_K2C;
-                    return vars.count(other) ? (int)K_K2K : (int)K_K2U;
-                };
-                if (ka) cands.push_back(Cand{Step{kind_for(b), a, p, WK_DIR_OUT, b, (int)p}, i, true});
-                if (kb) cands.push_back(Cand{Step{kind_for(a), b, p, WK_DIR_IN, a, (int)p}, i, true});
-            }
-            if (all) break;
         }
-        if (cands.empty()) {
-            *n_out = 0;   // no executable order
-            if (est_log_rows) *est_log_rows = INFINITY;
-            return WK_OK;
-        }
-        fb.assign(cands.size() * kF, 0.f);
-        pb.assign(cands.size(), 0);
-        for (size_t c = 0; c < cands.size(); ++c) {
-            const Step &s = cands[c].s;
-            const VarInfo *bind = nullptr;
-            if (s.kind != K_I2U && s.kind != K_C2U) bind = &vars[s.start];
-            features(ctx, st, s, step == 0 ? 0.0 : rows, step, cols, bind, fb.data() + c * kF);
-            pb[c] = s.feat_pid;
-        }
-        pred.assign(cands.size(), 0.f);
-        int rc = wk_mlp_predict(mlp, fb.data(), pb.data(), (int64_t)cands.size(), pred.data());
+        if (kids.empty()) break;
+        pred.assign(pb.size(), 0.f);
+        int rc = wk_mlp_predict(mlp, fb.data(), pb.data(), (int64_t)pb.size(), pred.data());
         if (rc) return rc;
-        size_t best = 0;
-        for (size_t c = 1; c < cands.size(); ++c)
-            if (pred[c] < pred[best]) best = c;
-        const Cand &ch = cands[best];
-        const Step &s = ch.s;
-        if (s.kind == K_I2U) plan.insert(plan.end(), {s.start, s.pid, s.dir, s.end});
-        else plan.insert(plan.end(), {s.start, s.pid, s.dir, s.end});
-        if (ch.consumes) used[(size_t)ch.pat] = 1;
-        if (s.kind == K_I2U || s.kind == K_C2U || s.kind == K_K2U) {
-            VarInfo v;
-            v.col = cols++;
-            v.pred = s.kind == K_I2U ? (int)s.start : (int)s.pid;
-            v.dir = (int)s.dir;
-            vars[s.end] = v;
+        // next beams: complete plans carried over, plus every child; cheapest first
+        size_t k = 0;
+        for (int q = 0; q < (int)qs.size(); ++q) {
+            QPlan &Q = qs[(size_t)q];
+            if (Q.failed) continue;
+            std::vector<PState> next;
+            for (const PState &S : Q.beam)
+                if (S.complete) next.push_back(S);
+            bool expanded = false;
+            while (k < kids.size() && kids[k].q == q) {
+                const Kid &kd = kids[k];
+                next.push_back(apply(Q.beam[(size_t)kd.parent], kd.c, std::expm1((double)std::max(0.f, pred[k]))));
+                expanded = true;
+                ++k;
+            }
+            if (!expanded && next.empty()) {
+                Q.failed = true;   // partial plans with no executable step left
+                continue;
+            }
+            // a partial plan that could not be extended (no step from a bound end) is dropped
+            std::stable_sort(next.begin(), next.end(),
+                             [](const PState &a, const PState &b) { return a.cost < b.cost; });
+            if ((int)next.size() > beam) next.resize((size_t)beam);
+            Q.beam.swap(next);
         }
-        rows = std::expm1((double)std::max(0.f, pred[best]));
-        total_est += rows;
     }
-    // renumber variables in binding order
+    for (auto &Q : qs) {
+        if (Q.failed) continue;
+        while (!Q.beam.empty() && !Q.beam.front().complete) Q.beam.erase(Q.beam.begin());
+        if (Q.beam.empty()) Q.failed = true;
+    }
+    return WK_OK;
+}
+
+// renumber variables in binding order (core/planner.hpp:991-1003)
+void renumber(std::vector<int64_t> &plan) {
     std::unordered_map<int64_t, int64_t> conv;
     for (auto &x : plan)
         if (x < 0) {
@@ -304,137 +395,109 @@ extern "C" int wk_plan_learned(wk_ctx *ctx, wk_mlp *mlp, const int64_t *cmd_in, 
                 x = it->second;
             }
         }
+}
+
+constexpr int kBeam = 4;
+
+}  // namespace
+}  // namespace wk
+
+// Learned plan of a BGP (SPARQL triple form, any variable numbering): beam
+// search over join orders scored by the model.  *est_log_rows receives
+// log1p of the plan's predicted cost (the sum of its tables' rows).
+extern "C" int wk_plan_learned(wk_ctx *ctx, wk_mlp *mlp, const int64_t *cmd_in, int32_t n, int64_t *cmd_out,
+                               int32_t *n_out, double *est_log_rows) {
+    if (!ctx || !mlp || !cmd_in || !cmd_out || !n_out || n < 1 || n > 10)
+        return set_error(WK_EINVAL, "wk_plan_learned: bad arguments");
+    if (!ctx->store) return set_error(WK_ENOSTORE, "wk_plan_learned: no store");
+    if (!wk_mlp_is_trusted(mlp)) {   // statistics fallback
+        int32_t room = *n_out, empty = 0;
+        double cost = 0.0;
+        int rc = wk_plan(ctx, cmd_in, n, cmd_out, &room, &cost, &empty);
+        if (rc) return rc;
+        if (room > 0) {
+            *n_out = room;
+            if (est_log_rows) *est_log_rows = std::log1p(cost);
+            return WK_OK;
+        }
+        // no statistics plan (proved empty, or no order found): the search below
+    }
+    std::vector<QPlan> qs(1);
+    qs[0].cmd = cmd_in;
+    qs[0].n = n;
+    int rc = plan_beam(ctx, mlp, qs, kBeam);
+    if (rc) return rc;
+    if (qs[0].failed) {
+        *n_out = 0;   // no executable order
+        if (est_log_rows) *est_log_rows = INFINITY;
+        return WK_OK;
+    }
+    std::vector<int64_t> plan = qs[0].beam[0].plan;
+    renumber(plan);
     const int32_t m = (int32_t)(plan.size() / 4);
     if (m > *n_out) return set_error(WK_EOVERFLOW, "wk_plan_learned: plan has %d patterns, room for %d", m, *n_out);
     std::memcpy(cmd_out, plan.data(), plan.size() * sizeof(int64_t));
     *n_out = m;
-    if (est_log_rows) *est_log_rows = std::log1p(total_est);
+    if (est_log_rows) *est_log_rows = std::log1p(qs[0].beam[0].cost);
     return WK_OK;
 }
 
-// Learned plans of many BGPs at once: the greedy steps of all queries run in
-// lockstep, so each step is one model call over every query's candidates.
-// cmd_in packs the queries back to back (n_in[q] patterns each); cmd_out must
-// hold sum(n_in[q] + 1) patterns; n_out[q] receives each plan's length (0:
-// no executable order).
+// Learned plans of many BGPs at once: every level of every query's beam
+// search is one model call.  cmd_in packs the queries back to back (n_in[q]
+// patterns each); cmd_out must hold sum(n_in[q] + 1) patterns; n_out[q]
+// receives each plan's length (0: no executable order).
 extern "C" int wk_plan_learned_batch(wk_ctx *ctx, wk_mlp *mlp, const int64_t *cmd_in, const int32_t *n_in, int32_t nq,
                                      int64_t *cmd_out, int32_t *n_out) {
     if (!ctx || !mlp || !cmd_in || !n_in || nq < 1 || !cmd_out || !n_out)
         return set_error(WK_EINVAL, "wk_plan_learned_batch: bad arguments");
     if (!ctx->store) return set_error(WK_ENOSTORE, "wk_plan_learned_batch: no store");
-    Stats &st = stats_of(ctx);
-    struct Cand { Step s; int pat; bool consumes; };
-    struct QState {
-        const int64_t *cmd;
-        int n;
-        std::vector<int> used;
-        std::unordered_map<int64_t, VarInfo> vars;
-        std::vector<int64_t> plan;
-        double rows = 0.0;
-        int cols = 0, step = 0;
-        bool done = false, failed = false;
-        std::vector<Cand> cands;
-    };
-    std::vector<QState> qs((size_t)nq);
+    std::vector<QPlan> qs((size_t)nq);
     int64_t at = 0;
     for (int q = 0; q < nq; ++q) {
-        if (n_in[q] < 1 || n_in[q] > 10) return set_error(WK_EINVAL, "wk_plan_learned_batch: query %d has %d patterns", q, n_in[q]);
+        if (n_in[q] < 1 || n_in[q] > 10)
+            return set_error(WK_EINVAL, "wk_plan_learned_batch: query %d has %d patterns", q, n_in[q]);
         qs[(size_t)q].cmd = cmd_in + at;
         qs[(size_t)q].n = n_in[q];
-        qs[(size_t)q].used.assign((size_t)n_in[q], 0);
         at += 4 * (int64_t)n_in[q];
     }
-    std::vector<float> fb, pred;
-    std::vector<int32_t> pb;
-    for (int round = 0; round < 11; ++round) {
-        fb.clear();
-        pb.clear();
-        for (auto &Q : qs) {
-            Q.cands.clear();
-            if (Q.done) continue;
-            const int n = Q.n;
-            if (Q.step == 0) {
-                for (int i = 0; i < n; ++i) {
-                    const int64_t a = Q.cmd[4 * i], p = Q.cmd[4 * i + 1], b = Q.cmd[4 * i + 3];
-                    if (a >= WK_VID_BASE) Q.cands.push_back(Cand{Step{K_C2U, a, p, WK_DIR_OUT, b, (int)p}, i, true});
-                    if (b >= WK_VID_BASE) Q.cands.push_back(Cand{Step{K_C2U, b, p, WK_DIR_IN, a, (int)p}, i, true});
-                    if (p == WK_TYPE_ID && a < 0 && b > 1 && b < WK_VID_BASE)
-                        Q.cands.push_back(Cand{Step{K_I2U, b, WK_TYPE_ID, WK_DIR_IN, a, (int)b}, i, true});
-                    if (a < 0 && b < 0 && p != WK_TYPE_ID) {
-                        Q.cands.push_back(Cand{Step{K_I2U, p, WK_PREDICATE_ID, WK_DIR_IN, a, (int)p}, i, false});
-                        Q.cands.push_back(Cand{Step{K_I2U, p, WK_PREDICATE_ID, WK_DIR_OUT, b, (int)p}, i, false});
-                    }
-                }
-            } else {
-                bool all = true;
-                for (int i = 0; i < n; ++i) {
-                    if (Q.used[(size_t)i]) continue;
-                    all = false;
-                    const int64_t a = Q.cmd[4 * i], p = Q.cmd[4 * i + 1], b = Q.cmd[4 * i + 3];
-                    const bool ka = a < 0 && Q.vars.count(a), kb = b < 0 && Q.vars.count(b);
-                    auto kind_for = [&](int64_t other) {
-                        if (other >= 0) return (int)K_K2C;
-                        return Q.vars.count(other) ? (int)K_K2K : (int)K_K2U;
-                    };
-                    if (ka) Q.cands.push_back(Cand{Step{kind_for(b), a, p, WK_DIR_OUT, b, (int)p}, i, true});
-                    if (kb) Q.cands.push_back(Cand{Step{kind_for(a), b, p, WK_DIR_IN, a, (int)p}, i, true});
-                }
-                if (all) { Q.done = true; continue; }
+    // statistics fallback for an untrusted model: queries with a statistics
+    // plan take it and skip the search
+    std::vector<std::vector<int64_t>> stats_plan((size_t)nq);
+    if (!wk_mlp_is_trusted(mlp)) {
+        std::vector<int64_t> buf;
+        for (int q = 0; q < nq; ++q) {
+            int32_t room = qs[(size_t)q].n + 1, empty = 0;
+            buf.assign((size_t)room * 4, 0);
+            double cost = 0.0;
+            int rc = wk_plan(ctx, qs[(size_t)q].cmd, qs[(size_t)q].n, buf.data(), &room, &cost, &empty);
+            if (rc) return rc;
+            if (room > 0) {
+                stats_plan[(size_t)q].assign(buf.begin(), buf.begin() + (ptrdiff_t)room * 4);
+                qs[(size_t)q].failed = true;   // excluded from the search
             }
-            if (Q.cands.empty()) { Q.done = true; Q.failed = true; continue; }
-            for (const Cand &c : Q.cands) {
-                const Step &s = c.s;
-                const VarInfo *bind = (s.kind != K_I2U && s.kind != K_C2U) ? &Q.vars[s.start] : nullptr;
-                fb.resize(fb.size() + kF);
-                features(ctx, st, s, Q.step == 0 ? 0.0 : Q.rows, Q.step, Q.cols, bind, fb.data() + fb.size() - kF);
-                pb.push_back(s.feat_pid);
-            }
-        }
-        if (pb.empty()) break;
-        pred.assign(pb.size(), 0.f);
-        int rc = wk_mlp_predict(mlp, fb.data(), pb.data(), (int64_t)pb.size(), pred.data());
-        if (rc) return rc;
-        size_t k = 0;
-        for (auto &Q : qs) {
-            if (Q.cands.empty()) continue;
-            size_t best = 0;
-            for (size_t c = 1; c < Q.cands.size(); ++c)
-                if (pred[k + c] < pred[k + best]) best = c;
-            const Cand &ch = Q.cands[best];
-            const Step &s = ch.s;
-            Q.plan.insert(Q.plan.end(), {s.start, s.pid, s.dir, s.end});
-            if (ch.consumes) Q.used[(size_t)ch.pat] = 1;
-            if (s.kind == K_I2U || s.kind == K_C2U || s.kind == K_K2U) {
-                VarInfo v;
-                v.col = Q.cols++;
-                v.pred = s.kind == K_I2U ? (int)s.start : (int)s.pid;
-                v.dir = (int)s.dir;
-                Q.vars[s.end] = v;
-            }
-            Q.rows = std::expm1((double)std::max(0.f, pred[k + best]));
-            Q.step++;
-            k += Q.cands.size();
         }
     }
+    int rc = plan_beam(ctx, mlp, qs, kBeam);
+    if (rc) return rc;
     int64_t out_at = 0;
     for (int q = 0; q < nq; ++q) {
-        QState &Q = qs[(size_t)q];
-        if (Q.failed) { n_out[q] = 0; continue; }
-        std::unordered_map<int64_t, int64_t> conv;
-        for (auto &x : Q.plan)
-            if (x < 0) {
-                auto it = conv.find(x);
-                if (it == conv.end()) {
-                    const int64_t v = -1 - (int64_t)conv.size();
-                    conv.emplace(x, v);
-                    x = v;
-                } else {
-                    x = it->second;
-                }
-            }
-        std::memcpy(cmd_out + out_at, Q.plan.data(), Q.plan.size() * sizeof(int64_t));
-        n_out[q] = (int32_t)(Q.plan.size() / 4);
-        out_at += (int64_t)Q.plan.size();
+        QPlan &Q = qs[(size_t)q];
+        if (!stats_plan[(size_t)q].empty()) {
+            const std::vector<int64_t> &sp = stats_plan[(size_t)q];
+            std::memcpy(cmd_out + out_at, sp.data(), sp.size() * sizeof(int64_t));
+            n_out[q] = (int32_t)(sp.size() / 4);
+            out_at += (int64_t)sp.size();
+            continue;
+        }
+        if (Q.failed) {
+            n_out[q] = 0;
+            continue;
+        }
+        std::vector<int64_t> plan = Q.beam[0].plan;
+        renumber(plan);
+        std::memcpy(cmd_out + out_at, plan.data(), plan.size() * sizeof(int64_t));
+        n_out[q] = (int32_t)(plan.size() / 4);
+        out_at += (int64_t)plan.size();
     }
     return WK_OK;
 }

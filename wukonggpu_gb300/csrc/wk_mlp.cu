@@ -248,6 +248,7 @@ using namespace wk::mlp;
 struct wk_mlp {
     wk_ctx *ctx = nullptr;
     int n_ids = 0;
+    int trusted = 1;             // cleared by wk_mlp_validate when held-out q-error exceeds its bound
     int cap_m = 0;               // padded batch capacity
     // fp32 master parameters, gradients, Adam moments (one contiguous block)
     float *params = nullptr, *grads = nullptr, *m1 = nullptr, *m2 = nullptr;
@@ -567,3 +568,29 @@ extern "C" int wk_mlp_predict(wk_mlp *m, const float *feats, const int32_t *pids
     m->kernels = 0;
     return WK_OK;
 }
+
+// Held-out check of the model: q-error of each sample is exp(|predicted -
+// true|) in log(1 + rows) (the ratio of the larger to the smaller of rows + 1;
+// a negative prediction counts as 0, as the planners clamp it).  The model is
+// trusted while the 95th percentile stays within qerror_bound; an untrusted
+// model makes the learned planners return the statistics plan.
+extern "C" int wk_mlp_validate(wk_mlp *m, const float *feats, const int32_t *pids, const float *target, int64_t n,
+                               double qerror_bound, double *p95_qerror, int32_t *trusted) {
+    if (!m || n < 1 || !feats || !pids || !target || !(qerror_bound >= 1.0))
+        return set_error(WK_EINVAL, "wk_mlp_validate: bad arguments");
+    std::vector<float> pred((size_t)n);
+    int st = wk_mlp_predict(m, feats, pids, n, pred.data());
+    if (st) return st;
+    std::vector<double> q((size_t)n);
+    for (int64_t i = 0; i < n; ++i)
+        q[(size_t)i] = std::exp(std::fabs((double)std::max(0.f, pred[(size_t)i]) - (double)target[(size_t)i]));
+    const size_t k = (size_t)std::ceil(0.95 * (double)n) - 1;
+    std::nth_element(q.begin(), q.begin() + (ptrdiff_t)k, q.end());
+    const double p95 = q[k];
+    m->trusted = p95 <= qerror_bound ? 1 : 0;
+    if (p95_qerror) *p95_qerror = p95;
+    if (trusted) *trusted = m->trusted;
+    return WK_OK;
+}
+
+extern "C" int wk_mlp_is_trusted(wk_mlp *m) { return m ? m->trusted : 0; }
