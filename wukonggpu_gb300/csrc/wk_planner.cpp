@@ -24,6 +24,8 @@
 #include "wk_stats.h"
 
 #include <algorithm>
+#include <mutex>
+#include <atomic>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -44,97 +46,214 @@ struct DirP {
 
 }  // namespace
 
-// Build the statistics from the host image.
+namespace {
+
+template <class F>
+void par_for(size_t n, F f) {
+    const int nt = (int)std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 64));
+    std::atomic<size_t> next{0};
+    auto w = [&]() {
+        for (;;) {
+            const size_t i = next.fetch_add(1);
+            if (i >= n) break;
+            f(i);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int i = 1; i < nt; ++i) th.emplace_back(w);
+    w();
+    for (auto &t : th) t.join();
+}
+
+// every pair of one vertex's list, by direction, into pp (p1 < p2 order)
+void count_pairs(const DirP *l, size_t k, std::vector<FourNum> &pp, size_t W) {
+    for (size_t x = 0; x < k; ++x) {
+        for (size_t y = x + 1; y < k; ++y) {
+            int p1, d1, p2, d2;
+            if (l[x].p() < l[y].p()) {
+                p1 = (int)l[x].p(); d1 = (int)l[x].dir(); p2 = (int)l[y].p(); d2 = (int)l[y].dir();
+            } else {
+                p1 = (int)l[y].p(); d1 = (int)l[y].dir(); p2 = (int)l[x].p(); d2 = (int)l[x].dir();
+            }
+            FourNum &f = pp[(size_t)p1 * W + (size_t)p2];
+            if (d1 == WK_DIR_OUT && d2 == WK_DIR_OUT) f.out_out++;
+            if (d1 == WK_DIR_OUT && d2 == WK_DIR_IN) f.out_in++;
+            if (d1 == WK_DIR_IN && d2 == WK_DIR_IN) f.in_in++;
+            if (d1 == WK_DIR_IN && d2 == WK_DIR_OUT) f.in_out++;
+        }
+    }
+}
+
+}  // namespace
+
+// Build the statistics from the host image, in parallel: per segment, the
+// counts and each key's (vertex, predicate/class, direction) entry; then the
+// entries are partitioned by vertex range, each range sorted by vertex, and
+// the pairs of every vertex's list counted.  The maps get an entry exactly
+// when the reference's iteration would create one (po[type] counts the
+// classes seen).  Pairs of one predicate with itself depend on the order of a
+// vertex's entries, but the planner never reads them (com_prune returns early
+// when pre_p == p).
 Stats *build_stats(const HostStore &hs) {
     Stats *st = new Stats();
-    st->num_ids = hs.num_ids;
-    st->pp.assign((size_t)(hs.num_ids + 1) * (size_t)(hs.num_ids + 1), FourNum());
-    std::vector<DirP> lists;
-    std::unordered_map<int, int64_t> pt, ps, po, tys;
-    for (int id = 1; id <= hs.num_ids; ++id) {
+    const int N = hs.num_ids;
+    st->num_ids = N;
+    const size_t W = (size_t)(N + 1);
+    st->pp.assign(W * W, FourNum());
+
+    // 1. entries per segment (a key, plus one per class of a typed vertex)
+    std::vector<uint64_t> cnt((size_t)N + 2, 0);
+    struct SegCounts {
+        int64_t pt = 0, ps = 0, po = 0;
+        bool has_in = false, has_out = false;
+    };
+    std::vector<SegCounts> sc((size_t)N + 1);
+    std::vector<int64_t> class_members(W, 0);   // from the type segment
+    par_for((size_t)N, [&](size_t k) {
+        const int id = (int)k + 1;
         const PredSeg &sg = hs.segs[(size_t)id];
         const uint64_t nb = (uint64_t)sg.nmain + sg.nover;
         const Bucket *base = hs.buckets + sg.bucket_off;
-        const uint32_t pid = (uint32_t)id;   // every key of a segment has the segment's id
+        uint64_t c = 0;
+        SegCounts &x = sc[(size_t)id];
+        for (uint64_t b = 0; b < nb; ++b) {
+            const uint32_t *w = base[b].w;
+            for (int i = 0; i < WK_DATA_SLOTS; ++i) {
+                const uint32_t key = w[i];
+                if (key == WK_EMPTY_KEY) continue;
+                const uint32_t deg = w[WK_DEG_WORD + i];
+                ++c;
+                if ((key & 1u) == WK_DIR_IN) {
+                    x.has_in = true;
+                    x.pt += deg;
+                    x.po += 1;
+                } else {
+                    x.has_out = true;
+                    x.ps += 1;
+                    if (id == WK_TYPE_ID) c += deg;
+                }
+            }
+        }
+        cnt[(size_t)id] = c;
+    });
+    std::vector<uint64_t> at((size_t)N + 2, 0);
+    for (int id = 1; id <= N; ++id) at[(size_t)id + 1] = at[(size_t)id] + cnt[(size_t)id];
+    const size_t n = at[(size_t)N + 1];
+    std::vector<DirP> lists(n);
+    uint32_t max_vid = 0;
+    std::mutex mu;
+    par_for((size_t)N, [&](size_t k) {
+        const int id = (int)k + 1;
+        const PredSeg &sg = hs.segs[(size_t)id];
+        const uint64_t nb = (uint64_t)sg.nmain + sg.nover;
+        const Bucket *base = hs.buckets + sg.bucket_off;
+        const uint32_t pid = (uint32_t)id;
+        DirP *o = lists.data() + at[(size_t)id];
+        uint32_t mv = 0;
+        std::vector<int64_t> local_classes;
+        if (id == WK_TYPE_ID) local_classes.assign(W, 0);
         for (uint64_t b = 0; b < nb; ++b) {
             const uint32_t *w = base[b].w;
             for (int i = 0; i < WK_DATA_SLOTS; ++i) {
                 const uint32_t key = w[i];
                 if (key == WK_EMPTY_KEY) continue;
                 const uint32_t vid = key >> 1, dir = key & 1u;
-                const uint32_t deg = w[WK_DEG_WORD + i];
-                if (dir == WK_DIR_IN) {
-                    pt[(int)pid] += deg;
-                    po[(int)pid] += 1;
-                    lists.push_back(DirP{vid, (pid << 1) | (uint32_t)WK_DIR_IN});
-                } else {
-                    ps[(int)pid] += 1;
-                    lists.push_back(DirP{vid, (pid << 1) | (uint32_t)WK_DIR_OUT});
-                    if (pid == WK_TYPE_ID) {
-                        const int32_t *e = hs.edges + sg.edge_off + w[WK_OFF_WORD + i];
-                        for (uint32_t k = 0; k < deg; ++k) {
-                            tys[e[k]] += 1;
-                            ps[e[k]] += 1;
-                            lists.push_back(DirP{vid, ((uint32_t)e[k] << 1) | (uint32_t)WK_DIR_OUT});
-                        }
+                mv = std::max(mv, vid);
+                *o++ = DirP{vid, (pid << 1) | dir};
+                if (dir == WK_DIR_OUT && id == WK_TYPE_ID) {
+                    const uint32_t deg = w[WK_DEG_WORD + i];
+                    const int32_t *e = hs.edges + sg.edge_off + w[WK_OFF_WORD + i];
+                    for (uint32_t q = 0; q < deg; ++q) {
+                        local_classes[(size_t)e[q]] += 1;
+                        *o++ = DirP{vid, ((uint32_t)e[q] << 1) | (uint32_t)WK_DIR_OUT};
                     }
                 }
             }
         }
+        std::lock_guard<std::mutex> lk(mu);
+        max_vid = std::max(max_vid, mv);
+        if (id == WK_TYPE_ID) class_members.swap(local_classes);
+    });
+
+    // 2. partition by vertex range, then per range: sort by vertex, count pairs
+    const size_t kBuckets = 4096;
+    const uint64_t span = (uint64_t)max_vid + 1;
+    auto bucket_of_vid = [&](uint32_t v) { return (size_t)(((uint64_t)v * kBuckets) / span); };
+    const size_t nchunk = 64;
+    std::vector<std::vector<uint64_t>> hist(nchunk, std::vector<uint64_t>(kBuckets, 0));
+    par_for(nchunk, [&](size_t c) {
+        const size_t a = n * c / nchunk, b = n * (c + 1) / nchunk;
+        for (size_t i = a; i < b; ++i) hist[c][bucket_of_vid(lists[i].vid)]++;
+    });
+    std::vector<uint64_t> bstart(kBuckets + 1, 0);
+    std::vector<std::vector<uint64_t>> cur(nchunk, std::vector<uint64_t>(kBuckets, 0));
+    {
+        uint64_t acc = 0;
+        for (size_t k = 0; k < kBuckets; ++k) {
+            bstart[k] = acc;
+            for (size_t c = 0; c < nchunk; ++c) {
+                cur[c][k] = acc;
+                acc += hist[c][k];
+            }
+        }
+        bstart[kBuckets] = acc;
     }
-    // correlation over each vertex's list (pairs of equal ids are never read by
-    // the planner, whose com_prune returns early when pre_p == p)
-    std::sort(lists.begin(), lists.end(), [](const DirP &a, const DirP &b) { return a.vid < b.vid; });
-    const size_t n = lists.size();
-    const int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    std::vector<std::vector<FourNum>> part((size_t)nt, std::vector<FourNum>(st->pp.size()));
+    std::vector<DirP> part(n);
+    par_for(nchunk, [&](size_t c) {
+        const size_t a = n * c / nchunk, b = n * (c + 1) / nchunk;
+        for (size_t i = a; i < b; ++i) part[cur[c][bucket_of_vid(lists[i].vid)]++] = lists[i];
+    });
+    std::vector<DirP>().swap(lists);
+    const int nt = (int)std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 64));
+    std::vector<std::vector<FourNum>> acc_pp((size_t)nt);
+    std::atomic<size_t> next{0};
     std::vector<std::thread> th;
     for (int t = 0; t < nt; ++t) {
         th.emplace_back([&, t]() {
-            size_t a = n * (size_t)t / (size_t)nt, b = n * (size_t)(t + 1) / (size_t)nt;
-            while (a > 0 && a < n && lists[a].vid == lists[a - 1].vid) ++a;   // start at a group boundary
-            while (b > 0 && b < n && lists[b].vid == lists[b - 1].vid) ++b;
-            std::vector<FourNum> &pp = part[(size_t)t];
-            const size_t W = (size_t)(st->num_ids + 1);
-            size_t i = a;
-            while (i < b) {
-                size_t j = i;
-                while (j < b && lists[j].vid == lists[i].vid) ++j;
-                for (size_t x = i; x < j; ++x) {
-                    for (size_t y = x + 1; y < j; ++y) {
-                        int p1, d1, p2, d2;
-                        if (lists[x].p() < lists[y].p()) {
-                            p1 = (int)lists[x].p(); d1 = (int)lists[x].dir(); p2 = (int)lists[y].p(); d2 = (int)lists[y].dir();
-                        } else {
-                            p1 = (int)lists[y].p(); d1 = (int)lists[y].dir(); p2 = (int)lists[x].p(); d2 = (int)lists[x].dir();
-                        }
-                        FourNum &f = pp[(size_t)p1 * W + (size_t)p2];
-                        if (d1 == WK_DIR_OUT && d2 == WK_DIR_OUT) f.out_out++;
-                        if (d1 == WK_DIR_OUT && d2 == WK_DIR_IN) f.out_in++;
-                        if (d1 == WK_DIR_IN && d2 == WK_DIR_IN) f.in_in++;
-                        if (d1 == WK_DIR_IN && d2 == WK_DIR_OUT) f.in_out++;
-                    }
+            std::vector<FourNum> &pp = acc_pp[(size_t)t];
+            pp.assign(W * W, FourNum());
+            for (;;) {
+                const size_t k = next.fetch_add(1);
+                if (k >= kBuckets) break;
+                DirP *l = part.data() + bstart[k];
+                const size_t m = bstart[k + 1] - bstart[k];
+                std::stable_sort(l, l + m, [](const DirP &x, const DirP &y) { return x.vid < y.vid; });
+                size_t i = 0;
+                while (i < m) {
+                    size_t j = i;
+                    while (j < m && l[j].vid == l[i].vid) ++j;
+                    count_pairs(l + i, j - i, pp, W);
+                    i = j;
                 }
-                i = j;
             }
         });
     }
     for (auto &x : th) x.join();
-    for (auto &pp : part)
+    for (auto &pp : acc_pp)
         for (size_t i = 0; i < pp.size(); ++i) {
             st->pp[i].out_out += pp[i].out_out;
             st->pp[i].out_in += pp[i].out_in;
             st->pp[i].in_in += pp[i].in_in;
             st->pp[i].in_out += pp[i].in_out;
         }
-    // the one-server gather (core/data_statistic.hpp:150-156)
-    st->pt = pt;
-    st->ps = ps;
-    st->po = po;
-    st->tys = tys;
-    st->po[WK_TYPE_ID] = (int64_t)tys.size();
+
+    // 3. per-predicate counts, then the one-server gather (core/data_statistic.hpp:150-156)
+    for (int id = 1; id <= N; ++id) {
+        const SegCounts &x = sc[(size_t)id];
+        if (x.has_in) {
+            st->pt[id] += x.pt;
+            st->po[id] += x.po;
+        }
+        if (x.has_out) st->ps[id] += x.ps;
+    }
+    for (size_t c = 0; c < W; ++c)
+        if (class_members[c] > 0) {
+            st->tys[(int)c] += class_members[c];
+            st->ps[(int)c] += class_members[c];
+        }
+    st->po[WK_TYPE_ID] = (int64_t)st->tys.size();
     int64_t tri = 0;
-    for (auto &kv : tys) tri += kv.second;
+    for (auto &kv : st->tys) tri += kv.second;
     st->pt[WK_TYPE_ID] = tri;
     return st;
 }
