@@ -59,6 +59,11 @@ def parse():
     ap.add_argument("--sections", default="batched,estimator,serving",
                     help="extra sections after the headline: batched, estimator, serving (comma list, or none)")
     ap.add_argument("--est-queries", type=int, default=4000, help="random BGPs executed to train the estimator")
+    ap.add_argument("--serving-scale", type=float, default=1.0,
+                    help="entity scale of the serving section's own graph (1.0 = 20M entities, 1e9 triples); "
+                         "0 serves on the single-query graph")
+    ap.add_argument("--heavy-workers", type=int, default=2,
+                    help="contexts running heavy requests in the serving loop")
     ap.add_argument("--one-query", type=int, default=-1,
                     help="run query N of the mix once, op by op, print each op's stats and exit "
                          "(a fixed launch sequence for ncu captures)")
@@ -451,7 +456,12 @@ def run_gb300(args, dist):
             if "estimator" in wanted:
                 sections["estimator"] = r
         if "serving" in wanted:
-            sections["serving"] = section_serving(rc, g, est)
+            if args.serving_scale > 0:
+                sections["serving"] = section_serving_graph(dist.local, args.serving_scale, args.est_queries,
+                                                            heavy_workers=args.heavy_workers)
+            else:
+                from wukonggpu_gb300 import workloads as _wl
+                sections["serving"] = section_serving(rc, _wl.SQ, est, heavy_workers=args.heavy_workers)
 
     if dist.rank == 0:
         line = {
@@ -601,15 +611,54 @@ def section_estimator(rc, g, n_queries: int):
             "_estimator": est}
 
 
-def section_serving(rc, g, est, n_req: int = 20000):
+def section_serving_graph(device: int, scale: float, n_bgps: int, n_req: int = 20000, heavy_workers: int = 2):
+    """The serving section on its own graph (20M entities x scale, 64 predicates,
+    ~1e9 triples at 1.0): store, statistics, an estimator trained on BGPs
+    executed on that graph, then section_serving."""
+    import wukonggpu_gb300 as W
+    from wukonggpu_gb300 import estimator, workloads
+    setup = {}
+    t0 = time.perf_counter()
+    g = W.Graph(W.spec_serving(scale=scale))
+    n_triples = int(g.n)
+    layout = workloads.Layout(16, 32, 16, 15, int(g.spec.n_entities))
+    rc = W.RCache(device=device)
+    rc.build_store_graph(g)
+    g.close()
+    setup["graph_and_store_s"] = time.perf_counter() - t0
+    info = rc.store_info()
+    t0 = time.perf_counter()
+    rc.stat(0, 1)   # the statistics are built on first use
+    setup["statistics_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    rc.set_row_limit(50_000_000)
+    bgps = workloads.random_bgps_store(rc, layout, n_bgps, seed=99)
+    ds = estimator.build_dataset(rc, bgps)
+    rc.set_row_limit(0)
+    tr, te = estimator.split(ds, 0.9, seed=3)
+    est = W.Estimator(rc, int(info["num_ids"]), max_batch=4096, seed=11)
+    est.train(tr["feats"], tr["pids"], tr["target"], epochs=30, batch=1024, lr=2e-3)
+    ev = estimator.evaluate(est, te)
+    p95_val, trusted = est.validate(te["feats"], te["pids"], te["target"], QERROR_BOUND_P95)
+    setup["estimator_s"] = time.perf_counter() - t0
+    out = section_serving(rc, layout, est, n_req, heavy_workers)
+    out["graph"] = {"triples": n_triples, "entities": layout.n_entities, "predicates": len(layout.preds),
+                    "store_device_bytes": info["device_bytes"], "setup": setup,
+                    "estimator": {"bgps": n_bgps, "qerror": ev, "held_out_qerror_p95": p95_val,
+                                  "learned_plans_used": trusted}}
+    est.close()
+    rc.close()
+    return out
+
+
+def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2):
     """Open-loop Poisson arrivals, 95% light constant-start / 5% heavy type-index
     requests: batched serving with learned plans against query-at-a-time with
     statistics plans, at swept rates."""
     import wukonggpu_gb300 as W
     from wukonggpu_gb300 import workloads
-    preds = workloads.SQ_FUNC + workloads.SQ_ZIPF + workloads.SQ_M2O
-    light = workloads.light_queries_store(rc, int(g.spec.n_entities), preds, int(n_req * 0.95), seed=23)
-    heavy_shapes = workloads.serving_heavy_queries()
+    light = workloads.light_queries_store(rc, layout.n_entities, layout.preds, int(n_req * 0.95), seed=23)
+    heavy_shapes = workloads.serving_heavy_queries(layout)
     rng = np.random.default_rng(5)
     mix = light + [heavy_shapes[int(rng.integers(0, len(heavy_shapes)))] for _ in range(n_req - len(light))]
     mix = [mix[i] for i in rng.permutation(len(mix))]
@@ -625,7 +674,7 @@ def section_serving(rc, g, est, n_req: int = 20000):
     t_learned = (time.perf_counter() - t0) / len(mix)
 
     def run(mode, plans, rate):
-        srv = W.Server(rc, mode=mode, plan=0, max_batch=4096, heavy_workers=2, batch_capacity_ints=1 << 27,
+        srv = W.Server(rc, mode=mode, plan=0, max_batch=4096, heavy_workers=heavy_workers, batch_capacity_ints=1 << 27,
                        keep_results=0)
         arr = W.poisson_arrivals(len(plans), rate, seed=7) if rate > 0 else np.zeros(len(plans))
         for q, t in zip(plans, arr):
@@ -639,9 +688,10 @@ def section_serving(rc, g, est, n_req: int = 20000):
     # capacity of the baseline: every request present at t=0
     cap0 = run(0, stats_plans, 0.0)["qps"]
     out = {"config": f"{n_req} requests: 95% light constant-start (1..4 patterns), 5% heavy type-index (4..6 patterns), "
-                     "Poisson arrivals", "baseline_capacity_qps": cap0,
+                     f"Poisson arrivals, {layout.n_entities} entities, {heavy_workers} heavy workers",
+           "baseline_capacity_qps": cap0,
            "plan_us": {"statistics": t_stats * 1e6, "learned_batched": t_learned * 1e6}, "sweep": []}
-    for f in (0.9, 1.5, 3.0, 5.0):
+    for f in (0.9, 1.5, 2.0, 2.5, 3.0, 5.0):
         rate = f * cap0
         row = {"rate_qps": rate, "query_at_a_time_stats": run(0, stats_plans, rate) if f <= 1.5 else None,
                "batched_learned": run(1, learned_plans, rate)}

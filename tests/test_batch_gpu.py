@@ -79,3 +79,21 @@ def test_bad_batch_queries_rejected(gpu_small):
         b.run([[W.VID_BASE, 2, W.OUT, -1, -1, 2, W.OUT, -2, -2, 2, W.OUT, -3]])   # 3 patterns > 2
     with pytest.raises(W.WkError):
         b.run([[-1, 2, W.OUT, -2]])                                               # no constant start
+
+
+def test_index_starts_in_a_batch(gpu_small, small_oracle, small_graph, light):
+    """Type-index and predicate-index starts run in a batch (as the list of the
+    index key) beside constant starts, each with the rows it has alone."""
+    g, s, p, o = small_graph
+    C0 = g.first_class
+    qs = [[C0, W.TYPE_ID, W.IN, -1, -1, 2, W.OUT, -2],
+          [C0 + 1, W.TYPE_ID, W.IN, -1, -1, 3, W.OUT, -2, -2, 5, W.OUT, -3],
+          [4, W.PREDICATE_ID, W.OUT, -1, -1, 4, W.IN, -2],
+          [6, W.PREDICATE_ID, W.IN, -1, -1, 6, W.OUT, -2, -1, W.TYPE_ID, W.OUT, -3]] + light[:60]
+    b = W.Batch(gpu_small, max_queries=128, max_steps=4, capacity_ints=1 << 24)
+    tabs = b.download(b.run(qs))
+    for q, t in zip(qs, tabs):
+        exp, _ = small_oracle.execute(q)
+        assert np.array_equal(oracle.canonical(t), oracle.canonical(exp)), q
+    with pytest.raises(W.WkError):
+        b.run([[C0, W.TYPE_ID, W.OUT, -1]])      # a type index is an IN list

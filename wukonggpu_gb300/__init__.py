@@ -237,6 +237,17 @@ def spec_single_query(seed: int = 20240602, scale: float = 1.0) -> wk_graph_spec
     ])
 
 
+def spec_serving(seed: int = 20240604, scale: float = 1.0) -> wk_graph_spec:
+    """20M entities (x scale), 15 classes, 16 one-to-one, 32 Zipf(1.1, cap 4096), 16 many-to-one onto
+    1% hubs: the single-query graph's degree mixes on 64 predicates.  About 1.0e9 triples at scale 1.0."""
+    n = int(20_000_000 * scale)
+    return graph_spec(seed, n, 15, [
+        dict(kind=1, count=16, participation=1.0),
+        dict(kind=0, count=32, zipf_s=1.1, zipf_cap=4096, participation=0.0017),
+        dict(kind=2, count=16, participation=1.0, hub_frac=0.01),
+    ])
+
+
 class Graph:
     """A seeded synthetic ID-form RDF graph (owned by the library)."""
 

@@ -372,6 +372,17 @@ struct wk_batch {
 
 namespace {
 
+// A batch's stream has the device's highest priority: batches are short runs
+// of small persistent kernels, and when they share the GPU with a large query
+// (a serving loop's heavy requests) the block scheduler then places their
+// blocks ahead of the large kernels' remaining blocks.
+cudaError_t create_priority_stream(cudaStream_t *st) {
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e != cudaSuccess) return e;
+    return cudaStreamCreateWithPriority(st, cudaStreamNonBlocking, greatest);
+}
+
 int64_t max_tiles(const wk_batch *b, int rounds) {
     const int64_t tr = (int64_t)kBT * rounds;
     return (b->cap_rows + tr - 1) / tr + 1;
@@ -468,7 +479,7 @@ extern "C" int wk_batch_create(wk_ctx *ctx, int32_t max_queries, int32_t max_ste
               cudaHostAlloc((void **)&b->h_desc, sizeof(StepDesc) * (size_t)max_queries * max_steps, 0) == cudaSuccess &&
               cudaHostAlloc((void **)&b->h_layout, 8 * (size_t)(3 * max_queries + 1), 0) == cudaSuccess &&
               cudaHostAlloc((void **)&b->h_flags, 64, 0) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              create_priority_stream(&b->stream) == cudaSuccess &&
               cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) == cudaSuccess;
     for (int i = 0; ok && i < 2; ++i)
         ok = cudaMalloc(&b->d_row_off[i], 8 * (size_t)(max_queries + 1)) == cudaSuccess &&
@@ -508,7 +519,10 @@ extern "C" int wk_batch_get_tuning(wk_batch *b, int32_t *blocks_per_sm, int32_t 
     return WK_OK;
 }
 
-// Fill the step descriptors from the queries; every query starts from a constant.
+// Fill the step descriptors from the queries.  A query starts from a
+// constant vertex or from an index: a type index [c, type, IN, -1] is the list
+// of key [0|c|IN] and a predicate index [p, 0, d, -1] the list of key [0|p|d]
+// (core/gstore.hpp:546-560), so both run as a constant start at vertex 0.
 static int fill_desc(wk_batch *b, const int64_t *cmd, const int32_t *npat, int32_t Q) {
     int64_t at = 0;
     const int num_ids = b->ctx->store->hs->num_ids;
@@ -520,13 +534,21 @@ static int fill_desc(wk_batch *b, const int64_t *cmd, const int32_t *npat, int32
             StepDesc &d = b->h_desc[(size_t)s * b->max_q + q];
             if (s >= n) { d = StepDesc{BK_NOP, 1, 0, 0, 0, 0}; continue; }
             const int64_t st = cmd[at + 4 * s], pid = cmd[at + 4 * s + 1], dir = cmd[at + 4 * s + 2], en = cmd[at + 4 * s + 3];
+            if (s == 0 && st > 1 && st < WK_VID_BASE) {   // index start
+                const bool ok = en == -1 && st <= num_ids &&
+                                ((pid == WK_TYPE_ID && dir == WK_DIR_IN) || (pid == WK_PREDICATE_ID && (dir == 0 || dir == 1)));
+                if (!ok) return set_error(WK_EINVAL, "wk_batch_run: query %d: bad index start", q);
+                d = StepDesc{BK_C2U, (int32_t)st, (int32_t)dir, 0, 0, 0};
+                col = 1;
+                continue;
+            }
             if (pid < 1 || pid > num_ids || (dir != 0 && dir != 1))
                 return set_error(WK_EINVAL, "wk_batch_run: query %d step %d: predicate %lld / direction %lld", q, s,
                                  (long long)pid, (long long)dir);
             const bool start_known = st < 0 && -st <= col, end_unknown = en < 0 && -en > col, end_known = en < 0 && -en <= col;
             if (s == 0) {
                 if (st < WK_VID_BASE || st > 0x7fffffffll || en != -1)
-                    return set_error(WK_EINVAL, "wk_batch_run: query %d must start from a constant vertex binding -1", q);
+                    return set_error(WK_EINVAL, "wk_batch_run: query %d must start from a constant vertex or an index, binding -1", q);
                 d = StepDesc{BK_C2U, (int32_t)pid, (int32_t)dir, 0, 0, (int32_t)st};
                 col = 1;
             } else if (start_known && end_unknown) {

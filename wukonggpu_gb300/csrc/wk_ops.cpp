@@ -121,6 +121,24 @@ int fail_corrupt(wk_ctx *ctx) {
     return set_error(WK_EDEVICE, "probe found an overflow chain longer than the segment's overflow area (corrupt store)");
 }
 
+}  // namespace
+
+int wk::reserve_op_scratch(wk_ctx *ctx, int64_t rows) {
+    if (!ctx || rows < 0) return set_error(WK_EINVAL, "reserve_op_scratch: bad arguments");
+    if (ctx->device < 0) return WK_OK;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    const int64_t nblk = (rows + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock + 1;
+    int st;
+    if ((st = ctx->deg.reserve((size_t)rows * 4)) || (st = ctx->off.reserve((size_t)rows * 4)) ||
+        (st = ctx->mask.reserve((size_t)((rows + 31) / 32) * 4)) || (st = ctx->blk_sum.reserve((size_t)nblk * 8)) ||
+        (st = ctx->blk_nz.reserve((size_t)nblk * 4)) || (st = ctx->lb_flags.reserve((size_t)nblk * 8)))
+        return st;
+    return WK_OK;
+}
+
+namespace {
+
 // zero the op totals (dscal[1..3]) before a first pass accumulates into them
 int clear_totals(wk_ctx *ctx) {
     cudaError_t e = cudaMemsetAsync(ctx->dscal.as<unsigned long long>() + 1, 0, 24, ctx->stream);

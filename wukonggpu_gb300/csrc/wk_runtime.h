@@ -91,3 +91,9 @@ struct wk_ctx {
 
     ~wk_ctx();
 };
+
+namespace wk {
+// Reserve a context's per-op scratch (per-row degree/offset/mask, per-block
+// counts and look-back words) for steps of up to `rows` input rows.
+int reserve_op_scratch(wk_ctx *ctx, int64_t rows);
+}  // namespace wk

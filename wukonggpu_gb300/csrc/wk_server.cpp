@@ -234,14 +234,13 @@ void batch_loop(wk_server *s) {
             s->batched_reqs += (int64_t)inflight[freeb].reqs.size();
             continue;
         }
-        if (idle) {
-            std::unique_lock<std::mutex> lk(s->mu);
-            double wait = 1e-3;
-            if (!s->light_q.empty()) wait = std::max(0.0, s->light_q.front()->arrival - s->now());
-            if (wait > 0) s->cv.wait_for(lk, std::chrono::duration<double>(std::min(wait, 1e-3)));
-        } else {
-            std::this_thread::yield();
-        }
+        // nothing to launch: sleep until the next arrival (at most 1 ms when
+        // idle, 20 us while a batch runs) rather than polling the device,
+        // which would contend for the driver with the heavy workers
+        std::unique_lock<std::mutex> lk(s->mu);
+        double wait = idle ? 1e-3 : 2e-5;
+        if (!s->light_q.empty()) wait = std::min(wait, std::max(0.0, s->light_q.front()->arrival - s->now()));
+        if (wait > 0) s->cv.wait_for(lk, std::chrono::duration<double>(wait));
     }
 }
 
@@ -273,11 +272,14 @@ double projected_bytes(wk_ctx *ctx, const std::vector<int64_t> &cmd, int n) {
     return bytes;
 }
 
-// the batch accepts: `<const> p d -1` first, then k2u binding the next
-// column, k2k, or k2c (mirrors fill_desc in wk_batch.cu)
-bool batch_compatible(const std::vector<int64_t> &cmd, int n, int max_steps) {
-    if (n < 1 || n > max_steps) return false;
-    if (cmd[0] < WK_VID_BASE || cmd[0] > 0x7fffffffll || cmd[3] != -1) return false;
+// the batch accepts: `<const> p d -1` or an index start first, then k2u
+// binding the next column, k2k, or k2c (mirrors fill_desc in wk_batch.cu)
+bool batch_compatible(const std::vector<int64_t> &cmd, int n, int max_steps, int num_ids) {
+    if (n < 1 || n > max_steps || cmd[3] != -1) return false;
+    const bool index_start = cmd[0] > 1 && cmd[0] < WK_VID_BASE && cmd[0] <= num_ids &&
+                             ((cmd[1] == WK_TYPE_ID && cmd[2] == WK_DIR_IN) ||
+                              (cmd[1] == WK_PREDICATE_ID && (cmd[2] == 0 || cmd[2] == 1)));
+    if (!index_start && (cmd[0] < WK_VID_BASE || cmd[0] > 0x7fffffffll)) return false;
     int col = 1;
     for (int i = 1; i < n; ++i) {
         const int64_t st = cmd[4 * i], en = cmd[4 * i + 3];
@@ -303,6 +305,11 @@ void stop_threads(wk_server *s) {
 }  // namespace
 
 using namespace wk;
+
+// Worker contexts reserve their per-op scratch for steps of this many input
+// rows up front: growing a buffer later frees the old one, and cudaFree
+// synchronises the device, stalling the light batches.
+constexpr int64_t kWorkerRows = 16ll << 20;
 
 extern "C" void wk_server_config_default(wk_server_config *c) {
     if (!c) return;
@@ -334,7 +341,9 @@ extern "C" int wk_server_create(wk_ctx *ctx, const wk_server_config *cfg, wk_ser
         wk_config_default(&wc);
         wc.device = ctx->device;
         wk_ctx *w = nullptr;
-        if ((st = wk_ctx_create(&wc, &w)) == WK_OK && (st = wk_ctx_share_store(w, ctx)) == WK_OK) s->workers.push_back(w);
+        if ((st = wk_ctx_create(&wc, &w)) == WK_OK && (st = wk_ctx_share_store(w, ctx)) == WK_OK &&
+            (st = wk::reserve_op_scratch(w, kWorkerRows)) == WK_OK)
+            s->workers.push_back(w);
         else if (w) wk_ctx_destroy(w);
     }
     if (st == WK_OK && cfg->mode == 1) {
@@ -377,7 +386,9 @@ extern "C" int64_t wk_server_submit(wk_server *s, const int64_t *cmd, int32_t np
             }
         }
     }
-    r->heavy = s->cfg.mode == 0 || !batch_compatible(r->cmd, r->npat, s->cfg.max_steps);
+    // light: a constant start the batch accepts; index starts stay heavy
+    r->heavy = s->cfg.mode == 0 || r->cmd[0] < WK_VID_BASE ||
+               !batch_compatible(r->cmd, r->npat, s->cfg.max_steps, s->ctx->store->hs->num_ids);
     r->proj_bytes = projected_bytes(s->ctx, r->cmd, r->npat);
     Req *raw = r.get();
     std::lock_guard<std::mutex> lk(s->mu);

@@ -81,12 +81,32 @@ def small_queries(s, p, o, n_ent: int = 200_000, seed: int = 7):
     ]
 
 
-# ------------------------------------------- single-query scale (100M triples)
-# spec_single_query layout: 2..9 functional, 10..25 Zipf(1.1, 4096), 26..33 many-to-one, classes 34..48
-SQ_FUNC = list(range(2, 10))
-SQ_ZIPF = list(range(10, 26))
-SQ_M2O = list(range(26, 34))
-SQ_FIRST_CLASS = 34
+# --------------------------------------------------------- predicate layouts
+class Layout:
+    """Predicate ids of a generated graph, by degree mix (generator order)."""
+
+    def __init__(self, n_func: int, n_zipf: int, n_m2o: int, n_classes: int, n_entities: int):
+        self.func = list(range(2, 2 + n_func))
+        self.zipf = list(range(2 + n_func, 2 + n_func + n_zipf))
+        self.m2o = list(range(2 + n_func + n_zipf, 2 + n_func + n_zipf + n_m2o))
+        self.first_class = 2 + n_func + n_zipf + n_m2o
+        self.n_classes = n_classes
+        self.n_entities = n_entities
+
+    @property
+    def preds(self):
+        return self.func + self.zipf + self.m2o
+
+
+# spec_single_query (100M triples): 2..9 functional, 10..25 Zipf(1.1, 4096), 26..33 many-to-one, classes 34..48
+SQ = Layout(8, 16, 8, 15, 2_000_000)
+# spec_serving (1.0e9 triples): 2..17 functional, 18..49 Zipf, 50..65 many-to-one, classes 66..80
+SV = Layout(16, 32, 16, 15, 20_000_000)
+
+SQ_FUNC = SQ.func
+SQ_ZIPF = SQ.zipf
+SQ_M2O = SQ.m2o
+SQ_FIRST_CLASS = SQ.first_class
 
 
 def scale_queries(per_shape: int = 5):
@@ -121,8 +141,22 @@ def random_bgps(s, p, o, n: int, seed: int, min_pat: int = 2, max_pat: int = 6, 
     its first variable).  A query is anchored either on a type constraint
     (``?x rdf:type C``) or on a constant vertex drawn from the subjects of its
     first predicate.  Predicates are drawn among those present in the graph."""
-    rng = np.random.default_rng(seed)
     preds = [int(x) for x in np.unique(p) if x != TYPE_ID]
+    return _random_bgps(preds, lambda pid: np.unique(s[p == pid]), n, seed, min_pat, max_pat, first_class,
+                        n_classes, const_frac)
+
+
+def random_bgps_store(rc, layout: Layout, n: int, seed: int, min_pat: int = 2, max_pat: int = 6,
+                      const_frac: float = 0.4):
+    """random_bgps for graphs too large to scan in numpy: the subjects of a
+    predicate come from the store's predicate index [0|p|IN] (ascending, the
+    same list np.unique gives), the predicates from the layout."""
+    return _random_bgps(layout.preds, lambda pid: rc.get_edges(0, pid, IN), n, seed, min_pat, max_pat,
+                        layout.first_class, layout.n_classes, const_frac)
+
+
+def _random_bgps(preds, subjects_of, n, seed, min_pat, max_pat, first_class, n_classes, const_frac):
+    rng = np.random.default_rng(seed)
     subj_by_pred = {}
     out = []
     for q in range(n):
@@ -152,7 +186,7 @@ def random_bgps(s, p, o, n: int, seed: int, min_pat: int = 2, max_pat: int = 6, 
         else:
             pid0 = pats[0][1]
             if pid0 not in subj_by_pred:
-                subj_by_pred[pid0] = np.unique(s[p == pid0])
+                subj_by_pred[pid0] = subjects_of(pid0)
             cands = subj_by_pred[pid0]
             c = int(cands[int(rng.integers(0, len(cands)))])
             # replace variable -1 by the constant everywhere
@@ -258,13 +292,14 @@ def light_queries_store(rc, n_entities: int, preds, n: int, seed: int, max_pat: 
     return out
 
 
-def serving_heavy_queries(n_classes: int = 15):
+def serving_heavy_queries(layout: Layout = SQ):
     """Heavy requests of the serving mix: 4..6 patterns from a type index,
-    widening through one-to-one and many-to-one predicates (~1.3e5 rows)."""
-    C = SQ_FIRST_CLASS
-    f, m = SQ_FUNC, SQ_M2O
+    widening through one-to-one and many-to-one predicates (one class's
+    members: ~1.3e5 rows on the 100M graph, ~1.3e6 on the 1B graph)."""
+    C = layout.first_class
+    f, m = layout.func, layout.m2o
     out = []
-    for k in range(n_classes):
+    for k in range(layout.n_classes):
         c = C + k
         base = [c, TYPE_ID, IN, -1, -1, f[k % 8], OUT, -2, -1, m[k % 8], OUT, -3, -2, f[(k + 1) % 8], OUT, -4]
         if k % 3 == 1:
