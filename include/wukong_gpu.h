@@ -291,6 +291,9 @@ typedef struct {
     int64_t light_budget_bytes;   /* admission budget of one batch                */
     int32_t plan;                 /* 0 run as given, 1 statistics planner          */
     int32_t keep_results;         /* 1 keep every result table on the host         */
+    int32_t batch_window_us;      /* a light batch launches once its oldest request
+                                     has waited this long, or it is full (0: as
+                                     soon as a batch object is free)             */
 } wk_server_config;
 
 typedef struct {

@@ -22,9 +22,10 @@ def mix(small_graph, golden_small):
     return [qs[i] for i in order]
 
 
-@pytest.mark.parametrize("mode,plan", [(0, 0), (1, 0), (1, 1)])
-def test_results_alone_equal_results_in_the_mix(gpu_small, small_oracle, mix, mode, plan):
-    srv = W.Server(gpu_small, mode=mode, plan=plan, max_batch=512, heavy_workers=2, batch_capacity_ints=1 << 24)
+@pytest.mark.parametrize("mode,plan,window_us", [(0, 0, 0), (1, 0, 0), (1, 1, 0), (1, 0, 400)])
+def test_results_alone_equal_results_in_the_mix(gpu_small, small_oracle, mix, mode, plan, window_us):
+    srv = W.Server(gpu_small, mode=mode, plan=plan, max_batch=512, heavy_workers=2, batch_capacity_ints=1 << 24,
+                   batch_window_us=window_us)
     arr = W.poisson_arrivals(len(mix), rate_qps=50_000.0, seed=1)
     ids = [srv.submit(q, float(t)) for q, t in zip(mix, arr)]
     srv.start()

@@ -60,7 +60,7 @@ class wk_op_stats(C.Structure):
 class wk_server_config(C.Structure):
     _fields_ = [("mode", C.c_int32), ("max_batch", C.c_int32), ("max_steps", C.c_int32), ("heavy_workers", C.c_int32),
                 ("batch_capacity_ints", C.c_int64), ("light_budget_bytes", C.c_int64), ("plan", C.c_int32),
-                ("keep_results", C.c_int32)]
+                ("keep_results", C.c_int32), ("batch_window_us", C.c_int32)]
 
 
 class wk_server_stats(C.Structure):

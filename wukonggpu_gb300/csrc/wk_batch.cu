@@ -28,6 +28,7 @@
 // out in exactly the order the query produces alone.
 #include <algorithm>
 #include <cstring>
+#include <unordered_map>
 #include <vector>
 
 #include "wk_probe.cuh"
@@ -362,9 +363,11 @@ struct wk_batch {
     int64_t *h_layout = nullptr;            // row_off (Q+1), int_off (Q), cols as int64 (Q)
     int *h_flags = nullptr;
     // graph
-    cudaGraphExec_t gexec = nullptr;
-    int graph_q = -1;
+    // executable graphs by batch size (a serving loop's batch sizes vary from
+    // batch to batch; each size is captured once), all for graph_tune
+    std::unordered_map<int, cudaGraphExec_t> graphs;
     BatchTune graph_tune{0, 0, 0};
+    cudaGraphExec_t gexec = nullptr;   // the last one launched
     int32_t last_q = 0;
     int final_buf = 0;
     int64_t kernels = 0;
@@ -391,7 +394,8 @@ int64_t max_tiles(const wk_batch *b, int rounds) {
 void free_batch(wk_batch *b) {
     cudaSetDevice(b->ctx->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
-    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
     if (b->done) cudaEventDestroy(b->done);
     if (b->stream) cudaStreamDestroy(b->stream);
     cudaFree(b->d_pvs); cudaFree(b->d_desc);
@@ -429,12 +433,21 @@ StepIO make_io(wk_batch *b, int s, int Q) {
 
 // the whole batch: descriptor upload, layout init, max_steps x (count, scan, write)
 int enqueue(wk_batch *b, int Q, const BatchTune &t, cudaStream_t st) {
-    cudaError_t e = cudaMemcpyAsync(b->d_desc, b->h_desc, sizeof(StepDesc) * (size_t)b->max_q * b->max_steps,
-                                    cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(e, "batch descriptors");
+    // the Q descriptors of each step (step s's start at s * max_q)
+    for (int s = 0; s < b->max_steps; ++s) {
+        const size_t at = (size_t)s * b->max_q;
+        cudaError_t e = cudaMemcpyAsync(b->d_desc + at, b->h_desc + at, sizeof(StepDesc) * (size_t)Q,
+                                        cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(e, "batch descriptors");
+    }
     batch_init_kernel<<<(Q + 256) / 256, 256, 0, st>>>(Q, b->d_row_off[0], b->d_int_off[0], b->d_cols[0], b->d_qrows,
                                                        b->d_flags);
-    const unsigned grid = (unsigned)(b->sms * t.blocks_per_sm);
+    // The step kernels loop over tiles, so any grid gives the same rows.  A
+    // small batch gets a grid in proportion to its queries (at least a
+    // quarter of the SMs): beside a large query on another stream, a few
+    // light queries then hold a few SMs, not all of them.
+    const int64_t full = (int64_t)b->sms * t.blocks_per_sm;
+    const unsigned grid = (unsigned)std::min<int64_t>(full, std::max<int64_t>(b->sms / 4, 2 * (int64_t)Q));
     const size_t sm_off = sizeof(int64_t) * (size_t)(Q + 1);
     for (int s = 0; s < b->max_steps; ++s) {
         StepIO io = make_io(b, s, Q);
@@ -442,7 +455,7 @@ int enqueue(wk_batch *b, int Q, const BatchTune &t, cudaStream_t st) {
         batch_scan_kernel<<<1, 1024, 0, st>>>(io, t.rounds);
         batch_write_kernel<<<grid, kBT, sm_off, st>>>(io, t.rounds, t.split);
     }
-    e = cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "batch launch");
     b->kernels += 1 + 3 * (int64_t)b->max_steps;
     return WK_OK;
@@ -581,8 +594,13 @@ extern "C" int wk_batch_launch(wk_batch *b, const int64_t *cmd_chains, const int
     if (st) return st;
     cudaStream_t s = b->stream;
     if (use_graph) {
-        if (!b->gexec || b->graph_q != nq || std::memcmp(&b->graph_tune, &b->tune, sizeof(BatchTune)) != 0) {
-            if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
+        if (std::memcmp(&b->graph_tune, &b->tune, sizeof(BatchTune)) != 0 || b->graphs.size() >= 512) {
+            for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+            b->graphs.clear();
+            b->graph_tune = b->tune;
+        }
+        auto it = b->graphs.find(nq);
+        if (it == b->graphs.end()) {
             cudaGraph_t g;
             if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
                 return cuda_fail(e, "batch capture");
@@ -590,13 +608,14 @@ extern "C" int wk_batch_launch(wk_batch *b, const int64_t *cmd_chains, const int
             e = cudaStreamEndCapture(s, &g);
             if (st) { if (e == cudaSuccess) cudaGraphDestroy(g); return st; }
             if (e != cudaSuccess) return cuda_fail(e, "batch capture end");
-            e = cudaGraphInstantiate(&b->gexec, g, 0);
+            cudaGraphExec_t ge = nullptr;
+            e = cudaGraphInstantiate(&ge, g, 0);
             cudaGraphDestroy(g);
-            if (e != cudaSuccess) { b->gexec = nullptr; return cuda_fail(e, "batch graph instantiate"); }
-            b->graph_q = nq;
-            b->graph_tune = b->tune;
+            if (e != cudaSuccess) return cuda_fail(e, "batch graph instantiate");
+            it = b->graphs.emplace(nq, ge).first;
             b->kernels -= 1 + 3 * (int64_t)b->max_steps;   // capture does not launch
         }
+        b->gexec = it->second;
         if ((e = cudaGraphLaunch(b->gexec, s)) != cudaSuccess) return cuda_fail(e, "batch graph launch");
         b->kernels += 1 + 3 * (int64_t)b->max_steps;
     } else {

@@ -194,6 +194,7 @@ void batch_loop(wk_server *s) {
     std::vector<int64_t> cmd;
     std::vector<int32_t> npat;
     const double budget = (double)s->cfg.light_budget_bytes;
+    const double window = 1e-6 * (double)std::max(0, s->cfg.batch_window_us);
     while (true) {
         // retire finished batches
         for (int i = 0; i < 2; ++i)
@@ -205,8 +206,21 @@ void batch_loop(wk_server *s) {
         if (freeb >= 0) {
             std::lock_guard<std::mutex> lk(s->mu);
             const double t = s->now();
+            // the batching window: wait for more arrivals while the oldest
+            // request has waited less than the window and the batch is not full
+            bool ready = !s->light_q.empty() && s->light_q.front()->arrival <= t;
+            if (ready && window > 0.0 && t - s->light_q.front()->arrival < window) {
+                double pb = 0.0;
+                int n = 0;
+                for (Req *r : s->light_q) {
+                    if (r->arrival > t || n >= s->cfg.max_batch) break;
+                    pb += r->proj_bytes;
+                    ++n;
+                }
+                ready = n >= s->cfg.max_batch || pb > budget;
+            }
             double bytes = 0.0;
-            while (!s->light_q.empty() && (int)take.size() < s->cfg.max_batch) {
+            while (ready && !s->light_q.empty() && (int)take.size() < s->cfg.max_batch) {
                 Req *r = s->light_q.front();
                 if (r->arrival > t) break;
                 if (!take.empty() && bytes + r->proj_bytes > budget) break;
@@ -239,7 +253,11 @@ void batch_loop(wk_server *s) {
         // which would contend for the driver with the heavy workers
         std::unique_lock<std::mutex> lk(s->mu);
         double wait = idle ? 1e-3 : 2e-5;
-        if (!s->light_q.empty()) wait = std::min(wait, std::max(0.0, s->light_q.front()->arrival - s->now()));
+        if (!s->light_q.empty()) {
+            const double a0 = s->light_q.front()->arrival, t = s->now();
+            const double next = a0 <= t ? a0 + window : a0;   // window end, or the next arrival
+            wait = std::min(wait, std::max(0.0, next - t));
+        }
         if (wait > 0) s->cv.wait_for(lk, std::chrono::duration<double>(wait));
     }
 }
