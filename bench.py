@@ -611,6 +611,21 @@ def section_estimator(rc, g, n_queries: int):
             "_estimator": est}
 
 
+def _bindings_digest(table, cols):
+    """Order-free digest of a table's columns `cols` (row count, sum of mixed row hashes)."""
+    if table.size == 0:
+        return (0, 0)
+    t = np.ascontiguousarray(table[:, cols]).astype(np.uint64)
+    h = np.zeros(t.shape[0], np.uint64)
+    with np.errstate(over="ignore"):
+        for j in range(t.shape[1]):
+            h = (h * np.uint64(0x100000001B3)) ^ t[:, j]
+            h ^= h >> np.uint64(29)
+            h *= np.uint64(0xBF58476D1CE4E5B9)
+            h ^= h >> np.uint64(32)
+        return (int(t.shape[0]), int(h.sum(dtype=np.uint64)))
+
+
 def section_serving_graph(device: int, scale: float, n_bgps: int, n_req: int = 20000, heavy_workers: int = 2):
     """The serving section on its own graph (20M entities x scale, 64 predicates,
     ~1e9 triples at 1.0): store, statistics, an estimator trained on BGPs
@@ -658,20 +673,41 @@ def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2)
     import wukonggpu_gb300 as W
     from wukonggpu_gb300 import workloads
     light = workloads.light_queries_store(rc, layout.n_entities, layout.preds, int(n_req * 0.95), seed=23)
-    heavy_shapes = workloads.serving_heavy_queries(layout)
+    heavy_shapes = workloads.serving_heavy_queries(layout)          # SPARQL triple form
+    heavy_exec = workloads.executable_heavy_queries(layout)         # the same shapes, executable
     rng = np.random.default_rng(5)
-    mix = light + [heavy_shapes[int(rng.integers(0, len(heavy_shapes)))] for _ in range(n_req - len(light))]
+    # (query, what runs when a planner gives no plan): light queries are executable as written
+    mix = [(q, q) for q in light]
+    for _ in range(n_req - len(light)):
+        k = int(rng.integers(0, len(heavy_shapes)))
+        mix.append((heavy_shapes[k], heavy_exec[k]))
     mix = [mix[i] for i in rng.permutation(len(mix))]
     t0 = time.perf_counter()
     stats_plans = []
-    for q in mix:
+    for q, ex in mix:
         pq, _ = rc.plan(q)
-        stats_plans.append(pq if pq else q)
+        stats_plans.append(pq if pq else ex)
     t_stats = (time.perf_counter() - t0) / len(mix)
     t0 = time.perf_counter()
-    lp = est.plan_many(mix) if est is not None else stats_plans
-    learned_plans = [x if x else q for x, q in zip(lp, mix)]
+    lp = est.plan_many([q for q, _ in mix]) if est is not None else [[] for _ in mix]
+    learned_plans = [x if x else ex for x, (q, ex) in zip(lp, mix)]
     t_learned = (time.perf_counter() - t0) / len(mix)
+    # every heavy shape: its statistics and learned plans bind the same rows as its executable form
+    from wukonggpu_gb300 import plans as _plans
+    shape_plans = {}
+    for (q, ex), sp, lq in zip(mix, stats_plans, learned_plans):
+        if q is not ex:
+            shape_plans[tuple(q)] = (ex, sp, lq)
+    checked = mismatched = 0
+    for q, (ex, sp, lq) in shape_plans.items():
+        req, _ = rc.execute(ex)
+        ref = _bindings_digest(req.result_table, list(range(req.result_table.shape[1])))
+        for pl in (sp, lq):
+            req, _ = rc.execute(pl)
+            cols = _plans.plan_columns(list(q), pl) if pl is not ex else list(range(req.result_table.shape[1]))
+            ok = cols is not None and _bindings_digest(req.result_table, cols) == ref
+            mismatched += 0 if ok else 1
+            checked += 1
 
     def run(mode, plans, rate):
         srv = W.Server(rc, mode=mode, plan=0, max_batch=4096, heavy_workers=heavy_workers, batch_capacity_ints=1 << 27,
@@ -690,7 +726,8 @@ def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2)
     out = {"config": f"{n_req} requests: 95% light constant-start (1..4 patterns), 5% heavy type-index (4..6 patterns), "
                      f"Poisson arrivals, {layout.n_entities} entities, {heavy_workers} heavy workers",
            "baseline_capacity_qps": cap0,
-           "plan_us": {"statistics": t_stats * 1e6, "learned_batched": t_learned * 1e6}, "sweep": []}
+           "plan_us": {"statistics": t_stats * 1e6, "learned_batched": t_learned * 1e6},
+           "heavy_plans_checked": {"plans": checked, "bindings_differ": mismatched}, "sweep": []}
     for f in (0.9, 1.5, 2.0, 2.5, 3.0, 5.0):
         rate = f * cap0
         row = {"rate_qps": rate, "query_at_a_time_stats": run(0, stats_plans, rate) if f <= 1.5 else None,

@@ -336,7 +336,10 @@ int wk_sync(wk_ctx *ctx);
  * Statistics-based plan of a BGP: Planner::generate_plan
  * (core/planner.hpp:927-1028) over the statistics of
  * GStore::generate_statistic (core/gstore.hpp:1010-1127).  The input is a
- * BGP in cmd_chains form (any variable numbering, 1..10 patterns); the output
+ * BGP in SPARQL triple form (every pattern (subject, predicate, OUT, object),
+ * any variable numbering, 1..10 patterns); a query already in executable form
+ * (IN steps, an index start) gets no plan (*n_out = 0, cost +inf) and is run
+ * as written.  The output
  * is the executable order (possibly starting with an inserted index pattern)
  * with variables renumbered -1, -2, ... in plan order.  *n_out holds the room
  * of cmd_out in patterns on entry and the plan's patterns on return.  When

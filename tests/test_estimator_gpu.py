@@ -136,3 +136,16 @@ def test_untrusted_model_falls_back_to_statistics_plans(gpu_small, small_graph):
     # a bound the model meets restores it
     p95b, okb = est.validate(ds["feats"], ds["pids"], ds["target"], qerror_bound=p95 * 2 + 1.0)
     assert okb and est.trusted
+
+
+def test_learned_planner_leaves_executable_queries_as_written(gpu_small, small_graph):
+    """Like the statistics planner, the learned one plans SPARQL triple form
+    only: an IN step or an index start means the query is already executable."""
+    g, s, p, o = small_graph
+    est = W.Estimator(gpu_small, g.num_ids, max_batch=1024, seed=3)
+    qs = [[W.VID_BASE + 5, 2, W.IN, -1],
+          [g.first_class, W.TYPE_ID, W.IN, -1, -1, 2, W.OUT, -2],
+          [2, W.PREDICATE_ID, W.OUT, -1, -1, 2, W.IN, -2]]
+    for q in qs:
+        assert est.plan(q)[0] == [], q
+    assert est.plan_many(qs) == [[], [], []]

@@ -107,3 +107,32 @@ def test_plans_match_reference_fixture(host_ctx, golden_small):
     for rec in golden_small["plans"]:
         mine, _ = host_ctx.plan(rec["bgp"])
         assert mine == rec["plan"], rec
+
+
+def test_executable_queries_are_left_as_written(host_ctx):
+    """The planner's input is SPARQL triple form.  A query already in the
+    engine's executable form (IN steps, an index start) gets no plan and is run
+    as written, never re-read as triples."""
+    for q in ([W.VID_BASE + 5, 2, W.IN, -1],
+              [17, W.TYPE_ID, W.IN, -1, -1, 2, W.OUT, -2],
+              [2, W.PREDICATE_ID, W.OUT, -1, -1, 2, W.IN, -2]):
+        pq, cost = host_ctx.plan(q)
+        assert pq == [] and cost == float("inf"), q
+
+
+def test_planned_heavy_shapes_keep_their_bindings(host_ctx, small_graph, small_oracle):
+    """The serving mix's heavy shapes, written as triples, planned by the
+    statistics planner, bind the same rows as their executable form."""
+    from wukonggpu_gb300 import plans, workloads
+    g, s, p, o = small_graph
+    layout = workloads.Layout(8, 0, 7, 10, 200_000)   # ids only: 2..9 and 10..16 as the two predicate groups
+    assert layout.first_class == g.first_class
+    layout.m2o = layout.m2o + [2]                      # the shapes take 8 of each group
+    for q, ex in zip(workloads.serving_heavy_queries(layout), workloads.executable_heavy_queries(layout)):
+        pq, _ = host_ctx.plan(q)
+        assert pq, q
+        cols = plans.plan_columns(q, pq)
+        a, _ = small_oracle.execute(pq)
+        b, _ = small_oracle.execute(ex)
+        A = oracle.canonical(a[:, cols]) if a.size else a.reshape(0, len(cols))
+        assert A.shape == b.shape and np.array_equal(A, oracle.canonical(b)), (q, pq)

@@ -62,6 +62,20 @@ WK_HD uint32_t seg_bucket(uint32_t key, uint32_t n) {
     return (uint32_t)(((uint64_t)seg_mix(key) * (uint64_t)n) >> 32);
 }
 
+// A BGP in SPARQL triple form, the planners' input: every pattern is
+// (subject, predicate, OUT, object) with a variable or a vertex as subject,
+// and a variable, a vertex, or (for rdf:type) a class as object.  The
+// engine's executable form (IN steps, index starts) is not triple form.
+inline bool triple_form(const int64_t *cmd, int n) {
+    for (int i = 0; i < n; ++i) {
+        const int64_t s = cmd[4 * i], p = cmd[4 * i + 1], d = cmd[4 * i + 2], o = cmd[4 * i + 3];
+        if (d != WK_DIR_OUT || p < 1) return false;
+        if (s >= 0 && s < WK_VID_BASE) return false;
+        if (o >= 0 && o < WK_VID_BASE && !(p == WK_TYPE_ID && o > 1)) return false;
+    }
+    return true;
+}
+
 struct alignas(WK_BUCKET_BYTES) Bucket {
     uint32_t w[WK_BUCKET_WORDS];
 };

@@ -32,7 +32,8 @@
 // Learned planner: beam search over join orders.  A partial plan is extended
 // by every executable pattern -- oriented from a bound end, or for the first
 // step from a constant, a type index or a predicate index -- and the model
-// predicts the rows after each extension.  A plan's cost is the sum of the
+// predicts the rows after each extension (a first step's rows are exact: the
+// length of one stored list).  A plan's cost is the sum of the
 // predicted rows of every table it builds; each level keeps the cheapest few
 // partial plans (ties: lower pattern index, then OUT before IN).  The result
 // has the statistics planner's output format: executable order, variables
@@ -312,6 +313,7 @@ int plan_beam(wk_ctx *ctx, wk_mlp *mlp, std::vector<QPlan> &qs, int beam) {
     struct Kid {
         int q, parent;
         Cand c;
+        double exact;   // the rows of an index or constant start (one list's length), else < 0
     };
     std::vector<float> fb, pred;
     std::vector<int32_t> pb;
@@ -339,7 +341,10 @@ int plan_beam(wk_ctx *ctx, wk_mlp *mlp, std::vector<QPlan> &qs, int beam) {
                     features(ctx, st, s, S.step == 0 ? 0.0 : S.rows, S.step, S.cols, bind,
                              fb.data() + fb.size() - kF);
                     pb.push_back(s.feat_pid);
-                    kids.push_back(Kid{q, si, c});
+                    double exact = -1.0;
+                    if (s.kind == K_I2U) exact = (double)list_len(ctx, 0, (int)s.start, (int)s.dir);
+                    else if (s.kind == K_C2U) exact = (double)list_len(ctx, (uint64_t)s.start, (int)s.pid, (int)s.dir);
+                    kids.push_back(Kid{q, si, c, exact});
                 }
             }
         }
@@ -358,7 +363,8 @@ int plan_beam(wk_ctx *ctx, wk_mlp *mlp, std::vector<QPlan> &qs, int beam) {
             bool expanded = false;
             while (k < kids.size() && kids[k].q == q) {
                 const Kid &kd = kids[k];
-                next.push_back(apply(Q.beam[(size_t)kd.parent], kd.c, std::expm1((double)std::max(0.f, pred[k]))));
+                const double rows = kd.exact >= 0.0 ? kd.exact : std::expm1((double)std::max(0.f, pred[k]));
+                next.push_back(apply(Q.beam[(size_t)kd.parent], kd.c, rows));
                 expanded = true;
                 ++k;
             }
@@ -410,6 +416,11 @@ extern "C" int wk_plan_learned(wk_ctx *ctx, wk_mlp *mlp, const int64_t *cmd_in, 
     if (!ctx || !mlp || !cmd_in || !cmd_out || !n_out || n < 1 || n > 10)
         return set_error(WK_EINVAL, "wk_plan_learned: bad arguments");
     if (!ctx->store) return set_error(WK_ENOSTORE, "wk_plan_learned: no store");
+    if (!triple_form(cmd_in, n)) {   // already executable: no plan, run as written
+        *n_out = 0;
+        if (est_log_rows) *est_log_rows = INFINITY;
+        return WK_OK;
+    }
     if (!wk_mlp_is_trusted(mlp)) {   // statistics fallback
         int32_t room = *n_out, empty = 0;
         double cost = 0.0;
@@ -458,6 +469,7 @@ extern "C" int wk_plan_learned_batch(wk_ctx *ctx, wk_mlp *mlp, const int64_t *cm
             return set_error(WK_EINVAL, "wk_plan_learned_batch: query %d has %d patterns", q, n_in[q]);
         qs[(size_t)q].cmd = cmd_in + at;
         qs[(size_t)q].n = n_in[q];
+        if (!triple_form(qs[(size_t)q].cmd, n_in[q])) qs[(size_t)q].failed = true;   // no plan: run as written
         at += 4 * (int64_t)n_in[q];
     }
     // statistics fallback for an untrusted model: queries with a statistics

@@ -556,6 +556,11 @@ extern "C" int wk_plan(wk_ctx *ctx, const int64_t *cmd_in, int32_t n, int64_t *c
         return set_error(WK_EINVAL, "wk_plan: bad arguments (1..10 patterns)");
     if (!ctx->store) return set_error(WK_ENOSTORE, "wk_plan: no store built");
     if (proved_empty) *proved_empty = 0;
+    if (!triple_form(cmd_in, n)) {   // already executable (IN steps, an index start): run as written
+        *n_out = 0;
+        if (est_cost) *est_cost = std::numeric_limits<double>::infinity();
+        return WK_OK;
+    }
     if (!ctx->store->stats) ctx->store->stats.reset(build_stats(*ctx->store->hs), free_stats);
     std::vector<int64_t> cmd(cmd_in, cmd_in + (size_t)n * 4);
     double cost = 0.0;

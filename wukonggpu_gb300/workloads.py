@@ -293,9 +293,20 @@ def light_queries_store(rc, n_entities: int, preds, n: int, seed: int, max_pat: 
 
 
 def serving_heavy_queries(layout: Layout = SQ):
-    """Heavy requests of the serving mix: 4..6 patterns from a type index,
-    widening through one-to-one and many-to-one predicates (one class's
-    members: ~1.3e5 rows on the 100M graph, ~1.3e6 on the 1B graph)."""
+    """Heavy requests of the serving mix, in SPARQL triple form: 4..6 patterns
+    around the members of one class (?x rdf:type C), widening through
+    one-to-one and many-to-one predicates (one class's members: ~1.3e5 rows
+    on the 100M graph, ~1.3e6 on the 1B graph).  A planner starts them from
+    the type index; executable_heavy_queries gives that order directly."""
+    out = []
+    for ex in executable_heavy_queries(layout):
+        c = ex[0]
+        out.append([-1, TYPE_ID, OUT, c] + ex[4:])
+    return out
+
+
+def executable_heavy_queries(layout: Layout = SQ):
+    """The heavy shapes in executable form: type index [C, type, IN, ?x] first."""
     C = layout.first_class
     f, m = layout.func, layout.m2o
     out = []
