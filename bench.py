@@ -58,7 +58,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sections", default="batched,estimator,serving",
                     help="extra sections after the headline: batched, estimator, serving (comma list, or none)")
-    ap.add_argument("--est-queries", type=int, default=4000, help="random BGPs executed to train the estimator")
+    ap.add_argument("--est-queries", type=int, default=200000,
+                    help="random BGPs executed to train and test the estimator section's model")
+    ap.add_argument("--serving-est-queries", type=int, default=4000,
+                    help="random BGPs executed on the serving graph to train its planner's model")
     ap.add_argument("--serving-scale", type=float, default=1.0,
                     help="entity scale of the serving section's own graph (1.0 = 20M entities, 1e9 triples); "
                          "0 serves on the single-query graph")
@@ -457,7 +460,7 @@ def run_gb300(args, dist):
                 sections["estimator"] = r
         if "serving" in wanted:
             if args.serving_scale > 0:
-                sections["serving"] = section_serving_graph(dist.local, args.serving_scale, args.est_queries,
+                sections["serving"] = section_serving_graph(dist.local, args.serving_scale, args.serving_est_queries,
                                                             heavy_workers=args.heavy_workers)
             else:
                 from wukonggpu_gb300 import workloads as _wl
