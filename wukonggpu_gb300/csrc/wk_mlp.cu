@@ -4,9 +4,10 @@
 // Model: x = [48 pattern features | 32-d embedding of the predicate] (80)
 //        -> 256 -> 256 -> 256 (GELU after each) -> 1
 // It predicts log(1 + rows) of the table after a pattern is applied.  Weights
-// and activations are BF16, every product accumulates in FP32 on the tensor
-// cores (mma.sync m16n8k16 bf16), and the optimiser is FP32 Adam over FP32
-// master weights whose BF16 copies are refreshed after each step.
+// and activations are BF16, every product accumulates in FP32 in tensor
+// memory on the 5th-generation tensor cores (tcgen05.mma with TMA-staged
+// operands, wk_tc_gemm.cuh), and the optimiser is FP32 Adam over FP32 master
+// weights whose BF16 copies are refreshed after each step.
 //
 // One GEMM kernel does all products: C[M x N] = A[M x K] . B[N x K]^T with A
 // and B row-major (K contiguous), which is the natural form for the forward
@@ -23,6 +24,7 @@
 #include <cuda_bf16.h>
 
 #include "wk_runtime.h"
+#include "wk_tc_gemm.cuh"
 
 namespace wk {
 namespace mlp {
@@ -33,76 +35,6 @@ constexpr int kX = kIn + kEmb;   // 80
 constexpr int kH = 256;
 constexpr int kOutPad = 64;   // output layer padded to one GEMM tile
 constexpr int kXPadN = 128;   // W1^T rows padded (dX GEMM has N = 80 -> 128)
-
-// ------------------------------------------------------------------ GEMM
-constexpr int BM = 64, BN = 64, BK = 16, SK = 24;   // smem row stride (bf16) avoids bank conflicts
-
-__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
-
-// C = A . B^T (+ bias[n]); A [M x K] lda, B [N x K] ldb, C fp32 [M x N] ldc.
-// M, N multiples of 64; K multiple of 16.  128 threads, 64 x 64 tile, each
-// warp a 32 x 32 sub-tile of 2 x 4 m16n8k16 products.
-__global__ void __launch_bounds__(128)
-gemm_tn_kernel(const __nv_bfloat16 *__restrict__ A, int lda, const __nv_bfloat16 *__restrict__ B, int ldb,
-               float *__restrict__ C, int ldc, int K, const float *__restrict__ bias) {
-    __shared__ __align__(16) __nv_bfloat16 As[BM * SK];
-    __shared__ __align__(16) __nv_bfloat16 Bs[BN * SK];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-    float acc[2][4][4];
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
-    const int lr = tid >> 1, lc = (tid & 1) * 8;   // one 16 B load per thread per operand
-    for (int k0 = 0; k0 < K; k0 += BK) {
-        *reinterpret_cast<uint4 *>(&As[lr * SK + lc]) =
-            *reinterpret_cast<const uint4 *>(A + (size_t)(m0 + lr) * lda + k0 + lc);
-        *reinterpret_cast<uint4 *>(&Bs[lr * SK + lc]) =
-            *reinterpret_cast<const uint4 *>(B + (size_t)(n0 + lr) * ldb + k0 + lc);
-        __syncthreads();
-        uint32_t a[2][4], b[4][2];
-#pragma unroll
-        for (int mi = 0; mi < 2; ++mi) {
-            const int r = wm + mi * 16 + g;
-            a[mi][0] = ld32(&As[r * SK + 2 * t]);
-            a[mi][1] = ld32(&As[(r + 8) * SK + 2 * t]);
-            a[mi][2] = ld32(&As[r * SK + 2 * t + 8]);
-            a[mi][3] = ld32(&As[(r + 8) * SK + 2 * t + 8]);
-        }
-#pragma unroll
-        for (int ni = 0; ni < 4; ++ni) {
-            const int c = wn + ni * 8 + g;
-            b[ni][0] = ld32(&Bs[c * SK + 2 * t]);
-            b[ni][1] = ld32(&Bs[c * SK + 2 * t + 8]);
-        }
-#pragma unroll
-        for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-            for (int ni = 0; ni < 4; ++ni)
-                asm volatile(
-                    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-                    "{%8,%9}, {%0,%1,%2,%3};"
-                    : "+f"(acc[mi][ni][0]), "+f"(acc[mi][ni][1]), "+f"(acc[mi][ni][2]), "+f"(acc[mi][ni][3])
-                    : "r"(a[mi][0]), "r"(a[mi][1]), "r"(a[mi][2]), "r"(a[mi][3]), "r"(b[ni][0]), "r"(b[ni][1]));
-        __syncthreads();
-    }
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-        for (int ni = 0; ni < 4; ++ni) {
-            const int r = m0 + wm + mi * 16 + g, c = n0 + wn + ni * 8 + 2 * t;
-            const float b0 = bias ? bias[c] : 0.f, b1 = bias ? bias[c + 1] : 0.f;
-            C[(size_t)r * ldc + c] = acc[mi][ni][0] + b0;
-            C[(size_t)r * ldc + c + 1] = acc[mi][ni][1] + b1;
-            C[(size_t)(r + 8) * ldc + c] = acc[mi][ni][2] + b0;
-            C[(size_t)(r + 8) * ldc + c + 1] = acc[mi][ni][3] + b1;
-        }
-}
 
 // ------------------------------------------------------------ elementwise
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
@@ -264,6 +196,9 @@ struct wk_mlp {
     int32_t *pids = nullptr;
     int64_t step = 0;
     int64_t kernels = 0;
+    int *d_err = nullptr;        // device flag of the tensor-core GEMM (bit 2: a wait ran out)
+    int *h_err = nullptr;        // pinned mirror
+    int status = 0;              // a host-side GEMM failure since the last check
 };
 
 namespace {
@@ -286,11 +221,45 @@ void refresh_bf16(wk_mlp *m, cudaStream_t s) {
     m->kernels += 4;
 }
 
+// C = A . B^T (+ bias) on the tensor cores (wk_tc_gemm.cuh); N is 64, 128 or 256.
+// A tensor-map failure or an unsupported N is recorded in m->status and
+// reported by the entry point that called this.
 void gemm(wk_mlp *m, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N,
           int K, const float *bias, cudaStream_t s) {
-    dim3 grid((unsigned)(N / BN), (unsigned)(M / BM));
-    gemm_tn_kernel<<<grid, 128, 0, s>>>(A, lda, B, ldb, C, ldc, K, bias);
+    CUtensorMap ta, tb;
+    if (!tc::make_map(&ta, A, (uint64_t)M, (uint64_t)K, (uint64_t)lda, tc::kTM) ||
+        !tc::make_map(&tb, B, (uint64_t)N, (uint64_t)K, (uint64_t)ldb, (uint32_t)N)) {
+        if (!m->status) m->status = set_error(WK_EDEVICE, "estimator GEMM: tensor map (M %d, N %d, K %d)", M, N, K);
+        return;
+    }
+    const dim3 grid((unsigned)((M + tc::kTM - 1) / tc::kTM), 1);
+    switch (N) {
+        case 64: tc::gemm_tc_kernel<64><<<grid, tc::kThreads, tc::smem_bytes(64), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
+        case 128: tc::gemm_tc_kernel<128><<<grid, tc::kThreads, tc::smem_bytes(128), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
+        case 256: tc::gemm_tc_kernel<256><<<grid, tc::kThreads, tc::smem_bytes(256), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
+        default:
+            if (!m->status) m->status = set_error(WK_EINVAL, "estimator GEMM: N = %d", N);
+            return;
+    }
     m->kernels++;
+}
+
+// the status of the work queued since the last check: a host-side failure, a
+// launch error, or a tensor-core wait that ran out (bit 2 of the device flag)
+int check_status(wk_mlp *m, cudaStream_t s, const char *what) {
+    int st = m->status;
+    m->status = WK_OK;
+    if (st) return st;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m->h_err, m->d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    if (*m->h_err) {
+        *m->h_err = 0;
+        cudaMemsetAsync(m->d_err, 0, sizeof(int), s);
+        return set_error(WK_ETIMEDOUT, "%s: a tensor-core GEMM wait ran out", what);
+    }
+    return WK_OK;
 }
 
 // forward over M rows already uploaded (feats, pids); Y in z[3] col 0
@@ -383,6 +352,8 @@ void free_mlp(wk_mlp *m) {
     for (int l = 0; l < 3; ++l) { cudaFree(m->h[l]); cudaFree(m->ht[l]); }
     cudaFree(m->x0); cudaFree(m->x0t); cudaFree(m->dz); cudaFree(m->dzt); cudaFree(m->dy); cudaFree(m->dyt);
     cudaFree(m->dh); cudaFree(m->dx); cudaFree(m->feats); cudaFree(m->tgt); cudaFree(m->loss); cudaFree(m->pids);
+    cudaFree(m->d_err);
+    if (m->h_err) cudaFreeHost(m->h_err);
     delete m;
 }
 
@@ -422,7 +393,15 @@ extern "C" int wk_mlp_create(wk_ctx *ctx, int32_t n_ids, int32_t max_batch, uint
          cudaMalloc(&m->dh, 4 * Mp * kH) == cudaSuccess &&
          cudaMalloc(&m->dx, 4 * std::max(Mp * (size_t)kXPadN, (size_t)kH * kXPadN)) == cudaSuccess &&
          cudaMalloc(&m->feats, 4 * Mp * kIn) == cudaSuccess && cudaMalloc(&m->tgt, 4 * Mp) == cudaSuccess &&
-         cudaMalloc(&m->loss, 16) == cudaSuccess && cudaMalloc(&m->pids, 4 * Mp) == cudaSuccess;
+         cudaMalloc(&m->loss, 16) == cudaSuccess && cudaMalloc(&m->pids, 4 * Mp) == cudaSuccess &&
+         cudaMalloc(&m->d_err, sizeof(int)) == cudaSuccess &&
+         cudaHostAlloc((void **)&m->h_err, sizeof(int), 0) == cudaSuccess &&
+         cudaFuncSetAttribute(tc::gemm_tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tc::smem_bytes(64)) == cudaSuccess &&
+         cudaFuncSetAttribute(tc::gemm_tc_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tc::smem_bytes(128)) == cudaSuccess &&
+         cudaFuncSetAttribute(tc::gemm_tc_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tc::smem_bytes(256)) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         free_mlp(m);
@@ -449,6 +428,8 @@ extern "C" int wk_mlp_create(wk_ctx *ctx, int32_t n_ids, int32_t max_batch, uint
     if (e == cudaSuccess) e = cudaMemsetAsync(m->x0t, 0, 2 * Mp * kXPadN, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->dy, 0, 2 * Mp * kOutPad, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->dyt, 0, 2 * Mp * kOutPad, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->d_err, 0, sizeof(int), s);
+    if (m->h_err) *m->h_err = 0;
     if (e != cudaSuccess) { int r = cuda_fail(e, "wk_mlp_create init"); free_mlp(m); return r; }
     refresh_bf16(m, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) { int r = cuda_fail(e, "wk_mlp_create sync"); free_mlp(m); return r; }
@@ -496,8 +477,8 @@ extern "C" int wk_mlp_gradients(wk_mlp *m, const float *feats, const int32_t *pi
     if (e == cudaSuccess && grads_host)
         e = cudaMemcpyAsync(grads_host, m->grads, sizeof(float) * (size_t)m->n_params, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && loss_host) e = cudaMemcpyAsync(loss_host, m->loss, 4, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    return e == cudaSuccess ? WK_OK : cuda_fail(e, "wk_mlp_gradients");
+    if (e != cudaSuccess) return cuda_fail(e, "wk_mlp_gradients");
+    return check_status(m, s, "wk_mlp_gradients");
 }
 
 // Mini-batch training: `epochs` passes over n samples in batches of `batch`
@@ -535,8 +516,7 @@ extern "C" int wk_mlp_train(wk_mlp *m, const float *feats, const int32_t *pids, 
             add_out_bias_kernel<<<nblk(M), 256, 0, s>>>(m->z[3], m->params + m->off_b[3], M);
             backward_step(m, M, lr, true, s);
             cudaMemcpyAsync(h_loss, m->loss, 4, cudaMemcpyDeviceToHost, s);
-            cudaError_t e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) { cudaFreeHost(h_loss); return cuda_fail(e, "wk_mlp_train"); }
+            if ((st = check_status(m, s, "wk_mlp_train"))) { cudaFreeHost(h_loss); return st; }
             tot += *h_loss;
             ++nb;
         }
@@ -561,8 +541,8 @@ extern "C" int wk_mlp_predict(wk_mlp *m, const float *feats, const int32_t *pids
         forward(m, M, s);
         add_bias_read_kernel<<<nblk(M), 256, 0, s>>>(m->z[3], m->params + m->off_b[3], M, m->tgt);
         cudaError_t e = cudaMemcpyAsync(out + b0, m->tgt, sizeof(float) * (size_t)M, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return cuda_fail(e, "wk_mlp_predict");
+        if ((st = check_status(m, s, "wk_mlp_predict"))) return st;
     }
     m->ctx->launches += m->kernels;
     m->kernels = 0;

@@ -1,0 +1,221 @@
+// The estimator's GEMM on the 5th-generation tensor cores (sm_100 family):
+// C[M x N] fp32 = A[M x K] . B[N x K]^T (+ bias[n]), A and B bf16 row-major
+// (K contiguous), FP32 accumulation in tensor memory (TMEM).
+//
+// One CTA of 4 warps computes a 128 x N tile (N <= 256: one MMA shape).  K is
+// walked in slabs of 64 bf16 -- one 128-byte row of the 128 B swizzle -- through
+// two shared-memory stages:
+//   - thread 0 loads each slab's A box (64 x 128) and B box (64 x N) with TMA
+//     (cp.async.bulk.tensor.2d, 128 B swizzle; rows past M and columns past K
+//     read as zero), completing on the stage's "full" mbarrier;
+//   - thread 0 issues the slab's tcgen05.mma (kind::f16, 128 x N x 16 each)
+//     from shared-memory descriptors and commits them to the stage's "empty"
+//     mbarrier, which the TMA of the slab two ahead waits for;
+//   - after the last commit, warp w reads TMEM lanes 32w..32w+31 (rows) with
+//     tcgen05.ld, adds the bias and stores C.
+// Every mbarrier wait is bounded; a wait that runs out sets bit 2 of *err,
+// waits (bounded) for the copies and products already issued, frees TMEM and
+// returns.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace wk {
+namespace tc {
+
+constexpr int kTM = 128;            // tile rows = MMA M
+constexpr int kSlab = 64;           // K elements per stage (128 B rows)
+constexpr int kThreads = 128;
+constexpr uint32_t kTmemCols = 256; // fp32 accumulator columns (>= N)
+constexpr long kWaitIters = 1l << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, 128 B swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);   // start address / 16
+    d |= (uint64_t)1 << 16;                   // leading byte offset (not used by swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset: the next group of 8 rows
+    d |= (uint64_t)1 << 46;                   // descriptor version
+    d |= (uint64_t)2 << 61;                   // 128 B swizzle
+    return d;
+}
+
+// instruction descriptor of kind::f16: BF16 A and B, FP32 D, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    uint32_t done = 0;
+    for (long it = 0; it < kWaitIters && !done; ++it)
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(mbar), "r"(parity) : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(map), "r"(x), "r"(y), "r"(mbar) : "memory");
+}
+
+template <int N>
+__global__ void __launch_bounds__(kThreads)
+gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               float *__restrict__ C, int ldc, int M, int K, const float *__restrict__ bias, int *err) {
+    static_assert(N % 16 == 0 && N >= 16 && N <= 256, "MMA N");
+    constexpr uint32_t kABytes = kTM * 128, kBBytes = N * 128, kStage = kABytes + kBBytes;
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ uint32_t s_tmem;
+    __shared__ __align__(8) uint64_t s_full[2], s_empty[2];
+    __shared__ int s_fail;
+    // 128 B swizzle: stage bases 1024 B aligned
+    unsigned char *sm = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * N;
+    const int nslab = (K + kSlab - 1) / kSlab;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_u32(&s_tmem)), "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (t == 0) {
+        s_fail = 0;
+        for (int i = 0; i < 2; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_full[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_empty[i])));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = s_tmem;
+    if (t == 0) {
+        // slab sl lives in stage sl % 2; each barrier completes once per use of its stage,
+        // so the wait for slab sl's use is parity (sl / 2) % 2
+        auto issue_tma = [&](int sl) {
+            const int s = sl & 1;
+            const uint32_t a = smem_u32(sm + s * kStage), b = a + kABytes, fb = smem_u32(&s_full[s]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStage) : "memory");
+            tma_load_2d(a, &tmA, sl * kSlab, m0, fb);
+            tma_load_2d(b, &tmB, sl * kSlab, n0, fb);
+        };
+        bool ok = true;
+        int issued = 1, committed = 0;
+        issue_tma(0);
+        for (int sl = 0; sl < nslab && ok; ++sl) {
+            const int s = sl & 1;
+            if (sl + 1 < nslab) {
+                // the next slab's stage was last read by slab sl - 1
+                if (sl >= 1) ok = mbar_wait(smem_u32(&s_empty[(sl + 1) & 1]), (uint32_t)(((sl - 1) >> 1) & 1));
+                if (!ok) break;
+                issue_tma(sl + 1);
+                issued = sl + 2;
+            }
+            ok = mbar_wait(smem_u32(&s_full[s]), (uint32_t)((sl >> 1) & 1));
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t ad = smem_u32(sm + s * kStage), bd = ad + kABytes;
+            const int ksteps = (K - sl * kSlab) >= kSlab ? kSlab / 16 : (K - sl * kSlab + 15) / 16;
+            for (int kk = 0; kk < ksteps; ++kk) {
+                const uint32_t acc = (sl > 0 || kk > 0) ? 1u : 0u;
+                asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                             " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                             ::"r"(tmem), "l"(sw128_desc(ad + kk * 32)), "l"(sw128_desc(bd + kk * 32)),
+                               "r"(idesc_bf16(kTM, N)), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"(smem_u32(&s_empty[s])) : "memory");
+            committed = sl + 1;
+        }
+        if (!ok) {
+            // a wait ran out: let the last copy and the last products finish (bounded) before TMEM is freed
+            s_fail = 1;
+            const int li = issued - 1;
+            mbar_wait(smem_u32(&s_full[li & 1]), (uint32_t)((li >> 1) & 1));
+            if (committed > 0) {
+                const int lc = committed - 1;
+                mbar_wait(smem_u32(&s_empty[lc & 1]), (uint32_t)((lc >> 1) & 1));
+            }
+        }
+    }
+    __syncthreads();
+    if (!s_fail) {
+        const int last = nslab - 1;   // its commit covers every product of the tile
+        if (!mbar_wait(smem_u32(&s_empty[last & 1]), (uint32_t)((last >> 1) & 1))) s_fail = 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (!s_fail) {
+        const int row = m0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            uint32_t r[16];
+            const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                           "=r"(r[14]), "=r"(r[15])
+                         : "r"(ta));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < M) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int col = n0 + c0 + j;
+                    C[(size_t)row * ldc + col] = __uint_as_float(r[j]) + (bias ? bias[col] : 0.f);
+                }
+            }
+        }
+    } else if (t == 0) {
+        atomicOr(err, 4);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+    }
+}
+
+inline size_t smem_bytes(int N) { return 2 * ((size_t)kTM * 128 + (size_t)N * 128) + 1024; }
+
+// 2-D tensor map of a row-major bf16 matrix (rows x cols, row pitch ld elements,
+// 16 B aligned): boxes of 64 columns x box_rows rows, 128 B swizzle, zero outside.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+inline EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+inline bool make_map(CUtensorMap *map, const void *base, uint64_t rows, uint64_t cols, uint64_t ld,
+                     uint32_t box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn || ((uintptr_t)base & 15u) || ((ld * 2) & 15u)) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)kSlab, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace tc
+}  // namespace wk
