@@ -199,6 +199,7 @@ struct wk_mlp {
     int *d_err = nullptr;        // device flag of the tensor-core GEMM (bit 2: a wait ran out)
     int *h_err = nullptr;        // pinned mirror
     int status = 0;              // a host-side GEMM failure since the last check
+    int sms = 152;               // multiprocessors of the device (GEMM tile width choice)
 };
 
 namespace {
@@ -221,25 +222,28 @@ void refresh_bf16(wk_mlp *m, cudaStream_t s) {
     m->kernels += 4;
 }
 
-// C = A . B^T (+ bias) on the tensor cores (wk_tc_gemm.cuh); N is 64, 128 or 256.
-// A tensor-map failure or an unsupported N is recorded in m->status and
-// reported by the entry point that called this.
+// C = A . B^T (+ bias) on the tensor cores (wk_tc_gemm.cuh); N is a multiple of 64.
+// The tile width is the widest that still gives a full wave of CTAs, else 64:
+// these products are small, and more CTAs means more copies and products in flight.
 void gemm(wk_mlp *m, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N,
           int K, const float *bias, cudaStream_t s) {
+    if (M <= 0 || K <= 0 || N <= 0 || N % 64 || ldc % 4 || ((uintptr_t)C & 15u) || ((uintptr_t)bias & 15u)) {
+        if (!m->status) m->status = set_error(WK_EINVAL, "estimator GEMM: shape or alignment (M %d, N %d, K %d)", M, N, K);
+        return;
+    }
+    const int mt = (M + tc::kTM - 1) / tc::kTM;
+    const int bn = (N % 256 == 0 && mt * (N / 256) >= m->sms) ? 256 : (N % 128 == 0 && mt * (N / 128) >= m->sms) ? 128 : 64;
     CUtensorMap ta, tb;
     if (!tc::make_map(&ta, A, (uint64_t)M, (uint64_t)K, (uint64_t)lda, tc::kTM) ||
-        !tc::make_map(&tb, B, (uint64_t)N, (uint64_t)K, (uint64_t)ldb, (uint32_t)N)) {
+        !tc::make_map(&tb, B, (uint64_t)N, (uint64_t)K, (uint64_t)ldb, (uint32_t)bn)) {
         if (!m->status) m->status = set_error(WK_EDEVICE, "estimator GEMM: tensor map (M %d, N %d, K %d)", M, N, K);
         return;
     }
-    const dim3 grid((unsigned)((M + tc::kTM - 1) / tc::kTM), 1);
-    switch (N) {
+    const dim3 grid((unsigned)mt, (unsigned)(N / bn));
+    switch (bn) {
         case 64: tc::gemm_tc_kernel<64><<<grid, tc::kThreads, tc::smem_bytes(64), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
         case 128: tc::gemm_tc_kernel<128><<<grid, tc::kThreads, tc::smem_bytes(128), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
-        case 256: tc::gemm_tc_kernel<256><<<grid, tc::kThreads, tc::smem_bytes(256), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
-        default:
-            if (!m->status) m->status = set_error(WK_EINVAL, "estimator GEMM: N = %d", N);
-            return;
+        default: tc::gemm_tc_kernel<256><<<grid, tc::kThreads, tc::smem_bytes(256), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
     }
     m->kernels++;
 }
@@ -369,6 +373,7 @@ extern "C" int wk_mlp_create(wk_ctx *ctx, int32_t n_ids, int32_t max_batch, uint
     m->ctx = ctx;
     m->n_ids = n_ids;
     m->cap_m = pad64(max_batch);
+    cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, ctx->device);
     int64_t at = 0;
     for (int l = 0; l < 4; ++l) { m->off_w[l] = at; at += (int64_t)kRows[l] * kCols[l]; }
     for (int l = 0; l < 4; ++l) { m->off_b[l] = at; at += kRowsPad[l]; }

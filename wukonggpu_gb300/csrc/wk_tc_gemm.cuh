@@ -2,17 +2,20 @@
 // C[M x N] fp32 = A[M x K] . B[N x K]^T (+ bias[n]), A and B bf16 row-major
 // (K contiguous), FP32 accumulation in tensor memory (TMEM).
 //
-// One CTA of 4 warps computes a 128 x N tile (N <= 256: one MMA shape).  K is
-// walked in slabs of 64 bf16 -- one 128-byte row of the 128 B swizzle -- through
-// two shared-memory stages:
-//   - thread 0 loads each slab's A box (64 x 128) and B box (64 x N) with TMA
-//     (cp.async.bulk.tensor.2d, 128 B swizzle; rows past M and columns past K
-//     read as zero), completing on the stage's "full" mbarrier;
-//   - thread 0 issues the slab's tcgen05.mma (kind::f16, 128 x N x 16 each)
-//     from shared-memory descriptors and commits them to the stage's "empty"
-//     mbarrier, which the TMA of the slab two ahead waits for;
-//   - after the last commit, warp w reads TMEM lanes 32w..32w+31 (rows) with
-//     tcgen05.ld, adds the bias and stores C.
+// One CTA of 4 warps computes a 128 x BN tile (BN = 64, 128 or 256: one MMA
+// shape); the grid is M tiles x N / BN.  K is walked in slabs of 64 bf16 -- one
+// 128-byte row of the 128 B swizzle -- through kStages shared-memory stages:
+//   - thread 0 (the producer) loads each slab's A box (64 x 128) and B box
+//     (64 x BN) with TMA (cp.async.bulk.tensor.2d, 128 B swizzle; rows past M
+//     and columns past K read as zero), completing on the stage's "full"
+//     mbarrier, once the stage's "empty" mbarrier says its last products ran;
+//   - thread 32 (the MMA issuer) waits for "full", issues the slab's
+//     tcgen05.mma (kind::f16, 128 x BN x 16 each) from shared-memory
+//     descriptors and commits them to the stage's "empty" mbarrier;
+//   - after the last commit, warp w reads TMEM lanes 32w..32w+31 (rows) in
+//     32-column chunks with tcgen05.ld, stages each chunk in shared memory (the
+//     pipeline stages are free by then) and writes it out as whole rows of
+//     float4 with the bias added, so a store instruction covers 4 rows x 128 B.
 // Every mbarrier wait is bounded; a wait that runs out sets bit 2 of *err,
 // waits (bounded) for the copies and products already issued, frees TMEM and
 // returns.
@@ -29,8 +32,9 @@ namespace tc {
 
 constexpr int kTM = 128;            // tile rows = MMA M
 constexpr int kSlab = 64;           // K elements per stage (128 B rows)
+constexpr int kStages = 4;
 constexpr int kThreads = 128;
-constexpr uint32_t kTmemCols = 256; // fp32 accumulator columns (>= N)
+constexpr int kEpiPitch = 36;       // floats per staged output row: rows 16 B apart modulo 128 B
 constexpr long kWaitIters = 1l << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -65,29 +69,45 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         ::"r"(dst), "l"(map), "r"(x), "r"(y), "r"(mbar) : "memory");
 }
 
-template <int N>
+// 32 consecutive fp32 columns of the warp's 32 TMEM lanes: lane i gets row i
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                   "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// C must be 16 B aligned with ldc a multiple of 4, and bias (if any) 16 B aligned.
+template <int BN>
 __global__ void __launch_bounds__(kThreads)
 gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                float *__restrict__ C, int ldc, int M, int K, const float *__restrict__ bias, int *err) {
-    static_assert(N % 16 == 0 && N >= 16 && N <= 256, "MMA N");
-    constexpr uint32_t kABytes = kTM * 128, kBBytes = N * 128, kStage = kABytes + kBBytes;
+    static_assert(BN == 64 || BN == 128 || BN == 256, "tile width: an MMA N and a TMEM allocation");
+    constexpr uint32_t kABytes = kTM * 128, kBBytes = BN * 128, kStage = kABytes + kBBytes;
+    static_assert(4 * 32 * kEpiPitch * 4 <= kStage, "the output staging fits in stage 0");
     extern __shared__ unsigned char smem_raw[];
     __shared__ uint32_t s_tmem;
-    __shared__ __align__(8) uint64_t s_full[2], s_empty[2];
-    __shared__ int s_fail;
+    __shared__ __align__(8) uint64_t s_full[kStages], s_empty[kStages];
+    __shared__ volatile int s_fail;
     // 128 B swizzle: stage bases 1024 B aligned
     unsigned char *sm = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * N;
+    const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * BN;
     const int nslab = (K + kSlab - 1) / kSlab;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     ::"r"(smem_u32(&s_tmem)), "r"(kTmemCols));
+                     ::"r"(smem_u32(&s_tmem)), "r"((uint32_t)BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (t == 0) {
         s_fail = 0;
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < kStages; ++i) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_full[i])));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_empty[i])));
         }
@@ -97,30 +117,33 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s_tmem;
+    // slab j lives in stage j % kStages as that stage's use u = j / kStages; each
+    // barrier completes once per use, so the wait for use u is parity u % 2
     if (t == 0) {
-        // slab sl lives in stage sl % 2; each barrier completes once per use of its stage,
-        // so the wait for slab sl's use is parity (sl / 2) % 2
-        auto issue_tma = [&](int sl) {
-            const int s = sl & 1;
+        int issued = 0;
+        for (int j = 0; j < nslab; ++j) {
+            const int s = j % kStages, u = j / kStages;
+            if (u > 0 && !mbar_wait(smem_u32(&s_empty[s]), (uint32_t)((u - 1) & 1))) {
+                s_fail = 1;
+                break;
+            }
             const uint32_t a = smem_u32(sm + s * kStage), b = a + kABytes, fb = smem_u32(&s_full[s]);
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kStage) : "memory");
-            tma_load_2d(a, &tmA, sl * kSlab, m0, fb);
-            tma_load_2d(b, &tmB, sl * kSlab, n0, fb);
-        };
-        bool ok = true;
-        int issued = 1, committed = 0;
-        issue_tma(0);
-        for (int sl = 0; sl < nslab && ok; ++sl) {
-            const int s = sl & 1;
-            if (sl + 1 < nslab) {
-                // the next slab's stage was last read by slab sl - 1
-                if (sl >= 1) ok = mbar_wait(smem_u32(&s_empty[(sl + 1) & 1]), (uint32_t)(((sl - 1) >> 1) & 1));
-                if (!ok) break;
-                issue_tma(sl + 1);
-                issued = sl + 2;
+            tma_load_2d(a, &tmA, j * kSlab, m0, fb);
+            tma_load_2d(b, &tmB, j * kSlab, n0, fb);
+            issued = j + 1;
+        }
+        // every copy in flight lands before the CTA can leave (immediate when all were consumed)
+        for (int j = issued > kStages ? issued - kStages : 0; j < issued; ++j)
+            mbar_wait(smem_u32(&s_full[j % kStages]), (uint32_t)((j / kStages) & 1));
+    } else if (t == 32) {
+        int committed = 0;
+        for (int sl = 0; sl < nslab; ++sl) {
+            const int s = sl % kStages;
+            if (!mbar_wait(smem_u32(&s_full[s]), (uint32_t)((sl / kStages) & 1))) {
+                s_fail = 1;
+                break;
             }
-            ok = mbar_wait(smem_u32(&s_full[s]), (uint32_t)((sl >> 1) & 1));
-            if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t ad = smem_u32(sm + s * kStage), bd = ad + kABytes;
             const int ksteps = (K - sl * kSlab) >= kSlab ? kSlab / 16 : (K - sl * kSlab + 15) / 16;
@@ -129,62 +152,57 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
                              ::"r"(tmem), "l"(sw128_desc(ad + kk * 32)), "l"(sw128_desc(bd + kk * 32)),
-                               "r"(idesc_bf16(kTM, N)), "r"(acc));
+                               "r"(idesc_bf16(kTM, BN)), "r"(acc));
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                          ::"r"(smem_u32(&s_empty[s])) : "memory");
             committed = sl + 1;
         }
-        if (!ok) {
-            // a wait ran out: let the last copy and the last products finish (bounded) before TMEM is freed
-            s_fail = 1;
-            const int li = issued - 1;
-            mbar_wait(smem_u32(&s_full[li & 1]), (uint32_t)((li >> 1) & 1));
-            if (committed > 0) {
-                const int lc = committed - 1;
-                mbar_wait(smem_u32(&s_empty[lc & 1]), (uint32_t)((lc >> 1) & 1));
-            }
+        // the last commit covers every product issued: they complete before TMEM is read or freed
+        if (committed > 0) {
+            const int c = committed - 1;
+            if (!mbar_wait(smem_u32(&s_empty[c % kStages]), (uint32_t)((c / kStages) & 1))) s_fail = 1;
         }
     }
     __syncthreads();
-    if (!s_fail) {
-        const int last = nslab - 1;   // its commit covers every product of the tile
-        if (!mbar_wait(smem_u32(&s_empty[last & 1]), (uint32_t)((last >> 1) & 1))) s_fail = 1;
-    }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (!s_fail) {
-        const int row = m0 + warp * 32 + lane;
-        for (int c0 = 0; c0 < N; c0 += 16) {
-            uint32_t r[16];
-            const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                           "=r"(r[14]), "=r"(r[15])
-                         : "r"(ta));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (row < M) {
+    if (!s_fail && nslab > 0) {
+        // every copy landed and every product ran: stage 0 is free for the output rows
+        float *stg = reinterpret_cast<float *>(sm) + warp * 32 * kEpiPitch;
+        const int q = lane & 7;
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+            uint32_t r[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+            float4 *mine = reinterpret_cast<float4 *>(stg + lane * kEpiPitch);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int col = n0 + c0 + j;
-                    C[(size_t)row * ldc + col] = __uint_as_float(r[j]) + (bias ? bias[col] : 0.f);
-                }
+            for (int i = 0; i < 8; ++i)
+                mine[i] = make_float4(__uint_as_float(r[4 * i]), __uint_as_float(r[4 * i + 1]),
+                                      __uint_as_float(r[4 * i + 2]), __uint_as_float(r[4 * i + 3]));
+            __syncwarp();
+            const int col = n0 + c0 + q * 4;
+            const float4 bv = bias ? *reinterpret_cast<const float4 *>(bias + col) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int rr = i * 4 + (lane >> 3);
+                const int row = m0 + warp * 32 + rr;
+                float4 v = *reinterpret_cast<const float4 *>(stg + rr * kEpiPitch + q * 4);
+                v.x += bv.x; v.y += bv.y; v.z += bv.z; v.w += bv.w;
+                if (row < M) *reinterpret_cast<float4 *>(C + (size_t)row * ldc + col) = v;
             }
+            __syncwarp();
         }
-    } else if (t == 0) {
+    } else if (s_fail && t == 0) {
         atomicOr(err, 4);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN));
     }
 }
 
-inline size_t smem_bytes(int N) { return 2 * ((size_t)kTM * 128 + (size_t)N * 128) + 1024; }
+inline size_t smem_bytes(int BN) { return kStages * ((size_t)kTM * 128 + (size_t)BN * 128) + 1024; }
 
 // 2-D tensor map of a row-major bf16 matrix (rows x cols, row pitch ld elements,
 // 16 B aligned): boxes of 64 columns x box_rows rows, 128 B swizzle, zero outside.
