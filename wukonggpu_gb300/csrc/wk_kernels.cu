@@ -5,17 +5,18 @@
 // new table.  No tensor cores are involved.
 //
 //   k2u     : count (probe; per-row degree and edge offset; per-block output
-//             count; op total) -> the host reads the total and sizes the
-//             output -> expand (per input block: local scan, output prefix by
-//             look-back, rows written)
+//             count; op total) -> plan (one CTA: every block's output prefix
+//             and its number of slices of at most kSliceRows output rows) ->
+//             the host reads the totals and sizes the output -> expand (one
+//             CTA per slice: the block's local scan, the slice's rows written)
 //   k2k/k2c : probe + membership (per-row ballot masks; per-block count; op
 //             total) -> filtered copy (per input block: output prefix by
 //             look-back, selected rows copied)
 //
-// The look-back never waits: the first kernel of an op has written every
-// block's count before the second kernel starts, so a block finds its output
-// prefix by adding its predecessors' counts back to the nearest predecessor
-// that has already published its inclusive prefix (or back to block 0).
+// The filter's look-back never waits: the first kernel of the op has written
+// every block's count before the second kernel starts, so a block finds its
+// output prefix by adding its predecessors' counts back to the nearest
+// predecessor that has already published its inclusive prefix (or to block 0).
 //
 // Result order equals the reference CPU engine's (core/engine.hpp:126-225):
 // output rows follow input row order, and for k2u each input row's block of
@@ -95,19 +96,27 @@ __device__ __forceinline__ unsigned long long lookback_prefix(const A *__restric
 }
 
 // --------------------------------------------------------------- k2u count
+// A block's output rows are written by slices_of(count) expansion CTAs (none
+// for an empty block), so a block that holds hub rows is spread over many
+// CTAs and an op with few input blocks but a large fan-out still fills the
+// GPU.  The + 3 covers the 16 B alignment lead of the block's first row.
+__device__ __forceinline__ unsigned long long slices_of(unsigned long long t) {
+    return t == 0ull ? 0ull : (t + 3ull + kSliceRows - 1) / kSliceRows;
+}
+
 // A warp owns kRounds * 32 consecutive rows.  Their start vertices are loaded
 // first (kRounds independent coalesced loads), then each round of 32 rows is
 // probed, so the history read does not sit in front of every bucket read.
 constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
 
-// totals[0] += output rows, totals[1] += rows with a match; err bit 1 when a
-// block's output count reaches 2^31 (the expansion keeps block-local
-// positions in 32 bits).
+// totals[0] += output rows, totals[1] += rows with a match; blk_sum[b] = the
+// block's output rows.  Err bit 1 when a block's output count reaches 2^31
+// (the expansion keeps block-local positions in 32 bits).
 __global__ void __launch_bounds__(kThreads)
 k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
                  uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
-                 unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ flags,
-                 unsigned long long *__restrict__ totals, int *err) {
+                 unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ totals,
+                 unsigned long long *__restrict__ tile_sums, int *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t wrow0 = (int64_t)blockIdx.x * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
     int32_t v[kRounds];
@@ -135,10 +144,113 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
     block_sum2(my_sum, my_nz);
     if (threadIdx.x == 0) {
         blk_sum[blockIdx.x] = my_sum;
-        flags[blockIdx.x] = 0ull;
-        if (my_sum) atomicAdd(totals, my_sum);
+        if (my_sum) {
+            atomicAdd(totals, my_sum);
+            unsigned long long *ts = tile_sums + 2 * (blockIdx.x >> kPlanTileShift);
+            atomicAdd(ts, my_sum);
+            atomicAdd(ts + 1, slices_of(my_sum));
+        }
         if (my_nz) atomicAdd(totals + 1, (unsigned long long)my_nz);
         if (my_sum >> 31) atomicOr(err, 2);
+    }
+}
+
+// -------------------------------------------------------------- k2u plan
+constexpr int kPlanThreads = 1024;
+constexpr int kPlanPer = (1 << kPlanTileShift) / kPlanThreads;   // blocks per thread: 8
+
+// exclusive scan of (a, b) pairs over the kPlanThreads threads of the CTA
+__device__ __forceinline__ void plan_scan2(unsigned long long &a, unsigned long long &b, unsigned long long &ta,
+                                           unsigned long long &tb) {
+    __shared__ unsigned long long sa[kPlanThreads / 32], sb[kPlanThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned long long ia = a, ib = b;
+#pragma unroll
+    for (int sh = 1; sh < 32; sh <<= 1) {
+        const unsigned long long xa = __shfl_up_sync(FULL, ia, sh), xb = __shfl_up_sync(FULL, ib, sh);
+        if (lane >= sh) { ia += xa; ib += xb; }
+    }
+    if (lane == 31) { sa[wid] = ia; sb[wid] = ib; }
+    __syncthreads();
+    if (wid == 0) {
+        unsigned long long wa = sa[lane], wb = sb[lane];   // kPlanThreads / 32 == 32 warps
+#pragma unroll
+        for (int sh = 1; sh < 32; sh <<= 1) {
+            const unsigned long long xa = __shfl_up_sync(FULL, wa, sh), xb = __shfl_up_sync(FULL, wb, sh);
+            if (lane >= sh) { wa += xa; wb += xb; }
+        }
+        sa[lane] = wa;
+        sb[lane] = wb;
+    }
+    __syncthreads();
+    const unsigned long long pa = wid ? sa[wid - 1] : 0ull, pb = wid ? sb[wid - 1] : 0ull;
+    ta = sa[kPlanThreads / 32 - 1];
+    tb = sb[kPlanThreads / 32 - 1];
+    a = pa + ia - a;
+    b = pb + ib - b;
+}
+
+// bp[b] = output rows of blocks before b, sp[b] = slices of blocks before b
+// (bp[nblk], sp[nblk] = the totals); totals[2] = slices.  CTA c scans blocks
+// [c 8192, (c + 1) 8192), thread t 8 consecutive ones; the tiles before c
+// contribute their sums from the count kernel, so no CTA waits on another.
+__global__ void __launch_bounds__(kPlanThreads)
+k2u_plan_kernel(const unsigned long long *__restrict__ blk_sum, int64_t nblk,
+                const unsigned long long *__restrict__ tile_sums, unsigned long long *__restrict__ bp,
+                unsigned long long *__restrict__ sp, unsigned long long *__restrict__ totals) {
+    __shared__ unsigned long long s_po, s_ps;
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const int c = blockIdx.x;
+    if (wid == 0) {
+        unsigned long long po = 0, ps = 0;
+        for (int k = lane; k < c; k += 32) {
+            po += tile_sums[2 * k];
+            ps += tile_sums[2 * k + 1];
+        }
+        po = warp_sum(po);
+        ps = warp_sum(ps);
+        if (lane == 0) {
+            s_po = po;
+            s_ps = ps;
+        }
+    }
+    const int64_t b0 = ((int64_t)c << kPlanTileShift) + (int64_t)t * kPlanPer;
+    unsigned long long T[kPlanPer];
+    if (b0 + kPlanPer <= nblk) {
+        // b0 is a multiple of 8 entries: four aligned 16 B loads
+#pragma unroll
+        for (int q = 0; q < kPlanPer; q += 2) {
+            const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(blk_sum + b0 + q);
+            T[q] = x.x;
+            T[q + 1] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < kPlanPer; ++q) T[q] = b0 + q < nblk ? blk_sum[b0 + q] : 0ull;
+    }
+    unsigned long long so = 0, ss = 0;
+#pragma unroll
+    for (int q = 0; q < kPlanPer; ++q) {
+        so += T[q];
+        ss += slices_of(T[q]);
+    }
+    unsigned long long to, tsl;
+    plan_scan2(so, ss, to, tsl);   // its barriers also publish s_po / s_ps
+    so += s_po;
+    ss += s_ps;
+#pragma unroll
+    for (int q = 0; q < kPlanPer; ++q) {
+        if (b0 + q < nblk) {
+            bp[b0 + q] = so;
+            sp[b0 + q] = ss;
+        }
+        so += T[q];
+        ss += slices_of(T[q]);
+    }
+    if (c == (int)gridDim.x - 1 && t == 0) {
+        bp[nblk] = s_po + to;
+        sp[nblk] = s_ps + tsl;
+        totals[2] = s_ps + tsl;
     }
 }
 
@@ -202,41 +314,45 @@ __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint3
     }
 }
 
-// One CTA per block of kRowsPerBlock input rows; it writes that block's output
-// rows.  W = C + 1 output columns for 2 <= W <= 8; W = 0 for any width (one
-// output row per thread and step, scalar stores).  Warp 0 first finds and
-// publishes the block's output prefix, so the look-back's latency overlaps
-// the other warps' loads of the block's degrees, and later blocks find a
-// published prefix sooner.  History rows are read through L1 (consecutive
-// output rows of one input row reuse it).
+// One CTA per slice: CTA k writes local rows [k' kSliceRows, (k' + 1)
+// kSliceRows) of block b, where sp[b] <= k < sp[b + 1] and k' = k - sp[b].
+// Every warp finds b itself (a 32-way search over sp), so no warp waits for
+// another before loading the block's degrees.  W = C + 1 output columns for
+// 2 <= W <= 8; W = 0 for any width (one output row per thread and step,
+// scalar stores).  History rows are read through L1 (consecutive output rows
+// of one input row reuse it).
 template <int W>
 __global__ void __launch_bounds__(kThreads)
 k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const int32_t *__restrict__ edges,
                   const uint32_t *__restrict__ deg, const uint32_t *__restrict__ off,
-                  const unsigned long long *__restrict__ blk_sum, unsigned long long *flags,
-                  int32_t *__restrict__ out) {
+                  const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ bp,
+                  const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out) {
     constexpr int kRPT = kRowsPerBlock / kThreads;
     static_assert(kRPT == 4, "4 input rows per thread");
     __shared__ uint32_t pos[kRowsPerBlock + 1];
     __shared__ uint32_t eoff[kRowsPerBlock];
     __shared__ uint32_t s_w[kThreads / 32];
-    __shared__ unsigned long long s_P;
     const int C = W >= 2 ? W - 1 : C_rt;
-    const int64_t b = blockIdx.x;
-    const unsigned long long Tb = blk_sum[b];
-    if (Tb == 0ull) return;   // no output; successors add this block's count (0) as they walk past
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const unsigned long long k = blockIdx.x;
+
+    // 1. the block: last b in [0, nblk) with sp[b] <= k (an empty block's sp equals its successor's)
+    int64_t lo = 0, hi = nblk - 1;
+    while (hi > lo) {
+        const int64_t step = (hi - lo + 32) / 32;
+        int64_t bl = lo + (int64_t)lane * step;   // lane 0 probes lo, which qualifies
+        if (bl > hi) bl = hi;
+        const unsigned m = __ballot_sync(FULL, sp[bl] <= k);
+        const int L = 31 - __clz(m);
+        const int64_t blo = __shfl_sync(FULL, bl, L);
+        const int64_t bnx = L < 31 ? __shfl_sync(FULL, bl, L + 1) : hi + 1;
+        lo = blo;
+        hi = bnx > blo ? bnx - 1 : blo;
+    }
+    const int64_t b = lo;
+    const uint32_t slice = (uint32_t)(k - sp[b]);
     const int64_t r0 = b * kRowsPerBlock;
     const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
-
-    // 1. output prefix of the block (warp 0), published for the blocks after it
-    if (wid == 0) {
-        const unsigned long long P = lookback_prefix(blk_sum, flags, b);
-        if (lane == 0) {
-            st_flag(flags + b, kPrefixReady | (P + Tb));
-            s_P = P;
-        }
-    }
 
     // 2. the block's degrees and edge offsets, 4 rows per thread; local exclusive scan
     const int q0 = t * kRPT;
@@ -274,20 +390,24 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
     }
     if (t == kThreads - 1) pos[kRowsPerBlock] = e;   // the block's total; rows >= n have no list
     __syncthreads();
-    const unsigned long long P = s_P;
-    const uint32_t T = (uint32_t)Tb;   // below 2^31 (the count kernel flags larger blocks)
+    const unsigned long long P = bp[b];
+    const uint32_t T = (uint32_t)blk_sum[b];   // below 2^31 (the count kernel flags larger blocks)
     const int32_t *hblk = hist + r0 * C;
 
-    // 3. output rows [P, P + T)
+    // 3. the slice's share of output rows [P, P + T)
     if constexpr (W >= 2) {
         const uint32_t lead = (uint32_t)(P & 3ull), span = T + lead;
+        const uint32_t u0 = slice * (uint32_t)kSliceRows;
+        const uint32_t u1 = u0 >= span ? u0 : (span - u0 < (uint32_t)kSliceRows ? span : u0 + (uint32_t)kSliceRows);
         int32_t *obase = out + (P - lead) * W;
-        for (uint32_t u = 4u * (uint32_t)t; u < span; u += 4u * kThreads)
+        for (uint32_t u = u0 + 4u * (uint32_t)t; u < u1; u += 4u * kThreads)
             k2u_write_group<W>(u, lead, span, pos, eoff, n, hblk, edges, obase);
     } else {
         const int Wd = C + 1;
         int32_t *oblk = out + P * Wd;
-        for (uint32_t j = (uint32_t)t; j < T; j += kThreads) {
+        const uint32_t j0 = slice * (uint32_t)kSliceRows;
+        const uint32_t j1 = j0 >= T ? j0 : (T - j0 < (uint32_t)kSliceRows ? T : j0 + (uint32_t)kSliceRows);
+        for (uint32_t j = j0 + (uint32_t)t; j < j1; j += kThreads) {
             const int i = row_of(pos, n, j);
             int32_t *dst = oblk + (size_t)j * Wd;
             const int32_t *src = hblk + (int64_t)i * C;
@@ -425,18 +545,26 @@ static inline unsigned int nblocks_rows(int64_t R) {
 }
 
 void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg,
-                      uint32_t *off, unsigned long long *blk_sum, unsigned long long *flags,
-                      unsigned long long *totals, int *err, cudaStream_t st) {
-    k2u_count_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, flags,
-                                                           totals, err);
+                      uint32_t *off, unsigned long long *blk_sum, unsigned long long *totals,
+                      unsigned long long *tile_sums, int *err, cudaStream_t st) {
+    k2u_count_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, totals,
+                                                           tile_sums, err);
+}
+
+void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, const unsigned long long *tile_sums,
+                     unsigned long long *bp, unsigned long long *sp, unsigned long long *totals, cudaStream_t st) {
+    const unsigned int g = (unsigned int)((nblk + (1 << kPlanTileShift) - 1) >> kPlanTileShift);
+    k2u_plan_kernel<<<g, kPlanThreads, 0, st>>>(blk_sum, nblk, tile_sums, bp, sp, totals);
 }
 
 void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edges, const uint32_t *deg,
-                       const uint32_t *off, const unsigned long long *blk_sum, unsigned long long *flags,
-                       int32_t *out, cudaStream_t st) {
-    const unsigned int g = nblocks_rows(R);
+                       const uint32_t *off, const unsigned long long *blk_sum, const unsigned long long *bp,
+                       const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st) {
+    if (slices == 0ull) return;
+    const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
+    const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND(WC) \
-    k2u_expand_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, C, edges, deg, off, blk_sum, flags, out)
+    k2u_expand_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, C, edges, deg, off, blk_sum, bp, sp, nblk, out)
     switch (C + 1) {
         case 2: WK_EXPAND(2); break;
         case 3: WK_EXPAND(3); break;

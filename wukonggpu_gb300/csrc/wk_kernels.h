@@ -11,20 +11,30 @@ namespace dev {
 constexpr int kRowsPerBlock = 1024;   // input rows per CTA of every op kernel
 constexpr int kThreads = 256;
 
-// k2u pass 1: probe hist[r][scol] -> deg[r], off[r]; per-block output counts
-// blk_sum[b]; clears the look-back flags; totals[0] += output rows,
-// totals[1] += rows with a match; err bit 0: overflow chain longer than the
-// segment's overflow area, bit 1: a block's count reached 2^31.
-void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg,
-                      uint32_t *off, unsigned long long *blk_sum, unsigned long long *flags,
-                      unsigned long long *totals, int *err, cudaStream_t st);
+constexpr int kSliceRows = 8192;      // k2u output rows per expansion CTA (a multiple of 4)
+constexpr int kPlanTileShift = 13;    // input blocks per k2u plan CTA: 8192
+constexpr int kMaxPlanTiles = 250;    // plan CTAs per op (tile sums live beside the op totals)
 
-// k2u pass 2: every input block writes its output rows (row || neighbour) at
-// the prefix it finds by look-back; out holds totals[0] rows of C + 1 columns
-// and is 16 B aligned.
+// k2u pass 1: probe hist[r][scol] -> deg[r], off[r]; per-block output counts
+// blk_sum[b]; totals[0] += output rows, totals[1] += rows with a match;
+// tile_sums[2c] += output rows and tile_sums[2c + 1] += slices of the blocks of
+// plan tile c (zeroed before the launch); err bit 0: overflow chain longer
+// than the segment's overflow area, bit 1: a block's count reached 2^31.
+void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg,
+                      uint32_t *off, unsigned long long *blk_sum, unsigned long long *totals,
+                      unsigned long long *tile_sums, int *err, cudaStream_t st);
+
+// k2u plan: bp[b] = the block's output prefix, sp[b] = its first slice
+// (nblk + 1 entries each); totals[2] = slices, the expansion's CTA count.
+// One CTA per plan tile (at most kMaxPlanTiles).
+void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, const unsigned long long *tile_sums,
+                     unsigned long long *bp, unsigned long long *sp, unsigned long long *totals, cudaStream_t st);
+
+// k2u pass 2: one CTA per slice writes its rows (row || neighbour) of its
+// block's output; out holds totals[0] rows of C + 1 columns and is 16 B aligned.
 void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edges, const uint32_t *deg,
-                       const uint32_t *off, const unsigned long long *blk_sum, unsigned long long *flags,
-                       int32_t *out, cudaStream_t st);
+                       const uint32_t *off, const unsigned long long *blk_sum, const unsigned long long *bp,
+                       const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st);
 
 // k2k/k2c pass 1: probe + membership of the end value; per-row ballot masks,
 // per-block kept-row counts, flags cleared; totals[0] += adjacency entries a

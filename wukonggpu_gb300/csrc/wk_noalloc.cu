@@ -32,15 +32,16 @@ namespace {
 
 constexpr int64_t kMaxRows = 1 << 18;                 // input rows per call
 constexpr int64_t kMaxBlocks = kMaxRows / wk::dev::kRowsPerBlock;
+static_assert(kMaxBlocks <= (1 << wk::dev::kPlanTileShift), "one k2u plan tile per call");
 
 constexpr size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // byte layout of the scratch array
-constexpr size_t kOffFlags = 0;                                         // err (int) + totals (3 x u64)
+constexpr size_t kOffFlags = 0;       // err (int), totals (3 x u64), the plan tile's sums (2 x u64)
 constexpr size_t kOffDeg = al(kOffFlags + 64);
 constexpr size_t kOffOff = al(kOffDeg + 4 * kMaxRows);
 constexpr size_t kOffBlkSum = al(kOffOff + 4 * kMaxRows);
-constexpr size_t kOffLookback = al(kOffBlkSum + 8 * kMaxBlocks);
-constexpr size_t kScratchBytes = al(kOffLookback + 8 * kMaxBlocks);
+constexpr size_t kOffPlan = al(kOffBlkSum + 8 * kMaxBlocks);            // output and slice prefixes
+constexpr size_t kScratchBytes = al(kOffPlan + 16 * (kMaxBlocks + 1));
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -98,15 +99,18 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     uint32_t *deg = reinterpret_cast<uint32_t *>(sc + kOffDeg);
     uint32_t *off = reinterpret_cast<uint32_t *>(sc + kOffOff);
     unsigned long long *blk_sum = reinterpret_cast<unsigned long long *>(sc + kOffBlkSum);
-    unsigned long long *flags = reinterpret_cast<unsigned long long *>(sc + kOffLookback);
+    const int64_t nblk = (rows + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
+    unsigned long long *bp = reinterpret_cast<unsigned long long *>(sc + kOffPlan), *sp = bp + (nblk + 1);
 
     const PredView pv = ctx->store->views[(size_t)predict];
     const int scol = (int)(-start - 1);
     cudaStream_t s = ctx->stream;
-    if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 32, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
-    dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, flags, tot, err, s);
+    if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 48, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
+    // kMaxRows input rows are one plan tile: its two sums follow the totals
+    dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, tot, tot + 3, err, s);
+    dev::launch_k2u_plan(blk_sum, nblk, tot + 3, bp, sp, tot, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: count launch");
-    ctx->launches += 1;
+    ctx->launches += 2;
     if ((e = cudaMemcpyAsync(ctx->h_scal, sc + kOffFlags, 32, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "noalloc: totals");
@@ -122,7 +126,7 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
                          "known_to_unknown_noalloc: output needs %lld int32 elements, capacity is %lld "
                          "(*out_rows holds the row count)",
                          (long long)(R_out * (cols + 1)), (long long)out_capacity);
-    dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, flags, out, s);
+    dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, bp, sp, ctx->h_scal[3], out, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: expand launch");
     ctx->launches += 1;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "noalloc: sync");

@@ -139,13 +139,14 @@ int wk::reserve_op_scratch(wk_ctx *ctx, int64_t rows) {
 
 namespace {
 
-// zero the op totals (dscal[1..3]) before a first pass accumulates into them
-int clear_totals(wk_ctx *ctx) {
-    cudaError_t e = cudaMemsetAsync(ctx->dscal.as<unsigned long long>() + 1, 0, 24, ctx->stream);
+// zero the op totals (dscal[1..3]) and `tiles` k2u plan tile sums (from
+// dscal[8]) before a first pass accumulates into them
+int clear_totals(wk_ctx *ctx, int64_t tiles = 0) {
+    cudaError_t e = cudaMemsetAsync(ctx->dscal.as<unsigned long long>() + 1, 0, 56 + 16 * (size_t)tiles, ctx->stream);
     return e == cudaSuccess ? WK_OK : cuda_fail(e, "clear totals");
 }
 
-// two-pass k2u (count -> host reads the total -> expand)
+// two-pass k2u (count + plan -> host reads the totals -> expand)
 int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     const int C = h->col_num;
     const int64_t R = h->size / C;
@@ -166,16 +167,25 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         return WK_OK;
     }
     const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
+    const int64_t tiles = (nblk + (1 << dev::kPlanTileShift) - 1) >> dev::kPlanTileShift;
+    if (tiles > dev::kMaxPlanTiles)
+        return set_error(WK_EINVAL, "k2u: %lld input rows exceed one op's maximum of %lld", (long long)R,
+                         (long long)dev::kMaxPlanTiles << dev::kPlanTileShift << 10);
     if ((st = ctx->deg.reserve((size_t)R * 4)) || (st = ctx->off.reserve((size_t)R * 4)) ||
-        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->lb_flags.reserve((size_t)nblk * 8)) ||
-        (st = clear_totals(ctx)))
+        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16)) ||
+        (st = clear_totals(ctx, tiles)))
         return st;
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
+    unsigned long long *tile_sums = ctx->dscal.as<unsigned long long>() + 8;
     int *err = ctx->dscal.as<int>();
+    // block output prefixes and slice prefixes share the look-back scratch
+    unsigned long long *bp = ctx->lb_flags.as<unsigned long long>(), *sp = bp + (nblk + 1);
     if ((st = clk.begin())) return st;
     dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
-                          ctx->blk_sum.as<unsigned long long>(), ctx->lb_flags.as<unsigned long long>(), tot, err,
-                          ctx->stream);
+                          ctx->blk_sum.as<unsigned long long>(), tot, tile_sums, err, ctx->stream);
+    dev::launch_k2u_plan(ctx->blk_sum.as<unsigned long long>(), nblk, tile_sums, bp, sp, tot, ctx->stream);
+    ++ctx->launches;   // the plan kernel, timed with the count
+    ++ctx->last.kernels;
     if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;
     int errf = 0;
     if ((st = read_totals(ctx, &errf))) return st;
@@ -196,8 +206,8 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         if ((st = ob.reserve((size_t)R_out * (C + 1) * 4))) return st;
         if ((st = clk.begin())) return st;
         dev::launch_k2u_expand(h->data, R, C, pv.edges, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
-                               ctx->blk_sum.as<unsigned long long>(), ctx->lb_flags.as<unsigned long long>(),
-                               ob.as<int32_t>(), ctx->stream);
+                               ctx->blk_sum.as<unsigned long long>(), bp, sp, ctx->h_scal[3], ob.as<int32_t>(),
+                               ctx->stream);
         if ((st = launch_check("k2u expand")) || (st = clk.end(true))) return st;
         if (ctx->timing) {
             cudaError_t e = cudaStreamSynchronize(ctx->stream);

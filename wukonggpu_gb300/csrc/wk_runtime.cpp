@@ -299,8 +299,8 @@ extern "C" int wk_ctx_create(const wk_config *cfg_in, wk_ctx **out) {
         delete ctx;
         return r;
     }
-    if ((st = ctx->dscal.reserve(256)) != WK_OK) { delete ctx; return st; }
-    if ((e = cudaMemset(ctx->dscal.ptr, 0, 256)) != cudaSuccess) { int r = cuda_fail(e, "wk_ctx_create"); delete ctx; return r; }
+    if ((st = ctx->dscal.reserve(4096)) != WK_OK) { delete ctx; return st; }
+    if ((e = cudaMemset(ctx->dscal.ptr, 0, 4096)) != cudaSuccess) { int r = cuda_fail(e, "wk_ctx_create"); delete ctx; return r; }
     const int64_t hc = cfg.history_capacity > 0 ? cfg.history_capacity : (16ll << 20);
     for (auto &b : ctx->hbuf)
         if ((st = b.reserve((size_t)hc * 4)) != WK_OK) { delete ctx; return st; }

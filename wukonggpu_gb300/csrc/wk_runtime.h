@@ -73,7 +73,7 @@ struct wk_ctx {
     // scratch of the two-pass ops
     wk::DevBuf deg, off, mask, blk_sum, blk_nz;
     wk::DevBuf lb_flags;             // per-block look-back prefixes of the second pass
-    wk::DevBuf dscal;                // [0] error flags, [8..] totals
+    wk::DevBuf dscal;                // [0] error flags, [8..32) totals, [64..) k2u plan tile sums
     unsigned long long *h_scal = nullptr;   // pinned mirror of the totals
 
     // timing
