@@ -104,7 +104,8 @@ int wk_ctx_share_store(wk_ctx *ctx, wk_ctx *owner);
 typedef struct {
     int64_t num_keys;        /* packed (vid,pid,dir) keys                     */
     int64_t num_edges;       /* int32 edge entries incl. index lists          */
-    int64_t key_bytes;       /* bytes of bucket storage (all predicates)      */
+    int64_t key_bytes;       /* bytes of key storage: hash buckets and dense  */
+                             /* offsets arrays (all predicates)               */
     int64_t edge_bytes;      /* bytes of edge segments (all predicates)       */
     int64_t overflow_buckets;/* indirect (overflow) buckets in use            */
     int64_t device_bytes;    /* bytes of the store resident on the device     */
@@ -113,6 +114,8 @@ typedef struct {
     int64_t cache_loads;     /* segment loads (H2D) so far, paged mode        */
     int64_t cache_evictions; /* segment evictions so far, paged mode          */
     int64_t cache_bytes_loaded;
+    int64_t dense_dirs;      /* (id, direction) pairs stored as dense offsets */
+                             /* arrays instead of hashed keys                 */
 } wk_store_info;
 int wk_store_get_info(wk_ctx *ctx, wk_store_info *info);
 

@@ -186,7 +186,9 @@ def test_high_degree_and_wide_tables(lib_built):
 
 def test_paged_segment_cache_gives_same_rows(small_graph, small_oracle, golden_small):
     g, s, p, o = small_graph
-    rc = W.RCache(device=0, cache_budget_mb=20)   # the store is ~37 MB: evictions happen
+    # the store is ~26 MB, its largest segment (the type lists) ~2.5 MB: the
+    # queries' segments do not fit together, a step's pair does
+    rc = W.RCache(device=0, cache_budget_mb=5)
     rc.build_store_graph(g)
     assert rc.store_info()["paged"] == 1
     for q in golden_small["queries"]:

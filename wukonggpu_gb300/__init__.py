@@ -49,7 +49,7 @@ class wk_store_info(C.Structure):
     _fields_ = [("num_keys", C.c_int64), ("num_edges", C.c_int64), ("key_bytes", C.c_int64),
                 ("edge_bytes", C.c_int64), ("overflow_buckets", C.c_int64), ("device_bytes", C.c_int64),
                 ("num_ids", C.c_int32), ("paged", C.c_int32), ("cache_loads", C.c_int64),
-                ("cache_evictions", C.c_int64), ("cache_bytes_loaded", C.c_int64)]
+                ("cache_evictions", C.c_int64), ("cache_bytes_loaded", C.c_int64), ("dense_dirs", C.c_int64)]
 
 
 class wk_op_stats(C.Structure):

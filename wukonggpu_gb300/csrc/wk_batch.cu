@@ -110,7 +110,7 @@ batch_count_kernel(StepIO io, int rounds) {
             int q = 0;
             StepDesc d{BK_NOP, 0, 0, 0, 0, 0};
             if (valid) { q = find_query(s_off, io.Q, g); d = io.desc[q]; }
-            PredView pv{nullptr, nullptr, 0u, 0u};
+            PredView pv{};
             int32_t vid = -1;
             bool probe = valid && d.kind != BK_NOP;
             int32_t target = 0;

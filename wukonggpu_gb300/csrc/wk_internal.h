@@ -22,6 +22,16 @@
 // The predicate is implied by the segment, so a slot key needs 32 bits; the
 // full packed key of the reference (vid << 18 | pid << 1 | dir,
 // core/gstore.hpp:117-149) is never stored.
+//
+// Dense directions.  When the vertex keys of one direction of a segment cover
+// at least 1/WK_DENSE_RATIO of their id range [vmin, vmin + n), that
+// direction is stored as an offsets array instead: rowptr[v - vmin] is the
+// first edge of v's list and rowptr[v - vmin + 1] its end (equal for an
+// absent vertex), over the same edge list, whose lists of a direction are
+// already in ascending vertex order.  A probe then reads 8 B (one sector)
+// instead of a 64 B bucket, the array costs 4 B per id of the range (a hash
+// key costs about 26 B), and dense arrays of a few million vertices stay in
+// L2.  Index keys (vid 0) always stay in the hash table.
 #define WK_BUCKET_WORDS 16
 #define WK_BUCKET_BYTES 64
 #define WK_DATA_SLOTS 5
@@ -30,6 +40,7 @@
 #define WK_DEG_WORD 11
 #define WK_EMPTY_KEY 0xffffffffu
 #define WK_NO_LINK 0xffffffffu
+#define WK_DENSE_RATIO 8
 
 #if defined(__CUDACC__)
 #define WK_HD __host__ __device__ __forceinline__
@@ -87,11 +98,18 @@ struct PredSeg {
     uint32_t nover = 0;        // overflow buckets appended after the main ones
     uint64_t edge_off = 0;     // first int32 in the host edge image
     uint64_t nedges = 0;       // int32 entries in this id's edge segment
-    uint64_t nkeys = 0;
+    uint64_t nkeys = 0;        // all keys, hashed or dense
+    // dense directions (index = dir): ids [dvmin, dvmin + dn); dn = 0 when hashed.
+    // The offsets arrays of both directions are contiguous in the host
+    // rowptr image from rp_off: dir IN (dn[0] + 1 entries, if dense), then OUT.
+    uint32_t dvmin[2] = {0u, 0u}, dn[2] = {0u, 0u};
+    uint64_t rp_off = 0;
     // statistics (GStore::generate_statistic, core/gstore.hpp:1010-1127)
     int64_t triples = 0, subjects = 0, objects = 0;
     uint64_t bucket_bytes() const { return (uint64_t)(nmain + nover) * WK_BUCKET_BYTES; }
     uint64_t edge_bytes() const { return nedges * 4; }
+    uint64_t rp_entries(int dir) const { return dn[dir] ? (uint64_t)dn[dir] + 1 : 0; }
+    uint64_t rowptr_bytes() const { return 4 * (rp_entries(0) + rp_entries(1)); }
 };
 
 struct HostStore {
@@ -99,11 +117,30 @@ struct HostStore {
     std::vector<PredSeg> segs;     // indexed by id, size num_ids + 1
     Bucket *buckets = nullptr;     // all segments' buckets, segment after segment
     int32_t *edges = nullptr;
-    uint64_t total_buckets = 0, total_edges = 0, total_keys = 0, total_over = 0;
+    uint32_t *rowptr = nullptr;    // all dense directions' offsets arrays
+    uint64_t total_buckets = 0, total_edges = 0, total_keys = 0, total_over = 0, total_rowptr = 0;
     bool pinned = false;
     ~HostStore();
     // host lookup in the image; returns degree (0 if absent) and the edge pointer
     uint64_t lookup(uint64_t vid, uint32_t pid, uint32_t dir, const int32_t **edges_out) const;
+    // every key of segment id: f(vid, dir, edge offset in the segment, degree)
+    template <class F>
+    void for_each_key(int id, F f) const {
+        const PredSeg &sg = segs[(size_t)id];
+        const Bucket *base = buckets + sg.bucket_off;
+        const uint64_t nb = (uint64_t)sg.nmain + sg.nover;
+        for (uint64_t b = 0; b < nb; ++b) {
+            const uint32_t *w = base[b].w;
+            for (int i = 0; i < WK_DATA_SLOTS; ++i)
+                if (w[i] != WK_EMPTY_KEY) f(w[i] >> 1, w[i] & 1u, w[WK_OFF_WORD + i], w[WK_DEG_WORD + i]);
+        }
+        const uint32_t *rp = rowptr + sg.rp_off;
+        for (uint32_t dir = 0; dir < 2; ++dir) {
+            for (uint32_t x = 0; x < sg.dn[dir]; ++x)
+                if (rp[x + 1] > rp[x]) f(sg.dvmin[dir] + x, dir, rp[x], rp[x + 1] - rp[x]);
+            rp += sg.rp_entries((int)dir);
+        }
+    }
 };
 
 struct Stats;   // planner statistics (wk_planner.cpp)
@@ -115,10 +152,31 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
 
 // Device view of one predicate segment (passed to kernels by value).
 struct PredView {
-    const Bucket *buckets;     // nmain + nover buckets
-    const int32_t *edges;
-    uint32_t nmain;
-    uint32_t nover;            // bound on overflow hops (corruption guard)
+    const Bucket *buckets = nullptr;        // nmain + nover buckets
+    const int32_t *edges = nullptr;
+    uint32_t nmain = 0;
+    uint32_t nover = 0;                     // bound on overflow hops (corruption guard)
+    const uint32_t *rp[2] = {nullptr, nullptr};   // dense offsets per direction, or null
+    uint32_t vmin[2] = {0u, 0u}, dn[2] = {0u, 0u};
 };
+
+// The device view of segment sg whose buckets, offsets arrays and edges start
+// at the given device addresses (offsets arrays in the rowptr image order).
+inline PredView make_view(const PredSeg &sg, const Bucket *bk, const uint32_t *rp, const int32_t *edges) {
+    PredView v;
+    v.buckets = bk;
+    v.edges = edges;
+    v.nmain = sg.nmain;
+    v.nover = sg.nover;
+    for (int d = 0; d < 2; ++d) {
+        if (sg.dn[d]) {
+            v.rp[d] = rp;
+            v.vmin[d] = sg.dvmin[d];
+            v.dn[d] = sg.dn[d];
+        }
+        rp += sg.rp_entries(d);
+    }
+    return v;
+}
 
 }  // namespace wk

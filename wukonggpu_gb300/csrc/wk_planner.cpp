@@ -111,29 +111,20 @@ Stats *build_stats(const HostStore &hs) {
     std::vector<int64_t> class_members(W, 0);   // from the type segment
     par_for((size_t)N, [&](size_t k) {
         const int id = (int)k + 1;
-        const PredSeg &sg = hs.segs[(size_t)id];
-        const uint64_t nb = (uint64_t)sg.nmain + sg.nover;
-        const Bucket *base = hs.buckets + sg.bucket_off;
         uint64_t c = 0;
         SegCounts &x = sc[(size_t)id];
-        for (uint64_t b = 0; b < nb; ++b) {
-            const uint32_t *w = base[b].w;
-            for (int i = 0; i < WK_DATA_SLOTS; ++i) {
-                const uint32_t key = w[i];
-                if (key == WK_EMPTY_KEY) continue;
-                const uint32_t deg = w[WK_DEG_WORD + i];
-                ++c;
-                if ((key & 1u) == WK_DIR_IN) {
-                    x.has_in = true;
-                    x.pt += deg;
-                    x.po += 1;
-                } else {
-                    x.has_out = true;
-                    x.ps += 1;
-                    if (id == WK_TYPE_ID) c += deg;
-                }
+        hs.for_each_key(id, [&](uint32_t, uint32_t dir, uint32_t, uint32_t deg) {
+            ++c;
+            if (dir == WK_DIR_IN) {
+                x.has_in = true;
+                x.pt += deg;
+                x.po += 1;
+            } else {
+                x.has_out = true;
+                x.ps += 1;
+                if (id == WK_TYPE_ID) c += deg;
             }
-        }
+        });
         cnt[(size_t)id] = c;
     });
     std::vector<uint64_t> at((size_t)N + 2, 0);
@@ -145,31 +136,22 @@ Stats *build_stats(const HostStore &hs) {
     par_for((size_t)N, [&](size_t k) {
         const int id = (int)k + 1;
         const PredSeg &sg = hs.segs[(size_t)id];
-        const uint64_t nb = (uint64_t)sg.nmain + sg.nover;
-        const Bucket *base = hs.buckets + sg.bucket_off;
         const uint32_t pid = (uint32_t)id;
         DirP *o = lists.data() + at[(size_t)id];
         uint32_t mv = 0;
         std::vector<int64_t> local_classes;
         if (id == WK_TYPE_ID) local_classes.assign(W, 0);
-        for (uint64_t b = 0; b < nb; ++b) {
-            const uint32_t *w = base[b].w;
-            for (int i = 0; i < WK_DATA_SLOTS; ++i) {
-                const uint32_t key = w[i];
-                if (key == WK_EMPTY_KEY) continue;
-                const uint32_t vid = key >> 1, dir = key & 1u;
-                mv = std::max(mv, vid);
-                *o++ = DirP{vid, (pid << 1) | dir};
-                if (dir == WK_DIR_OUT && id == WK_TYPE_ID) {
-                    const uint32_t deg = w[WK_DEG_WORD + i];
-                    const int32_t *e = hs.edges + sg.edge_off + w[WK_OFF_WORD + i];
-                    for (uint32_t q = 0; q < deg; ++q) {
-                        local_classes[(size_t)e[q]] += 1;
-                        *o++ = DirP{vid, ((uint32_t)e[q] << 1) | (uint32_t)WK_DIR_OUT};
-                    }
+        hs.for_each_key(id, [&](uint32_t vid, uint32_t dir, uint32_t off, uint32_t deg) {
+            mv = std::max(mv, vid);
+            *o++ = DirP{vid, (pid << 1) | dir};
+            if (dir == WK_DIR_OUT && id == WK_TYPE_ID) {
+                const int32_t *e = hs.edges + sg.edge_off + off;
+                for (uint32_t q = 0; q < deg; ++q) {
+                    local_classes[(size_t)e[q]] += 1;
+                    *o++ = DirP{vid, ((uint32_t)e[q] << 1) | (uint32_t)WK_DIR_OUT};
                 }
             }
-        }
+        });
         std::lock_guard<std::mutex> lk(mu);
         max_vid = std::max(max_vid, mv);
         if (id == WK_TYPE_ID) class_members.swap(local_classes);

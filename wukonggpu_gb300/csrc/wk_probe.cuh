@@ -1,8 +1,10 @@
 // Device-side segment probe, shared by the single-query and batched kernels.
 //
-// One lane looks up one key.  A 64 B bucket is fetched as two independent
-// 32 B loads, so a lane has the whole bucket after one memory round trip and
-// resolves the slot in registers: no cross-lane traffic on the hit path.
+// One lane looks up one key.  In a dense direction that is two 4 B reads of
+// the offsets array; in a hashed one a 64 B bucket is fetched as two
+// independent 32 B loads, so a lane has the whole bucket after one memory
+// round trip and resolves the slot in registers: no cross-lane traffic on the
+// hit path.
 // The reference's lookup is GStore::get_edges_global / get_edges_local
 // (core/gstore.hpp:389-409): a key that is absent yields an empty list.
 #pragma once
@@ -53,6 +55,26 @@ __device__ __forceinline__ uint32_t probe_seg(const Bucket *bk, uint32_t nmain, 
     }
 }
 
+// Look up vertex or index key (vid, dir) of a segment: through the
+// direction's offsets array when it is dense (two 4 B reads, normally one
+// sector), else through the hash table.  Returns the degree, the edge offset
+// in *off.
+__device__ __forceinline__ uint32_t probe_view(const PredView &pv, uint32_t vid, uint32_t dir, uint32_t *off,
+                                               int *err) {
+    const uint32_t *rp = dir ? pv.rp[1] : pv.rp[0];
+    if (rp != nullptr && vid != 0u) {
+        const uint32_t x = vid - (dir ? pv.vmin[1] : pv.vmin[0]);   // wraps above n below vmin
+        if (x >= (dir ? pv.dn[1] : pv.dn[0])) {
+            *off = 0u;
+            return 0u;
+        }
+        const uint32_t a = __ldg(rp + x), b = __ldg(rp + x + 1);
+        *off = a;
+        return b - a;
+    }
+    return probe_seg(pv.buckets, pv.nmain, pv.nover, seg_key(vid, dir), off, err);
+}
+
 // Probe the 32 keys (vid, dir) of a warp in one segment.  A run of equal keys
 // on consecutive lanes (the same start vertex on consecutive rows, as an
 // expansion leaves them) is looked up once, by the run's first lane; the
@@ -70,7 +92,7 @@ __device__ __forceinline__ void probe_warp(const PredView &pv, int32_t vid, uint
     const unsigned heads = __ballot_sync(WK_FULL_MASK, lane == 0 || prev != kk);
     const int lead = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));   // run head at or below this lane
     uint32_t o = 0u, d = 0u;
-    if (ok && lead == lane) d = probe_seg(pv.buckets, pv.nmain, pv.nover, key, &o, err);
+    if (ok && lead == lane) d = probe_view(pv, (uint32_t)vid, dir, &o, err);
     r_off = __shfl_sync(WK_FULL_MASK, o, lead);
     r_deg = __shfl_sync(WK_FULL_MASK, d, lead);
 }
@@ -85,7 +107,7 @@ __device__ __forceinline__ void probe_warp_multi(const PredView &pv, uint32_t se
     const unsigned same = __match_any_sync(WK_FULL_MASK, ok ? (((uint64_t)seg << 32) | key) : ~0ull);
     const int lead = __ffs(same) - 1;
     uint32_t o = 0u, d = 0u;
-    if (ok && lead == lane) d = probe_seg(pv.buckets, pv.nmain, pv.nover, key, &o, err);
+    if (ok && lead == lane) d = probe_view(pv, (uint32_t)vid, dir, &o, err);
     r_off = __shfl_sync(WK_FULL_MASK, o, lead);
     r_deg = __shfl_sync(WK_FULL_MASK, d, lead);
 }

@@ -56,6 +56,7 @@ void DevBuf::release() {
 // ------------------------------------------------------- DeviceStore
 DeviceStore::~DeviceStore() {
     if (d_buckets) cudaFree(d_buckets);
+    if (d_rowptr) cudaFree(d_rowptr);
     if (d_edges) cudaFree(d_edges);
     if (pool) cudaFree(pool);
     for (auto &r : res)
@@ -65,21 +66,25 @@ DeviceStore::~DeviceStore() {
 static inline uint64_t align256(uint64_t x) { return (x + 255) & ~(uint64_t)255; }
 
 int DeviceStore::upload_resident() {
-    const uint64_t bbytes = hs->total_buckets * sizeof(Bucket), ebytes = hs->total_edges * 4;
+    const uint64_t bbytes = hs->total_buckets * sizeof(Bucket), ebytes = hs->total_edges * 4,
+                   rbytes = hs->total_rowptr * 4;
     cudaError_t e;
     if ((e = cudaMalloc(&d_buckets, bbytes ? bbytes : 16)) != cudaSuccess) { d_buckets = nullptr; return cuda_fail(e, "store upload (buckets)"); }
     if ((e = cudaMalloc(&d_edges, ebytes ? ebytes : 16)) != cudaSuccess) { d_edges = nullptr; return cuda_fail(e, "store upload (edges)"); }
+    if ((e = cudaMalloc(&d_rowptr, rbytes ? rbytes : 16)) != cudaSuccess) { d_rowptr = nullptr; return cuda_fail(e, "store upload (offsets)"); }
     if (bbytes && (e = cudaMemcpy(d_buckets, hs->buckets, bbytes, cudaMemcpyHostToDevice)) != cudaSuccess)
         return cuda_fail(e, "store upload copy (buckets)");
     if (ebytes && (e = cudaMemcpy(d_edges, hs->edges, ebytes, cudaMemcpyHostToDevice)) != cudaSuccess)
         return cuda_fail(e, "store upload copy (edges)");
-    views.assign((size_t)hs->num_ids + 1, PredView{nullptr, nullptr, 0, 0});
+    if (rbytes && (e = cudaMemcpy(d_rowptr, hs->rowptr, rbytes, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "store upload copy (offsets)");
+    views.assign((size_t)hs->num_ids + 1, PredView{});
     for (int id = 1; id <= hs->num_ids; ++id) {
         const PredSeg &sg = hs->segs[(size_t)id];
-        views[(size_t)id] = PredView{static_cast<const Bucket *>(d_buckets) + sg.bucket_off,
-                                     d_edges + sg.edge_off, sg.nmain, sg.nover};
+        views[(size_t)id] = make_view(sg, static_cast<const Bucket *>(d_buckets) + sg.bucket_off,
+                                      d_rowptr + sg.rp_off, d_edges + sg.edge_off);
     }
-    device_bytes = bbytes + ebytes;
+    device_bytes = bbytes + ebytes + rbytes;
     return WK_OK;
 }
 
@@ -90,14 +95,14 @@ int DeviceStore::init_paged(uint64_t budget) {
     free_list.clear();
     free_list[0] = budget;
     res.assign((size_t)hs->num_ids + 1, Resident());
-    views.assign((size_t)hs->num_ids + 1, PredView{nullptr, nullptr, 0, 0});
+    views.assign((size_t)hs->num_ids + 1, PredView{});
     device_bytes = budget;
     return WK_OK;
 }
 
 uint64_t DeviceStore::seg_bytes(int id) const {
     const PredSeg &sg = hs->segs[(size_t)id];
-    return align256(sg.bucket_bytes()) + align256(sg.edge_bytes());
+    return align256(sg.bucket_bytes()) + align256(sg.rowptr_bytes()) + align256(sg.edge_bytes());
 }
 
 bool DeviceStore::pool_alloc(uint64_t need, uint64_t *off) {
@@ -177,7 +182,7 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
         pool_free(x.off, x.bytes);
         x.resident = false;
         x.bytes = 0;
-        views[(size_t)victim] = PredView{nullptr, nullptr, 0, 0};
+        views[(size_t)victim] = PredView{};
         ++evictions;
     }
     // a copy on a side stream must not overwrite memory that kernels already
@@ -188,10 +193,13 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
         if ((e = cudaStreamWaitEvent(copy_st, use_ready, 0)) != cudaSuccess) return cuda_fail(e, "segment cache wait");
     }
     char *base = static_cast<char *>(pool) + off;
-    const uint64_t bb = sg.bucket_bytes(), eb = sg.edge_bytes();
+    const uint64_t bb = sg.bucket_bytes(), eb = sg.edge_bytes(), rb = sg.rowptr_bytes();
     if (bb && (e = cudaMemcpyAsync(base, hs->buckets + sg.bucket_off, bb, cudaMemcpyHostToDevice, copy_st)) != cudaSuccess)
         return cuda_fail(e, "segment cache copy (buckets)");
-    char *ebase = base + align256(bb);
+    char *rbase = base + align256(bb);
+    if (rb && (e = cudaMemcpyAsync(rbase, hs->rowptr + sg.rp_off, rb, cudaMemcpyHostToDevice, copy_st)) != cudaSuccess)
+        return cuda_fail(e, "segment cache copy (offsets)");
+    char *ebase = rbase + align256(rb);
     if (eb && (e = cudaMemcpyAsync(ebase, hs->edges + sg.edge_off, eb, cudaMemcpyHostToDevice, copy_st)) != cudaSuccess)
         return cuda_fail(e, "segment cache copy (edges)");
     if (!r.ev && (e = cudaEventCreateWithFlags(&r.ev, cudaEventDisableTiming)) != cudaSuccess) {
@@ -205,10 +213,10 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
     r.off = off;
     r.bytes = need;
     r.last_use = clock;
-    views[(size_t)id] = PredView{reinterpret_cast<const Bucket *>(base), reinterpret_cast<const int32_t *>(ebase),
-                                 sg.nmain, sg.nover};
+    views[(size_t)id] = make_view(sg, reinterpret_cast<const Bucket *>(base), reinterpret_cast<const uint32_t *>(rbase),
+                                  reinterpret_cast<const int32_t *>(ebase));
     ++loads;
-    bytes_loaded += bb + eb;
+    bytes_loaded += bb + rb + eb;
     return WK_OK;
 }
 
@@ -360,7 +368,7 @@ extern "C" int wk_store_get_info(wk_ctx *ctx, wk_store_info *info) {
     const HostStore *hs = ctx->store->hs.get();
     info->num_keys = (int64_t)hs->total_keys;
     info->num_edges = (int64_t)hs->total_edges;
-    info->key_bytes = (int64_t)(hs->total_buckets * sizeof(Bucket));
+    info->key_bytes = (int64_t)(hs->total_buckets * sizeof(Bucket) + hs->total_rowptr * 4);
     info->edge_bytes = (int64_t)hs->total_edges * 4;
     info->overflow_buckets = (int64_t)hs->total_over;
     info->device_bytes = (int64_t)ctx->store->device_bytes;
@@ -369,6 +377,9 @@ extern "C" int wk_store_get_info(wk_ctx *ctx, wk_store_info *info) {
     info->cache_loads = ctx->store->loads;
     info->cache_evictions = ctx->store->evictions;
     info->cache_bytes_loaded = (int64_t)ctx->store->bytes_loaded;
+    info->dense_dirs = 0;
+    for (int id = 1; id <= hs->num_ids; ++id)
+        info->dense_dirs += (hs->segs[(size_t)id].dn[0] ? 1 : 0) + (hs->segs[(size_t)id].dn[1] ? 1 : 0);
     return WK_OK;
 }
 

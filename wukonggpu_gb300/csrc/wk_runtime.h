@@ -41,6 +41,7 @@ struct DeviceStore {
     // resident mode
     void *d_buckets = nullptr;
     int32_t *d_edges = nullptr;
+    uint32_t *d_rowptr = nullptr;
     // paged mode
     void *pool = nullptr;
     uint64_t pool_bytes = 0, clock = 0;

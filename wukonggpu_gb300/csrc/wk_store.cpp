@@ -14,8 +14,10 @@
 //    :460-524).
 // The layout is this library's own: per id, a hash table of 64 B buckets
 // (5 slots of 32-bit segment-local keys + 1 overflow link) sized for a load of
-// at most 1/2, followed by overflow buckets, and one contiguous int32 edge
-// segment holding the id's out-lists, in-lists and index lists.
+// at most 1/2, followed by overflow buckets, an offsets array for each
+// direction whose vertices are dense in their id range (those vertices then
+// leave the hash table), and one contiguous int32 edge segment holding the
+// id's out-lists, in-lists and index lists.
 #include "wk_internal.h"
 
 #include <cuda_runtime.h>
@@ -33,9 +35,11 @@ HostStore::~HostStore() {
     if (pinned) {
         if (buckets) cudaFreeHost(buckets);
         if (edges) cudaFreeHost(edges);
+        if (rowptr) cudaFreeHost(rowptr);
     } else {
         free(buckets);
         free(edges);
+        free(rowptr);
     }
 }
 
@@ -43,6 +47,14 @@ uint64_t HostStore::lookup(uint64_t vid, uint32_t pid, uint32_t dir, const int32
     *edges_out = nullptr;
     if (pid < 1 || (int32_t)pid > num_ids || vid >= 0x7fffffffull || dir > 1u) return 0;
     const PredSeg &sg = segs[pid];
+    if (vid != 0 && sg.dn[dir]) {
+        const uint64_t x = vid - sg.dvmin[dir];
+        if (vid < sg.dvmin[dir] || x >= sg.dn[dir]) return 0;
+        const uint32_t *rp = rowptr + sg.rp_off + (dir ? sg.rp_entries(0) : 0);
+        if (rp[x + 1] == rp[x]) return 0;
+        *edges_out = edges + sg.edge_off + rp[x];
+        return rp[x + 1] - rp[x];
+    }
     if (sg.nmain == 0) return 0;
     const uint32_t key = seg_key((uint32_t)vid, dir);
     uint32_t b = seg_bucket(key, sg.nmain);
@@ -70,10 +82,67 @@ struct KeyRec {       // one key of a segment before insertion
 };
 
 struct SegBuild {
-    std::vector<KeyRec> keys;
+    std::vector<KeyRec> keys;      // after split_dense: the hashed keys only
     std::vector<int32_t> edges;
+    std::vector<uint32_t> rp;      // offsets arrays of the dense directions (IN, then OUT)
+    uint64_t nkeys = 0;            // every key
+    uint32_t dvmin[2] = {0u, 0u}, dn[2] = {0u, 0u};
     int64_t triples = 0, subjects = 0, objects = 0;
 };
+
+// Move the vertex keys of each direction that is dense enough into an offsets
+// array.  A direction's vertex keys were emitted in ascending vertex order
+// with their lists back to back, which the check below confirms.
+void split_dense(SegBuild &sb) {
+    sb.nkeys = sb.keys.size();
+    bool dense[2] = {false, false};
+    for (uint32_t dir = 0; dir < 2; ++dir) {
+        uint64_t count = 0;
+        uint32_t vmin = 0, vmax = 0, prev_end = 0;
+        bool ordered = true;
+        for (const KeyRec &kr : sb.keys) {
+            const uint32_t vid = kr.key >> 1;
+            if ((kr.key & 1u) != dir || vid == 0) continue;
+            if (count == 0) {
+                vmin = vid;
+            } else if (vid <= vmax || kr.off != prev_end) {
+                ordered = false;
+            }
+            vmax = vid;
+            prev_end = kr.off + kr.deg;
+            ++count;
+        }
+        if (count == 0 || !ordered) continue;
+        const uint64_t range = (uint64_t)vmax - vmin + 1;
+        if (count * WK_DENSE_RATIO < range) continue;
+        dense[dir] = true;
+        sb.dvmin[dir] = vmin;
+        sb.dn[dir] = (uint32_t)range;
+    }
+    if (!dense[0] && !dense[1]) return;
+    std::vector<KeyRec> hashed;
+    for (uint32_t dir = 0; dir < 2; ++dir) {
+        if (!dense[dir]) continue;
+        const size_t base = sb.rp.size();
+        sb.rp.resize(base + (size_t)sb.dn[dir] + 1);
+        uint32_t *rp = sb.rp.data() + base;
+        uint64_t pos = 0;
+        uint32_t end = 0;
+        for (const KeyRec &kr : sb.keys) {
+            const uint32_t vid = kr.key >> 1;
+            if ((kr.key & 1u) != dir || vid == 0) continue;
+            const uint64_t x = vid - sb.dvmin[dir];
+            while (pos <= x) rp[pos++] = kr.off;   // absent ids before v: empty lists ending at v's
+            end = kr.off + kr.deg;
+        }
+        while (pos <= sb.dn[dir]) rp[pos++] = end;
+    }
+    for (const KeyRec &kr : sb.keys) {
+        const uint32_t vid = kr.key >> 1, dir = kr.key & 1u;
+        if (vid == 0 || !dense[dir]) hashed.push_back(kr);
+    }
+    sb.keys.swap(hashed);
+}
 
 // Sort (hi,lo) pairs packed as hi<<32|lo, dedup, and emit one key per hi
 // group with the group's lo values as the adjacency list.
@@ -199,16 +268,27 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         }
     });
     std::vector<uint64_t>().swap(so);
+    parallel_for((size_t)num_ids + 1, [&](size_t id) {
+        if (id) split_dense(sb[id]);
+    });
 
     // sizes and image allocation
     HostStore *hs = new HostStore();
     hs->num_ids = num_ids;
     hs->segs.resize((size_t)num_ids + 1);
-    uint64_t bucket_at = 0, edge_at = 0;
+    uint64_t bucket_at = 0, edge_at = 0, rp_at = 0;
+    std::vector<uint64_t> nhash((size_t)num_ids + 1, 0);   // keys in the hash table
     for (size_t id = 1; id <= (size_t)num_ids; ++id) {
         PredSeg &sg = hs->segs[id];
         SegBuild &b = sb[id];
-        sg.nkeys = b.keys.size();
+        sg.nkeys = b.nkeys;
+        nhash[id] = b.keys.size();
+        for (int d = 0; d < 2; ++d) {
+            sg.dvmin[d] = b.dvmin[d];
+            sg.dn[d] = b.dn[d];
+        }
+        sg.rp_off = rp_at;
+        rp_at += b.rp.size();
         sg.nedges = b.edges.size();
         sg.triples = b.triples; sg.subjects = b.subjects; sg.objects = b.objects;
         if (sg.nedges > 0xffffffffull) {
@@ -217,15 +297,16 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         }
         // main buckets: keys / (5 * 0.5), at least one bucket when there are keys;
         // overflow room: worst case one bucket per 5 keys beyond the first
-        const uint64_t nm = sg.nkeys ? (sg.nkeys * 2 + WK_DATA_SLOTS - 1) / WK_DATA_SLOTS : 0;
-        if (nm + sg.nkeys / WK_DATA_SLOTS + 1 >= 0xffffffffull) {
+        const uint64_t nk = nhash[id];
+        const uint64_t nm = nk ? (nk * 2 + WK_DATA_SLOTS - 1) / WK_DATA_SLOTS : 0;
+        if (nm + nk / WK_DATA_SLOTS + 1 >= 0xffffffffull) {
             delete hs;
             return set_error(WK_EINVAL, "store build: id %zu has too many keys", id);
         }
         sg.nmain = (uint32_t)nm;
         sg.bucket_off = bucket_at;
         sg.edge_off = edge_at;
-        if (sg.nkeys) bucket_at += nm + sg.nkeys / WK_DATA_SLOTS + 1;
+        if (nk) bucket_at += nm + nk / WK_DATA_SLOTS + 1;
         edge_at += sg.nedges;
     }
     // reserve the upper bound, compact after insertion
@@ -239,9 +320,9 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
     parallel_for((size_t)num_ids + 1, [&](size_t id) {
         if (id == 0) return;
         PredSeg &sg = hs->segs[id];
-        if (!sg.nkeys) return;
+        if (!nhash[id]) return;
         Bucket *base = bk_tmp + sg.bucket_off;
-        const uint64_t cap = (uint64_t)sg.nmain + sg.nkeys / WK_DATA_SLOTS + 1;
+        const uint64_t cap = (uint64_t)sg.nmain + nhash[id] / WK_DATA_SLOTS + 1;
         for (uint64_t i = 0; i < cap; ++i) {
             uint32_t *w = base[i].w;
             for (int j = 0; j < WK_DATA_SLOTS; ++j) {
@@ -282,21 +363,27 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         total_buckets += (uint64_t)sg.nmain + sg.nover;
     }
     const uint64_t bbytes = (total_buckets ? total_buckets : 1) * sizeof(Bucket);
-    void *bp = nullptr, *ep = nullptr;
+    const uint64_t rbytes = (rp_at ? rp_at : 1) * 4;
+    void *bp = nullptr, *ep = nullptr, *rpp = nullptr;
     bool pinned = cudaHostAlloc(&bp, bbytes, cudaHostAllocPortable) == cudaSuccess &&
-                  cudaHostAlloc(&ep, edge_cap * 4, cudaHostAllocPortable) == cudaSuccess;
+                  cudaHostAlloc(&ep, edge_cap * 4, cudaHostAllocPortable) == cudaSuccess &&
+                  cudaHostAlloc(&rpp, rbytes, cudaHostAllocPortable) == cudaSuccess;
     if (!pinned) {
         cudaGetLastError();
         if (bp) cudaFreeHost(bp);
         if (ep) cudaFreeHost(ep);
+        if (rpp) cudaFreeHost(rpp);
         bp = aligned_alloc(WK_BUCKET_BYTES, bbytes);
         ep = malloc(edge_cap * 4);
-        if (!bp || !ep) { free(bp); free(ep); free(bk_tmp); delete hs;
-                          return set_error(WK_ENOMEM, "store build: out of host memory"); }
+        rpp = malloc(rbytes);
+        if (!bp || !ep || !rpp) { free(bp); free(ep); free(rpp); free(bk_tmp); delete hs;
+                                  return set_error(WK_ENOMEM, "store build: out of host memory"); }
     }
     hs->pinned = pinned;
     hs->buckets = static_cast<Bucket *>(bp);
     hs->edges = (int32_t *)ep;
+    hs->rowptr = static_cast<uint32_t *>(rpp);
+    hs->total_rowptr = rp_at;
     std::vector<uint64_t> new_off((size_t)num_ids + 1, 0);
     uint64_t at = 0;
     for (size_t id = 1; id <= (size_t)num_ids; ++id) {
@@ -310,8 +397,10 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         if (nb) std::memcpy(hs->buckets + new_off[id], bk_tmp + sg.bucket_off, nb * sizeof(Bucket));
         sg.bucket_off = new_off[id];
         if (sg.nedges) std::memcpy(hs->edges + sg.edge_off, sb[id].edges.data(), sg.nedges * 4);
+        if (!sb[id].rp.empty()) std::memcpy(hs->rowptr + sg.rp_off, sb[id].rp.data(), sb[id].rp.size() * 4);
         std::vector<KeyRec>().swap(sb[id].keys);
         std::vector<int32_t>().swap(sb[id].edges);
+        std::vector<uint32_t>().swap(sb[id].rp);
     });
     free(bk_tmp);
     hs->total_buckets = total_buckets;
