@@ -209,3 +209,26 @@ def test_kernel_launch_count_and_timing(gpu_small, golden_small):
     assert gpu_small.kernel_launches() > before
     assert st["kernels"] == 3 and st["ms"] > 0 and st["ms_main"] > 0   # k2u: count + plan + expand
     assert st["rows_out"] == q["rows"]
+
+
+def test_functional_direction_reaching_an_index_list(lib_built):
+    """A functional direction expands as a compaction; a history value 0 looks
+    up the index key [0|p|d] (core/gstore.hpp:389-409), a long list, and the op
+    must still give the reference's rows."""
+    s, p, o, nid = _hub_graph()
+    rc = W.RCache(device=0)
+    rc.build_store(s, p, o, nid)
+    orc = oracle.Oracle(s, p, o, nid)
+    assert rc.store_info()["dense_dirs"] > 0
+    rng = np.random.default_rng(5)
+    h = (W.VID_BASE + rng.integers(0, 20_000, size=(3000, 2))).astype(np.int32)
+    for with_zero in (False, True):
+        if with_zero:
+            h[1500, 0] = 0
+        for d in (W.OUT, W.IN):
+            req = W.Request([])
+            rc.upload_history(req, h)
+            rc.known_to_unknown(req, -1, d, 3)
+            got = rc.download(req)
+            exp, _ = orc.step(h, False, -1, 3, d, -3)
+            assert got.shape == exp.shape and np.array_equal(got, exp), (with_zero, d)

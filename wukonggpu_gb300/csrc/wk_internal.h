@@ -31,7 +31,10 @@
 // already in ascending vertex order.  A probe then reads 8 B (one sector)
 // instead of a 64 B bucket, the array costs 4 B per id of the range (a hash
 // key costs about 26 B), and dense arrays of a few million vertices stay in
-// L2.  Index keys (vid 0) always stay in the hash table.
+// L2.  Index keys (vid 0) always stay in the hash table.  A dense direction
+// whose lists hold at most one vertex (a functional predicate) also keeps
+// nb[v - vmin] = that vertex or -1, so a lookup that only needs the neighbour
+// is a single 4 B read.
 #define WK_BUCKET_WORDS 16
 #define WK_BUCKET_BYTES 64
 #define WK_DATA_SLOTS 5
@@ -104,12 +107,15 @@ struct PredSeg {
     // rowptr image from rp_off: dir IN (dn[0] + 1 entries, if dense), then OUT.
     uint32_t dvmin[2] = {0u, 0u}, dn[2] = {0u, 0u};
     uint64_t rp_off = 0;
+    uint32_t maxdeg[2] = {0u, 0u};   // longest vertex list per direction (index lists excluded)
     // statistics (GStore::generate_statistic, core/gstore.hpp:1010-1127)
     int64_t triples = 0, subjects = 0, objects = 0;
     uint64_t bucket_bytes() const { return (uint64_t)(nmain + nover) * WK_BUCKET_BYTES; }
     uint64_t edge_bytes() const { return nedges * 4; }
     uint64_t rp_entries(int dir) const { return dn[dir] ? (uint64_t)dn[dir] + 1 : 0; }
-    uint64_t rowptr_bytes() const { return 4 * (rp_entries(0) + rp_entries(1)); }
+    // neighbour array of a dense functional direction, after both offsets arrays
+    uint64_t nb_entries(int dir) const { return (dn[dir] && maxdeg[dir] <= 1u) ? (uint64_t)dn[dir] : 0; }
+    uint64_t rowptr_bytes() const { return 4 * (rp_entries(0) + rp_entries(1) + nb_entries(0) + nb_entries(1)); }
 };
 
 struct HostStore {
@@ -158,6 +164,8 @@ struct PredView {
     uint32_t nover = 0;                     // bound on overflow hops (corruption guard)
     const uint32_t *rp[2] = {nullptr, nullptr};   // dense offsets per direction, or null
     uint32_t vmin[2] = {0u, 0u}, dn[2] = {0u, 0u};
+    uint32_t func[2] = {0u, 0u};  // 1: every vertex of the direction has at most one neighbour
+    const int32_t *nb[2] = {nullptr, nullptr};    // dense functional: the neighbour per id, or -1
 };
 
 // The device view of segment sg whose buckets, offsets arrays and edges start
@@ -168,13 +176,17 @@ inline PredView make_view(const PredSeg &sg, const Bucket *bk, const uint32_t *r
     v.edges = edges;
     v.nmain = sg.nmain;
     v.nover = sg.nover;
+    const uint32_t *nb = rp + sg.rp_entries(0) + sg.rp_entries(1);
     for (int d = 0; d < 2; ++d) {
+        v.func[d] = sg.maxdeg[d] <= 1u ? 1u : 0u;
         if (sg.dn[d]) {
             v.rp[d] = rp;
             v.vmin[d] = sg.dvmin[d];
             v.dn[d] = sg.dn[d];
         }
+        if (sg.nb_entries(d)) v.nb[d] = reinterpret_cast<const int32_t *>(nb);
         rp += sg.rp_entries(d);
+        nb += sg.nb_entries(d);
     }
     return v;
 }

@@ -111,14 +111,22 @@ constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
 
 // totals[0] += output rows, totals[1] += rows with a match; blk_sum[b] = the
 // block's output rows.  Err bit 1 when a block's output count reaches 2^31
-// (the expansion keeps block-local positions in 32 bits).
+// (the expansion keeps block-local positions in 32 bits).  FUNC (a direction
+// whose lists hold at most one vertex): deg receives the neighbour itself as
+// an int32, or -1 for no match, and off is unused.  DENSE (the direction is
+// an offsets array): the rounds' lookups are issued phase by phase -- every
+// round's offsets, then every round's neighbour -- so a warp has its four
+// rounds' loads in flight at once instead of one dependent chain per round,
+// and a lane looks up its own key (no shuffles).
+template <bool FUNC, bool DENSE>
 __global__ void __launch_bounds__(kThreads)
 k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
                  uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
                  unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ totals,
                  unsigned long long *__restrict__ tile_sums, int *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t wrow0 = (int64_t)blockIdx.x * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
+    const int64_t b = blockIdx.x;
+    const int64_t wrow0 = b * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
     int32_t v[kRounds];
 #pragma unroll
     for (int rd = 0; rd < kRounds; ++rd) {
@@ -127,6 +135,61 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
     }
     unsigned long long my_sum = 0;
     unsigned int my_nz = 0;
+    if constexpr (DENSE) {
+        // no run dedup here: equal keys of a warp read the same sector, which the
+        // load unit merges, so shuffles would only add work
+        const uint32_t *rp = dir ? pv.rp[1] : pv.rp[0];
+        const uint32_t vmin = dir ? pv.vmin[1] : pv.vmin[0], dn = dir ? pv.dn[1] : pv.dn[0];
+        const int32_t *nba = dir ? pv.nb[1] : pv.nb[0];
+        uint32_t a[kRounds], e[kRounds];
+        int32_t g[kRounds];
+#pragma unroll
+        for (int rd = 0; rd < kRounds; ++rd) {
+            const int32_t vid = v[rd];
+            a[rd] = e[rd] = 0u;
+            g[rd] = -1;
+            const uint32_t x = (uint32_t)vid - vmin;   // wraps above dn below vmin
+            if (vid > 0 && x < dn) {
+                if (FUNC && nba != nullptr) {
+                    // the neighbour itself: one 4 B read, no offsets and no gather
+                    g[rd] = __ldg(nba + x);
+                    e[rd] = g[rd] >= 0 ? 1u : 0u;
+                } else {
+                    a[rd] = __ldg(rp + x);
+                    e[rd] = __ldg(rp + x + 1);
+                }
+            } else if (vid == 0) {   // index key: the hash table
+                e[rd] = probe_seg(pv.buckets, pv.nmain, pv.nover, seg_key(0u, dir), &a[rd], err);
+                e[rd] += a[rd];
+            }
+        }
+        if constexpr (FUNC) {
+            if (nba == nullptr) {
+#pragma unroll
+                for (int rd = 0; rd < kRounds; ++rd) g[rd] = e[rd] != a[rd] ? __ldg(pv.edges + a[rd]) : -1;
+            } else {
+#pragma unroll
+                for (int rd = 0; rd < kRounds; ++rd)
+                    if (v[rd] == 0 && e[rd] != a[rd]) g[rd] = __ldg(pv.edges + a[rd]);
+            }
+        }
+#pragma unroll
+        for (int rd = 0; rd < kRounds; ++rd) {
+            const int64_t r = wrow0 + rd * 32 + lane;
+            const uint32_t d = e[rd] - a[rd];
+            if (r < R) {
+                if constexpr (FUNC) {
+                    reinterpret_cast<int32_t *>(deg)[r] = g[rd];
+                    if (d > 1u) atomicOr(err, 8);   // an index list: the op reruns unspecialised
+                } else {
+                    deg[r] = d;
+                    off[r] = a[rd];
+                }
+                my_sum += d;
+                my_nz += d > 0u;
+            }
+        }
+    } else {
 #pragma unroll
     for (int rd = 0; rd < kRounds; ++rd) {
         const int64_t row0 = wrow0 + rd * 32;
@@ -135,18 +198,24 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
         uint32_t o, d;
         probe_warp(pv, v[rd], dir, o, d, err);
         if (r < R) {
-            deg[r] = d;
-            off[r] = o;
+            if constexpr (FUNC) {
+                reinterpret_cast<int32_t *>(deg)[r] = d ? __ldg(pv.edges + o) : -1;
+                if (d > 1u) atomicOr(err, 8);   // an index list: the op reruns unspecialised
+            } else {
+                deg[r] = d;
+                off[r] = o;
+            }
             my_sum += d;
             my_nz += d > 0u;
         }
     }
+    }
     block_sum2(my_sum, my_nz);
     if (threadIdx.x == 0) {
-        blk_sum[blockIdx.x] = my_sum;
+        blk_sum[b] = my_sum;
         if (my_sum) {
             atomicAdd(totals, my_sum);
-            unsigned long long *ts = tile_sums + 2 * (blockIdx.x >> kPlanTileShift);
+            unsigned long long *ts = tile_sums + 2 * (b >> kPlanTileShift);
             atomicAdd(ts, my_sum);
             atomicAdd(ts + 1, slices_of(my_sum));
         }
@@ -417,6 +486,101 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
     }
 }
 
+// ------------------------------------------------- k2u expand, functional
+// A direction whose lists hold at most one vertex: the expansion is a
+// compaction of the matched rows with their neighbour appended.  One CTA per
+// non-empty input block (its only slice).  Warp w takes rows 128 w .. 128 w +
+// 127 in four passes of 32 consecutive rows, finds each matched row's output
+// position by ballots, copies the row and its neighbour into shared memory
+// (rows kPitch words apart, an odd pitch so the 32 lanes' rows fall in 32
+// banks), and the CTA then streams the block's output words to HBM as
+// aligned int4 stores.
+template <int W>
+__global__ void __launch_bounds__(kThreads)
+k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_t *__restrict__ nbr,
+                       const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ bp,
+                       const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out) {
+    constexpr int C = W - 1;
+    constexpr int kPitch = W | 1;
+    __shared__ int32_t rows[kRowsPerBlock * kPitch];
+    __shared__ uint32_t s_w[kThreads / 32];
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const unsigned long long k = blockIdx.x;
+
+    // the block: last b with sp[b] <= k (every non-empty block has one slice)
+    int64_t lo = 0, hi = nblk - 1;
+    while (hi > lo) {
+        const int64_t step = (hi - lo + 32) / 32;
+        int64_t bl = lo + (int64_t)lane * step;
+        if (bl > hi) bl = hi;
+        const unsigned m = __ballot_sync(FULL, sp[bl] <= k);
+        const int L = 31 - __clz(m);
+        const int64_t blo = __shfl_sync(FULL, bl, L);
+        const int64_t bnx = L < 31 ? __shfl_sync(FULL, bl, L + 1) : hi + 1;
+        lo = blo;
+        hi = bnx > blo ? bnx - 1 : blo;
+    }
+    const int64_t b = lo;
+    const int64_t r0 = b * kRowsPerBlock;
+    const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
+
+    // matched rows and their block-local output positions
+    int32_t x[4];
+    unsigned bm[4];
+    unsigned wtot = 0;
+#pragma unroll
+    for (int ps = 0; ps < 4; ++ps) {
+        const int r = wid * 128 + ps * 32 + lane;
+        x[ps] = r < n ? __ldg(nbr + r0 + r) : -1;
+        bm[ps] = __ballot_sync(FULL, x[ps] >= 0);
+        wtot += __popc(bm[ps]);
+    }
+    if (lane == 0) s_w[wid] = wtot;
+    __syncthreads();
+    unsigned base = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w)
+        if (w < wid) base += s_w[w];
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int ps = 0; ps < 4; ++ps) {
+        if (x[ps] >= 0) {
+            const int r = wid * 128 + ps * 32 + lane;
+            const unsigned q = base + __popc(bm[ps] & below);
+            const int32_t *src = hist + (r0 + r) * C;
+            int32_t *dst = rows + q * kPitch;
+#pragma unroll
+            for (int c = 0; c < C; ++c) dst[c] = __ldg(src + c);
+            dst[C] = x[ps];
+        }
+        base += __popc(bm[ps]);
+    }
+    __syncthreads();
+
+    // output words [P W, (P + T) W): int4 stores aligned to 16 B of out
+    const unsigned long long P = bp[b];
+    const uint32_t T = (uint32_t)blk_sum[b];
+    const uint32_t lead = (uint32_t)((P * W) & 3ull), words = T * W;
+    int32_t *g = out + (P * W - lead);
+    for (uint32_t i = (uint32_t)t; 4u * i < lead + words; i += kThreads) {
+        int32_t v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t kk = 4u * i + j - lead;   // wraps above `words` before the lead
+            v[j] = kk < words ? rows[(kk / W) * kPitch + kk % W] : 0;
+        }
+        if (4u * i >= lead && 4u * i + 4u <= lead + words) {
+            reinterpret_cast<int4 *>(g)[i] = make_int4(v[0], v[1], v[2], v[3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t kk = 4u * i + j - lead;
+                if (kk < words) g[4u * i + j] = v[j];
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------- k2k / k2c probe
 // lower_bound of `v` in the ascending list e[0..n).  Lists hold distinct ids,
 // so lower_bound is also the position where the reference's linear scan
@@ -546,9 +710,36 @@ static inline unsigned int nblocks_rows(int64_t R) {
 
 void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg,
                       uint32_t *off, unsigned long long *blk_sum, unsigned long long *totals,
-                      unsigned long long *tile_sums, int *err, cudaStream_t st) {
-    k2u_count_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, totals,
-                                                           tile_sums, err);
+                      unsigned long long *tile_sums, int *err, bool func, cudaStream_t st) {
+    const bool dense = (dir ? pv.rp[1] : pv.rp[0]) != nullptr;
+    const unsigned int g = nblocks_rows(R);
+#define WK_COUNT(F, D) \
+    k2u_count_kernel<F, D><<<g, kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, totals, tile_sums, err)
+    if (func && dense) WK_COUNT(true, true);
+    else if (func) WK_COUNT(true, false);
+    else if (dense) WK_COUNT(false, true);
+    else WK_COUNT(false, false);
+#undef WK_COUNT
+}
+
+void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
+                            const unsigned long long *blk_sum, const unsigned long long *bp,
+                            const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st) {
+    if (slices == 0ull) return;
+    const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
+    const unsigned int g = (unsigned int)slices;
+#define WK_EXPAND_F(WC) \
+    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, bp, sp, nblk, out)
+    switch (C + 1) {
+        case 2: WK_EXPAND_F(2); break;
+        case 3: WK_EXPAND_F(3); break;
+        case 4: WK_EXPAND_F(4); break;
+        case 5: WK_EXPAND_F(5); break;
+        case 6: WK_EXPAND_F(6); break;
+        case 7: WK_EXPAND_F(7); break;
+        default: WK_EXPAND_F(8); break;
+    }
+#undef WK_EXPAND_F
 }
 
 void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, const unsigned long long *tile_sums,

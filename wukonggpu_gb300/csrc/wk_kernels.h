@@ -20,9 +20,19 @@ constexpr int kMaxPlanTiles = 250;    // plan CTAs per op (tile sums live beside
 // tile_sums[2c] += output rows and tile_sums[2c + 1] += slices of the blocks of
 // plan tile c (zeroed before the launch); err bit 0: overflow chain longer
 // than the segment's overflow area, bit 1: a block's count reached 2^31.
+// func (the direction is functional, PredView::func): deg receives each row's
+// neighbour as int32 (-1 when there is none) for launch_k2u_expand_func; err
+// bit 3 when a row's list had more than one entry (an index key), which the
+// functional expansion cannot write.
 void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg,
                       uint32_t *off, unsigned long long *blk_sum, unsigned long long *totals,
-                      unsigned long long *tile_sums, int *err, cudaStream_t st);
+                      unsigned long long *tile_sums, int *err, bool func, cudaStream_t st);
+
+// k2u pass 2 of a functional direction (2 <= C + 1 <= 8): the matched rows
+// with their neighbour appended, compacted in order; one CTA per non-empty block.
+void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
+                            const unsigned long long *blk_sum, const unsigned long long *bp,
+                            const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st);
 
 // k2u plan: bp[b] = the block's output prefix, sp[b] = its first slice
 // (nblk + 1 entries each); totals[2] = slices, the expansion's CTA count.

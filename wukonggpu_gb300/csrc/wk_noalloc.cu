@@ -107,7 +107,8 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     cudaStream_t s = ctx->stream;
     if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 48, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
     // kMaxRows input rows are one plan tile: its two sums follow the totals
-    dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, tot, tot + 3, err, s);
+    dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, tot, tot + 3, err, false,
+                          s);
     dev::launch_k2u_plan(blk_sum, nblk, tot + 3, bp, sp, tot, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: count launch");
     ctx->launches += 2;

@@ -172,23 +172,30 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         return set_error(WK_EINVAL, "k2u: %lld input rows exceed one op's maximum of %lld", (long long)R,
                          (long long)dev::kMaxPlanTiles << dev::kPlanTileShift << 10);
     if ((st = ctx->deg.reserve((size_t)R * 4)) || (st = ctx->off.reserve((size_t)R * 4)) ||
-        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16)) ||
-        (st = clear_totals(ctx, tiles)))
+        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16)))
         return st;
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
     unsigned long long *tile_sums = ctx->dscal.as<unsigned long long>() + 8;
     int *err = ctx->dscal.as<int>();
     // block output prefixes and slice prefixes share the look-back scratch
     unsigned long long *bp = ctx->lb_flags.as<unsigned long long>(), *sp = bp + (nblk + 1);
-    if ((st = clk.begin())) return st;
-    dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
-                          ctx->blk_sum.as<unsigned long long>(), tot, tile_sums, err, ctx->stream);
-    dev::launch_k2u_plan(ctx->blk_sum.as<unsigned long long>(), nblk, tile_sums, bp, sp, tot, ctx->stream);
-    ++ctx->launches;   // the plan kernel, timed with the count
-    ++ctx->last.kernels;
-    if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;
+    // a functional direction (at most one neighbour per vertex) expands as a
+    // compaction; if a row hits an index list (vertex 0) the op reruns unspecialised
+    bool func = pv.func[dir] != 0u && C + 1 <= 8;
     int errf = 0;
-    if ((st = read_totals(ctx, &errf))) return st;
+    for (;;) {
+        if ((st = clear_totals(ctx, tiles)) || (st = clk.begin())) return st;
+        dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
+                              ctx->blk_sum.as<unsigned long long>(), tot, tile_sums, err, func, ctx->stream);
+        dev::launch_k2u_plan(ctx->blk_sum.as<unsigned long long>(), nblk, tile_sums, bp, sp, tot, ctx->stream);
+        ++ctx->launches;   // the plan kernel, timed with the count
+        ++ctx->last.kernels;
+        if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;
+        if ((st = read_totals(ctx, &errf))) return st;
+        if (!(func && (errf & 8))) break;
+        cudaMemsetAsync(ctx->dscal.ptr, 0, 8, ctx->stream);
+        func = false;
+    }
     if (errf & 1) return fail_corrupt(ctx);
     if (errf & 2) {
         cudaMemsetAsync(ctx->dscal.ptr, 0, 8, ctx->stream);
@@ -205,9 +212,13 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     } else {
         if ((st = ob.reserve((size_t)R_out * (C + 1) * 4))) return st;
         if ((st = clk.begin())) return st;
-        dev::launch_k2u_expand(h->data, R, C, pv.edges, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
-                               ctx->blk_sum.as<unsigned long long>(), bp, sp, ctx->h_scal[3], ob.as<int32_t>(),
-                               ctx->stream);
+        if (func)
+            dev::launch_k2u_expand_func(h->data, R, C, ctx->deg.as<int32_t>(), ctx->blk_sum.as<unsigned long long>(),
+                                        bp, sp, ctx->h_scal[3], ob.as<int32_t>(), ctx->stream);
+        else
+            dev::launch_k2u_expand(h->data, R, C, pv.edges, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
+                                   ctx->blk_sum.as<unsigned long long>(), bp, sp, ctx->h_scal[3], ob.as<int32_t>(),
+                                   ctx->stream);
         if ((st = launch_check("k2u expand")) || (st = clk.end(true))) return st;
         if (ctx->timing) {
             cudaError_t e = cudaStreamSynchronize(ctx->stream);

@@ -87,6 +87,7 @@ struct SegBuild {
     std::vector<uint32_t> rp;      // offsets arrays of the dense directions (IN, then OUT)
     uint64_t nkeys = 0;            // every key
     uint32_t dvmin[2] = {0u, 0u}, dn[2] = {0u, 0u};
+    uint32_t maxdeg[2] = {0u, 0u};
     int64_t triples = 0, subjects = 0, objects = 0;
 };
 
@@ -95,6 +96,8 @@ struct SegBuild {
 // with their lists back to back, which the check below confirms.
 void split_dense(SegBuild &sb) {
     sb.nkeys = sb.keys.size();
+    for (const KeyRec &kr : sb.keys)
+        if ((kr.key >> 1) != 0) sb.maxdeg[kr.key & 1u] = std::max(sb.maxdeg[kr.key & 1u], kr.deg);
     bool dense[2] = {false, false};
     for (uint32_t dir = 0; dir < 2; ++dir) {
         uint64_t count = 0;
@@ -136,6 +139,18 @@ void split_dense(SegBuild &sb) {
             end = kr.off + kr.deg;
         }
         while (pos <= sb.dn[dir]) rp[pos++] = end;
+    }
+    // neighbour arrays of dense functional directions, after both offsets arrays
+    for (uint32_t dir = 0; dir < 2; ++dir) {
+        if (!dense[dir] || sb.maxdeg[dir] > 1u) continue;
+        const size_t base = sb.rp.size();
+        sb.rp.resize(base + (size_t)sb.dn[dir], 0xffffffffu);   // -1: no neighbour
+        uint32_t *nb = sb.rp.data() + base;
+        for (const KeyRec &kr : sb.keys) {
+            const uint32_t vid = kr.key >> 1;
+            if ((kr.key & 1u) != dir || vid == 0 || kr.deg == 0) continue;
+            nb[vid - sb.dvmin[dir]] = (uint32_t)sb.edges[kr.off];
+        }
     }
     for (const KeyRec &kr : sb.keys) {
         const uint32_t vid = kr.key >> 1, dir = kr.key & 1u;
@@ -286,6 +301,7 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         for (int d = 0; d < 2; ++d) {
             sg.dvmin[d] = b.dvmin[d];
             sg.dn[d] = b.dn[d];
+            sg.maxdeg[d] = b.maxdeg[d];
         }
         sg.rp_off = rp_at;
         rp_at += b.rp.size();
