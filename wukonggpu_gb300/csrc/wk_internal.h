@@ -34,7 +34,10 @@
 // L2.  Index keys (vid 0) always stay in the hash table.  A dense direction
 // whose lists hold at most one vertex (a functional predicate) also keeps
 // nb[v - vmin] = that vertex or -1, so a lookup that only needs the neighbour
-// is a single 4 B read.
+// is a single 4 B read.  A hashed direction whose keys are not too sparse in
+// their id range keeps a presence bitmap over it (at most 64 B per key), so a
+// probe of an absent vertex -- most probes of a sparse predicate -- is one
+// 4 B read instead of a 64 B bucket.
 #define WK_BUCKET_WORDS 16
 #define WK_BUCKET_BYTES 64
 #define WK_DATA_SLOTS 5
@@ -108,6 +111,7 @@ struct PredSeg {
     uint32_t dvmin[2] = {0u, 0u}, dn[2] = {0u, 0u};
     uint64_t rp_off = 0;
     uint32_t maxdeg[2] = {0u, 0u};   // longest vertex list per direction (index lists excluded)
+    uint32_t bvmin[2] = {0u, 0u}, bn[2] = {0u, 0u};   // presence bitmap of a hashed direction; bn = 0: none
     // statistics (GStore::generate_statistic, core/gstore.hpp:1010-1127)
     int64_t triples = 0, subjects = 0, objects = 0;
     uint64_t bucket_bytes() const { return (uint64_t)(nmain + nover) * WK_BUCKET_BYTES; }
@@ -115,7 +119,11 @@ struct PredSeg {
     uint64_t rp_entries(int dir) const { return dn[dir] ? (uint64_t)dn[dir] + 1 : 0; }
     // neighbour array of a dense functional direction, after both offsets arrays
     uint64_t nb_entries(int dir) const { return (dn[dir] && maxdeg[dir] <= 1u) ? (uint64_t)dn[dir] : 0; }
-    uint64_t rowptr_bytes() const { return 4 * (rp_entries(0) + rp_entries(1) + nb_entries(0) + nb_entries(1)); }
+    // presence bitmap words of a hashed direction, after the neighbour arrays
+    uint64_t bm_words(int dir) const { return ((uint64_t)bn[dir] + 31) / 32; }
+    uint64_t rowptr_bytes() const {
+        return 4 * (rp_entries(0) + rp_entries(1) + nb_entries(0) + nb_entries(1) + bm_words(0) + bm_words(1));
+    }
 };
 
 struct HostStore {
@@ -166,6 +174,8 @@ struct PredView {
     uint32_t vmin[2] = {0u, 0u}, dn[2] = {0u, 0u};
     uint32_t func[2] = {0u, 0u};  // 1: every vertex of the direction has at most one neighbour
     const int32_t *nb[2] = {nullptr, nullptr};    // dense functional: the neighbour per id, or -1
+    const uint32_t *bm[2] = {nullptr, nullptr};   // hashed: presence bitmap over [bvmin, bvmin + bn)
+    uint32_t bvmin[2] = {0u, 0u}, bn[2] = {0u, 0u};
 };
 
 // The device view of segment sg whose buckets, offsets arrays and edges start
@@ -177,6 +187,7 @@ inline PredView make_view(const PredSeg &sg, const Bucket *bk, const uint32_t *r
     v.nmain = sg.nmain;
     v.nover = sg.nover;
     const uint32_t *nb = rp + sg.rp_entries(0) + sg.rp_entries(1);
+    const uint32_t *bm = nb + sg.nb_entries(0) + sg.nb_entries(1);
     for (int d = 0; d < 2; ++d) {
         v.func[d] = sg.maxdeg[d] <= 1u ? 1u : 0u;
         if (sg.dn[d]) {
@@ -185,8 +196,14 @@ inline PredView make_view(const PredSeg &sg, const Bucket *bk, const uint32_t *r
             v.dn[d] = sg.dn[d];
         }
         if (sg.nb_entries(d)) v.nb[d] = reinterpret_cast<const int32_t *>(nb);
+        if (sg.bn[d]) {
+            v.bm[d] = bm;
+            v.bvmin[d] = sg.bvmin[d];
+            v.bn[d] = sg.bn[d];
+        }
         rp += sg.rp_entries(d);
         nb += sg.nb_entries(d);
+        bm += sg.bm_words(d);
     }
     return v;
 }

@@ -390,8 +390,13 @@ __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint3
 // 2 <= W <= 8; W = 0 for any width (one output row per thread and step,
 // scalar stores).  History rows are read through L1 (consecutive output rows
 // of one input row reuse it).
+// CTAs per SM the register budget is set for: the widest instantiations need
+// more registers to avoid spills
 template <int W>
-__global__ void __launch_bounds__(kThreads)
+constexpr int expand_min_ctas() { return (W >= 2 && W <= 5) || W == 0 ? 8 : (W <= 7 ? 6 : 5); }
+
+template <int W>
+__global__ void __launch_bounds__(kThreads, expand_min_ctas<W>())
 k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const int32_t *__restrict__ edges,
                   const uint32_t *__restrict__ deg, const uint32_t *__restrict__ off,
                   const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ bp,

@@ -72,6 +72,14 @@ __device__ __forceinline__ uint32_t probe_view(const PredView &pv, uint32_t vid,
         *off = a;
         return b - a;
     }
+    const uint32_t *bm = dir ? pv.bm[1] : pv.bm[0];
+    if (bm != nullptr && vid != 0u) {
+        const uint32_t x = vid - (dir ? pv.bvmin[1] : pv.bvmin[0]);   // wraps above bn below bvmin
+        if (x >= (dir ? pv.bn[1] : pv.bn[0]) || !((__ldg(bm + (x >> 5)) >> (x & 31u)) & 1u)) {
+            *off = 0u;
+            return 0u;
+        }
+    }
     return probe_seg(pv.buckets, pv.nmain, pv.nover, seg_key(vid, dir), off, err);
 }
 

@@ -88,8 +88,11 @@ struct SegBuild {
     uint64_t nkeys = 0;            // every key
     uint32_t dvmin[2] = {0u, 0u}, dn[2] = {0u, 0u};
     uint32_t maxdeg[2] = {0u, 0u};
+    uint32_t bvmin[2] = {0u, 0u}, bn[2] = {0u, 0u};
     int64_t triples = 0, subjects = 0, objects = 0;
 };
+
+constexpr uint64_t kBitmapBytesPerKey = 64;   // a presence bitmap may cost at most this per hashed key
 
 // Move the vertex keys of each direction that is dense enough into an offsets
 // array.  A direction's vertex keys were emitted in ascending vertex order
@@ -122,7 +125,39 @@ void split_dense(SegBuild &sb) {
         sb.dvmin[dir] = vmin;
         sb.dn[dir] = (uint32_t)range;
     }
-    if (!dense[0] && !dense[1]) return;
+    // presence bitmaps of hashed directions, appended after any offsets and neighbour arrays
+    auto add_bitmaps = [&]() {
+        for (uint32_t dir = 0; dir < 2; ++dir) {
+            if (dense[dir]) continue;
+            uint64_t count = 0;
+            uint32_t vmin = 0xffffffffu, vmax = 0;
+            for (const KeyRec &kr : sb.keys) {
+                const uint32_t vid = kr.key >> 1;
+                if ((kr.key & 1u) != dir || vid == 0) continue;
+                vmin = std::min(vmin, vid);
+                vmax = std::max(vmax, vid);
+                ++count;
+            }
+            if (count == 0) continue;
+            const uint64_t range = (uint64_t)vmax - vmin + 1;
+            if (range / 8 > count * kBitmapBytesPerKey) continue;
+            sb.bvmin[dir] = vmin;
+            sb.bn[dir] = (uint32_t)range;
+            const size_t base = sb.rp.size();
+            sb.rp.resize(base + (size_t)((range + 31) / 32), 0u);
+            uint32_t *bm = sb.rp.data() + base;
+            for (const KeyRec &kr : sb.keys) {
+                const uint32_t vid = kr.key >> 1;
+                if ((kr.key & 1u) != dir || vid == 0) continue;
+                const uint32_t x = vid - vmin;
+                bm[x >> 5] |= 1u << (x & 31u);
+            }
+        }
+    };
+    if (!dense[0] && !dense[1]) {
+        add_bitmaps();
+        return;
+    }
     std::vector<KeyRec> hashed;
     for (uint32_t dir = 0; dir < 2; ++dir) {
         if (!dense[dir]) continue;
@@ -152,6 +187,7 @@ void split_dense(SegBuild &sb) {
             nb[vid - sb.dvmin[dir]] = (uint32_t)sb.edges[kr.off];
         }
     }
+    add_bitmaps();
     for (const KeyRec &kr : sb.keys) {
         const uint32_t vid = kr.key >> 1, dir = kr.key & 1u;
         if (vid == 0 || !dense[dir]) hashed.push_back(kr);
@@ -302,6 +338,8 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
             sg.dvmin[d] = b.dvmin[d];
             sg.dn[d] = b.dn[d];
             sg.maxdeg[d] = b.maxdeg[d];
+            sg.bvmin[d] = b.bvmin[d];
+            sg.bn[d] = b.bn[d];
         }
         sg.rp_off = rp_at;
         rp_at += b.rp.size();
