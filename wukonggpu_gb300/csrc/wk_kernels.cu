@@ -109,8 +109,8 @@ __device__ __forceinline__ unsigned long long slices_of(unsigned long long t) {
 // probed, so the history read does not sit in front of every bucket read.
 constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
 
-// totals[0] += output rows, totals[1] += rows with a match; blk_sum[b] = the
-// block's output rows.  Err bit 1 when a block's output count reaches 2^31
+// blk_sum[b] = the block's output rows, added into its group's sums.  Err bit
+// 1 when a block's output count reaches 2^31
 // (the expansion keeps block-local positions in 32 bits).  FUNC (a direction
 // whose lists hold at most one vertex): deg receives the neighbour itself as
 // an int32, or -1 for no match, and off is unused.  DENSE (the direction is
@@ -119,19 +119,22 @@ constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
 // rounds' loads in flight at once instead of one dependent chain per round,
 // and a lane looks up its own key (no shuffles).
 template <bool FUNC, bool DENSE>
-__global__ void __launch_bounds__(kThreads)
-k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv,
-                 uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
-                 unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ totals,
-                 unsigned long long *__restrict__ tile_sums, int *err) {
+__global__ void __launch_bounds__(kThreads, DENSE ? 8 : 6)
+k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, const int32_t *__restrict__ vcol,
+                 uint32_t dir, PredView pv, uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
+                 unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ group_sums, int *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t b = blockIdx.x;
     const int64_t wrow0 = b * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
     int32_t v[kRounds];
+    // the start column: from its own dense array when the previous expansion wrote
+    // one (4 B per row), else from the row-major history (every sector of the rows)
+    const int32_t *vb = vcol != nullptr ? vcol : hist + scol;
+    const int64_t vs = vcol != nullptr ? 1 : C;
 #pragma unroll
     for (int rd = 0; rd < kRounds; ++rd) {
         const int64_t r = wrow0 + rd * 32 + lane;
-        v[rd] = r < R ? __ldg(hist + r * C + scol) : -1;
+        v[rd] = r < R ? __ldg(vb + r * vs) : -1;
     }
     unsigned long long my_sum = 0;
     unsigned int my_nz = 0;
@@ -158,19 +161,19 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
                     a[rd] = __ldg(rp + x);
                     e[rd] = __ldg(rp + x + 1);
                 }
-            } else if (vid == 0) {   // index key: the hash table
-                e[rd] = probe_seg(pv.buckets, pv.nmain, pv.nover, seg_key(0u, dir), &a[rd], err);
-                e[rd] += a[rd];
+            } else if (vid == 0) {
+                if constexpr (FUNC) {
+                    atomicOr(err, 8);   // an index key: the op reruns unspecialised
+                } else {            // index key: the hash table
+                    e[rd] = probe_seg(pv.buckets, pv.nmain, pv.nover, seg_key(0u, dir), &a[rd], err);
+                    e[rd] += a[rd];
+                }
             }
         }
         if constexpr (FUNC) {
             if (nba == nullptr) {
 #pragma unroll
                 for (int rd = 0; rd < kRounds; ++rd) g[rd] = e[rd] != a[rd] ? __ldg(pv.edges + a[rd]) : -1;
-            } else {
-#pragma unroll
-                for (int rd = 0; rd < kRounds; ++rd)
-                    if (v[rd] == 0 && e[rd] != a[rd]) g[rd] = __ldg(pv.edges + a[rd]);
             }
         }
 #pragma unroll
@@ -213,13 +216,13 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
     block_sum2(my_sum, my_nz);
     if (threadIdx.x == 0) {
         blk_sum[b] = my_sum;
+        // group sums spread the atomics over many addresses (256 blocks each);
+        // the op total comes from the plan kernel, so no address takes one per block
         if (my_sum) {
-            atomicAdd(totals, my_sum);
-            unsigned long long *ts = tile_sums + 2 * (b >> kPlanTileShift);
-            atomicAdd(ts, my_sum);
-            atomicAdd(ts + 1, slices_of(my_sum));
+            unsigned long long *gs = group_sums + 2 * (b >> kGroupShift);
+            atomicAdd(gs, my_sum);
+            atomicAdd(gs + 1, slices_of(my_sum));
         }
-        if (my_nz) atomicAdd(totals + 1, (unsigned long long)my_nz);
         if (my_sum >> 31) atomicOr(err, 2);
     }
 }
@@ -260,27 +263,40 @@ __device__ __forceinline__ void plan_scan2(unsigned long long &a, unsigned long 
 }
 
 // bp[b] = output rows of blocks before b, sp[b] = slices of blocks before b
-// (bp[nblk], sp[nblk] = the totals); totals[2] = slices.  CTA c scans blocks
-// [c 8192, (c + 1) 8192), thread t 8 consecutive ones; the tiles before c
-// contribute their sums from the count kernel, so no CTA waits on another.
+// (bp[nblk], sp[nblk] = the totals); totals[0] = output rows, totals[2] =
+// slices.  CTA c scans blocks [c 8192, (c + 1) 8192), thread t 8 consecutive
+// ones; the groups before the tile contribute their sums from the count
+// kernel, so no CTA waits on another.
 __global__ void __launch_bounds__(kPlanThreads)
 k2u_plan_kernel(const unsigned long long *__restrict__ blk_sum, int64_t nblk,
-                const unsigned long long *__restrict__ tile_sums, unsigned long long *__restrict__ bp,
+                const unsigned long long *__restrict__ group_sums, unsigned long long *__restrict__ bp,
                 unsigned long long *__restrict__ sp, unsigned long long *__restrict__ totals) {
     __shared__ unsigned long long s_po, s_ps;
+    __shared__ unsigned long long s_ga[kPlanThreads / 32], s_gb[kPlanThreads / 32];
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    const int c = blockIdx.x;
-    if (wid == 0) {
+    const int64_t c = blockIdx.x;
+    {
+        // the groups of all earlier tiles, summed by the whole CTA
+        const int64_t ng = c << (kPlanTileShift - kGroupShift);
         unsigned long long po = 0, ps = 0;
-        for (int k = lane; k < c; k += 32) {
-            po += tile_sums[2 * k];
-            ps += tile_sums[2 * k + 1];
+        for (int64_t k = t; k < ng; k += kPlanThreads) {
+            po += group_sums[2 * k];
+            ps += group_sums[2 * k + 1];
         }
         po = warp_sum(po);
         ps = warp_sum(ps);
         if (lane == 0) {
-            s_po = po;
-            s_ps = ps;
+            s_ga[wid] = po;
+            s_gb[wid] = ps;
+        }
+        __syncthreads();
+        if (wid == 0) {
+            po = warp_sum(s_ga[lane]);
+            ps = warp_sum(s_gb[lane]);
+            if (lane == 0) {
+                s_po = po;
+                s_ps = ps;
+            }
         }
     }
     const int64_t b0 = ((int64_t)c << kPlanTileShift) + (int64_t)t * kPlanPer;
@@ -316,9 +332,10 @@ k2u_plan_kernel(const unsigned long long *__restrict__ blk_sum, int64_t nblk,
         so += T[q];
         ss += slices_of(T[q]);
     }
-    if (c == (int)gridDim.x - 1 && t == 0) {
+    if (c == (int64_t)gridDim.x - 1 && t == 0) {
         bp[nblk] = s_po + to;
         sp[nblk] = s_ps + tsl;
+        totals[0] = s_po + to;
         totals[2] = s_ps + tsl;
     }
 }
@@ -346,7 +363,8 @@ __device__ __forceinline__ int row_of(const uint32_t *pos, int n, uint32_t j) {
 template <int W>
 __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint32_t span, const uint32_t *pos,
                                                 const uint32_t *eoff, int n, const int32_t *__restrict__ rows,
-                                                const int32_t *__restrict__ edges, int32_t *__restrict__ obase) {
+                                                const int32_t *__restrict__ edges, int32_t *__restrict__ obase,
+                                                int32_t *__restrict__ cbase, int ccol) {
     constexpr int C = W - 1;
     int i = row_of(pos, n, u >= lead ? u - lead : 0u);
     uint32_t nxt = pos[i + 1];
@@ -361,6 +379,8 @@ __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint3
 #pragma unroll
             for (int c = 0; c < C; ++c) v[q * W + c] = __ldg(src + c);
             v[q * W + C] = __ldg(edges + (eoff[i] + (j - pos[i])));
+            // the next step's start column: the row's column (again from L1) or the neighbour
+            if (cbase != nullptr) cbase[uq] = ccol < C ? __ldg(src + ccol) : v[q * W + C];
         } else {
 #pragma unroll
             for (int c = 0; c < W; ++c) v[q * W + c] = 0;
@@ -393,14 +413,15 @@ __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint3
 // CTAs per SM the register budget is set for: the widest instantiations need
 // more registers to avoid spills
 template <int W>
-constexpr int expand_min_ctas() { return (W >= 2 && W <= 5) || W == 0 ? 8 : (W <= 7 ? 6 : 5); }
+constexpr int expand_min_ctas() { return (W >= 2 && W <= 4) || W == 0 ? 8 : (W <= 7 ? 6 : 4); }
 
 template <int W>
 __global__ void __launch_bounds__(kThreads, expand_min_ctas<W>())
 k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const int32_t *__restrict__ edges,
                   const uint32_t *__restrict__ deg, const uint32_t *__restrict__ off,
                   const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ bp,
-                  const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out) {
+                  const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out,
+                  int32_t *__restrict__ ocol, int ccol) {
     constexpr int kRPT = kRowsPerBlock / kThreads;
     static_assert(kRPT == 4, "4 input rows per thread");
     __shared__ uint32_t pos[kRowsPerBlock + 1];
@@ -474,8 +495,9 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
         const uint32_t u0 = slice * (uint32_t)kSliceRows;
         const uint32_t u1 = u0 >= span ? u0 : (span - u0 < (uint32_t)kSliceRows ? span : u0 + (uint32_t)kSliceRows);
         int32_t *obase = out + (P - lead) * W;
+        int32_t *cbase = ocol != nullptr ? ocol + (P - lead) : nullptr;
         for (uint32_t u = u0 + 4u * (uint32_t)t; u < u1; u += 4u * kThreads)
-            k2u_write_group<W>(u, lead, span, pos, eoff, n, hblk, edges, obase);
+            k2u_write_group<W>(u, lead, span, pos, eoff, n, hblk, edges, obase, cbase, ccol);
     } else {
         const int Wd = C + 1;
         int32_t *oblk = out + P * Wd;
@@ -487,6 +509,7 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
             const int32_t *src = hblk + (int64_t)i * C;
             for (int c = 0; c < C; ++c) dst[c] = __ldg(src + c);
             dst[C] = __ldg(edges + (eoff[i] + (j - pos[i])));
+            if (ocol != nullptr) ocol[P + j] = dst[ccol];
         }
     }
 }
@@ -504,7 +527,8 @@ template <int W>
 __global__ void __launch_bounds__(kThreads)
 k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_t *__restrict__ nbr,
                        const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ bp,
-                       const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out) {
+                       const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out,
+                       int32_t *__restrict__ ocol, int ccol) {
     constexpr int C = W - 1;
     constexpr int kPitch = W | 1;
     __shared__ int32_t rows[kRowsPerBlock * kPitch];
@@ -565,6 +589,26 @@ k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_
     // output words [P W, (P + T) W): int4 stores aligned to 16 B of out
     const unsigned long long P = bp[b];
     const uint32_t T = (uint32_t)blk_sum[b];
+    if (ocol != nullptr) {
+        // column ccol of the block's output rows, read back from the staged rows
+        const uint32_t cl = (uint32_t)(P & 3ull);
+        int32_t *cg = ocol + (P - cl);
+        for (uint32_t i = (uint32_t)t; 4u * i < cl + T; i += kThreads) {
+            int32_t cv[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t q = 4u * i + j - cl;
+                cv[j] = q < T ? rows[q * kPitch + ccol] : 0;
+            }
+            if (4u * i >= cl && 4u * i + 4u <= cl + T) {
+                reinterpret_cast<int4 *>(cg)[i] = make_int4(cv[0], cv[1], cv[2], cv[3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (4u * i + j - cl < T) cg[4u * i + j] = cv[j];
+            }
+        }
+    }
     const uint32_t lead = (uint32_t)((P * W) & 3ull), words = T * W;
     int32_t *g = out + (P * W - lead);
     for (uint32_t i = (uint32_t)t; 4u * i < lead + words; i += kThreads) {
@@ -713,13 +757,13 @@ static inline unsigned int nblocks_rows(int64_t R) {
     return (unsigned int)((R + kRowsPerBlock - 1) / kRowsPerBlock);
 }
 
-void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg,
-                      uint32_t *off, unsigned long long *blk_sum, unsigned long long *totals,
-                      unsigned long long *tile_sums, int *err, bool func, cudaStream_t st) {
+void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, const int32_t *vcol, uint32_t dir, PredView pv,
+                      uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums,
+                      int *err, bool func, cudaStream_t st) {
     const bool dense = (dir ? pv.rp[1] : pv.rp[0]) != nullptr;
     const unsigned int g = nblocks_rows(R);
 #define WK_COUNT(F, D) \
-    k2u_count_kernel<F, D><<<g, kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, totals, tile_sums, err)
+    k2u_count_kernel<F, D><<<g, kThreads, 0, st>>>(hist, R, C, scol, vcol, dir, pv, deg, off, blk_sum, group_sums, err)
     if (func && dense) WK_COUNT(true, true);
     else if (func) WK_COUNT(true, false);
     else if (dense) WK_COUNT(false, true);
@@ -729,12 +773,13 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t 
 
 void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
                             const unsigned long long *blk_sum, const unsigned long long *bp,
-                            const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st) {
+                            const unsigned long long *sp, unsigned long long slices, int32_t *out, int32_t *ocol,
+                            int ccol, cudaStream_t st) {
     if (slices == 0ull) return;
     const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
     const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND_F(WC) \
-    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, bp, sp, nblk, out)
+    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, bp, sp, nblk, out, ocol, ccol)
     switch (C + 1) {
         case 2: WK_EXPAND_F(2); break;
         case 3: WK_EXPAND_F(3); break;
@@ -747,20 +792,21 @@ void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t
 #undef WK_EXPAND_F
 }
 
-void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, const unsigned long long *tile_sums,
+void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, const unsigned long long *group_sums,
                      unsigned long long *bp, unsigned long long *sp, unsigned long long *totals, cudaStream_t st) {
     const unsigned int g = (unsigned int)((nblk + (1 << kPlanTileShift) - 1) >> kPlanTileShift);
-    k2u_plan_kernel<<<g, kPlanThreads, 0, st>>>(blk_sum, nblk, tile_sums, bp, sp, totals);
+    k2u_plan_kernel<<<g, kPlanThreads, 0, st>>>(blk_sum, nblk, group_sums, bp, sp, totals);
 }
 
 void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edges, const uint32_t *deg,
                        const uint32_t *off, const unsigned long long *blk_sum, const unsigned long long *bp,
-                       const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st) {
+                       const unsigned long long *sp, unsigned long long slices, int32_t *out, int32_t *ocol,
+                       int ccol, cudaStream_t st) {
     if (slices == 0ull) return;
     const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
     const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND(WC) \
-    k2u_expand_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, C, edges, deg, off, blk_sum, bp, sp, nblk, out)
+    k2u_expand_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, C, edges, deg, off, blk_sum, bp, sp, nblk, out, ocol, ccol)
     switch (C + 1) {
         case 2: WK_EXPAND(2); break;
         case 3: WK_EXPAND(3); break;

@@ -32,11 +32,11 @@ namespace {
 
 constexpr int64_t kMaxRows = 1 << 18;                 // input rows per call
 constexpr int64_t kMaxBlocks = kMaxRows / wk::dev::kRowsPerBlock;
-static_assert(kMaxBlocks <= (1 << wk::dev::kPlanTileShift), "one k2u plan tile per call");
+static_assert(kMaxBlocks <= (1 << wk::dev::kGroupShift), "one k2u group sum per call");
 
 constexpr size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // byte layout of the scratch array
-constexpr size_t kOffFlags = 0;       // err (int), totals (3 x u64), the plan tile's sums (2 x u64)
+constexpr size_t kOffFlags = 0;       // err (int), totals (3 x u64), the block group's sums (2 x u64)
 constexpr size_t kOffDeg = al(kOffFlags + 64);
 constexpr size_t kOffOff = al(kOffDeg + 4 * kMaxRows);
 constexpr size_t kOffBlkSum = al(kOffOff + 4 * kMaxRows);
@@ -106,8 +106,8 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     const int scol = (int)(-start - 1);
     cudaStream_t s = ctx->stream;
     if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 48, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
-    // kMaxRows input rows are one plan tile: its two sums follow the totals
-    dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, tot, tot + 3, err, false,
+    // kMaxRows input rows are one group: its two sums follow the totals
+    dev::launch_k2u_count(hist, rows, cols, scol, nullptr, (uint32_t)direction, pv, deg, off, blk_sum, tot + 3, err, false,
                           s);
     dev::launch_k2u_plan(blk_sum, nblk, tot + 3, bp, sp, tot, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: count launch");
@@ -127,7 +127,7 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
                          "known_to_unknown_noalloc: output needs %lld int32 elements, capacity is %lld "
                          "(*out_rows holds the row count)",
                          (long long)(R_out * (cols + 1)), (long long)out_capacity);
-    dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, bp, sp, ctx->h_scal[3], out, s);
+    dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, bp, sp, ctx->h_scal[3], out, nullptr, 0, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: expand launch");
     ctx->launches += 1;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "noalloc: sync");

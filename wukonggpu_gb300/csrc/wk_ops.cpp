@@ -139,10 +139,9 @@ int wk::reserve_op_scratch(wk_ctx *ctx, int64_t rows) {
 
 namespace {
 
-// zero the op totals (dscal[1..3]) and `tiles` k2u plan tile sums (from
-// dscal[8]) before a first pass accumulates into them
-int clear_totals(wk_ctx *ctx, int64_t tiles = 0) {
-    cudaError_t e = cudaMemsetAsync(ctx->dscal.as<unsigned long long>() + 1, 0, 56 + 16 * (size_t)tiles, ctx->stream);
+// zero the op totals (dscal[1..3]) before a first pass accumulates into them
+int clear_totals(wk_ctx *ctx) {
+    cudaError_t e = cudaMemsetAsync(ctx->dscal.as<unsigned long long>() + 1, 0, 24, ctx->stream);
     return e == cudaSuccess ? WK_OK : cuda_fail(e, "clear totals");
 }
 
@@ -150,6 +149,16 @@ int clear_totals(wk_ctx *ctx, int64_t tiles = 0) {
 int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     const int C = h->col_num;
     const int64_t R = h->size / C;
+    // the start column as its own array, when the previous step of this query
+    // wrote it; the state is cleared before anything else, so an early return
+    // cannot leave it pointing at a table this op replaces
+    const int32_t *vcol = (ctx->col_for != nullptr && ctx->col_for == h->data && ctx->col_idx == scol)
+                              ? ctx->colbuf[ctx->col_buf].as<int32_t>()
+                              : nullptr;
+    const int ccol = ctx->col_want;   // the column of this step's output the next step starts from
+    const int cbuf = vcol ? 1 - ctx->col_buf : 0;
+    ctx->col_for = nullptr;
+    ctx->col_want = -1;
     OpClock clk(ctx);
     ctx->last.kind = KIND_K2U;
     ctx->last.rows_in = R;
@@ -167,27 +176,28 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         return WK_OK;
     }
     const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
-    const int64_t tiles = (nblk + (1 << dev::kPlanTileShift) - 1) >> dev::kPlanTileShift;
-    if (tiles > dev::kMaxPlanTiles)
-        return set_error(WK_EINVAL, "k2u: %lld input rows exceed one op's maximum of %lld", (long long)R,
-                         (long long)dev::kMaxPlanTiles << dev::kPlanTileShift << 10);
+    const int64_t groups = (nblk + (1 << dev::kGroupShift) - 1) >> dev::kGroupShift;
     if ((st = ctx->deg.reserve((size_t)R * 4)) || (st = ctx->off.reserve((size_t)R * 4)) ||
-        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16)))
+        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) ||
+        (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16 + (size_t)groups * 16)))
         return st;
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
-    unsigned long long *tile_sums = ctx->dscal.as<unsigned long long>() + 8;
     int *err = ctx->dscal.as<int>();
-    // block output prefixes and slice prefixes share the look-back scratch
+    // block output prefixes, slice prefixes and the group sums share the look-back scratch
     unsigned long long *bp = ctx->lb_flags.as<unsigned long long>(), *sp = bp + (nblk + 1);
+    unsigned long long *group_sums = sp + (nblk + 1);
     // a functional direction (at most one neighbour per vertex) expands as a
     // compaction; if a row hits an index list (vertex 0) the op reruns unspecialised
     bool func = pv.func[dir] != 0u && C + 1 <= 8;
     int errf = 0;
     for (;;) {
-        if ((st = clear_totals(ctx, tiles)) || (st = clk.begin())) return st;
-        dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
-                              ctx->blk_sum.as<unsigned long long>(), tot, tile_sums, err, func, ctx->stream);
-        dev::launch_k2u_plan(ctx->blk_sum.as<unsigned long long>(), nblk, tile_sums, bp, sp, tot, ctx->stream);
+        if ((st = clear_totals(ctx))) return st;
+        cudaError_t eg = cudaMemsetAsync(group_sums, 0, (size_t)groups * 16, ctx->stream);
+        if (eg != cudaSuccess) return cuda_fail(eg, "k2u: clear group sums");
+        if ((st = clk.begin())) return st;
+        dev::launch_k2u_count(h->data, R, C, scol, vcol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
+                              ctx->blk_sum.as<unsigned long long>(), group_sums, err, func, ctx->stream);
+        dev::launch_k2u_plan(ctx->blk_sum.as<unsigned long long>(), nblk, group_sums, bp, sp, tot, ctx->stream);
         ++ctx->launches;   // the plan kernel, timed with the count
         ++ctx->last.kernels;
         if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;
@@ -211,14 +221,24 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         if ((st = ob.reserve(16))) return st;
     } else {
         if ((st = ob.reserve((size_t)R_out * (C + 1) * 4))) return st;
+        int32_t *ocol = nullptr;
+        if (ccol >= 0 && ccol <= C) {
+            if ((st = ctx->colbuf[cbuf].reserve((size_t)R_out * 4))) return st;
+            ocol = ctx->colbuf[cbuf].as<int32_t>();
+        }
         if ((st = clk.begin())) return st;
         if (func)
             dev::launch_k2u_expand_func(h->data, R, C, ctx->deg.as<int32_t>(), ctx->blk_sum.as<unsigned long long>(),
-                                        bp, sp, ctx->h_scal[3], ob.as<int32_t>(), ctx->stream);
+                                        bp, sp, ctx->h_scal[3], ob.as<int32_t>(), ocol, ccol, ctx->stream);
         else
             dev::launch_k2u_expand(h->data, R, C, pv.edges, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
                                    ctx->blk_sum.as<unsigned long long>(), bp, sp, ctx->h_scal[3], ob.as<int32_t>(),
-                                   ctx->stream);
+                                   ocol, ccol, ctx->stream);
+        if (ocol) {
+            ctx->col_for = ob.as<int32_t>();
+            ctx->col_idx = ccol;
+            ctx->col_buf = cbuf;
+        }
         if ((st = launch_check("k2u expand")) || (st = clk.end(true))) return st;
         if (ctx->timing) {
             cudaError_t e = cudaStreamSynchronize(ctx->stream);
@@ -236,6 +256,8 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
 // two-pass k2k / k2c (probe + membership -> filtered copy); the output is
 // sized by the input, so the host reads the totals only at the end
 int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const, uint32_t pid, uint32_t dir) {
+    ctx->col_for = nullptr;   // this op writes a new table and no column array
+    ctx->col_want = -1;
     const int C = h->col_num;
     const int64_t R = h->size / C;
     OpClock clk(ctx);
@@ -284,6 +306,8 @@ int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const,
 
 // one adjacency list -> one-column table (index or constant start)
 int op_list(wk_ctx *ctx, wk_history *h, uint64_t vid, uint32_t pid, uint32_t dir, int kind) {
+    ctx->col_for = nullptr;   // this op writes a new table and no column array
+    ctx->col_want = -1;
     OpClock clk(ctx);
     ctx->last.kind = kind;
     ctx->last.rows_in = 1;
@@ -393,10 +417,23 @@ extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history
     if (ctx->device < 0) return set_error(WK_EDEVICE, "wk_execute: host-only context");
     wk_history_init(h);
     ctx->protect.clear();
+    // column arrays live only inside this call, whichever way it returns
+    struct ColGuard {
+        wk_ctx *c;
+        explicit ColGuard(wk_ctx *x) : c(x) { c->col_for = nullptr; c->col_want = -1; }
+        ~ColGuard() { c->col_for = nullptr; c->col_want = -1; }
+    } col_guard(ctx);
     DeviceStore &ds = *ctx->store;
     int st = WK_OK;
     for (int i = 0; i < n && st == WK_OK; ++i) {
         const int64_t start = cmd[i * 4], pid = cmd[i * 4 + 1], d = cmd[i * 4 + 2], end = cmd[i * 4 + 3];
+        // a k2u step followed by a k2u step: write the column the next one starts from
+        ctx->col_want = -1;
+        if (i + 1 < n && start < 0 && end < 0) {
+            const int64_t ns = cmd[(i + 1) * 4], ne = cmd[(i + 1) * 4 + 3];
+            const int64_t out_cols = -end;   // this step binds column -end - 1
+            if (ns < 0 && -ns <= out_cols && ne < 0 && -ne == out_cols + 1) ctx->col_want = (int)(-ns - 1);
+        }
         // the segment of the next pattern is paged in on the side stream
         if (ds.pool && ctx->cfg.enable_prefetch && i + 1 < n) {
             const int64_t np = cmd[(i + 1) * 4 + 1];

@@ -74,7 +74,7 @@ struct wk_ctx {
     // scratch of the two-pass ops
     wk::DevBuf deg, off, mask, blk_sum, blk_nz;
     wk::DevBuf lb_flags;             // per-block look-back prefixes of the second pass
-    wk::DevBuf dscal;                // [0] error flags, [8..32) totals, [64..) k2u plan tile sums
+    wk::DevBuf dscal;                // [0] error flags, [8..32) totals
     unsigned long long *h_scal = nullptr;   // pinned mirror of the totals
 
     // timing
@@ -89,6 +89,15 @@ struct wk_ctx {
 
     // query-level state (segment cache protection / prefetch)
     std::vector<int> protect;
+    // Within one wk_execute, a k2u step also writes the column the next step
+    // starts from as a dense int32 array (colbuf), and that step's count reads
+    // it instead of the row-major history.  col_for is the history data the
+    // array describes (null: none); every op clears it before writing a new
+    // history, so an array is never read for any other table.
+    wk::DevBuf colbuf[2];
+    int col_want = -1;                   // column of the next output to write (-1: none)
+    const int32_t *col_for = nullptr;
+    int col_idx = -1, col_buf = 0;
 
     ~wk_ctx();
 };
