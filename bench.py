@@ -13,7 +13,7 @@ executed once.
           the library's stream around each query, max over ranks).
   e2e   : queries/s through the public C ABI with host buffers: each query
           goes in from the host and its final table comes back to pinned host
-          memory inside the timed region (two contexts sharing the store, one
+          memory inside the timed region (four contexts sharing the store, one
           host thread each, so copies overlap the next query's kernels).
   roofline : the k2u op (count + expand kernels) -- the expansion path that
           dominates the step -- algorithmic bytes per op / its summed kernel
@@ -70,7 +70,7 @@ def parse():
     ap.add_argument("--one-query", type=int, default=-1,
                     help="run query N of the mix once, op by op, print each op's stats and exit "
                          "(a fixed launch sequence for ncu captures)")
-    ap.add_argument("--e2e-contexts", type=int, default=2,
+    ap.add_argument("--e2e-contexts", type=int, default=4,
                     help="contexts (one host thread each) that share the store in the end-to-end pass")
     return ap.parse_args()
 
@@ -392,10 +392,10 @@ def run_gb300(args, dist):
                 "expand_share_of_k2u_time": write_ms / k2u_ms if k2u_ms else None}
 
     # ---- end to end through the C ABI with host buffers: the query goes in from
-    # the host and its final table comes back to pinned host memory.  Two
+    # the host and its final table comes back to pinned host memory.  Four
     # contexts (--e2e-contexts) share the store and run alternate queries from
-    # one host thread each, so one query's device->host copy overlaps the next
-    # query's kernels.
+    # one host thread each, so device->host copies overlap other queries'
+    # kernels and the copy link stays busy.
     maxrows = 0
     for _, q in queries:
         req, rows = rc.execute(q, download=False)

@@ -232,3 +232,29 @@ def test_functional_direction_reaching_an_index_list(lib_built):
             got = rc.download(req)
             exp, _ = orc.step(h, False, -1, 3, d, -3)
             assert got.shape == exp.shape and np.array_equal(got, exp), (with_zero, d)
+
+
+def test_sparse_functional_direction(lib_built):
+    """A functional predicate whose subjects are sparse in the id range: its OUT
+    direction stays hashed (with a presence bitmap) and still takes the one-pass
+    functional k2u; rows, order and misses equal the oracle's."""
+    rng = np.random.default_rng(17)
+    V = W.VID_BASE
+    n = 50_000
+    subj = V + np.arange(0, n, 40)                            # 1 in 40 ids: hashed, not dense
+    s = np.concatenate([subj, V + rng.integers(0, n, 30_000), V + np.arange(n)]).astype(np.int32)
+    o = np.concatenate([V + rng.integers(0, n, len(subj)), V + rng.integers(0, n, 30_000),
+                        np.full(n, 3)]).astype(np.int32)
+    p = np.concatenate([np.full(len(subj), 2), np.full(30_000, 4), np.ones(n)]).astype(np.int32)
+    rc = W.RCache(device=0)
+    rc.build_store(s, p, o, 4)
+    orc = oracle.Oracle(s, p, o, 4)
+    for C in (1, 3, 7):
+        h = (V + rng.integers(0, n, size=(20_011, C))).astype(np.int32)
+        h[::7, 0] = subj[rng.integers(0, len(subj), size=len(h[::7]))]   # many hits among misses
+        req = W.Request([])
+        rc.upload_history(req, h)
+        rc.known_to_unknown(req, -1, W.OUT, 2)
+        got = rc.download(req)
+        exp, _ = orc.step(h, False, -1, 2, W.OUT, -C - 1)
+        assert got.shape == exp.shape and np.array_equal(got, exp), C
