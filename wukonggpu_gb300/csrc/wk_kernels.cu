@@ -110,120 +110,136 @@ __device__ __forceinline__ unsigned long long slices_of(unsigned long long t) {
 constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
 
 // blk_sum[b] = the block's output rows, added into its group's sums.  Err bit
-// 1 when a block's output count reaches 2^31
-// (the expansion keeps block-local positions in 32 bits).  FUNC (a direction
-// whose lists hold at most one vertex): deg receives the neighbour itself as
-// an int32, or -1 for no match, and off is unused.  DENSE (the direction is
-// an offsets array): the rounds' lookups are issued phase by phase -- every
-// round's offsets, then every round's neighbour -- so a warp has its four
-// rounds' loads in flight at once instead of one dependent chain per round,
-// and a lane looks up its own key (no shuffles).
+// 1 when a block's output count reaches 2^31 (the expansion keeps block-local
+// positions in 32 bits).  FUNC (a direction whose lists hold at most one
+// vertex): deg receives the neighbour itself as an int32, or -1 for no match,
+// and off is unused.  DENSE (the direction is an offsets array): a CTA takes
+// two blocks, a warp issues the lookups of all its eight rounds phase by
+// phase -- every round's start vertex, then every round's offsets or
+// neighbour -- and a lane looks up its own key (no shuffles), so each warp
+// keeps many loads in flight and a CTA's fixed costs (reduction, exit) are
+// shared by 2048 rows.
+template <bool DENSE>
+__host__ __device__ constexpr int count_blocks_per_cta() { return DENSE ? 2 : 1; }
+
 template <bool FUNC, bool DENSE>
-__global__ void __launch_bounds__(kThreads, DENSE ? 8 : 6)
+__global__ void __launch_bounds__(kThreads, (DENSE && FUNC) ? 8 : 6)
 k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, const int32_t *__restrict__ vcol,
                  uint32_t dir, PredView pv, uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
                  unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ group_sums, int *err) {
+    constexpr int BPC = count_blocks_per_cta<DENSE>();
+    constexpr int NR = kRounds * BPC;   // rounds of 32 rows per warp
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t b = blockIdx.x;
-    const int64_t wrow0 = b * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
-    int32_t v[kRounds];
+    const int64_t b0 = (int64_t)blockIdx.x * BPC;
+    const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
+    // round rd: block b0 + rd / kRounds, the warp's rows 32 (rd % kRounds) + lane
+    auto row_at = [&](int rd) -> int64_t {
+        return (b0 + rd / kRounds) * kRowsPerBlock + (int64_t)warp * (kRounds * 32) + (rd % kRounds) * 32 + lane;
+    };
+    int32_t v[NR];
     // the start column: from its own dense array when the previous expansion wrote
     // one (4 B per row), else from the row-major history (every sector of the rows)
     const int32_t *vb = vcol != nullptr ? vcol : hist + scol;
     const int64_t vs = vcol != nullptr ? 1 : C;
 #pragma unroll
-    for (int rd = 0; rd < kRounds; ++rd) {
-        const int64_t r = wrow0 + rd * 32 + lane;
+    for (int rd = 0; rd < NR; ++rd) {
+        const int64_t r = row_at(rd);
         v[rd] = r < R ? __ldg(vb + r * vs) : -1;
     }
-    unsigned long long my_sum = 0;
-    unsigned int my_nz = 0;
-    if constexpr (DENSE) {
-        // no run dedup here: equal keys of a warp read the same sector, which the
-        // load unit merges, so shuffles would only add work
-        const uint32_t *rp = dir ? pv.rp[1] : pv.rp[0];
-        const uint32_t vmin = dir ? pv.vmin[1] : pv.vmin[0], dn = dir ? pv.dn[1] : pv.dn[0];
-        const int32_t *nba = dir ? pv.nb[1] : pv.nb[0];
-        uint32_t a[kRounds], e[kRounds];
-        int32_t g[kRounds];
+    unsigned long long my_sum[BPC];
+    unsigned int my_nz[BPC];
 #pragma unroll
-        for (int rd = 0; rd < kRounds; ++rd) {
-            const int32_t vid = v[rd];
-            a[rd] = e[rd] = 0u;
-            g[rd] = -1;
-            const uint32_t x = (uint32_t)vid - vmin;   // wraps above dn below vmin
-            if (vid > 0 && x < dn) {
-                if (FUNC && nba != nullptr) {
-                    // the neighbour itself: one 4 B read, no offsets and no gather
-                    g[rd] = __ldg(nba + x);
-                    e[rd] = g[rd] >= 0 ? 1u : 0u;
-                } else {
+    for (int j = 0; j < BPC; ++j) {
+        my_sum[j] = 0ull;
+        my_nz[j] = 0u;
+    }
+    if constexpr (DENSE) {
+        const uint32_t vmin = dir ? pv.vmin[1] : pv.vmin[0], dn = dir ? pv.dn[1] : pv.dn[0];
+        if constexpr (FUNC) {
+            // a dense functional direction keeps the neighbour per id: one 4 B read
+            const int32_t *nba = dir ? pv.nb[1] : pv.nb[0];
+            int32_t g[NR];
+#pragma unroll
+            for (int rd = 0; rd < NR; ++rd) {
+                const int32_t vid = v[rd];
+                const uint32_t x = (uint32_t)vid - vmin;   // wraps above dn below vmin
+                g[rd] = (vid > 0 && x < dn) ? __ldg(nba + x) : -1;
+                if (vid == 0) atomicOr(err, 8);   // an index key: the op reruns unspecialised
+            }
+#pragma unroll
+            for (int rd = 0; rd < NR; ++rd) {
+                const int64_t r = row_at(rd);
+                if (r < R) {
+                    reinterpret_cast<int32_t *>(deg)[r] = g[rd];
+                    my_sum[rd / kRounds] += g[rd] >= 0 ? 1ull : 0ull;
+                    my_nz[rd / kRounds] += g[rd] >= 0 ? 1u : 0u;
+                }
+            }
+        } else {
+            const uint32_t *rp = dir ? pv.rp[1] : pv.rp[0];
+            uint32_t a[NR], e[NR];
+#pragma unroll
+            for (int rd = 0; rd < NR; ++rd) {
+                const int32_t vid = v[rd];
+                a[rd] = e[rd] = 0u;
+                const uint32_t x = (uint32_t)vid - vmin;   // wraps above dn below vmin
+                if (vid > 0 && x < dn) {
                     a[rd] = __ldg(rp + x);
                     e[rd] = __ldg(rp + x + 1);
-                }
-            } else if (vid == 0) {
-                if constexpr (FUNC) {
-                    atomicOr(err, 8);   // an index key: the op reruns unspecialised
-                } else {            // index key: the hash table
+                } else if (vid == 0) {   // index key: the hash table
                     e[rd] = probe_seg(pv.buckets, pv.nmain, pv.nover, seg_key(0u, dir), &a[rd], err);
                     e[rd] += a[rd];
                 }
             }
-        }
-        if constexpr (FUNC) {
-            if (nba == nullptr) {
 #pragma unroll
-                for (int rd = 0; rd < kRounds; ++rd) g[rd] = e[rd] != a[rd] ? __ldg(pv.edges + a[rd]) : -1;
-            }
-        }
-#pragma unroll
-        for (int rd = 0; rd < kRounds; ++rd) {
-            const int64_t r = wrow0 + rd * 32 + lane;
-            const uint32_t d = e[rd] - a[rd];
-            if (r < R) {
-                if constexpr (FUNC) {
-                    reinterpret_cast<int32_t *>(deg)[r] = g[rd];
-                    if (d > 1u) atomicOr(err, 8);   // an index list: the op reruns unspecialised
-                } else {
+            for (int rd = 0; rd < NR; ++rd) {
+                const int64_t r = row_at(rd);
+                const uint32_t d = e[rd] - a[rd];
+                if (r < R) {
                     deg[r] = d;
                     off[r] = a[rd];
+                    my_sum[rd / kRounds] += d;
+                    my_nz[rd / kRounds] += d > 0u;
                 }
-                my_sum += d;
-                my_nz += d > 0u;
             }
         }
     } else {
+        // hashed: runs of equal keys probed once (probe_warp), a round at a time
 #pragma unroll
-    for (int rd = 0; rd < kRounds; ++rd) {
-        const int64_t row0 = wrow0 + rd * 32;
-        if (row0 >= R) break;   // warp-uniform
-        const int64_t r = row0 + lane;
-        uint32_t o, d;
-        probe_warp(pv, v[rd], dir, o, d, err);
-        if (r < R) {
-            if constexpr (FUNC) {
-                reinterpret_cast<int32_t *>(deg)[r] = d ? __ldg(pv.edges + o) : -1;
-                if (d > 1u) atomicOr(err, 8);   // an index list: the op reruns unspecialised
-            } else {
-                deg[r] = d;
-                off[r] = o;
+        for (int rd = 0; rd < NR; ++rd) {
+            const int64_t r = row_at(rd);
+            if (r - lane >= R) break;   // warp-uniform
+            uint32_t o, d;
+            probe_warp(pv, v[rd], dir, o, d, err);
+            if (r < R) {
+                if constexpr (FUNC) {
+                    reinterpret_cast<int32_t *>(deg)[r] = d ? __ldg(pv.edges + o) : -1;
+                    if (d > 1u) atomicOr(err, 8);   // an index list: the op reruns unspecialised
+                } else {
+                    deg[r] = d;
+                    off[r] = o;
+                }
+                my_sum[rd / kRounds] += d;
+                my_nz[rd / kRounds] += d > 0u;
             }
-            my_sum += d;
-            my_nz += d > 0u;
         }
     }
-    }
-    block_sum2(my_sum, my_nz);
-    if (threadIdx.x == 0) {
-        blk_sum[b] = my_sum;
-        // group sums spread the atomics over many addresses (256 blocks each);
-        // the op total comes from the plan kernel, so no address takes one per block
-        if (my_sum) {
-            unsigned long long *gs = group_sums + 2 * (b >> kGroupShift);
-            atomicAdd(gs, my_sum);
-            atomicAdd(gs + 1, slices_of(my_sum));
+#pragma unroll
+    for (int j = 0; j < BPC; ++j) {
+        const int64_t b = b0 + j;
+        block_sum2(my_sum[j], my_nz[j]);
+        if (threadIdx.x == 0 && b < nblk) {
+            blk_sum[b] = my_sum[j];
+            // group sums spread the atomics over many addresses (256 blocks each);
+            // the op total comes from the plan kernel, so no address takes one per block
+            if (my_sum[j]) {
+                unsigned long long *gs = group_sums + 2 * (b >> kGroupShift);
+                atomicAdd(gs, my_sum[j]);
+                atomicAdd(gs + 1, slices_of(my_sum[j]));
+            }
+            if (my_sum[j] >> 31) atomicOr(err, 2);
         }
-        if (my_sum >> 31) atomicOr(err, 2);
+        __syncthreads();   // block_sum2's shared partial sums are reused
     }
 }
 
@@ -761,9 +777,10 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, const int
                       uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums,
                       int *err, bool func, cudaStream_t st) {
     const bool dense = (dir ? pv.rp[1] : pv.rp[0]) != nullptr;
-    const unsigned int g = nblocks_rows(R);
-#define WK_COUNT(F, D) \
-    k2u_count_kernel<F, D><<<g, kThreads, 0, st>>>(hist, R, C, scol, vcol, dir, pv, deg, off, blk_sum, group_sums, err)
+    const unsigned int nb = nblocks_rows(R);
+#define WK_COUNT(F, D)                                                                                             \
+    k2u_count_kernel<F, D><<<(nb + count_blocks_per_cta<D>() - 1) / count_blocks_per_cta<D>(), kThreads, 0, st>>>( \
+        hist, R, C, scol, vcol, dir, pv, deg, off, blk_sum, group_sums, err)
     if (func && dense) WK_COUNT(true, true);
     else if (func) WK_COUNT(true, false);
     else if (dense) WK_COUNT(false, true);
