@@ -321,25 +321,13 @@ def run_gb300(args, dist):
     rc.sync()
 
     def step_with_ops(lat):
+        # the same wk_execute path as the headline, with per-kernel CUDA events,
+        # so each op's device time is recorded for the roofline
         for _, q in queries:
-            req = W.Request(q)
-            n = len(req.cmd_chains) // 4
             rc.timer_begin()
-            # execute pattern by pattern through the ops so each op's device time is recorded
-            for i in range(n):
-                st, pid, d, en = req.cmd_chains[4 * i:4 * i + 4]
-                if i == 0 and 1 < st < W.VID_BASE:
-                    rc.index_to_unknown(req, st, d)
-                elif st >= 0:
-                    rc.const_to_unknown(req, st, d, pid)
-                elif en < 0 and -en > req.col_num:
-                    rc.known_to_unknown(req, st, d, pid)
-                elif en < 0:
-                    rc.known_to_known(req, st, d, pid, en)
-                else:
-                    rc.known_to_const(req, st, d, pid, en)
-                op_log.append(rc.last_op_stats())
+            rc.execute(q, download=False)
             lat.append(rc.timer_end())
+            op_log.extend(rc.query_op_stats())
 
     # ---- headline: whole queries through wk_execute, device time from query-level events
     rc.enable_timing(False)
@@ -362,7 +350,7 @@ def run_gb300(args, dist):
     n_done = dist.reduce(float(args.steps * nq), "sum")
     value = n_done / (max_ms / 1000.0)
 
-    # ---- the same steps again, op by op with per-kernel CUDA events (for the roofline)
+    # ---- the same steps again with per-kernel CUDA events (for the roofline)
     rc.enable_timing(True)
     op_log = []
     lat_ops = []

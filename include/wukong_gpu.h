@@ -333,6 +333,10 @@ typedef struct {
 } wk_op_stats;
 int wk_enable_timing(wk_ctx *ctx, int enable);
 int wk_last_op_stats(wk_ctx *ctx, wk_op_stats *st);
+/* The per-op statistics of every op of the context's last wk_execute, in
+ * pattern order, recorded while timing is enabled: up to `cap` entries into
+ * `st`, their number in *n. */
+int wk_query_op_stats(wk_ctx *ctx, wk_op_stats *st, int32_t cap, int32_t *n);
 int64_t wk_kernel_launches(wk_ctx *ctx);   /* cumulative kernel launches */
 int wk_sync(wk_ctx *ctx);
 /* ------------------------------------------------------- the planner

@@ -258,3 +258,15 @@ def test_sparse_functional_direction(lib_built):
         got = rc.download(req)
         exp, _ = orc.step(h, False, -1, 2, W.OUT, -C - 1)
         assert got.shape == exp.shape and np.array_equal(got, exp), C
+
+
+def test_query_op_stats_cover_every_pattern(gpu_small, golden_small):
+    q = next(x for x in golden_small["queries"] if x["name"] == "type_chain")
+    gpu_small.enable_timing(True)
+    req, rows = gpu_small.execute(q["cmd_chains"])
+    stats = gpu_small.query_op_stats()
+    gpu_small.enable_timing(False)
+    assert len(stats) == len(q["cmd_chains"]) // 4
+    assert [s["rows_out"] for s in stats] == list(rows)
+    assert all(s["ms"] > 0 for s in stats if s["rows_out"] > 0)
+    assert stats[0]["kind"] == 3 and all(s["kind"] in (0, 1, 2) for s in stats[1:])

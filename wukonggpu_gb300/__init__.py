@@ -109,6 +109,7 @@ _SIGS = {
     "wk_execute": (C.c_int, [_P, _I64P, C.c_int32, C.POINTER(wk_history), _I64P]),
     "wk_enable_timing": (C.c_int, [_P, C.c_int]),
     "wk_last_op_stats": (C.c_int, [_P, C.POINTER(wk_op_stats)]),
+    "wk_query_op_stats": (C.c_int, [_P, C.POINTER(wk_op_stats), C.c_int32, C.POINTER(C.c_int32)]),
     "wk_kernel_launches": (C.c_int64, [_P]),
     "wk_sync": (C.c_int, [_P]),
     "wk_plan": (C.c_int, [_P, _I64P, C.c_int32, _I64P, C.POINTER(C.c_int32), C.POINTER(C.c_double),
@@ -431,6 +432,15 @@ class RCache:
         st = wk_op_stats()
         _check(load_library().wk_last_op_stats(self._h, C.byref(st)))
         return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def query_op_stats(self) -> list:
+        """Per-op statistics of every op of the last execute() (timing enabled)."""
+        lib = load_library()
+        n = C.c_int32()
+        _check(lib.wk_query_op_stats(self._h, None, 0, C.byref(n)))
+        arr = (wk_op_stats * max(n.value, 1))()
+        _check(lib.wk_query_op_stats(self._h, arr, n.value, C.byref(n)))
+        return [{f: getattr(arr[i], f) for f, _ in wk_op_stats._fields_} for i in range(n.value)]
 
     def kernel_launches(self) -> int:
         return load_library().wk_kernel_launches(self._h)

@@ -124,8 +124,7 @@ __host__ __device__ constexpr int count_blocks_per_cta() { return DENSE ? 2 : 1;
 
 template <bool FUNC, bool DENSE>
 __global__ void __launch_bounds__(kThreads, (DENSE && FUNC) ? 8 : 6)
-k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, const int32_t *__restrict__ vcol,
-                 uint32_t dir, PredView pv, uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
+k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
                  unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ group_sums, int *err) {
     constexpr int BPC = count_blocks_per_cta<DENSE>();
     constexpr int NR = kRounds * BPC;   // rounds of 32 rows per warp
@@ -137,14 +136,10 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, c
         return (b0 + rd / kRounds) * kRowsPerBlock + (int64_t)warp * (kRounds * 32) + (rd % kRounds) * 32 + lane;
     };
     int32_t v[NR];
-    // the start column: from its own dense array when the previous expansion wrote
-    // one (4 B per row), else from the row-major history (every sector of the rows)
-    const int32_t *vb = vcol != nullptr ? vcol : hist + scol;
-    const int64_t vs = vcol != nullptr ? 1 : C;
 #pragma unroll
     for (int rd = 0; rd < NR; ++rd) {
         const int64_t r = row_at(rd);
-        v[rd] = r < R ? __ldg(vb + r * vs) : -1;
+        v[rd] = r < R ? __ldg(hist + r * C + scol) : -1;
     }
     unsigned long long my_sum[BPC];
     unsigned int my_nz[BPC];
@@ -379,8 +374,7 @@ __device__ __forceinline__ int row_of(const uint32_t *pos, int n, uint32_t j) {
 template <int W>
 __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint32_t span, const uint32_t *pos,
                                                 const uint32_t *eoff, int n, const int32_t *__restrict__ rows,
-                                                const int32_t *__restrict__ edges, int32_t *__restrict__ obase,
-                                                int32_t *__restrict__ cbase, int ccol) {
+                                                const int32_t *__restrict__ edges, int32_t *__restrict__ obase) {
     constexpr int C = W - 1;
     int i = row_of(pos, n, u >= lead ? u - lead : 0u);
     uint32_t nxt = pos[i + 1];
@@ -395,8 +389,6 @@ __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint3
 #pragma unroll
             for (int c = 0; c < C; ++c) v[q * W + c] = __ldg(src + c);
             v[q * W + C] = __ldg(edges + (eoff[i] + (j - pos[i])));
-            // the next step's start column: the row's column (again from L1) or the neighbour
-            if (cbase != nullptr) cbase[uq] = ccol < C ? __ldg(src + ccol) : v[q * W + C];
         } else {
 #pragma unroll
             for (int c = 0; c < W; ++c) v[q * W + c] = 0;
@@ -436,8 +428,7 @@ __global__ void __launch_bounds__(kThreads, expand_min_ctas<W>())
 k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const int32_t *__restrict__ edges,
                   const uint32_t *__restrict__ deg, const uint32_t *__restrict__ off,
                   const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ bp,
-                  const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out,
-                  int32_t *__restrict__ ocol, int ccol) {
+                  const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out) {
     constexpr int kRPT = kRowsPerBlock / kThreads;
     static_assert(kRPT == 4, "4 input rows per thread");
     __shared__ uint32_t pos[kRowsPerBlock + 1];
@@ -511,9 +502,8 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
         const uint32_t u0 = slice * (uint32_t)kSliceRows;
         const uint32_t u1 = u0 >= span ? u0 : (span - u0 < (uint32_t)kSliceRows ? span : u0 + (uint32_t)kSliceRows);
         int32_t *obase = out + (P - lead) * W;
-        int32_t *cbase = ocol != nullptr ? ocol + (P - lead) : nullptr;
         for (uint32_t u = u0 + 4u * (uint32_t)t; u < u1; u += 4u * kThreads)
-            k2u_write_group<W>(u, lead, span, pos, eoff, n, hblk, edges, obase, cbase, ccol);
+            k2u_write_group<W>(u, lead, span, pos, eoff, n, hblk, edges, obase);
     } else {
         const int Wd = C + 1;
         int32_t *oblk = out + P * Wd;
@@ -525,7 +515,6 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
             const int32_t *src = hblk + (int64_t)i * C;
             for (int c = 0; c < C; ++c) dst[c] = __ldg(src + c);
             dst[C] = __ldg(edges + (eoff[i] + (j - pos[i])));
-            if (ocol != nullptr) ocol[P + j] = dst[ccol];
         }
     }
 }
@@ -543,8 +532,7 @@ template <int W>
 __global__ void __launch_bounds__(kThreads)
 k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_t *__restrict__ nbr,
                        const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ bp,
-                       const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out,
-                       int32_t *__restrict__ ocol, int ccol) {
+                       const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out) {
     constexpr int C = W - 1;
     constexpr int kPitch = W | 1;
     __shared__ int32_t rows[kRowsPerBlock * kPitch];
@@ -605,26 +593,6 @@ k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_
     // output words [P W, (P + T) W): int4 stores aligned to 16 B of out
     const unsigned long long P = bp[b];
     const uint32_t T = (uint32_t)blk_sum[b];
-    if (ocol != nullptr) {
-        // column ccol of the block's output rows, read back from the staged rows
-        const uint32_t cl = (uint32_t)(P & 3ull);
-        int32_t *cg = ocol + (P - cl);
-        for (uint32_t i = (uint32_t)t; 4u * i < cl + T; i += kThreads) {
-            int32_t cv[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const uint32_t q = 4u * i + j - cl;
-                cv[j] = q < T ? rows[q * kPitch + ccol] : 0;
-            }
-            if (4u * i >= cl && 4u * i + 4u <= cl + T) {
-                reinterpret_cast<int4 *>(cg)[i] = make_int4(cv[0], cv[1], cv[2], cv[3]);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (4u * i + j - cl < T) cg[4u * i + j] = cv[j];
-            }
-        }
-    }
     const uint32_t lead = (uint32_t)((P * W) & 3ull), words = T * W;
     int32_t *g = out + (P * W - lead);
     for (uint32_t i = (uint32_t)t; 4u * i < lead + words; i += kThreads) {
@@ -773,14 +741,13 @@ static inline unsigned int nblocks_rows(int64_t R) {
     return (unsigned int)((R + kRowsPerBlock - 1) / kRowsPerBlock);
 }
 
-void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, const int32_t *vcol, uint32_t dir, PredView pv,
-                      uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums,
+void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums,
                       int *err, bool func, cudaStream_t st) {
     const bool dense = (dir ? pv.rp[1] : pv.rp[0]) != nullptr;
     const unsigned int nb = nblocks_rows(R);
 #define WK_COUNT(F, D)                                                                                             \
     k2u_count_kernel<F, D><<<(nb + count_blocks_per_cta<D>() - 1) / count_blocks_per_cta<D>(), kThreads, 0, st>>>( \
-        hist, R, C, scol, vcol, dir, pv, deg, off, blk_sum, group_sums, err)
+        hist, R, C, scol, dir, pv, deg, off, blk_sum, group_sums, err)
     if (func && dense) WK_COUNT(true, true);
     else if (func) WK_COUNT(true, false);
     else if (dense) WK_COUNT(false, true);
@@ -790,13 +757,12 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, const int
 
 void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
                             const unsigned long long *blk_sum, const unsigned long long *bp,
-                            const unsigned long long *sp, unsigned long long slices, int32_t *out, int32_t *ocol,
-                            int ccol, cudaStream_t st) {
+                            const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st) {
     if (slices == 0ull) return;
     const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
     const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND_F(WC) \
-    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, bp, sp, nblk, out, ocol, ccol)
+    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, bp, sp, nblk, out)
     switch (C + 1) {
         case 2: WK_EXPAND_F(2); break;
         case 3: WK_EXPAND_F(3); break;
@@ -817,13 +783,12 @@ void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, const unsi
 
 void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edges, const uint32_t *deg,
                        const uint32_t *off, const unsigned long long *blk_sum, const unsigned long long *bp,
-                       const unsigned long long *sp, unsigned long long slices, int32_t *out, int32_t *ocol,
-                       int ccol, cudaStream_t st) {
+                       const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st) {
     if (slices == 0ull) return;
     const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
     const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND(WC) \
-    k2u_expand_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, C, edges, deg, off, blk_sum, bp, sp, nblk, out, ocol, ccol)
+    k2u_expand_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, C, edges, deg, off, blk_sum, bp, sp, nblk, out)
     switch (C + 1) {
         case 2: WK_EXPAND(2); break;
         case 3: WK_EXPAND(3); break;

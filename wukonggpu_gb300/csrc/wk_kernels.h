@@ -24,20 +24,14 @@ constexpr int kGroupShift = 8;        // input blocks per k2u group sum: 256
 // neighbour as int32 (-1 when there is none) for launch_k2u_expand_func; err
 // bit 3 when a row's list had more than one entry (an index key), which the
 // functional expansion cannot write.
-// vcol (may be null): column scol of the R rows as a dense int32 array, read
-// instead of the history.
-void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, const int32_t *vcol, uint32_t dir, PredView pv,
-                      uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums,
+void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums,
                       int *err, bool func, cudaStream_t st);
 
 // k2u pass 2 of a functional direction (2 <= C + 1 <= 8): the matched rows
 // with their neighbour appended, compacted in order; one CTA per non-empty block.
-// ocol (may be null, 16 B aligned): also receives column ccol (0..C) of every
-// output row as a dense int32 array, for the next pattern's count.
 void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
                             const unsigned long long *blk_sum, const unsigned long long *bp,
-                            const unsigned long long *sp, unsigned long long slices, int32_t *out, int32_t *ocol,
-                            int ccol, cudaStream_t st);
+                            const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st);
 
 // k2u plan: bp[b] = the block's output prefix, sp[b] = its first slice
 // (nblk + 1 entries each); totals[0] = output rows, totals[2] = slices, the
@@ -47,11 +41,9 @@ void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, const unsi
 
 // k2u pass 2: one CTA per slice writes its rows (row || neighbour) of its
 // block's output; out holds totals[0] rows of C + 1 columns and is 16 B aligned.
-// ocol / ccol as for launch_k2u_expand_func.
 void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edges, const uint32_t *deg,
                        const uint32_t *off, const unsigned long long *blk_sum, const unsigned long long *bp,
-                       const unsigned long long *sp, unsigned long long slices, int32_t *out, int32_t *ocol,
-                       int ccol, cudaStream_t st);
+                       const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st);
 
 // k2k/k2c pass 1: probe + membership of the end value; per-row ballot masks,
 // per-block kept-row counts, flags cleared; totals[0] += adjacency entries a

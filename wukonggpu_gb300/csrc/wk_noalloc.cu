@@ -107,8 +107,7 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     cudaStream_t s = ctx->stream;
     if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 48, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
     // kMaxRows input rows are one group: its two sums follow the totals
-    dev::launch_k2u_count(hist, rows, cols, scol, nullptr, (uint32_t)direction, pv, deg, off, blk_sum, tot + 3, err, false,
-                          s);
+    dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, tot + 3, err, false, s);
     dev::launch_k2u_plan(blk_sum, nblk, tot + 3, bp, sp, tot, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: count launch");
     ctx->launches += 2;
@@ -127,7 +126,7 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
                          "known_to_unknown_noalloc: output needs %lld int32 elements, capacity is %lld "
                          "(*out_rows holds the row count)",
                          (long long)(R_out * (cols + 1)), (long long)out_capacity);
-    dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, bp, sp, ctx->h_scal[3], out, nullptr, 0, s);
+    dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, bp, sp, ctx->h_scal[3], out, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: expand launch");
     ctx->launches += 1;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "noalloc: sync");

@@ -149,16 +149,6 @@ int clear_totals(wk_ctx *ctx) {
 int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     const int C = h->col_num;
     const int64_t R = h->size / C;
-    // the start column as its own array, when the previous step of this query
-    // wrote it; the state is cleared before anything else, so an early return
-    // cannot leave it pointing at a table this op replaces
-    const int32_t *vcol = (ctx->col_for != nullptr && ctx->col_for == h->data && ctx->col_idx == scol)
-                              ? ctx->colbuf[ctx->col_buf].as<int32_t>()
-                              : nullptr;
-    const int ccol = ctx->col_want;   // the column of this step's output the next step starts from
-    const int cbuf = vcol ? 1 - ctx->col_buf : 0;
-    ctx->col_for = nullptr;
-    ctx->col_want = -1;
     OpClock clk(ctx);
     ctx->last.kind = KIND_K2U;
     ctx->last.rows_in = R;
@@ -195,7 +185,7 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         cudaError_t eg = cudaMemsetAsync(group_sums, 0, (size_t)groups * 16, ctx->stream);
         if (eg != cudaSuccess) return cuda_fail(eg, "k2u: clear group sums");
         if ((st = clk.begin())) return st;
-        dev::launch_k2u_count(h->data, R, C, scol, vcol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
+        dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
                               ctx->blk_sum.as<unsigned long long>(), group_sums, err, func, ctx->stream);
         dev::launch_k2u_plan(ctx->blk_sum.as<unsigned long long>(), nblk, group_sums, bp, sp, tot, ctx->stream);
         ++ctx->launches;   // the plan kernel, timed with the count
@@ -221,24 +211,14 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         if ((st = ob.reserve(16))) return st;
     } else {
         if ((st = ob.reserve((size_t)R_out * (C + 1) * 4))) return st;
-        int32_t *ocol = nullptr;
-        if (ccol >= 0 && ccol <= C) {
-            if ((st = ctx->colbuf[cbuf].reserve((size_t)R_out * 4))) return st;
-            ocol = ctx->colbuf[cbuf].as<int32_t>();
-        }
         if ((st = clk.begin())) return st;
         if (func)
             dev::launch_k2u_expand_func(h->data, R, C, ctx->deg.as<int32_t>(), ctx->blk_sum.as<unsigned long long>(),
-                                        bp, sp, ctx->h_scal[3], ob.as<int32_t>(), ocol, ccol, ctx->stream);
+                                        bp, sp, ctx->h_scal[3], ob.as<int32_t>(), ctx->stream);
         else
             dev::launch_k2u_expand(h->data, R, C, pv.edges, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
                                    ctx->blk_sum.as<unsigned long long>(), bp, sp, ctx->h_scal[3], ob.as<int32_t>(),
-                                   ocol, ccol, ctx->stream);
-        if (ocol) {
-            ctx->col_for = ob.as<int32_t>();
-            ctx->col_idx = ccol;
-            ctx->col_buf = cbuf;
-        }
+                                   ctx->stream);
         if ((st = launch_check("k2u expand")) || (st = clk.end(true))) return st;
         if (ctx->timing) {
             cudaError_t e = cudaStreamSynchronize(ctx->stream);
@@ -256,8 +236,6 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
 // two-pass k2k / k2c (probe + membership -> filtered copy); the output is
 // sized by the input, so the host reads the totals only at the end
 int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const, uint32_t pid, uint32_t dir) {
-    ctx->col_for = nullptr;   // this op writes a new table and no column array
-    ctx->col_want = -1;
     const int C = h->col_num;
     const int64_t R = h->size / C;
     OpClock clk(ctx);
@@ -306,8 +284,6 @@ int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const,
 
 // one adjacency list -> one-column table (index or constant start)
 int op_list(wk_ctx *ctx, wk_history *h, uint64_t vid, uint32_t pid, uint32_t dir, int kind) {
-    ctx->col_for = nullptr;   // this op writes a new table and no column array
-    ctx->col_want = -1;
     OpClock clk(ctx);
     ctx->last.kind = kind;
     ctx->last.rows_in = 1;
@@ -417,24 +393,11 @@ extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history
     if (ctx->device < 0) return set_error(WK_EDEVICE, "wk_execute: host-only context");
     wk_history_init(h);
     ctx->protect.clear();
-    // column arrays live only inside this call, whichever way it returns
-    struct ColGuard {
-        wk_ctx *c;
-        explicit ColGuard(wk_ctx *x) : c(x) { c->col_for = nullptr; c->col_want = -1; }
-        ~ColGuard() { c->col_for = nullptr; c->col_want = -1; }
-    } col_guard(ctx);
+    ctx->qstats.clear();
     DeviceStore &ds = *ctx->store;
     int st = WK_OK;
     for (int i = 0; i < n && st == WK_OK; ++i) {
         const int64_t start = cmd[i * 4], pid = cmd[i * 4 + 1], d = cmd[i * 4 + 2], end = cmd[i * 4 + 3];
-        // a k2u step followed by a k2u step: write the column the next one starts from
-        ctx->col_want = -1;
-        if (i + 1 < n && start < 0 && end < 0) {
-            const int64_t ns = cmd[(i + 1) * 4], ne = cmd[(i + 1) * 4 + 3];
-            const int64_t out_cols = -end;   // this step binds column -end - 1
-            if (ns < 0 && -ns <= out_cols && ne < 0 && -ne == out_cols + 1) ctx->col_want = (int)(-ns - 1);
-        }
-        // the segment of the next pattern is paged in on the side stream
         if (ds.pool && ctx->cfg.enable_prefetch && i + 1 < n) {
             const int64_t np = cmd[(i + 1) * 4 + 1];
             const int64_t cp = (i == 0 && is_tpid(cmd[0])) ? cmd[0] : pid;
@@ -469,6 +432,7 @@ extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history
             }
         }
         if (st == WK_OK && step_rows) step_rows[i] = h->col_num ? h->size / h->col_num : 0;
+        if (st == WK_OK && ctx->timing) ctx->qstats.push_back(ctx->last);
     }
     ctx->protect.clear();
     return st;

@@ -419,6 +419,14 @@ extern "C" int wk_last_op_stats(wk_ctx *ctx, wk_op_stats *st) {
     return WK_OK;
 }
 
+extern "C" int wk_query_op_stats(wk_ctx *ctx, wk_op_stats *st, int32_t cap, int32_t *n) {
+    if (!ctx || !n || cap < 0 || (cap > 0 && !st)) return set_error(WK_EINVAL, "wk_query_op_stats: bad arguments");
+    const int32_t k = (int32_t)std::min<size_t>((size_t)cap, ctx->qstats.size());
+    for (int32_t i = 0; i < k; ++i) st[i] = ctx->qstats[(size_t)i];
+    *n = (int32_t)ctx->qstats.size();
+    return WK_OK;
+}
+
 extern "C" int64_t wk_kernel_launches(wk_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
 extern "C" int wk_host_alloc(int64_t bytes, void **out) {

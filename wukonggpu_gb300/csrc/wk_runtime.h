@@ -83,21 +83,13 @@ struct wk_ctx {
     std::vector<int> tmain;          // index of kernel pairs that are the op's main kernel
     int tn = 0;
     wk_op_stats last{};
+    std::vector<wk_op_stats> qstats;   // every op of the last wk_execute, while timing
     int64_t launches = 0;
     int64_t row_limit = INT64_MAX;   // wk_set_row_limit
     cudaEvent_t tm0 = nullptr, tm1 = nullptr;   // wk_timer_begin / wk_timer_end
 
     // query-level state (segment cache protection / prefetch)
     std::vector<int> protect;
-    // Within one wk_execute, a k2u step also writes the column the next step
-    // starts from as a dense int32 array (colbuf), and that step's count reads
-    // it instead of the row-major history.  col_for is the history data the
-    // array describes (null: none); every op clears it before writing a new
-    // history, so an array is never read for any other table.
-    wk::DevBuf colbuf[2];
-    int col_want = -1;                   // column of the next output to write (-1: none)
-    const int32_t *col_for = nullptr;
-    int col_idx = -1, col_buf = 0;
 
     ~wk_ctx();
 };
