@@ -113,20 +113,17 @@ constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
 // 1 when a block's output count reaches 2^31 (the expansion keeps block-local
 // positions in 32 bits).  FUNC (a direction whose lists hold at most one
 // vertex): deg receives the neighbour itself as an int32, or -1 for no match,
-// and off is unused.  DENSE (the direction is an offsets array): a CTA takes
-// two blocks, a warp issues the lookups of all its eight rounds phase by
-// phase -- every round's start vertex, then every round's offsets or
-// neighbour -- and a lane looks up its own key (no shuffles), so each warp
-// keeps many loads in flight and a CTA's fixed costs (reduction, exit) are
-// shared by 2048 rows.
-template <bool DENSE>
-__host__ __device__ constexpr int count_blocks_per_cta() { return DENSE ? 2 : 1; }
-
-template <bool FUNC, bool DENSE>
+// and off is unused.  DENSE (the direction is an offsets array): a warp
+// issues the lookups of all its rounds phase by phase -- every round's start
+// vertex, then every round's offsets or neighbour -- and a lane looks up its
+// own key (no shuffles).  BPC blocks per CTA: 2 for a large dense op, so each
+// warp keeps eight rounds of loads in flight and a CTA's fixed costs
+// (reduction, exit) are shared by 2048 rows; 1 otherwise, so a small op still
+// spreads over many CTAs.
+template <bool FUNC, bool DENSE, int BPC>
 __global__ void __launch_bounds__(kThreads, (DENSE && FUNC) ? 8 : 6)
 k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
                  unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ group_sums, int *err) {
-    constexpr int BPC = count_blocks_per_cta<DENSE>();
     constexpr int NR = kRounds * BPC;   // rounds of 32 rows per warp
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t b0 = (int64_t)blockIdx.x * BPC;
@@ -142,12 +139,8 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
         v[rd] = r < R ? __ldg(hist + r * C + scol) : -1;
     }
     unsigned long long my_sum[BPC];
-    unsigned int my_nz[BPC];
 #pragma unroll
-    for (int j = 0; j < BPC; ++j) {
-        my_sum[j] = 0ull;
-        my_nz[j] = 0u;
-    }
+    for (int j = 0; j < BPC; ++j) my_sum[j] = 0ull;
     if constexpr (DENSE) {
         const uint32_t vmin = dir ? pv.vmin[1] : pv.vmin[0], dn = dir ? pv.dn[1] : pv.dn[0];
         if constexpr (FUNC) {
@@ -167,7 +160,6 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
                 if (r < R) {
                     reinterpret_cast<int32_t *>(deg)[r] = g[rd];
                     my_sum[rd / kRounds] += g[rd] >= 0 ? 1ull : 0ull;
-                    my_nz[rd / kRounds] += g[rd] >= 0 ? 1u : 0u;
                 }
             }
         } else {
@@ -194,7 +186,6 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
                     deg[r] = d;
                     off[r] = a[rd];
                     my_sum[rd / kRounds] += d;
-                    my_nz[rd / kRounds] += d > 0u;
                 }
             }
         }
@@ -215,26 +206,37 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
                     off[r] = o;
                 }
                 my_sum[rd / kRounds] += d;
-                my_nz[rd / kRounds] += d > 0u;
             }
         }
     }
+    // each block's output rows: a warp reduction (one REDUX instruction while the
+    // partial sums are small, as every valid block's are) and one barrier
+    __shared__ unsigned long long s_part[BPC][kThreads / 32];
 #pragma unroll
     for (int j = 0; j < BPC; ++j) {
+        unsigned long long ws;
+        if (!__any_sync(FULL, my_sum[j] >= (1ull << 26))) ws = __reduce_add_sync(FULL, (unsigned int)my_sum[j]);
+        else ws = warp_sum(my_sum[j]);
+        if (lane == 0) s_part[j][warp] = ws;
+    }
+    __syncthreads();
+    if (threadIdx.x < BPC) {
+        const int j = threadIdx.x;
         const int64_t b = b0 + j;
-        block_sum2(my_sum[j], my_nz[j]);
-        if (threadIdx.x == 0 && b < nblk) {
-            blk_sum[b] = my_sum[j];
+        unsigned long long sum = 0ull;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) sum += s_part[j][w];
+        if (b < nblk) {
+            blk_sum[b] = sum;
             // group sums spread the atomics over many addresses (256 blocks each);
             // the op total comes from the plan kernel, so no address takes one per block
-            if (my_sum[j]) {
+            if (sum) {
                 unsigned long long *gs = group_sums + 2 * (b >> kGroupShift);
-                atomicAdd(gs, my_sum[j]);
-                atomicAdd(gs + 1, slices_of(my_sum[j]));
+                atomicAdd(gs, sum);
+                atomicAdd(gs + 1, slices_of(sum));
             }
-            if (my_sum[j] >> 31) atomicOr(err, 2);
+            if (sum >> 31) atomicOr(err, 2);
         }
-        __syncthreads();   // block_sum2's shared partial sums are reused
     }
 }
 
@@ -279,9 +281,9 @@ __device__ __forceinline__ void plan_scan2(unsigned long long &a, unsigned long 
 // ones; the groups before the tile contribute their sums from the count
 // kernel, so no CTA waits on another.
 __global__ void __launch_bounds__(kPlanThreads)
-k2u_plan_kernel(const unsigned long long *__restrict__ blk_sum, int64_t nblk,
-                const unsigned long long *__restrict__ group_sums, unsigned long long *__restrict__ bp,
-                unsigned long long *__restrict__ sp, unsigned long long *__restrict__ totals) {
+k2u_plan_kernel(const unsigned long long *__restrict__ blk_sum, int64_t nblk, unsigned long long *group_sums,
+                unsigned int *plan_done, unsigned long long *__restrict__ bp, unsigned long long *__restrict__ sp,
+                unsigned long long *__restrict__ totals) {
     __shared__ unsigned long long s_po, s_ps;
     __shared__ unsigned long long s_ga[kPlanThreads / 32], s_gb[kPlanThreads / 32];
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
@@ -348,6 +350,20 @@ k2u_plan_kernel(const unsigned long long *__restrict__ blk_sum, int64_t nblk,
         sp[nblk] = s_ps + tsl;
         totals[0] = s_po + to;
         totals[2] = s_ps + tsl;
+    }
+    // the last CTA to finish zeroes the group sums for the next op (every CTA
+    // has read the groups it needs by then); the counter is reset with them
+    __shared__ bool s_last;
+    __syncthreads();
+    if (t == 0) {
+        __threadfence();
+        s_last = atomicAdd(plan_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        const int64_t ng = (nblk + (1 << kGroupShift) - 1) >> kGroupShift;
+        for (int64_t k = t; k < 2 * ng; k += kPlanThreads) group_sums[k] = 0ull;
+        if (t == 0) *plan_done = 0u;
     }
 }
 
@@ -745,13 +761,29 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t 
                       int *err, bool func, cudaStream_t st) {
     const bool dense = (dir ? pv.rp[1] : pv.rp[0]) != nullptr;
     const unsigned int nb = nblocks_rows(R);
-#define WK_COUNT(F, D)                                                                                             \
-    k2u_count_kernel<F, D><<<(nb + count_blocks_per_cta<D>() - 1) / count_blocks_per_cta<D>(), kThreads, 0, st>>>( \
-        hist, R, C, scol, dir, pv, deg, off, blk_sum, group_sums, err)
-    if (func && dense) WK_COUNT(true, true);
-    else if (func) WK_COUNT(true, false);
-    else if (dense) WK_COUNT(false, true);
-    else WK_COUNT(false, false);
+    // two blocks per CTA once the op has enough blocks to fill the GPU with half as many CTAs
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms < 1) sms = 1;
+    }
+    const bool pair = dense && nb >= 16u * (unsigned int)sms;
+#define WK_COUNT(F, D, B) \
+    k2u_count_kernel<F, D, B><<<(nb + B - 1) / B, kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, \
+                                                                     group_sums, err)
+    if (func && dense) {
+        if (pair) WK_COUNT(true, true, 2);
+        else WK_COUNT(true, true, 1);
+    } else if (func) {
+        WK_COUNT(true, false, 1);
+    } else if (dense) {
+        if (pair) WK_COUNT(false, true, 2);
+        else WK_COUNT(false, true, 1);
+    } else {
+        WK_COUNT(false, false, 1);
+    }
 #undef WK_COUNT
 }
 
@@ -775,10 +807,11 @@ void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t
 #undef WK_EXPAND_F
 }
 
-void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, const unsigned long long *group_sums,
-                     unsigned long long *bp, unsigned long long *sp, unsigned long long *totals, cudaStream_t st) {
+void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, unsigned long long *group_sums,
+                     unsigned int *plan_done, unsigned long long *bp, unsigned long long *sp, unsigned long long *totals,
+                     cudaStream_t st) {
     const unsigned int g = (unsigned int)((nblk + (1 << kPlanTileShift) - 1) >> kPlanTileShift);
-    k2u_plan_kernel<<<g, kPlanThreads, 0, st>>>(blk_sum, nblk, group_sums, bp, sp, totals);
+    k2u_plan_kernel<<<g, kPlanThreads, 0, st>>>(blk_sum, nblk, group_sums, plan_done, bp, sp, totals);
 }
 
 void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edges, const uint32_t *deg,

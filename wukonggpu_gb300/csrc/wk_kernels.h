@@ -35,9 +35,11 @@ void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t
 
 // k2u plan: bp[b] = the block's output prefix, sp[b] = its first slice
 // (nblk + 1 entries each); totals[0] = output rows, totals[2] = slices, the
-// expansion's CTA count.  One CTA per 8192 blocks.
-void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, const unsigned long long *group_sums,
-                     unsigned long long *bp, unsigned long long *sp, unsigned long long *totals, cudaStream_t st);
+// expansion's CTA count.  One CTA per 8192 blocks; the last one to finish
+// zeroes the group sums and *plan_done (both must be zero at launch).
+void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, unsigned long long *group_sums,
+                     unsigned int *plan_done, unsigned long long *bp, unsigned long long *sp, unsigned long long *totals,
+                     cudaStream_t st);
 
 // k2u pass 2: one CTA per slice writes its rows (row || neighbour) of its
 // block's output; out holds totals[0] rows of C + 1 columns and is 16 B aligned.

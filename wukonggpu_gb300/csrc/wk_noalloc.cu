@@ -36,7 +36,7 @@ static_assert(kMaxBlocks <= (1 << wk::dev::kGroupShift), "one k2u group sum per 
 
 constexpr size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // byte layout of the scratch array
-constexpr size_t kOffFlags = 0;       // err (int), totals (3 x u64), the block group's sums (2 x u64)
+constexpr size_t kOffFlags = 0;       // err (int), totals (3 x u64), group sums (2 x u64), plan counter
 constexpr size_t kOffDeg = al(kOffFlags + 64);
 constexpr size_t kOffOff = al(kOffDeg + 4 * kMaxRows);
 constexpr size_t kOffBlkSum = al(kOffOff + 4 * kMaxRows);
@@ -105,10 +105,10 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     const PredView pv = ctx->store->views[(size_t)predict];
     const int scol = (int)(-start - 1);
     cudaStream_t s = ctx->stream;
-    if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 48, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
+    if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 56, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
     // kMaxRows input rows are one group: its two sums follow the totals
     dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, tot + 3, err, false, s);
-    dev::launch_k2u_plan(blk_sum, nblk, tot + 3, bp, sp, tot, s);
+    dev::launch_k2u_plan(blk_sum, nblk, tot + 3, reinterpret_cast<unsigned int *>(tot + 5), bp, sp, tot, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: count launch");
     ctx->launches += 2;
     if ((e = cudaMemcpyAsync(ctx->h_scal, sc + kOffFlags, 32, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||

@@ -123,6 +123,19 @@ int fail_corrupt(wk_ctx *ctx) {
 
 }  // namespace
 
+namespace {
+// The k2u group sums and the plan kernel's done counter: zero when allocated,
+// and zeroed again by the plan kernel after every use.
+int reserve_gsum(wk_ctx *ctx, int64_t groups) {
+    const size_t need = 16 + (size_t)groups * 16;
+    if (need <= ctx->gsum.cap) return WK_OK;
+    int st = ctx->gsum.reserve(need);
+    if (st) return st;
+    cudaError_t e = cudaMemsetAsync(ctx->gsum.ptr, 0, ctx->gsum.cap, ctx->stream);
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "k2u: clear group sums");
+}
+}  // namespace
+
 int wk::reserve_op_scratch(wk_ctx *ctx, int64_t rows) {
     if (!ctx || rows < 0) return set_error(WK_EINVAL, "reserve_op_scratch: bad arguments");
     if (ctx->device < 0) return WK_OK;
@@ -132,7 +145,8 @@ int wk::reserve_op_scratch(wk_ctx *ctx, int64_t rows) {
     int st;
     if ((st = ctx->deg.reserve((size_t)rows * 4)) || (st = ctx->off.reserve((size_t)rows * 4)) ||
         (st = ctx->mask.reserve((size_t)((rows + 31) / 32) * 4)) || (st = ctx->blk_sum.reserve((size_t)nblk * 8)) ||
-        (st = ctx->blk_nz.reserve((size_t)nblk * 4)) || (st = ctx->lb_flags.reserve((size_t)nblk * 8)))
+        (st = ctx->blk_nz.reserve((size_t)nblk * 4)) || (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16)) ||
+        (st = reserve_gsum(ctx, (nblk + (1 << dev::kGroupShift) - 1) >> dev::kGroupShift)))
         return st;
     return WK_OK;
 }
@@ -168,26 +182,27 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
     const int64_t groups = (nblk + (1 << dev::kGroupShift) - 1) >> dev::kGroupShift;
     if ((st = ctx->deg.reserve((size_t)R * 4)) || (st = ctx->off.reserve((size_t)R * 4)) ||
-        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) ||
-        (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16 + (size_t)groups * 16)))
+        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16)) ||
+        (st = reserve_gsum(ctx, groups)))
         return st;
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
     int *err = ctx->dscal.as<int>();
-    // block output prefixes, slice prefixes and the group sums share the look-back scratch
+    // block output prefixes and slice prefixes share the look-back scratch
     unsigned long long *bp = ctx->lb_flags.as<unsigned long long>(), *sp = bp + (nblk + 1);
-    unsigned long long *group_sums = sp + (nblk + 1);
+    unsigned int *plan_done = ctx->gsum.as<unsigned int>();
+    unsigned long long *group_sums = ctx->gsum.as<unsigned long long>() + 2;
     // a functional direction (at most one neighbour per vertex) expands as a
     // compaction; if a row hits an index list (vertex 0) the op reruns unspecialised
     bool func = pv.func[dir] != 0u && C + 1 <= 8;
     int errf = 0;
+    // the plan kernel writes the op totals and zeroes the group sums after use,
+    // so nothing is cleared before the count kernel
     for (;;) {
-        if ((st = clear_totals(ctx))) return st;
-        cudaError_t eg = cudaMemsetAsync(group_sums, 0, (size_t)groups * 16, ctx->stream);
-        if (eg != cudaSuccess) return cuda_fail(eg, "k2u: clear group sums");
         if ((st = clk.begin())) return st;
         dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
                               ctx->blk_sum.as<unsigned long long>(), group_sums, err, func, ctx->stream);
-        dev::launch_k2u_plan(ctx->blk_sum.as<unsigned long long>(), nblk, group_sums, bp, sp, tot, ctx->stream);
+        dev::launch_k2u_plan(ctx->blk_sum.as<unsigned long long>(), nblk, group_sums, plan_done, bp, sp, tot,
+                             ctx->stream);
         ++ctx->launches;   // the plan kernel, timed with the count
         ++ctx->last.kernels;
         if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;

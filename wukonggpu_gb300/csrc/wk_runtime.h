@@ -73,7 +73,8 @@ struct wk_ctx {
     wk::DevBuf hbuf[2];              // ping-pong history buffers (core/rcache.hpp:87-88)
     // scratch of the two-pass ops
     wk::DevBuf deg, off, mask, blk_sum, blk_nz;
-    wk::DevBuf lb_flags;             // per-block look-back prefixes of the second pass
+    wk::DevBuf lb_flags;             // per-block prefixes: k2u output and slice prefixes, filter look-back
+    wk::DevBuf gsum;                 // k2u: plan kernel's done counter (first 16 B) + group sums; kept zero
     wk::DevBuf dscal;                // [0] error flags, [8..32) totals
     unsigned long long *h_scal = nullptr;   // pinned mirror of the totals
 
