@@ -709,8 +709,11 @@ def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2)
         srv.start()
         srv.drain(600)
         st = srv.stats()
+        cdf = {c: srv.latency_cdf(c) for c in ("light", "heavy")}
         srv.close()
-        return {k: st[k] for k in ("qps", "p50_ms", "p99_ms", "light_p99_ms", "heavy_p99_ms", "mean_batch", "failed")}
+        out = {k: st[k] for k in ("qps", "p50_ms", "p99_ms", "light_p99_ms", "heavy_p99_ms", "mean_batch", "failed")}
+        out["_cdf"] = cdf
+        return out
 
     # capacity of the baseline: every request present at t=0
     cap0 = run(0, stats_plans, 0.0)["qps"]
@@ -732,7 +735,14 @@ def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2)
             best = t
     out["headline"] = {"baseline_qps": base["qps"], "baseline_p99_ms": base["p99_ms"],
                        "batched_learned_qps_at_le_p99": best["qps"] if best else None,
-                       "ratio": (best["qps"] / base["qps"]) if best else None}
+                       "ratio": (best["qps"] / base["qps"]) if best else None,
+                       # the reference Logger's 25-point CDF (ms) of light and heavy requests
+                       "cdf_rates": W.Server.CDF_RATES,
+                       "baseline_cdf_ms": base["_cdf"], "batched_cdf_ms": best["_cdf"] if best else None}
+    for row in out["sweep"]:
+        for t in (row["query_at_a_time_stats"], row["batched_learned"]):
+            if t:
+                t.pop("_cdf", None)
     return out
 
 

@@ -305,6 +305,8 @@ typedef struct {
     double  span_s;               /* first arrival .. last completion             */
     double  qps;                  /* completed / span                             */
     double  p50_ms, p99_ms, light_p50_ms, light_p99_ms, heavy_p50_ms, heavy_p99_ms;
+                                  /* percentiles by the reference Logger's rule:
+                                     sorted latencies, element floor(n q)         */
 } wk_server_stats;
 
 typedef struct wk_server wk_server;
@@ -317,6 +319,11 @@ int     wk_server_drain(wk_server *s, double timeout_s);
 int     wk_server_result(wk_server *s, int64_t id, int64_t *rows, int32_t *cols, int32_t *host, int64_t cap,
                          double *latency_s, int32_t *status);
 int     wk_server_get_stats(wk_server *s, wk_server_stats *out);
+/* Latency CDF of the completed requests (cls 0 all, 1 light, 2 heavy): the
+ * reference Logger's 25 points (core/logger.hpp print_cdf), at rates 0.01,
+ * 0.05 .. 0.95 by 0.05 and 0.96 .. 1.00 by 0.01, into out_ms[WK_CDF_POINTS]. */
+#define WK_CDF_POINTS 25
+int     wk_server_latency_cdf(wk_server *s, int32_t cls, double *out_ms);
 int     wk_server_destroy(wk_server *s);
 
 /* Per-op timing of the last op (device time from CUDA events, ms) and its

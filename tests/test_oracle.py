@@ -105,3 +105,16 @@ def test_reference_harness_edge_graph(lib_built):
     orc = oracle.Oracle(s, p, o, g.num_ids)
     ref = oracle.RefStore(s, p, o, g.num_ids, keys_million=16, memstore_mb=1024)
     assert ref.digest() == orc.digest()
+
+
+def test_logger_rule_restatement():
+    """The Logger's percentile rule (core/logger.hpp:197-305): element floor(n q)
+    of the sorted latencies, the last one at q = 1; 25 CDF rates."""
+    from oracle import logger_ref
+    lats = [5.0, 1.0, 4.0, 2.0, 3.0, 9.0, 7.0, 8.0, 6.0, 10.0]
+    assert logger_ref.at_rate(lats, 0.5) == 6.0      # element 5 of 1..10
+    assert logger_ref.at_rate(lats, 0.99) == 10.0    # element floor(9.9) = 9
+    assert logger_ref.at_rate(lats, 1.0) == 10.0     # clamped
+    assert logger_ref.at_rate(lats, 0.01) == 1.0
+    r = logger_ref.cdf_rates()
+    assert len(r) == 25 and r[0] == 0.01 and abs(r[19] - 0.95) < 1e-12 and abs(r[-1] - 1.0) < 1e-12

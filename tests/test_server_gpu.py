@@ -62,3 +62,25 @@ def test_latency_and_throughput_reported(gpu_small, mix):
     assert st["qps"] > 0 and 0 < st["p50_ms"] <= st["p99_ms"]
     assert st["span_s"] >= arr[-1] - arr[0] - 1e-3
     srv.close()
+
+
+def test_latency_statistics_follow_the_logger(gpu_small, mix):
+    """p50/p99 and the 25-point CDF are the reference Logger's statistics
+    (core/logger.hpp:197-305) of the requests' own latencies."""
+    from oracle import logger_ref
+    srv = W.Server(gpu_small, mode=1, plan=0, max_batch=1024)
+    arr = W.poisson_arrivals(len(mix), rate_qps=30_000.0, seed=3)
+    ids = [srv.submit(q, float(t)) for q, t in zip(mix, arr)]
+    srv.start()
+    srv.drain(300)
+    lats = [srv.result(i, fetch=False)[1] * 1e3 for i in ids]
+    st = srv.stats()
+    assert st["p50_ms"] == pytest.approx(logger_ref.at_rate(lats, 0.50), rel=1e-9)
+    assert st["p99_ms"] == pytest.approx(logger_ref.at_rate(lats, 0.99), rel=1e-9)
+    cdf = srv.latency_cdf("all")
+    assert cdf == pytest.approx(logger_ref.cdf(lats), rel=1e-9)
+    for cls in ("light", "heavy"):
+        c = srv.latency_cdf(cls)
+        assert all(a <= b for a, b in zip(c, c[1:])) and c[-1] <= cdf[-1] + 1e-9
+    assert W.Server.CDF_RATES == pytest.approx(logger_ref.cdf_rates())
+    srv.close()

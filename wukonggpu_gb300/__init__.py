@@ -135,6 +135,7 @@ _SIGS = {
     "wk_server_result": (C.c_int, [_P, C.c_int64, _I64P, _I32P, _I32P, C.c_int64, C.POINTER(C.c_double),
                                    _I32P]),
     "wk_server_get_stats": (C.c_int, [_P, C.POINTER(wk_server_stats)]),
+    "wk_server_latency_cdf": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double)]),
     "wk_server_destroy": (C.c_int, [_P]),
     "wk_mlp_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P)]),
     "wk_mlp_destroy": (C.c_int, [_P]),
@@ -707,6 +708,15 @@ class Server:
         st = wk_server_stats()
         _check(load_library().wk_server_get_stats(self._h, C.byref(st)))
         return {f: getattr(st, f) for f, _ in st._fields_}
+
+    CDF_RATES = [0.01] + [0.05 * i for i in range(1, 20)] + [0.95 + 0.01 * i for i in range(1, 6)]
+
+    def latency_cdf(self, cls: str = "all") -> list:
+        """The reference Logger's 25-point latency CDF (ms) at CDF_RATES, of all,
+        light or heavy requests."""
+        out = (C.c_double * 25)()
+        _check(load_library().wk_server_latency_cdf(self._h, {"all": 0, "light": 1, "heavy": 2}[cls], out))
+        return list(out)
 
     def close(self):
         if getattr(self, "_h", None):

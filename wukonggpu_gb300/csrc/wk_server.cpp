@@ -72,14 +72,23 @@ struct Req {
     double done_t = 0.0;
 };
 
-double pct(std::vector<double> v, double q) {
-    if (v.empty()) return 0.0;
-    std::sort(v.begin(), v.end());
-    const double pos = q * (double)(v.size() - 1);
-    const size_t i = (size_t)pos;
-    const double f = pos - (double)i;
-    return i + 1 < v.size() ? v[i] * (1.0 - f) + v[i + 1] * f : v[i];
+// Latency at rate q of a sorted sample by the reference Logger's rule
+// (core/logger.hpp:197-305): element floor(n q), the last one for q = 1.
+double rank_at(const std::vector<double> &sorted, double q) {
+    if (sorted.empty()) return 0.0;
+    size_t i = (size_t)((double)sorted.size() * q);
+    if (i >= sorted.size()) i = sorted.size() - 1;
+    return sorted[i];
 }
+
+double pct(std::vector<double> v, double q) {
+    std::sort(v.begin(), v.end());
+    return rank_at(v, q);
+}
+
+// The Logger's 25 CDF rates: 0.01, 0.05 .. 0.95 by 0.05, 0.96 .. 1.00 by 0.01
+// (core/logger.hpp print_cdf).
+double cdf_rate(int k) { return k == 0 ? 0.01 : (k < 20 ? 0.05 * k : 0.95 + 0.01 * (k - 19)); }
 
 }  // namespace
 
@@ -506,6 +515,23 @@ extern "C" int wk_server_get_stats(wk_server *s, wk_server_stats *out) {
     out->light_p99_ms = pct(light, 0.99) * 1e3;
     out->heavy_p50_ms = pct(heavy, 0.50) * 1e3;
     out->heavy_p99_ms = pct(heavy, 0.99) * 1e3;
+    return WK_OK;
+}
+
+extern "C" int wk_server_latency_cdf(wk_server *s, int32_t cls, double *out_ms) {
+    if (!s || !out_ms || cls < 0 || cls > 2) return set_error(WK_EINVAL, "wk_server_latency_cdf: bad arguments");
+    std::vector<double> v;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto &r : s->all) {
+            if (r->state.load() < 2) continue;
+            if (cls == 1 && r->heavy) continue;
+            if (cls == 2 && !r->heavy) continue;
+            v.push_back(r->done_t - r->arrival);
+        }
+    }
+    std::sort(v.begin(), v.end());
+    for (int k = 0; k < WK_CDF_POINTS; ++k) out_ms[k] = rank_at(v, cdf_rate(k)) * 1e3;
     return WK_OK;
 }
 
