@@ -98,6 +98,14 @@ int         wk_device_count(int *count);
  */
 int wk_store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o,
                    int64_t n_triples, int32_t num_ids);
+/* As wk_store_build, with the per-predicate sorts of the triples -- by (s, o)
+ * and by (o, s) -- done on the context's device (a radix sort); the image is
+ * byte-identical to wk_store_build's.  Needs a device context and n < 2^32 - 1. */
+int wk_store_build_device(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o,
+                          int64_t n, int32_t num_ids);
+/* FNV-1a digest of the host store image (metadata, buckets, edges, offsets
+ * arrays): equal for two builds exactly when their images are identical. */
+int wk_store_digest(wk_ctx *ctx, uint64_t *digest);
 /* Attach the store of `owner` to `ctx` (read-only sharing, one copy on HBM). */
 int wk_ctx_share_store(wk_ctx *ctx, wk_ctx *owner);
 

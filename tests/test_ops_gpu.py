@@ -270,3 +270,26 @@ def test_query_op_stats_cover_every_pattern(gpu_small, golden_small):
     assert [s["rows_out"] for s in stats] == list(rows)
     assert all(s["ms"] > 0 for s in stats if s["rows_out"] > 0)
     assert stats[0]["kind"] == 3 and all(s["kind"] in (0, 1, 2) for s in stats[1:])
+
+
+@pytest.mark.parametrize("which", ["small", "hub", "dups"])
+def test_device_sorted_build_gives_the_same_image(lib_built, small_graph, which):
+    """wk_store_build_device sorts the triples on the GPU; the image (buckets,
+    edges, offsets arrays, metadata) must be byte-identical to the host build's."""
+    if which == "small":
+        g, s, p, o = small_graph
+        nid = g.num_ids
+    else:
+        s, p, o, nid = _hub_graph()
+        if which == "dups":   # duplicates and a shuffled order
+            rng = np.random.default_rng(8)
+            k = rng.integers(0, len(s), size=len(s) // 3)
+            s, p, o = (np.concatenate([x, x[k]]) for x in (s, p, o))
+            perm = rng.permutation(len(s))
+            s, p, o = s[perm], p[perm], o[perm]
+    a = W.RCache(device=0)
+    a.build_store(s, p, o, nid)
+    b = W.RCache(device=0)
+    b.build_store(s, p, o, nid, sort_on_device=True)
+    assert a.store_digest() == b.store_digest()
+    assert a.store_info()["num_keys"] == b.store_info()["num_keys"]

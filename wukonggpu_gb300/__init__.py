@@ -92,6 +92,8 @@ _SIGS = {
     "wk_status_str": (C.c_char_p, [C.c_int]),
     "wk_device_count": (C.c_int, [C.POINTER(C.c_int)]),
     "wk_store_build": (C.c_int, [_P, _I32P, _I32P, _I32P, C.c_int64, C.c_int32]),
+    "wk_store_build_device": (C.c_int, [_P, _I32P, _I32P, _I32P, C.c_int64, C.c_int32]),
+    "wk_store_digest": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "wk_ctx_share_store": (C.c_int, [_P, _P]),
     "wk_store_get_info": (C.c_int, [_P, C.POINTER(wk_store_info)]),
     "wk_store_get_edges": (C.c_int, [_P, C.c_int64, C.c_int32, C.c_int32, _I32P, C.c_int64, _I64P]),
@@ -328,11 +330,19 @@ class RCache:
         self._h = h
 
     # -- store
-    def build_store(self, s, p, o, num_ids: int):
+    def build_store(self, s, p, o, num_ids: int, sort_on_device: bool = False):
+        """Build the store from ID-form triples; sort_on_device runs the
+        per-predicate sorts on the GPU (same image)."""
         s = np.ascontiguousarray(s, np.int32)
         p = np.ascontiguousarray(p, np.int32)
         o = np.ascontiguousarray(o, np.int32)
-        _check(load_library().wk_store_build(self._h, _i32(s), _i32(p), _i32(o), len(s), num_ids))
+        f = load_library().wk_store_build_device if sort_on_device else load_library().wk_store_build
+        _check(f(self._h, _i32(s), _i32(p), _i32(o), len(s), num_ids))
+
+    def store_digest(self) -> int:
+        d = C.c_uint64()
+        _check(load_library().wk_store_digest(self._h, C.byref(d)))
+        return d.value
 
     def build_store_graph(self, g: Graph):
         _check(load_library().wk_store_build_graph(self._h, g._h))

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstddef>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -137,6 +138,7 @@ struct HostStore {
     ~HostStore();
     // host lookup in the image; returns degree (0 if absent) and the edge pointer
     uint64_t lookup(uint64_t vid, uint32_t pid, uint32_t dir, const int32_t **edges_out) const;
+    uint64_t digest() const;   // of the whole image, for comparing two builds
     // every key of segment id: f(vid, dir, edge offset in the segment, degree)
     template <class F>
     void for_each_key(int id, F f) const {
@@ -161,8 +163,16 @@ struct Stats;   // planner statistics (wk_planner.cpp)
 Stats *build_stats(const HostStore &hs);
 void free_stats(Stats *s);
 
+// A device sort for the build: given the largest vertex id and predicate,
+// fills keys[k] (hi << 32 | lo) and pids[k] with all n triples sorted by
+// (predicate, hi, lo), order 0 (s, o) and order 1 (o, s).
+using SortTriples = std::function<int(uint32_t max_vid, uint32_t max_pid, std::vector<uint64_t> (&keys)[2],
+                                      std::vector<uint32_t> (&pids)[2])>;
+
+// The store image from ID-form triples; the per-predicate sorts run on the
+// host, or through device_sort when given (the image is the same either way).
 int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
-                     int32_t num_ids, HostStore **out);
+                     int32_t num_ids, HostStore **out, const SortTriples *device_sort = nullptr);
 
 // Device view of one predicate segment (passed to kernels by value).
 struct PredView {

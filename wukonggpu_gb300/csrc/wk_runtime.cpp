@@ -328,13 +328,27 @@ extern "C" int wk_sync(wk_ctx *ctx) {
     return e == cudaSuccess ? WK_OK : cuda_fail(e, "wk_sync");
 }
 
-extern "C" int wk_store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o,
-                              int64_t n, int32_t num_ids) {
-    if (!ctx) return set_error(WK_EINVAL, "wk_store_build: null ctx");
+namespace wk {
+int device_sort_triples(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
+                        uint32_t max_vid, uint32_t max_pid, std::vector<uint64_t> (&keys)[2],
+                        std::vector<uint32_t> (&pids)[2]);
+}
+
+static int store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
+                       int32_t num_ids, bool on_device) {
     int st;
     if (ctx->device >= 0 && (st = make_current(ctx))) return st;
     HostStore *hs = nullptr;
-    if ((st = build_host_store(s, p, o, n, num_ids, &hs)) != WK_OK) return st;
+    if (on_device) {
+        const SortTriples sorter = [&](uint32_t max_vid, uint32_t max_pid, std::vector<uint64_t> (&keys)[2],
+                                       std::vector<uint32_t> (&pids)[2]) {
+            return device_sort_triples(ctx, s, p, o, n, max_vid, max_pid, keys, pids);
+        };
+        st = build_host_store(s, p, o, n, num_ids, &hs, &sorter);
+    } else {
+        st = build_host_store(s, p, o, n, num_ids, &hs);
+    }
+    if (st != WK_OK) return st;
     auto ds = std::make_shared<DeviceStore>();
     ds->hs.reset(hs);
     ds->device = ctx->device;
@@ -346,6 +360,28 @@ extern "C" int wk_store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, c
     else st = ds->upload_resident();
     if (st != WK_OK) return st;
     ctx->store = ds;
+    return WK_OK;
+}
+
+extern "C" int wk_store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o,
+                              int64_t n, int32_t num_ids) {
+    if (!ctx) return set_error(WK_EINVAL, "wk_store_build: null ctx");
+    return store_build(ctx, s, p, o, n, num_ids, false);
+}
+
+extern "C" int wk_store_build_device(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o,
+                                     int64_t n, int32_t num_ids) {
+    if (!ctx) return set_error(WK_EINVAL, "wk_store_build_device: null ctx");
+    if (ctx->device < 0) return set_error(WK_EDEVICE, "wk_store_build_device: host-only context");
+    if (n >= (int64_t)0xffffffffll) return set_error(WK_EINVAL, "wk_store_build_device: %lld triples exceed 2^32 - 1",
+                                                     (long long)n);
+    return store_build(ctx, s, p, o, n, num_ids, true);
+}
+
+extern "C" int wk_store_digest(wk_ctx *ctx, uint64_t *digest) {
+    if (!ctx || !digest) return set_error(WK_EINVAL, "wk_store_digest: null");
+    if (!ctx->store) return set_error(WK_ENOSTORE, "wk_store_digest: no store");
+    *digest = ctx->store->hs->digest();
     return WK_OK;
 }
 

@@ -27,6 +27,7 @@
 #include <cstdlib>
 #include <atomic>
 #include <cstring>
+#include <functional>
 #include <thread>
 
 namespace wk {
@@ -71,6 +72,28 @@ uint64_t HostStore::lookup(uint64_t vid, uint32_t pid, uint32_t dir, const int32
         b = w[WK_LINK_WORD];
     }
     return 0;
+}
+
+// FNV-1a over the image (segment metadata, buckets, edges, offsets arrays):
+// two builds of the same triples give the same digest exactly when their
+// images are byte-identical.
+uint64_t HostStore::digest() const {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void *p, size_t n) {
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+    };
+    for (size_t id = 1; id < segs.size(); ++id) {
+        const PredSeg &g = segs[id];
+        const uint64_t meta[] = {g.bucket_off, g.nmain, g.nover, g.edge_off, g.nedges, g.nkeys, g.rp_off,
+                                 g.dvmin[0], g.dvmin[1], g.dn[0], g.dn[1], g.maxdeg[0], g.maxdeg[1],
+                                 g.bvmin[0], g.bvmin[1], g.bn[0], g.bn[1]};
+        mix(meta, sizeof(meta));
+    }
+    mix(buckets, total_buckets * sizeof(Bucket));
+    mix(edges, total_edges * 4);
+    mix(rowptr, total_rowptr * 4);
+    return h;
 }
 
 namespace {
@@ -195,28 +218,40 @@ void split_dense(SegBuild &sb) {
     sb.keys.swap(hashed);
 }
 
-// Sort (hi,lo) pairs packed as hi<<32|lo, dedup, and emit one key per hi
-// group with the group's lo values as the adjacency list.
-void emit_groups(std::vector<uint64_t> &pairs, uint32_t dir, SegBuild &sb,
-                 std::vector<int32_t> *distinct_hi) {
-    std::sort(pairs.begin(), pairs.end());
-    pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
-    size_t i = 0, n = pairs.size();
+// From (hi,lo) pairs packed as hi<<32|lo, sorted, duplicates allowed: one key
+// per hi group with the group's distinct lo values as the adjacency list.
+// Returns the number of distinct pairs.
+size_t emit_sorted(const uint64_t *a, size_t n, uint32_t dir, SegBuild &sb, std::vector<int32_t> *distinct_hi) {
+    size_t i = 0, uniq = 0;
     while (i < n) {
-        uint32_t hi = (uint32_t)(pairs[i] >> 32);
-        size_t j = i;
+        const uint32_t hi = (uint32_t)(a[i] >> 32);
         KeyRec kr;
         kr.key = seg_key(hi, dir);
         kr.off = (uint32_t)sb.edges.size();
-        while (j < n && (uint32_t)(pairs[j] >> 32) == hi) {
-            sb.edges.push_back((int32_t)(uint32_t)pairs[j]);
+        size_t j = i;
+        uint64_t prev = ~0ull;
+        while (j < n && (uint32_t)(a[j] >> 32) == hi) {
+            if (a[j] != prev) {
+                sb.edges.push_back((int32_t)(uint32_t)a[j]);
+                prev = a[j];
+                ++uniq;
+            }
             ++j;
         }
-        kr.deg = (uint32_t)(j - i);
+        kr.deg = (uint32_t)(sb.edges.size() - kr.off);
         sb.keys.push_back(kr);
         if (distinct_hi) distinct_hi->push_back((int32_t)hi);
         i = j;
     }
+    return uniq;
+}
+
+// Sort (hi,lo) pairs, dedup, and emit them as emit_sorted does.
+void emit_groups(std::vector<uint64_t> &pairs, uint32_t dir, SegBuild &sb,
+                 std::vector<int32_t> *distinct_hi) {
+    std::sort(pairs.begin(), pairs.end());
+    pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+    emit_sorted(pairs.data(), pairs.size(), dir, sb, distinct_hi);
 }
 
 void add_index(uint32_t dir, const std::vector<int32_t> &list, SegBuild &sb) {
@@ -249,12 +284,14 @@ void parallel_for(size_t n, F f) {
 }  // namespace
 
 int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
-                     int32_t num_ids, HostStore **out) {
+                     int32_t num_ids, HostStore **out, const SortTriples *device_sort) {
     if (n < 0 || (n > 0 && (!s || !p || !o)) || num_ids < 1 || num_ids >= WK_VID_BASE)
         return set_error(WK_EINVAL, "store build: bad arguments (n=%lld, num_ids=%d)", (long long)n, num_ids);
     // validate and bucket triples by predicate (counting sort)
     std::vector<int64_t> cnt((size_t)num_ids + 2, 0);
+    uint32_t max_vid = 0;
     for (int64_t i = 0; i < n; ++i) {
+        max_vid = std::max(max_vid, (uint32_t)std::max(s[i], o[i]));
         int32_t pi = p[i];
         if (pi < 1 || pi > num_ids)
             return set_error(WK_EINVAL, "store build: triple %lld has predicate %d outside [1,%d]",
@@ -274,8 +311,17 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
     }
     std::vector<int64_t> start((size_t)num_ids + 2, 0);
     for (int32_t i = 1; i <= num_ids + 1; ++i) start[(size_t)i] = start[(size_t)i - 1] + cnt[(size_t)i - 1];
-    std::vector<uint64_t> so((size_t)n);       // packed s<<32|o, grouped by p
-    {
+    // Either the triples sorted by (p, s, o) and (p, o, s) on the device
+    // (order k in keys[k], each id's run at [start[id], start[id + 1])), or the
+    // host's counting sort by p, whose runs emit_groups sorts per id.
+    std::vector<uint64_t> keys[2];
+    std::vector<uint32_t> kpid[2];
+    std::vector<uint64_t> so;       // host path: packed s<<32|o, grouped by p
+    if (device_sort) {
+        int st = (*device_sort)(max_vid, (uint32_t)num_ids, keys, kpid);
+        if (st) return st;
+    } else {
+        so.resize((size_t)n);
         std::vector<int64_t> at(start);
         for (int64_t i = 0; i < n; ++i)
             so[(size_t)at[(size_t)p[i]]++] = ((uint64_t)(uint32_t)s[i] << 32) | (uint32_t)o[i];
@@ -286,14 +332,21 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
     std::vector<std::vector<int32_t>> class_members((size_t)num_ids + 1);
     {
         const int64_t a = start[WK_TYPE_ID], b = start[WK_TYPE_ID + 1];
-        std::vector<uint64_t> out_pairs(so.begin() + a, so.begin() + b);
-        emit_groups(out_pairs, WK_DIR_OUT, sb[WK_TYPE_ID], nullptr);
-        sb[WK_TYPE_ID].triples = (int64_t)out_pairs.size();
-        sb[WK_TYPE_ID].subjects = (int64_t)sb[WK_TYPE_ID].keys.size();
         std::vector<uint64_t> cs;
-        cs.reserve(out_pairs.size());
-        for (uint64_t x : out_pairs) cs.push_back(((x & 0xffffffffull) << 32) | (x >> 32));
-        std::sort(cs.begin(), cs.end());
+        if (device_sort) {
+            sb[WK_TYPE_ID].triples = (int64_t)emit_sorted(keys[0].data() + a, (size_t)(b - a), WK_DIR_OUT,
+                                                          sb[WK_TYPE_ID], nullptr);
+            cs.assign(keys[1].begin() + a, keys[1].begin() + b);   // (class, s), sorted
+            cs.erase(std::unique(cs.begin(), cs.end()), cs.end());
+        } else {
+            std::vector<uint64_t> out_pairs(so.begin() + a, so.begin() + b);
+            emit_groups(out_pairs, WK_DIR_OUT, sb[WK_TYPE_ID], nullptr);
+            sb[WK_TYPE_ID].triples = (int64_t)out_pairs.size();
+            cs.reserve(out_pairs.size());
+            for (uint64_t x : out_pairs) cs.push_back(((x & 0xffffffffull) << 32) | (x >> 32));
+            std::sort(cs.begin(), cs.end());
+        }
+        sb[WK_TYPE_ID].subjects = (int64_t)sb[WK_TYPE_ID].keys.size();
         for (uint64_t x : cs) class_members[(size_t)(x >> 32)].push_back((int32_t)(uint32_t)x);
     }
     // normal predicates in parallel
@@ -301,12 +354,18 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         if (id == 0) return;
         SegBuild &b = sb[id];
         if (id != WK_TYPE_ID && cnt[id] > 0) {
-            std::vector<uint64_t> pairs(so.begin() + start[id], so.begin() + start[id + 1]);
             std::vector<int32_t> subjects, objects;
-            emit_groups(pairs, WK_DIR_OUT, b, &subjects);
-            b.triples = (int64_t)pairs.size();
-            for (auto &x : pairs) x = ((x & 0xffffffffull) << 32) | (x >> 32);
-            emit_groups(pairs, WK_DIR_IN, b, &objects);
+            if (device_sort) {
+                const size_t a0 = (size_t)start[id], len = (size_t)(start[id + 1] - start[id]);
+                b.triples = (int64_t)emit_sorted(keys[0].data() + a0, len, WK_DIR_OUT, b, &subjects);
+                emit_sorted(keys[1].data() + a0, len, WK_DIR_IN, b, &objects);
+            } else {
+                std::vector<uint64_t> pairs(so.begin() + start[id], so.begin() + start[id + 1]);
+                emit_groups(pairs, WK_DIR_OUT, b, &subjects);
+                b.triples = (int64_t)pairs.size();
+                for (auto &x : pairs) x = ((x & 0xffffffffull) << 32) | (x >> 32);
+                emit_groups(pairs, WK_DIR_IN, b, &objects);
+            }
             add_index(WK_DIR_IN, subjects, b);    // [0|p|IN]  subjects of p
             add_index(WK_DIR_OUT, objects, b);    // [0|p|OUT] objects of p
             b.subjects = (int64_t)subjects.size();
@@ -319,6 +378,10 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         }
     });
     std::vector<uint64_t>().swap(so);
+    for (int k = 0; k < 2; ++k) {
+        std::vector<uint64_t>().swap(keys[k]);
+        std::vector<uint32_t>().swap(kpid[k]);
+    }
     parallel_for((size_t)num_ids + 1, [&](size_t id) {
         if (id) split_dense(sb[id]);
     });
