@@ -5,10 +5,12 @@
 // new table.  No tensor cores are involved.
 //
 //   k2u     : count (probe; per-row degree and edge offset; per-block output
-//             count; op total) -> plan (one CTA: every block's output prefix
-//             and its number of slices of at most kSliceRows output rows) ->
-//             the host reads the totals and sizes the output -> expand (one
-//             CTA per slice: the block's local scan, the slice's rows written)
+//             count; per-group sums of output rows and of slices, a slice
+//             being at most kSliceRows output rows of one block) -> the host
+//             adds up the group sums, sizes the output and passes the groups'
+//             prefixes -> expand (one CTA per slice: finds its block from the
+//             group prefixes and the group's block counts, the block's local
+//             scan, the slice's rows written)
 //   k2k/k2c : probe + membership (per-row ballot masks; per-block count; op
 //             total) -> filtered copy (per input block: output prefix by
 //             look-back, selected rows copied)
@@ -123,10 +125,15 @@ constexpr int kRounds = kRowsPerBlock / (kThreads / 32) / 32;
 template <bool FUNC, bool DENSE, int BPC>
 __global__ void __launch_bounds__(kThreads, (DENSE && FUNC) ? 8 : 6)
 k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *__restrict__ deg, uint32_t *__restrict__ off,
-                 unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ group_sums, int *err) {
+                 unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ group_sums, int *err,
+                 unsigned long long *__restrict__ clear, int64_t nclear) {
     constexpr int NR = kRounds * BPC;   // rounds of 32 rows per warp
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t b0 = (int64_t)blockIdx.x * BPC;
+    // the other sums buffer, read by the previous op's expansion, is cleared
+    // for the next op (a few hundred words at most)
+    for (int64_t w = (int64_t)blockIdx.x * kThreads + threadIdx.x; w < nclear; w += (int64_t)gridDim.x * kThreads)
+        clear[w] = 0ull;
     const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
     // round rd: block b0 + rd / kRounds, the warp's rows 32 (rd % kRounds) + lane
     auto row_at = [&](int rd) -> int64_t {
@@ -229,7 +236,7 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
         if (b < nblk) {
             blk_sum[b] = sum;
             // group sums spread the atomics over many addresses (256 blocks each);
-            // the op total comes from the plan kernel, so no address takes one per block
+            // the host adds them up for the op totals, so no address takes one per block
             if (sum) {
                 unsigned long long *gs = group_sums + 2 * (b >> kGroupShift);
                 atomicAdd(gs, sum);
@@ -240,131 +247,108 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
     }
 }
 
-// -------------------------------------------------------------- k2u plan
-constexpr int kPlanThreads = 1024;
-constexpr int kPlanPer = (1 << kPlanTileShift) / kPlanThreads;   // blocks per thread: 8
+// ------------------------------------------------------- k2u slice location
+static_assert(kThreads == (1 << kGroupShift), "one thread per group and per block of a group");
 
-// exclusive scan of (a, b) pairs over the kPlanThreads threads of the CTA
-__device__ __forceinline__ void plan_scan2(unsigned long long &a, unsigned long long &b, unsigned long long &ta,
-                                           unsigned long long &tb) {
-    __shared__ unsigned long long sa[kPlanThreads / 32], sb[kPlanThreads / 32];
+// inclusive scan of (x, y) pairs over the CTA's threads; sw is free again
+// after the caller's next barrier
+__device__ __forceinline__ void cta_scan2(unsigned long long &x, unsigned long long &y,
+                                          unsigned long long (&sw)[2][kThreads / 32]) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned long long ia = a, ib = b;
 #pragma unroll
     for (int sh = 1; sh < 32; sh <<= 1) {
-        const unsigned long long xa = __shfl_up_sync(FULL, ia, sh), xb = __shfl_up_sync(FULL, ib, sh);
-        if (lane >= sh) { ia += xa; ib += xb; }
+        const unsigned long long ax = __shfl_up_sync(FULL, x, sh), ay = __shfl_up_sync(FULL, y, sh);
+        if (lane >= sh) { x += ax; y += ay; }
     }
-    if (lane == 31) { sa[wid] = ia; sb[wid] = ib; }
+    if (lane == 31) { sw[0][wid] = x; sw[1][wid] = y; }
     __syncthreads();
-    if (wid == 0) {
-        unsigned long long wa = sa[lane], wb = sb[lane];   // kPlanThreads / 32 == 32 warps
 #pragma unroll
-        for (int sh = 1; sh < 32; sh <<= 1) {
-            const unsigned long long xa = __shfl_up_sync(FULL, wa, sh), xb = __shfl_up_sync(FULL, wb, sh);
-            if (lane >= sh) { wa += xa; wb += xb; }
-        }
-        sa[lane] = wa;
-        sb[lane] = wb;
-    }
-    __syncthreads();
-    const unsigned long long pa = wid ? sa[wid - 1] : 0ull, pb = wid ? sb[wid - 1] : 0ull;
-    ta = sa[kPlanThreads / 32 - 1];
-    tb = sb[kPlanThreads / 32 - 1];
-    a = pa + ia - a;
-    b = pb + ib - b;
+    for (int w = 0; w < kThreads / 32 - 1; ++w)
+        if (w < wid) { x += sw[0][w]; y += sw[1][w]; }
 }
 
-// bp[b] = output rows of blocks before b, sp[b] = slices of blocks before b
-// (bp[nblk], sp[nblk] = the totals); totals[0] = output rows, totals[2] =
-// slices.  CTA c scans blocks [c 8192, (c + 1) 8192), thread t 8 consecutive
-// ones; the groups before the tile contribute their sums from the count
-// kernel, so no CTA waits on another.
-__global__ void __launch_bounds__(kPlanThreads)
-k2u_plan_kernel(const unsigned long long *__restrict__ blk_sum, int64_t nblk, unsigned long long *group_sums,
-                unsigned int *plan_done, unsigned long long *__restrict__ bp, unsigned long long *__restrict__ sp,
-                unsigned long long *__restrict__ totals) {
-    __shared__ unsigned long long s_po, s_ps;
-    __shared__ unsigned long long s_ga[kPlanThreads / 32], s_gb[kPlanThreads / 32];
-    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    const int64_t c = blockIdx.x;
-    {
-        // the groups of all earlier tiles, summed by the whole CTA
-        const int64_t ng = c << (kPlanTileShift - kGroupShift);
-        unsigned long long po = 0, ps = 0;
-        for (int64_t k = t; k < ng; k += kPlanThreads) {
-            po += group_sums[2 * k];
-            ps += group_sums[2 * k + 1];
+struct SliceLoc {
+    int64_t b;              // the input block
+    unsigned long long P;   // output rows of the blocks before it
+    uint32_t T;             // its output rows
+    uint32_t slice;         // the slice's index within the block
+};
+
+// Where expansion CTA k works: the group whose slices cover k, then the
+// block within it (a scan of the group's 256 block counts).  The group comes
+// from the host's table when the op has one (a uniform binary search, every
+// read a broadcast from the parameter bank), else from a scan of the count
+// kernel's group sums, 256 groups per pass.  Every non-empty block has
+// slices_of(count) slices, in block order.  b is -1 if k is not below the
+// op's slice total.
+__device__ __forceinline__ SliceLoc locate_slice(unsigned long long k, const unsigned long long *__restrict__ blk_sum,
+                                                 const unsigned long long *__restrict__ group_sums, int64_t ngroups,
+                                                 int64_t nblk, const GroupTable &gt) {
+    __shared__ unsigned long long sw[2][kThreads / 32];
+    __shared__ unsigned long long s_tot[2];
+    __shared__ int64_t s_g;
+    __shared__ SliceLoc s_loc;
+    const int t = threadIdx.x;
+    SliceLoc none;
+    none.b = -1;
+    if (t == 0) s_loc.b = -1;
+    int64_t g;
+    unsigned long long opg, spg;
+    if (gt.n > 0) {
+        if (k >= gt.sl[gt.n]) return none;   // the same in every thread
+        int lo = 0, hi = gt.n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (gt.sl[mid] <= k) lo = mid;
+            else hi = mid - 1;
         }
-        po = warp_sum(po);
-        ps = warp_sum(ps);
-        if (lane == 0) {
-            s_ga[wid] = po;
-            s_gb[wid] = ps;
-        }
-        __syncthreads();
-        if (wid == 0) {
-            po = warp_sum(s_ga[lane]);
-            ps = warp_sum(s_gb[lane]);
-            if (lane == 0) {
-                s_po = po;
-                s_ps = ps;
-            }
-        }
-    }
-    const int64_t b0 = ((int64_t)c << kPlanTileShift) + (int64_t)t * kPlanPer;
-    unsigned long long T[kPlanPer];
-    if (b0 + kPlanPer <= nblk) {
-        // b0 is a multiple of 8 entries: four aligned 16 B loads
-#pragma unroll
-        for (int q = 0; q < kPlanPer; q += 2) {
-            const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(blk_sum + b0 + q);
-            T[q] = x.x;
-            T[q + 1] = x.y;
-        }
+        g = lo;
+        opg = gt.out[lo];
+        spg = gt.sl[lo];
     } else {
-#pragma unroll
-        for (int q = 0; q < kPlanPer; ++q) T[q] = b0 + q < nblk ? blk_sum[b0 + q] : 0ull;
-    }
-    unsigned long long so = 0, ss = 0;
-#pragma unroll
-    for (int q = 0; q < kPlanPer; ++q) {
-        so += T[q];
-        ss += slices_of(T[q]);
-    }
-    unsigned long long to, tsl;
-    plan_scan2(so, ss, to, tsl);   // its barriers also publish s_po / s_ps
-    so += s_po;
-    ss += s_ps;
-#pragma unroll
-    for (int q = 0; q < kPlanPer; ++q) {
-        if (b0 + q < nblk) {
-            bp[b0 + q] = so;
-            sp[b0 + q] = ss;
+        unsigned long long op = 0ull, sp = 0ull;   // sums of the groups before the pass
+        for (int64_t g0 = 0;; g0 += kThreads) {
+            const int64_t gi = g0 + t;
+            const unsigned long long x0 = gi < ngroups ? group_sums[2 * gi] : 0ull;
+            const unsigned long long y0 = gi < ngroups ? group_sums[2 * gi + 1] : 0ull;
+            unsigned long long x = x0, y = y0;
+            cta_scan2(x, y, sw);
+            if (t == kThreads - 1) { s_tot[0] = x; s_tot[1] = y; }
+            // the groups that end at or before slice k are a prefix of the pass
+            const int before = __syncthreads_count(gi < ngroups && sp + y <= k);
+            if (before < kThreads) {
+                if (t == before) {
+                    s_tot[0] = op + x - x0;
+                    s_tot[1] = sp + y - y0;
+                    s_g = gi < ngroups ? gi : -1;
+                }
+                __syncthreads();
+                break;
+            }
+            op += s_tot[0];
+            sp += s_tot[1];
+            __syncthreads();   // s_tot and sw are written again by the next pass
         }
-        so += T[q];
-        ss += slices_of(T[q]);
+        g = s_g;
+        if (g < 0) return none;   // the same in every thread
+        opg = s_tot[0];
+        spg = s_tot[1];
     }
-    if (c == (int64_t)gridDim.x - 1 && t == 0) {
-        bp[nblk] = s_po + to;
-        sp[nblk] = s_ps + tsl;
-        totals[0] = s_po + to;
-        totals[2] = s_ps + tsl;
+    const unsigned long long kk = k - spg;
+    const int64_t bi = (g << kGroupShift) + t;
+    const unsigned long long x0 = bi < nblk ? blk_sum[bi] : 0ull;
+    const unsigned long long y0 = slices_of(x0);
+    unsigned long long x = x0, y = y0;
+    cta_scan2(x, y, sw);
+    const int before = __syncthreads_count(bi < nblk && y <= kk);
+    if (t == before && bi < nblk) {
+        s_loc.b = bi;
+        s_loc.P = opg + x - x0;
+        s_loc.T = (uint32_t)x0;   // below 2^31 (the count kernel flags larger blocks)
+        s_loc.slice = (uint32_t)(kk - (y - y0));
     }
-    // the last CTA to finish zeroes the group sums for the next op (every CTA
-    // has read the groups it needs by then); the counter is reset with them
-    __shared__ bool s_last;
     __syncthreads();
-    if (t == 0) {
-        __threadfence();
-        s_last = atomicAdd(plan_done, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (s_last) {
-        const int64_t ng = (nblk + (1 << kGroupShift) - 1) >> kGroupShift;
-        for (int64_t k = t; k < 2 * ng; k += kPlanThreads) group_sums[k] = 0ull;
-        if (t == 0) *plan_done = 0u;
-    }
+    return s_loc;
 }
 
 // -------------------------------------------------------------- k2u expand
@@ -389,25 +373,36 @@ __device__ __forceinline__ int row_of(const uint32_t *pos, int n, uint32_t j) {
 // last group of a block may be partial.
 template <int W>
 __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint32_t span, const uint32_t *pos,
-                                                const uint32_t *eoff, int n, const int32_t *__restrict__ rows,
+                                                const uint32_t *erel, int n, const int32_t *__restrict__ rows,
                                                 const int32_t *__restrict__ edges, int32_t *__restrict__ obase) {
     constexpr int C = W - 1;
     int i = row_of(pos, n, u >= lead ? u - lead : 0u);
     uint32_t nxt = pos[i + 1];
     int32_t v[4 * W];
+    int ip = -1;       // input row of the previous output row of the group, if valid
+    uint32_t er = 0;   // erel[ip]
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const uint32_t uq = u + (uint32_t)q;
         if (uq >= lead && uq < span) {
             const uint32_t j = uq - lead;
             while (j >= nxt) nxt = pos[++i + 1];
-            const int32_t *src = rows + i * C;
+            if (q > 0 && i == ip) {
+                // the same input row as the previous output row: copied from registers
 #pragma unroll
-            for (int c = 0; c < C; ++c) v[q * W + c] = __ldg(src + c);
-            v[q * W + C] = __ldg(edges + (eoff[i] + (j - pos[i])));
+                for (int c = 0; c < C; ++c) v[q * W + c] = v[(q - 1) * W + c];
+            } else {
+                const int32_t *src = rows + i * C;
+#pragma unroll
+                for (int c = 0; c < C; ++c) v[q * W + c] = __ldg(src + c);
+                er = erel[i];
+            }
+            v[q * W + C] = __ldg(edges + (er + j));
+            ip = i;
         } else {
 #pragma unroll
             for (int c = 0; c < W; ++c) v[q * W + c] = 0;
+            ip = -1;
         }
     }
     int32_t *g = obase + (size_t)u * W;
@@ -428,47 +423,36 @@ __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint3
 }
 
 // One CTA per slice: CTA k writes local rows [k' kSliceRows, (k' + 1)
-// kSliceRows) of block b, where sp[b] <= k < sp[b + 1] and k' = k - sp[b].
-// Every warp finds b itself (a 32-way search over sp), so no warp waits for
-// another before loading the block's degrees.  W = C + 1 output columns for
+// kSliceRows) of block b, where block b's slices are numbered from s_b (the
+// slices of the blocks before it) and k' = k - s_b; locate_slice finds b, s_b
+// and the block's output prefix.  W = C + 1 output columns for
 // 2 <= W <= 8; W = 0 for any width (one output row per thread and step,
 // scalar stores).  History rows are read through L1 (consecutive output rows
 // of one input row reuse it).
 // CTAs per SM the register budget is set for: the widest instantiations need
 // more registers to avoid spills
 template <int W>
-constexpr int expand_min_ctas() { return (W >= 2 && W <= 4) || W == 0 ? 8 : (W <= 7 ? 6 : 4); }
+constexpr int expand_min_ctas() { return (W >= 2 && W <= 4) || W == 0 ? 8 : (W <= 5 ? 6 : (W <= 7 ? 5 : 4)); }
 
 template <int W>
 __global__ void __launch_bounds__(kThreads, expand_min_ctas<W>())
 k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const int32_t *__restrict__ edges,
                   const uint32_t *__restrict__ deg, const uint32_t *__restrict__ off,
-                  const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ bp,
-                  const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out) {
+                  const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ group_sums,
+                  int64_t ngroups, int64_t nblk, const __grid_constant__ GroupTable gt, int32_t *__restrict__ out) {
     constexpr int kRPT = kRowsPerBlock / kThreads;
     static_assert(kRPT == 4, "4 input rows per thread");
     __shared__ uint32_t pos[kRowsPerBlock + 1];
-    __shared__ uint32_t eoff[kRowsPerBlock];
+    __shared__ uint32_t erel[kRowsPerBlock];   // a row's list offset minus its first output row
     __shared__ uint32_t s_w[kThreads / 32];
     const int C = W >= 2 ? W - 1 : C_rt;
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    const unsigned long long k = blockIdx.x;
 
-    // 1. the block: last b in [0, nblk) with sp[b] <= k (an empty block's sp equals its successor's)
-    int64_t lo = 0, hi = nblk - 1;
-    while (hi > lo) {
-        const int64_t step = (hi - lo + 32) / 32;
-        int64_t bl = lo + (int64_t)lane * step;   // lane 0 probes lo, which qualifies
-        if (bl > hi) bl = hi;
-        const unsigned m = __ballot_sync(FULL, sp[bl] <= k);
-        const int L = 31 - __clz(m);
-        const int64_t blo = __shfl_sync(FULL, bl, L);
-        const int64_t bnx = L < 31 ? __shfl_sync(FULL, bl, L + 1) : hi + 1;
-        lo = blo;
-        hi = bnx > blo ? bnx - 1 : blo;
-    }
-    const int64_t b = lo;
-    const uint32_t slice = (uint32_t)(k - sp[b]);
+    // 1. the slice's block, the block's output prefix and count
+    const SliceLoc loc = locate_slice(blockIdx.x, blk_sum, group_sums, ngroups, nblk, gt);
+    if (loc.b < 0) return;   // the same in every thread
+    const int64_t b = loc.b;
+    const uint32_t slice = loc.slice;
     const int64_t r0 = b * kRowsPerBlock;
     const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
 
@@ -503,13 +487,13 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
 #pragma unroll
     for (int q = 0; q < kRPT; ++q) {
         pos[q0 + q] = e;
-        eoff[q0 + q] = o[q];
+        erel[q0 + q] = o[q] - e;   // modulo 2^32: erel + j is the entry's index
         e += d[q];
     }
     if (t == kThreads - 1) pos[kRowsPerBlock] = e;   // the block's total; rows >= n have no list
     __syncthreads();
-    const unsigned long long P = bp[b];
-    const uint32_t T = (uint32_t)blk_sum[b];   // below 2^31 (the count kernel flags larger blocks)
+    const unsigned long long P = loc.P;
+    const uint32_t T = loc.T;
     const int32_t *hblk = hist + r0 * C;
 
     // 3. the slice's share of output rows [P, P + T)
@@ -519,7 +503,7 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
         const uint32_t u1 = u0 >= span ? u0 : (span - u0 < (uint32_t)kSliceRows ? span : u0 + (uint32_t)kSliceRows);
         int32_t *obase = out + (P - lead) * W;
         for (uint32_t u = u0 + 4u * (uint32_t)t; u < u1; u += 4u * kThreads)
-            k2u_write_group<W>(u, lead, span, pos, eoff, n, hblk, edges, obase);
+            k2u_write_group<W>(u, lead, span, pos, erel, n, hblk, edges, obase);
     } else {
         const int Wd = C + 1;
         int32_t *oblk = out + P * Wd;
@@ -530,7 +514,7 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
             int32_t *dst = oblk + (size_t)j * Wd;
             const int32_t *src = hblk + (int64_t)i * C;
             for (int c = 0; c < C; ++c) dst[c] = __ldg(src + c);
-            dst[C] = __ldg(edges + (eoff[i] + (j - pos[i])));
+            dst[C] = __ldg(edges + (erel[i] + j));
         }
     }
 }
@@ -547,29 +531,19 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
 template <int W>
 __global__ void __launch_bounds__(kThreads)
 k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_t *__restrict__ nbr,
-                       const unsigned long long *__restrict__ blk_sum, const unsigned long long *__restrict__ bp,
-                       const unsigned long long *__restrict__ sp, int64_t nblk, int32_t *__restrict__ out) {
+                       const unsigned long long *__restrict__ blk_sum,
+                       const unsigned long long *__restrict__ group_sums, int64_t ngroups, int64_t nblk,
+                       const __grid_constant__ GroupTable gt, int32_t *__restrict__ out) {
     constexpr int C = W - 1;
     constexpr int kPitch = W | 1;
     __shared__ int32_t rows[kRowsPerBlock * kPitch];
     __shared__ uint32_t s_w[kThreads / 32];
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    const unsigned long long k = blockIdx.x;
 
-    // the block: last b with sp[b] <= k (every non-empty block has one slice)
-    int64_t lo = 0, hi = nblk - 1;
-    while (hi > lo) {
-        const int64_t step = (hi - lo + 32) / 32;
-        int64_t bl = lo + (int64_t)lane * step;
-        if (bl > hi) bl = hi;
-        const unsigned m = __ballot_sync(FULL, sp[bl] <= k);
-        const int L = 31 - __clz(m);
-        const int64_t blo = __shfl_sync(FULL, bl, L);
-        const int64_t bnx = L < 31 ? __shfl_sync(FULL, bl, L + 1) : hi + 1;
-        lo = blo;
-        hi = bnx > blo ? bnx - 1 : blo;
-    }
-    const int64_t b = lo;
+    // the block (every non-empty block has one slice)
+    const SliceLoc loc = locate_slice(blockIdx.x, blk_sum, group_sums, ngroups, nblk, gt);
+    if (loc.b < 0) return;   // the same in every thread
+    const int64_t b = loc.b;
     const int64_t r0 = b * kRowsPerBlock;
     const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
 
@@ -607,8 +581,8 @@ k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_
     __syncthreads();
 
     // output words [P W, (P + T) W): int4 stores aligned to 16 B of out
-    const unsigned long long P = bp[b];
-    const uint32_t T = (uint32_t)blk_sum[b];
+    const unsigned long long P = loc.P;
+    const uint32_t T = loc.T;
     const uint32_t lead = (uint32_t)((P * W) & 3ull), words = T * W;
     int32_t *g = out + (P * W - lead);
     for (uint32_t i = (uint32_t)t; 4u * i < lead + words; i += kThreads) {
@@ -758,7 +732,7 @@ static inline unsigned int nblocks_rows(int64_t R) {
 }
 
 void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums,
-                      int *err, bool func, cudaStream_t st) {
+                      int *err, bool func, unsigned long long *clear, int64_t nclear, cudaStream_t st) {
     const bool dense = (dir ? pv.rp[1] : pv.rp[0]) != nullptr;
     const unsigned int nb = nblocks_rows(R);
     // two blocks per CTA once the op has enough blocks to fill the GPU with half as many CTAs
@@ -772,7 +746,7 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t 
     const bool pair = dense && nb >= 16u * (unsigned int)sms;
 #define WK_COUNT(F, D, B) \
     k2u_count_kernel<F, D, B><<<(nb + B - 1) / B, kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, \
-                                                                     group_sums, err)
+                                                                     group_sums, err, clear, nclear)
     if (func && dense) {
         if (pair) WK_COUNT(true, true, 2);
         else WK_COUNT(true, true, 1);
@@ -788,13 +762,14 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t 
 }
 
 void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
-                            const unsigned long long *blk_sum, const unsigned long long *bp,
-                            const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st) {
+                            const unsigned long long *blk_sum, const unsigned long long *group_sums,
+                            const GroupTable &gt, unsigned long long slices, int32_t *out, cudaStream_t st) {
     if (slices == 0ull) return;
     const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
+    const int64_t ng = (nblk + (1 << kGroupShift) - 1) >> kGroupShift;
     const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND_F(WC) \
-    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, bp, sp, nblk, out)
+    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, group_sums, ng, nblk, gt, out)
     switch (C + 1) {
         case 2: WK_EXPAND_F(2); break;
         case 3: WK_EXPAND_F(3); break;
@@ -807,21 +782,16 @@ void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t
 #undef WK_EXPAND_F
 }
 
-void launch_k2u_plan(const unsigned long long *blk_sum, int64_t nblk, unsigned long long *group_sums,
-                     unsigned int *plan_done, unsigned long long *bp, unsigned long long *sp, unsigned long long *totals,
-                     cudaStream_t st) {
-    const unsigned int g = (unsigned int)((nblk + (1 << kPlanTileShift) - 1) >> kPlanTileShift);
-    k2u_plan_kernel<<<g, kPlanThreads, 0, st>>>(blk_sum, nblk, group_sums, plan_done, bp, sp, totals);
-}
-
 void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edges, const uint32_t *deg,
-                       const uint32_t *off, const unsigned long long *blk_sum, const unsigned long long *bp,
-                       const unsigned long long *sp, unsigned long long slices, int32_t *out, cudaStream_t st) {
+                       const uint32_t *off, const unsigned long long *blk_sum, const unsigned long long *group_sums,
+                       const GroupTable &gt, unsigned long long slices, int32_t *out, cudaStream_t st) {
     if (slices == 0ull) return;
     const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
+    const int64_t ng = (nblk + (1 << kGroupShift) - 1) >> kGroupShift;
     const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND(WC) \
-    k2u_expand_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, C, edges, deg, off, blk_sum, bp, sp, nblk, out)
+    k2u_expand_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, C, edges, deg, off, blk_sum, group_sums, ng, nblk, gt, \
+                                                 out)
     switch (C + 1) {
         case 2: WK_EXPAND(2); break;
         case 3: WK_EXPAND(3); break;

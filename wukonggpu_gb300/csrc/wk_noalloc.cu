@@ -16,7 +16,7 @@
 //   - the array (about 2.1 MB) is held by every GPU that loads the library
 //     until the process exits;
 //   - every call shares it and it keeps the last call's contents: the fields
-//     that must start at zero (error flags and totals) are cleared at the
+//     that must start at zero (error flags and group sums) are cleared at the
 //     start of each call, everything else is fully written before it is read.
 //     Calls that overlap on the GPU (from several host threads or several
 //     contexts' streams at once) race on the array and must not be issued;
@@ -36,12 +36,11 @@ static_assert(kMaxBlocks <= (1 << wk::dev::kGroupShift), "one k2u group sum per 
 
 constexpr size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // byte layout of the scratch array
-constexpr size_t kOffFlags = 0;       // err (int), totals (3 x u64), group sums (2 x u64), plan counter
-constexpr size_t kOffDeg = al(kOffFlags + 64);
+constexpr size_t kOffFlags = 0;       // err (int, 16 B), the group's sums (output rows, slices)
+constexpr size_t kOffDeg = al(kOffFlags + 32);
 constexpr size_t kOffOff = al(kOffDeg + 4 * kMaxRows);
 constexpr size_t kOffBlkSum = al(kOffOff + 4 * kMaxRows);
-constexpr size_t kOffPlan = al(kOffBlkSum + 8 * kMaxBlocks);            // output and slice prefixes
-constexpr size_t kScratchBytes = al(kOffPlan + 16 * (kMaxBlocks + 1));
+constexpr size_t kScratchBytes = al(kOffBlkSum + 8 * kMaxBlocks);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -95,28 +94,26 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     int st = scratch_address(ctx->device, &sc);
     if (st) return st;
     int *err = reinterpret_cast<int *>(sc + kOffFlags);
-    unsigned long long *tot = reinterpret_cast<unsigned long long *>(sc + kOffFlags) + 1;
+    unsigned long long *gsum = reinterpret_cast<unsigned long long *>(sc + kOffFlags) + 2;
     uint32_t *deg = reinterpret_cast<uint32_t *>(sc + kOffDeg);
     uint32_t *off = reinterpret_cast<uint32_t *>(sc + kOffOff);
     unsigned long long *blk_sum = reinterpret_cast<unsigned long long *>(sc + kOffBlkSum);
-    const int64_t nblk = (rows + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
-    unsigned long long *bp = reinterpret_cast<unsigned long long *>(sc + kOffPlan), *sp = bp + (nblk + 1);
 
     const PredView pv = ctx->store->views[(size_t)predict];
     const int scol = (int)(-start - 1);
     cudaStream_t s = ctx->stream;
-    if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 56, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
-    // kMaxRows input rows are one group: its two sums follow the totals
-    dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, tot + 3, err, false, s);
-    dev::launch_k2u_plan(blk_sum, nblk, tot + 3, reinterpret_cast<unsigned int *>(tot + 5), bp, sp, tot, s);
+    if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 32, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
+    // kMaxRows input rows are one group: its two sums are the op's totals
+    dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, gsum, err, false,
+                          nullptr, 0, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: count launch");
-    ctx->launches += 2;
+    ctx->launches += 1;
     if ((e = cudaMemcpyAsync(ctx->h_scal, sc + kOffFlags, 32, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "noalloc: totals");
     if (ctx->h_scal[0] & 1ull)
         return set_error(WK_EDEVICE, "known_to_unknown_noalloc: corrupt overflow chain in the store");
-    const int64_t R_out = (int64_t)ctx->h_scal[1];
+    const int64_t R_out = (int64_t)ctx->h_scal[2];
     *out_rows = R_out;
     if (ctx->h_scal[0] & 2ull)
         return set_error(WK_EOVERFLOW, "known_to_unknown_noalloc: 1024 consecutive input rows expand to 2^31 rows or more");
@@ -126,7 +123,13 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
                          "known_to_unknown_noalloc: output needs %lld int32 elements, capacity is %lld "
                          "(*out_rows holds the row count)",
                          (long long)(R_out * (cols + 1)), (long long)out_capacity);
-    dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, bp, sp, ctx->h_scal[3], out, s);
+    dev::GroupTable gt;
+    gt.n = 1;
+    gt.out[0] = 0ull;
+    gt.sl[0] = 0u;
+    gt.out[1] = ctx->h_scal[2];
+    gt.sl[1] = (unsigned int)ctx->h_scal[3];   // at most 256 blocks' slices
+    dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, gsum, gt, ctx->h_scal[3], out, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: expand launch");
     ctx->launches += 1;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "noalloc: sync");

@@ -124,15 +124,34 @@ int fail_corrupt(wk_ctx *ctx) {
 }  // namespace
 
 namespace {
-// The k2u group sums and the plan kernel's done counter: zero when allocated,
-// and zeroed again by the plan kernel after every use.
+// The k2u sums buffers for ops of up to `groups` groups: zero when allocated
+// (both), then each count kernel clears the buffer it does not add into.
 int reserve_gsum(wk_ctx *ctx, int64_t groups) {
-    const size_t need = 16 + (size_t)groups * 16;
-    if (need <= ctx->gsum.cap) return WK_OK;
-    int st = ctx->gsum.reserve(need);
+    if (groups <= ctx->gs_groups) return WK_OK;
+    const int64_t want = std::max(groups, ctx->gs_groups + ctx->gs_groups / 2);
+    const size_t buf_bytes = 16 + (size_t)want * 16;
+    int st = ctx->gsum.reserve(2 * buf_bytes);
     if (st) return st;
     cudaError_t e = cudaMemsetAsync(ctx->gsum.ptr, 0, ctx->gsum.cap, ctx->stream);
-    return e == cudaSuccess ? WK_OK : cuda_fail(e, "k2u: clear group sums");
+    if (e != cudaSuccess) return cuda_fail(e, "k2u: clear group sums");
+    if (ctx->h_gs) cudaFreeHost(ctx->h_gs);
+    ctx->h_gs = nullptr;
+    ctx->h_gs_bytes = 0;
+    e = cudaHostAlloc((void **)&ctx->h_gs, buf_bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        ctx->h_gs = nullptr;
+        ctx->gs_groups = 0;
+        return cuda_fail(e, "k2u: pinned group sums");
+    }
+    ctx->h_gs_bytes = buf_bytes;
+    ctx->gs_groups = want;
+    ctx->gs_par = 0;
+    ctx->gs_used[0] = ctx->gs_used[1] = 0;
+    return WK_OK;
+}
+
+unsigned long long *gsum_buffer(wk_ctx *ctx, int par) {
+    return ctx->gsum.as<unsigned long long>() + (size_t)par * (size_t)(2 + 2 * ctx->gs_groups);
 }
 }  // namespace
 
@@ -159,7 +178,7 @@ int clear_totals(wk_ctx *ctx) {
     return e == cudaSuccess ? WK_OK : cuda_fail(e, "clear totals");
 }
 
-// two-pass k2u (count + plan -> host reads the totals -> expand)
+// two-pass k2u (count -> host adds up the group sums -> expand)
 int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     const int C = h->col_num;
     const int64_t R = h->size / C;
@@ -182,41 +201,54 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
     const int64_t groups = (nblk + (1 << dev::kGroupShift) - 1) >> dev::kGroupShift;
     if ((st = ctx->deg.reserve((size_t)R * 4)) || (st = ctx->off.reserve((size_t)R * 4)) ||
-        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16)) ||
-        (st = reserve_gsum(ctx, groups)))
+        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = reserve_gsum(ctx, groups)))
         return st;
-    unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
-    int *err = ctx->dscal.as<int>();
-    // block output prefixes and slice prefixes share the look-back scratch
-    unsigned long long *bp = ctx->lb_flags.as<unsigned long long>(), *sp = bp + (nblk + 1);
-    unsigned int *plan_done = ctx->gsum.as<unsigned int>();
-    unsigned long long *group_sums = ctx->gsum.as<unsigned long long>() + 2;
     // a functional direction (at most one neighbour per vertex) expands as a
     // compaction; if a row hits an index list (vertex 0) the op reruns unspecialised
     bool func = pv.func[dir] != 0u && C + 1 <= 8;
     int errf = 0;
-    // the plan kernel writes the op totals and zeroes the group sums after use,
-    // so nothing is cleared before the count kernel
+    unsigned long long *gs = nullptr;
     for (;;) {
+        const int par = ctx->gs_par;
+        gs = gsum_buffer(ctx, par);
         if ((st = clk.begin())) return st;
         dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
-                              ctx->blk_sum.as<unsigned long long>(), group_sums, err, func, ctx->stream);
-        dev::launch_k2u_plan(ctx->blk_sum.as<unsigned long long>(), nblk, group_sums, plan_done, bp, sp, tot,
-                             ctx->stream);
-        ++ctx->launches;   // the plan kernel, timed with the count
-        ++ctx->last.kernels;
+                              ctx->blk_sum.as<unsigned long long>(), gs + 2, reinterpret_cast<int *>(gs), func,
+                              gsum_buffer(ctx, par ^ 1), 2 + 2 * ctx->gs_used[par ^ 1], ctx->stream);
         if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;
-        if ((st = read_totals(ctx, &errf))) return st;
+        ctx->gs_par = par ^ 1;
+        ctx->gs_used[par ^ 1] = 0;
+        ctx->gs_used[par] = groups;
+        // the op's error flags and group sums: the host adds up the totals
+        cudaError_t e = cudaMemcpyAsync(ctx->h_gs, gs, (size_t)(16 + 16 * groups), cudaMemcpyDeviceToHost,
+                                        ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "k2u: group sums readback");
+        if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(e, "op sync");
+        errf = (int)(ctx->h_gs[0] & 0xffffffffull);
         if (!(func && (errf & 8))) break;
-        cudaMemsetAsync(ctx->dscal.ptr, 0, 8, ctx->stream);
-        func = false;
+        func = false;   // the next count adds into the other, cleared buffer
     }
-    if (errf & 1) return fail_corrupt(ctx);
-    if (errf & 2) {
-        cudaMemsetAsync(ctx->dscal.ptr, 0, 8, ctx->stream);
-        return set_error(WK_EOVERFLOW, "k2u: 1024 consecutive input rows expand to 2^31 rows or more");
+    if (errf & 1)
+        return set_error(WK_EDEVICE, "probe found an overflow chain longer than the segment's overflow area (corrupt store)");
+    if (errf & 2) return set_error(WK_EOVERFLOW, "k2u: 1024 consecutive input rows expand to 2^31 rows or more");
+    // the op totals, and the groups' prefixes for the expansion
+    dev::GroupTable gt;
+    gt.n = groups <= dev::kTableGroups ? (int)groups : 0;
+    unsigned long long rows_out = 0ull, slices = 0ull;
+    for (int64_t g = 0; g < groups; ++g) {
+        if (gt.n) {
+            gt.out[g] = rows_out;
+            gt.sl[g] = (unsigned int)slices;
+        }
+        rows_out += ctx->h_gs[2 + 2 * g];
+        slices += ctx->h_gs[3 + 2 * g];
     }
-    const int64_t R_out = (int64_t)ctx->h_scal[1];
+    if (slices >> 32) gt.n = 0;   // not reached: a slice holds up to 8192 of the output rows
+    if (gt.n) {
+        gt.out[gt.n] = rows_out;
+        gt.sl[gt.n] = (unsigned int)slices;
+    }
+    const int64_t R_out = (int64_t)rows_out;
     if (R_out > ctx->row_limit)
         return set_error(WK_EOVERFLOW, "k2u: %lld output rows exceed the context's row limit %lld", (long long)R_out,
                          (long long)ctx->row_limit);
@@ -229,10 +261,10 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         if ((st = clk.begin())) return st;
         if (func)
             dev::launch_k2u_expand_func(h->data, R, C, ctx->deg.as<int32_t>(), ctx->blk_sum.as<unsigned long long>(),
-                                        bp, sp, ctx->h_scal[3], ob.as<int32_t>(), ctx->stream);
+                                        gs + 2, gt, slices, ob.as<int32_t>(), ctx->stream);
         else
             dev::launch_k2u_expand(h->data, R, C, pv.edges, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
-                                   ctx->blk_sum.as<unsigned long long>(), bp, sp, ctx->h_scal[3], ob.as<int32_t>(),
+                                   ctx->blk_sum.as<unsigned long long>(), gs + 2, gt, slices, ob.as<int32_t>(),
                                    ctx->stream);
         if ((st = launch_check("k2u expand")) || (st = clk.end(true))) return st;
         if (ctx->timing) {

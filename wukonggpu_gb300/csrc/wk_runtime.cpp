@@ -239,6 +239,7 @@ wk_ctx::~wk_ctx() {
     deg.release(); off.release(); mask.release(); blk_sum.release(); blk_nz.release();
     lb_flags.release(); dscal.release();
     if (h_scal) cudaFreeHost(h_scal);
+    if (h_gs) cudaFreeHost(h_gs);
     for (auto &e : tev) cudaEventDestroy(e);
     if (use_ready) cudaEventDestroy(use_ready);
     if (tm0) cudaEventDestroy(tm0);

@@ -73,8 +73,16 @@ struct wk_ctx {
     wk::DevBuf hbuf[2];              // ping-pong history buffers (core/rcache.hpp:87-88)
     // scratch of the two-pass ops
     wk::DevBuf deg, off, mask, blk_sum, blk_nz;
-    wk::DevBuf lb_flags;             // per-block prefixes: k2u output and slice prefixes, filter look-back
-    wk::DevBuf gsum;                 // k2u: plan kernel's done counter (first 16 B) + group sums; kept zero
+    wk::DevBuf lb_flags;             // filter look-back words
+    // k2u: two alternating sums buffers, each a 16 B header (the op's error
+    // flags) and 16 B per group of 256 input blocks; a count kernel adds into
+    // one and clears the other for the next op
+    wk::DevBuf gsum;
+    int64_t gs_groups = 0;           // groups per buffer
+    int gs_par = 0;                  // the buffer the next count kernel adds into
+    int64_t gs_used[2] = {0, 0};     // groups written into each buffer since it was cleared
+    unsigned long long *h_gs = nullptr;   // pinned copy of one buffer
+    size_t h_gs_bytes = 0;
     wk::DevBuf dscal;                // [0] error flags, [8..32) totals
     unsigned long long *h_scal = nullptr;   // pinned mirror of the totals
 
