@@ -432,7 +432,7 @@ __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint3
 // CTAs per SM the register budget is set for: the widest instantiations need
 // more registers to avoid spills
 template <int W>
-constexpr int expand_min_ctas() { return (W >= 2 && W <= 4) || W == 0 ? 8 : (W <= 5 ? 6 : (W <= 7 ? 5 : 4)); }
+constexpr int expand_min_ctas() { return (W >= 2 && W <= 4) || W == 0 ? 8 : (W <= 7 ? 6 : 4); }
 
 template <int W>
 __global__ void __launch_bounds__(kThreads, expand_min_ctas<W>())
