@@ -56,8 +56,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="entity-count scale of the graph (1.0 = 2M)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="batched,estimator,serving",
-                    help="extra sections after the headline: batched, estimator, serving (comma list, or none)")
+    ap.add_argument("--sections", default="paged,batched,estimator,serving",
+                    help="extra sections after the headline: paged, batched, estimator, serving (comma list, or "
+                         "none)")
     ap.add_argument("--est-queries", type=int, default=200000,
                     help="random BGPs executed to train and test the estimator section's model")
     ap.add_argument("--serving-est-queries", type=int, default=4000,
@@ -72,6 +73,13 @@ def parse():
                          "(a fixed launch sequence for ncu captures)")
     ap.add_argument("--e2e-contexts", type=int, default=4,
                     help="contexts (one host thread each) that share the store in the end-to-end pass")
+    ap.add_argument("--parity-serving-scale", type=float, default=0.05,
+                    help="entity scale of the serving graph on which the serving mix is checked against the oracle")
+    ap.add_argument("--serving-mix", default="",
+                    help="mix file of the serving section (reference mix_config format); default: the packaged "
+                         "wukonggpu_gb300/mixes/serving/mix_config")
+    ap.add_argument("--clocks-csv", default="",
+                    help="where nvidia-smi clock samples are written (default: a temporary file)")
     return ap.parse_args()
 
 
@@ -116,10 +124,11 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device: int):
+    def __init__(self, device: int, path: str = ""):
+        import tempfile
         self.device = device
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_dev{device}.csv"
+        self.path = Path(path) if path else Path(tempfile.gettempdir()) / f"wk_bench_clocks_dev{device}_{os.getpid()}.csv"
 
     def __enter__(self):
         try:
@@ -205,29 +214,136 @@ def d2h_bandwidth(rc, pinned, n_int32: int, reps: int = 3) -> float:
     return reps * 4.0 * max(n_int32, 1) / (time.perf_counter() - t0) / 1e9
 
 
-def cpu_baseline(g, queries, nthreads: int, steps: int = 1):
-    """The oracle (C port of the reference store + CPU engine) on the mix; returns (qps, seconds, sample)."""
+def line_config(n_triples: int, n_entities: int, n_gpus: int, nq: int) -> dict:
+    """The workload's config dict, the same in both arms."""
+    return {"workload": WORKLOAD, "queries_per_step": nq, "triples": int(n_triples), "entities": int(n_entities),
+            "parallelism": f"replicas{n_gpus}",
+            "l2": "inputs larger than L2: the store and the histories exceed 129 MB",
+            "plans": "given (statistics/learned planners not in this line)"}
+
+
+def cpu_leg(rc, g, queries, nthreads: int, batch_sample=None, extra=None):
+    """The CPU leg: the oracle (a C port of the reference store and CPU engine)
+    timed on one pass over the mix with all host threads, and the same oracle
+    as the checker of the GPU's results.
+
+    * every query of the mix: the GPU's per-step row counts and the
+      order-independent digest of its final table against the oracle's (the
+      queries start from a type index, whose list order the reference leaves
+      to racing loader threads, so rows are compared as a multiset);
+    * the queries of each `extra` group (name -> queries) the same way;
+    * a sample of the batched light queries: rows equal, in order.
+    Returns (cpu_baseline dict, parity dict)."""
     import oracle
     s, p, o = g.arrays()
-    orc = oracle.Oracle(s, p, o, g.num_ids)
     t0 = time.perf_counter()
-    n = 0
-    for _ in range(steps):
-        for _, q in queries:
-            orc.execute(q, nthreads=nthreads)
-            n += 1
-    dt = time.perf_counter() - t0
+    orc = oracle.Oracle(s, p, o, g.num_ids)
+    build_s = time.perf_counter() - t0
+    secs = 0.0
+    bad = []
+    for name, q in queries:
+        req, grows = rc.execute(q)                  # the GPU result, downloaded
+        gd = oracle.rows_digest(req.result_table, nthreads)
+        req.result_table = None
+        a = time.perf_counter()
+        table, orows = orc.execute(q, nthreads=nthreads)
+        secs += time.perf_counter() - a
+        od = oracle.rows_digest(table, nthreads)
+        del table
+        if list(grows) != list(orows) or gd != od:
+            bad.append({"query": name, "gpu_rows": [int(x) for x in grows], "oracle_rows": [int(x) for x in orows]})
+    cpu = {"value": len(queries) / secs, "unit": "queries/s", "cores": nthreads, "kind": "port",
+           "sample": f"one pass over the {len(queries)}-query mix on the full graph, {nthreads} threads",
+           "seconds": secs, "oracle_build_s": build_s}
+    parity = {"single_query_mix": {"queries": len(queries), "mismatched": len(bad), "compared": "per-step rows and "
+                                   "order-independent digest of the final table", "mismatches": bad[:5]}}
+    for label, group in (extra or {}).items():
+        nbad = 0
+        for name, q in group:
+            req, grows = rc.execute(q)
+            gd = oracle.rows_digest(req.result_table, nthreads)
+            req.result_table = None
+            table, orows = orc.execute(q, nthreads=nthreads)
+            if list(grows) != list(orows) or gd != oracle.rows_digest(table, nthreads):
+                nbad += 1
+            del table
+        parity[label] = {"queries": len(group), "mismatched": nbad}
+    if batch_sample:
+        nb = 0
+        for q, got in batch_sample:
+            exp, _ = orc.execute(q)
+            if not np.array_equal(got.reshape(exp.shape) if got.size == 0 else got, exp):
+                nb += 1
+        parity["batched_sample"] = {"queries": len(batch_sample), "mismatched": nb, "compared": "rows, in order"}
     orc.close()
-    return n / dt, dt, f"{steps} pass(es) over the {len(queries)}-query mix on the full graph, {nthreads} threads"
+    return cpu, parity
+
+
+def parity_serving_scaled(device: int, scale: float, nthreads: int, n_req: int = 3000, mix_path: str = ""):
+    """The serving mix (the same weighted template mix as the serving
+    section) on a serving graph of the same generator with the entity count
+    times `scale` (the oracle of the 1e9-triple graph would need about 70 GB
+    of host memory for its 128 B buckets), run through the request loop in
+    serving mode (batched light requests, heavy workers) with statistics
+    plans; every result is checked against the oracle executing the same
+    plan: light requests (constant starts) row for row in order, heavy ones
+    (type-index starts) as a multiset digest."""
+    import oracle
+    import wukonggpu_gb300 as W
+    from wukonggpu_gb300 import workloads
+    if scale <= 0:
+        return None
+    g = W.Graph(W.spec_serving(scale=scale))
+    s, p, o = g.arrays()
+    n_triples = int(g.n)
+    layout = workloads.Layout(16, 32, 16, 15, int(g.spec.n_entities))
+    from wukonggpu_gb300 import mix as M
+    rc = W.RCache(device=device)
+    rc.build_store_graph(g)
+    mx = M.Mix(mix_path or (M.MIX_DIR / "serving" / "mix_config"), layout)
+    mx.fill_candidates(rc)
+    plans = []
+    for k, q in mx.draw(n_req, seed=23):
+        tq = M.Mix.triple_form(q) if mx.types[k].heavy else None
+        pq = rc.plan(tq)[0] if tq else None
+        plans.append(pq if pq else q)
+    srv = W.Server(rc, mode=1, plan=0, max_batch=1024, heavy_workers=2, batch_capacity_ints=1 << 26, keep_results=1)
+    arr = W.poisson_arrivals(len(plans), 20_000.0, seed=7)
+    ids = [srv.submit(q, float(t)) for q, t in zip(plans, arr)]
+    srv.start()
+    srv.drain(600)
+    st = srv.stats()
+    orc = oracle.Oracle(s, p, o, g.num_ids)
+    bad_l = bad_h = nl = nh = 0
+    for rid, q in zip(ids, plans):
+        got, _, status = srv.result(rid)
+        exp, _ = orc.execute(q)
+        if q[0] >= W.VID_BASE:
+            nl += 1
+            bad_l += 0 if status == 0 and np.array_equal(got.reshape(exp.shape) if got.size == 0 else got, exp) else 1
+        else:
+            nh += 1
+            bad_h += 0 if status == 0 and oracle.rows_digest(got) == oracle.rows_digest(exp) else 1
+    orc.close()
+    srv.close()
+    rc.close()
+    g.close()
+    return {"graph": f"serving generator at {scale} x 20M entities ({n_triples} triples)", "requests": len(plans),
+            "light": nl, "light_mismatched": bad_l, "heavy": nh, "heavy_mismatched": bad_h,
+            "mismatched": bad_l + bad_h, "batches": st["batches"], "failed": st["failed"]}
 
 
 def run_reference(args, dist):
+    # the graph comes from the generator library alone (libwkgen.so): this arm
+    # never loads the GPU library
     import wukonggpu_gb300 as W
+    from wukonggpu_gb300 import build as wb
     from wukonggpu_gb300 import workloads
     if dist.rank != 0:
         return
     import oracle
-    W.load_library()
+    if not W._GEN_LIB_PATH.exists():
+        wb.build()
     g = W.Graph(W.spec_single_query(scale=args.scale))
     s, p, o = g.arrays()
     queries = workloads.scale_queries()
@@ -249,7 +365,7 @@ def run_reference(args, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator, reference id encoding)",
-        "config": {"workload": WORKLOAD, "queries_per_step": len(queries), "triples": int(g.n)},
+        "config": line_config(g.n, g.spec.n_entities, args.gpus, len(queries)),
         "p50_ms": statistics.median(lat) * 1000, "p99_ms": float(np.percentile(lat, 99)) * 1000,
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port",
                          "sample": f"{args.steps} step(s) of the {len(queries)}-query mix on the full graph"},
@@ -306,13 +422,13 @@ def run_gb300(args, dist):
     t_store_host = time.perf_counter() - t0
     info = rc.store_info()
     t_setup = time.perf_counter() - t_setup
-    # the same store with its per-predicate sorts on the GPU: time and image identity
+    # the same store built on the GPU (wk_store_build_device): time and image identity
     gs, gp, go = g.arrays()
     x = W.RCache(device=dist.local)
     t0 = time.perf_counter()
-    x.build_store(gs, gp, go, g.num_ids, sort_on_device=True)
+    x.build_store(gs, gp, go, g.num_ids, on_device=True)
     t_store_dev = time.perf_counter() - t0
-    store_build = {"host_s": t_store_host, "device_sort_s": t_store_dev,
+    store_build = {"host_s": t_store_host, "device_s": t_store_dev,
                    "identical_image": x.store_digest() == rc.store_digest(), "graph_generation_s": t_graph}
     x.close()
     del gs, gp, go
@@ -328,7 +444,7 @@ def run_gb300(args, dist):
             if stats is not None:
                 stats.append(req)
 
-    clk = ClockSampler(dist.local).__enter__()
+    clk = ClockSampler(dist.local, args.clocks_csv).__enter__()
     for _ in range(args.warmup):
         one_step()
     rc.sync()
@@ -392,6 +508,36 @@ def run_gb300(args, dist):
                                       / (write_ms / 1000.0) / 1e9) if write_ms else None,
                 "expand_share_of_k2u_time": write_ms / k2u_ms if k2u_ms else None}
 
+    # ---- the filter group: the same shapes closed by known_to_known /
+    # known_to_const checks (not part of the headline mix), for the filter
+    # op's roofline, through the same wk_execute path with per-kernel events
+    fq = workloads.scale_filter_queries()
+    for _, q in fq:
+        rc.execute(q, download=False)
+    rc.enable_timing(True)
+    f_log = []
+    rc.sync()
+    for _ in range(args.steps):
+        for _, q in fq:
+            rc.execute(q, download=False)
+            f_log.extend(rc.query_op_stats())
+    rc.enable_timing(False)
+    flt = [op for op in f_log if op["kind"] in (1, 2) and op["rows_in"] > 0]
+    f_alg = sum(op["alg_bytes"] for op in flt)
+    f_ms = sum(op["ms"] for op in flt)
+    f_probe_ms = sum(op["ms_main"] for op in flt)
+    f_write_ms = f_ms - f_probe_ms
+    f_ach = f_alg / (f_ms / 1000.0) / 1e9 if f_ms > 0 else 0.0
+    roofline_filter = {"bound": "hbm", "achieved": f_ach, "peak": peak, "unit": "GB/s", "frac": f_ach / peak,
+                       "peak_source": peak_kind, "kernel": "k2k/k2c op (probe + write kernels)",
+                       "ops": len(flt), "rows_in_max": max((op["rows_in"] for op in flt), default=0),
+                       "alg_bytes_per_launch": f_alg / max(len(flt), 1),
+                       "write_kernel_gbs": (sum(8 * op["rows_out"] * op["cols_in"] for op in flt)
+                                            / (f_write_ms / 1000.0) / 1e9) if f_write_ms > 0 else None,
+                       "probe_share_of_op_time": f_probe_ms / f_ms if f_ms else None,
+                       "timing": "per-kernel CUDA events on the op stream; the filter group of "
+                                 f"{len(fq)} queries run {args.steps} times"}
+
     # ---- end to end through the C ABI with host buffers: the query goes in from
     # the host and its final table comes back to pinned host memory.  Four
     # contexts (--e2e-contexts) share the store and run alternate queries from
@@ -440,20 +586,16 @@ def run_gb300(args, dist):
     for x in ctxs[1:]:
         x.close()
 
-    # ---- CPU baseline (rank 0 only)
-    cpu = None
-    if dist.rank == 0 and not args.no_cpu_baseline:
-        nthreads = os.cpu_count() or 1
-        qps, secs, sample = cpu_baseline(g, queries, nthreads)
-        cpu = {"value": qps, "unit": "queries/s", "cores": nthreads, "kind": "port", "sample": sample,
-               "seconds": secs}
-
     sections = {}
+    batch_sample = None
     wanted = [x for x in args.sections.split(",") if x and x != "none"]
     if dist.rank == 0 and wanted:
         est = None
+        if "paged" in wanted:
+            sections["paged"] = section_paged(g, queries, int(info["device_bytes"]), value, dist.local)
         if "batched" in wanted:
             sections["batched"] = section_batched(rc, g)
+            batch_sample = sections["batched"].pop("_sample")
         if "estimator" in wanted or "serving" in wanted:
             r = section_estimator(rc, g, args.est_queries)
             est = r.pop("_estimator")
@@ -462,10 +604,21 @@ def run_gb300(args, dist):
         if "serving" in wanted:
             if args.serving_scale > 0:
                 sections["serving"] = section_serving_graph(dist.local, args.serving_scale, args.serving_est_queries,
-                                                            heavy_workers=args.heavy_workers)
+                                                            heavy_workers=args.heavy_workers, mix_path=args.serving_mix)
             else:
                 from wukonggpu_gb300 import workloads as _wl
-                sections["serving"] = section_serving(rc, _wl.SQ, est, heavy_workers=args.heavy_workers)
+                sections["serving"] = section_serving(rc, _wl.SQ, est, heavy_workers=args.heavy_workers,
+                                                      mix_path=args.serving_mix)
+
+    # ---- CPU leg (rank 0 only): the oracle timed as the baseline, and as the
+    # checker of the GPU's results
+    cpu = parity = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        cpu, parity = cpu_leg(rc, g, queries, nthreads, batch_sample, extra={"filter_group": fq})
+        if "serving" in wanted:
+            parity["serving_scaled"] = parity_serving_scaled(dist.local, args.parity_serving_scale, nthreads,
+                                                             mix_path=args.serving_mix)
 
     if dist.rank == 0:
         line = {
@@ -473,16 +626,15 @@ def run_gb300(args, dist):
             "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic (seeded generator, reference id encoding)",
-            "config": {"workload": WORKLOAD, "queries_per_step": nq, "triples": int(g.n),
-                       "entities": int(g.spec.n_entities), "parallelism": f"replicas{args.gpus}",
-                       "store_device_bytes": info["device_bytes"], "l2": "inputs larger than L2 "
-                       f"(store {info['device_bytes'] / 1e9:.1f} GB, histories up to "
-                       f"{maxrows * 4 / 1e9:.2f} GB)", "plans": "given (statistics/learned planners not in this line)",
-                       "setup_s": t_setup, "timed_wall_s": wall_s, "store_build": store_build},
+            "config": line_config(g.n, g.spec.n_entities, args.gpus, nq),
+            "setup": {"store_device_bytes": info["device_bytes"], "history_max_bytes": maxrows * 4,
+                      "setup_s": t_setup, "timed_wall_s": wall_s, "store_build": store_build},
+            "parity": parity,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "per_shape_ms": {sh: float(np.mean([x for i, x in enumerate(lat) if queries[i % nq][0].startswith(sh)]))
                              for sh in sorted({n.split("/")[0] for n, _ in queries})},
             "roofline": roofline,
+            "roofline_filter": roofline_filter,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d // args.steps,
                     "d2h_bytes_per_step": d2h // args.steps, "contexts": nctx,
@@ -496,6 +648,50 @@ def run_gb300(args, dist):
 
 
 # ---------------------------------------------------------------- sections
+def section_paged(g, queries, store_bytes: int, resident_qps: float, device: int, passes: int = 2):
+    """The single-query-scale mix with the store paged through a segment cache
+    smaller than the store (ShardManager, core/shard_manager.hpp:378-555):
+    budgets of 1/2 and 1/4 of the resident store's device bytes, with and
+    without prefetching the next pattern's segment on a side stream.  Each
+    configuration runs one untimed pass (the cache fills), then `passes`
+    timed passes; H2D GB/s is the segment bytes copied in the timed passes
+    over their wall time."""
+    import wukonggpu_gb300 as W
+    out = {"store_device_bytes": store_bytes, "resident_qps": resident_qps, "configs": []}
+    for frac in (0.5, 0.25):
+        for prefetch in (True, False):
+            budget_mb = max(1, int(store_bytes * frac) >> 20)
+            rc = W.RCache(device=device, cache_budget_mb=budget_mb, enable_prefetch=prefetch)
+            rc.build_store_graph(g)
+            for _, q in queries:
+                rc.execute(q, download=False)
+            rc.sync()
+            i0 = rc.store_info()
+            lat = []
+            t0 = time.perf_counter()
+            for _ in range(passes):
+                for _, q in queries:
+                    rc.timer_begin()
+                    rc.execute(q, download=False)
+                    lat.append(rc.timer_end())
+            rc.sync()
+            wall = time.perf_counter() - t0
+            i1 = rc.store_info()
+            req = i1["cache_requests"] - i0["cache_requests"]
+            hits = i1["cache_hits"] - i0["cache_hits"]
+            moved = i1["cache_bytes_loaded"] - i0["cache_bytes_loaded"]
+            out["configs"].append({
+                "budget_frac": frac, "budget_mb": budget_mb, "prefetch": prefetch,
+                "qps": len(lat) / (sum(lat) / 1000.0), "qps_wall": len(lat) / wall,
+                "loads": i1["cache_loads"] - i0["cache_loads"],
+                "evictions": i1["cache_evictions"] - i0["cache_evictions"],
+                "compactions": i1["cache_compactions"] - i0["cache_compactions"],
+                "hit_rate": hits / req if req else None, "h2d_bytes": moved, "h2d_gbs": moved / wall / 1e9,
+                "vs_resident": (len(lat) / (sum(lat) / 1000.0)) / resident_qps if resident_qps else None})
+            rc.close()
+    return out
+
+
 def section_batched(rc, g, nq: int = 4096, reps: int = 5):
     """Batched light queries (4096 constant-start queries of 1..4 patterns,
     one CUDA-graph replay per batch) against the same queries query-at-a-time."""
@@ -513,49 +709,56 @@ def section_batched(rc, g, nq: int = 4096, reps: int = 5):
     queries = [q for q, r in zip(cand, sizes) if 1 <= r <= 10_000][:nq]
     best_ms = b.autotune(queries, reps=3)
     tune = b.tuning()
-    packed = b.pack(queries)
     pinned = W.PinnedBuffer(1 << 26)
     rc.sync()
+    # each timed batch packs its queries, runs the graph and reads every result back
     lat = []
     t0 = time.perf_counter()
     for _ in range(reps):
         a = time.perf_counter()
-        k = b.run(queries, packed=packed)
+        k = b.run(queries)
         res = b.download(k, into=pinned)
         lat.append(time.perf_counter() - a)
     batched_s = time.perf_counter() - t0
     rows = [t.shape[0] for t in res]
-    # the same queries one at a time through wk_execute (host read of each result)
-    t0 = time.perf_counter()
-    qat = []
+    # the same queries one at a time, driven from C++: the request loop in
+    # query-at-a-time mode with every request present at the start (its
+    # capacity), each result read back to the host
+    srv = W.Server(rc, mode=0, plan=0, keep_results=1)
     for q in queries:
-        a = time.perf_counter()
-        req, _ = rc.execute(q)
-        qat.append(time.perf_counter() - a)
-    single_s = time.perf_counter() - t0
-    # exactness on a sample
+        srv.submit(q, 0.0)
+    srv.start()
+    srv.drain(600)
+    single = srv.stats()
+    srv.close()
+    single_s = single["span_s"]
+    # exactness on a sample: the same query alone through wk_execute here, and
+    # the oracle in the CPU leg (the "_sample" entry)
+    sample = list(range(0, len(queries), 8))
     exact = all(np.array_equal(rc.execute(queries[i])[0].result_table.reshape(res[i].shape) if res[i].size == 0
-                               else rc.execute(queries[i])[0].result_table, res[i]) for i in range(0, len(queries), 97))
-    return {"config": "4096 light constant-start queries of 1..4 patterns on the 100M-triple graph, "
+                               else rc.execute(queries[i])[0].result_table, res[i]) for i in sample[::12])
+    return {"_sample": [(queries[i], np.array(res[i])) for i in sample],
+            "config": "4096 light constant-start queries of 1..4 patterns on the 100M-triple graph, "
                       "final rows 1..1e4 (heavy-tailed)",
             "queries": len(queries), "rows_p50": float(np.median(rows)), "rows_max": int(max(rows)),
             "batched_qps": len(queries) * reps / batched_s, "batch_ms": float(np.median(lat) * 1e3),
             "device_graph_ms": best_ms, "tuning": {"blocks_per_sm": tune[0], "rows_per_warp": tune[1], "split": tune[2]},
-            "query_at_a_time_qps": len(queries) / single_s,
+            "query_at_a_time_qps": len(queries) / single_s, "query_at_a_time": "wk_server mode 0 (C++), all present",
+            "timed": "batched: pack + graph replay + download of every result per batch",
             "speedup": (len(queries) * reps / batched_s) / (len(queries) / single_s),
-            "bit_exact_sample": bool(exact), "gpu_launches_per_batch": 1 + 3 * 4}
+            "same_as_alone_sample": bool(exact), "gpu_launches_per_batch": 1 + 3 * 4}
 
 
 def _bindings_equal(oq, pa, ta, pb, tb):
     """Same bindings (original variables) from two plans' result tables."""
-    import oracle
+    import wukonggpu_gb300 as W
     from wukonggpu_gb300.plans import plan_columns
     ca, cb = plan_columns(oq, pa), plan_columns(oq, pb)
     if ca is None or cb is None:
         return False
     nv = len(ca)
-    A = oracle.canonical(ta[:, ca]) if ta.size else np.zeros((0, nv), np.int32)
-    B = oracle.canonical(tb[:, cb]) if tb.size else np.zeros((0, nv), np.int32)
+    A = W.canonical_rows(ta[:, ca]) if ta.size else np.zeros((0, nv), np.int32)
+    B = W.canonical_rows(tb[:, cb]) if tb.size else np.zeros((0, nv), np.int32)
     return bool(np.array_equal(A, B))
 
 
@@ -630,7 +833,8 @@ def _bindings_digest(table, cols):
         return (int(t.shape[0]), int(h.sum(dtype=np.uint64)))
 
 
-def section_serving_graph(device: int, scale: float, n_bgps: int, n_req: int = 20000, heavy_workers: int = 2):
+def section_serving_graph(device: int, scale: float, n_bgps: int, n_req: int = 20000, heavy_workers: int = 2,
+                          mix_path: str = ""):
     """The serving section on its own graph (20M entities x scale, 64 predicates,
     ~1e9 triples at 1.0): store, statistics, an estimator trained on BGPs
     executed on that graph, then section_serving."""
@@ -645,10 +849,10 @@ def section_serving_graph(device: int, scale: float, n_bgps: int, n_req: int = 2
     rc = W.RCache(device=device)
     t0 = time.perf_counter()
     gs, gp, go = g.arrays()
-    rc.build_store(gs, gp, go, g.num_ids, sort_on_device=True)   # per-predicate sorts on the GPU
+    rc.build_store(gs, gp, go, g.num_ids, on_device=True)   # the whole build on the GPU
     del gs, gp, go
     g.close()
-    setup["store_device_sort_s"] = time.perf_counter() - t0
+    setup["store_device_build_s"] = time.perf_counter() - t0
     info = rc.store_info()
     t0 = time.perf_counter()
     rc.stat(0, 1)   # the statistics are built on first use
@@ -664,7 +868,7 @@ def section_serving_graph(device: int, scale: float, n_bgps: int, n_req: int = 2
     ev = estimator.evaluate(est, te)
     p95_val, trusted = est.validate(te["feats"], te["pids"], te["target"], QERROR_BOUND_P95)
     setup["estimator_s"] = time.perf_counter() - t0
-    out = section_serving(rc, layout, est, n_req, heavy_workers)
+    out = section_serving(rc, layout, est, n_req, heavy_workers, mix_path)
     out["graph"] = {"triples": n_triples, "entities": layout.n_entities, "predicates": len(layout.preds),
                     "store_device_bytes": info["device_bytes"], "setup": setup,
                     "estimator": {"bgps": n_bgps, "qerror": ev, "held_out_qerror_p95": p95_val,
@@ -674,38 +878,42 @@ def section_serving_graph(device: int, scale: float, n_bgps: int, n_req: int = 2
     return out
 
 
-def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2):
-    """Open-loop Poisson arrivals, 95% light constant-start / 5% heavy type-index
-    requests: batched serving with learned plans against query-at-a-time with
-    statistics plans, at swept rates."""
+def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2, mix_path: str = ""):
+    """Open-loop Poisson arrivals of a weighted template mix in the reference
+    batch driver's format (light templates instantiated with random class
+    members, heavy type-index queries; default mixes/serving/mix_config:
+    95% light by weight): batched serving with learned plans against
+    query-at-a-time with statistics plans, at swept rates, with the
+    reference Logger's per-type statistics."""
     import wukonggpu_gb300 as W
-    from wukonggpu_gb300 import workloads
-    light = workloads.light_queries_store(rc, layout.n_entities, layout.preds, int(n_req * 0.95), seed=23)
-    heavy_shapes = workloads.serving_heavy_queries(layout)          # SPARQL triple form
-    heavy_exec = workloads.executable_heavy_queries(layout)         # the same shapes, executable
-    rng = np.random.default_rng(5)
-    # (query, what runs when a planner gives no plan): light queries are executable as written
-    mix = [(q, q) for q in light]
-    for _ in range(n_req - len(light)):
-        k = int(rng.integers(0, len(heavy_shapes)))
-        mix.append((heavy_shapes[k], heavy_exec[k]))
-    mix = [mix[i] for i in rng.permutation(len(mix))]
+    from wukonggpu_gb300 import mix as M
+    mx = M.Mix(mix_path or (M.MIX_DIR / "serving" / "mix_config"), layout)
+    mx.fill_candidates(rc)
+    reqs = mx.draw(n_req, seed=23)
+    # (type, SPARQL triple form for the planners or None, executable form):
+    # light templates are constant starts, executable as written
+    mix = [(k, M.Mix.triple_form(q) if mx.types[k].heavy else None, q) for k, q in reqs]
     t0 = time.perf_counter()
     stats_plans = []
-    for q, ex in mix:
-        pq, _ = rc.plan(q)
+    for k, tq, ex in mix:
+        pq = rc.plan(tq)[0] if tq else None
         stats_plans.append(pq if pq else ex)
     t_stats = (time.perf_counter() - t0) / len(mix)
     t0 = time.perf_counter()
-    lp = est.plan_many([q for q, _ in mix]) if est is not None else [[] for _ in mix]
-    learned_plans = [x if x else ex for x, (q, ex) in zip(lp, mix)]
+    planned = [i for i, (k, tq, ex) in enumerate(mix) if tq]
+    lp = est.plan_many([mix[i][1] for i in planned]) if (est is not None and planned) else [[] for _ in planned]
+    learned_plans = [ex for _, _, ex in mix]
+    for i, x in zip(planned, lp):
+        if x:
+            learned_plans[i] = x
     t_learned = (time.perf_counter() - t0) / len(mix)
-    # every heavy shape: its statistics and learned plans bind the same rows as its executable form
+    types = [k for k, _, _ in mix]
+    # every heavy query: its statistics and learned plans bind the same rows as its executable form
     from wukonggpu_gb300 import plans as _plans
     shape_plans = {}
-    for (q, ex), sp, lq in zip(mix, stats_plans, learned_plans):
-        if q is not ex:
-            shape_plans[tuple(q)] = (ex, sp, lq)
+    for (k, tq, ex), sp, lq in zip(mix, stats_plans, learned_plans):
+        if tq:
+            shape_plans[tuple(tq)] = (ex, sp, lq)
     checked = mismatched = 0
     for q, (ex, sp, lq) in shape_plans.items():
         req, _ = rc.execute(ex)
@@ -721,21 +929,31 @@ def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2)
         srv = W.Server(rc, mode=mode, plan=0, max_batch=4096, heavy_workers=heavy_workers, batch_capacity_ints=1 << 27,
                        keep_results=0)
         arr = W.poisson_arrivals(len(plans), rate, seed=7) if rate > 0 else np.zeros(len(plans))
-        for q, t in zip(plans, arr):
-            srv.submit(q, float(t))
+        for q, t, k in zip(plans, arr, types):
+            srv.submit(q, float(t), qtype=k)
         srv.start()
         srv.drain(600)
         st = srv.stats()
         cdf = {c: srv.latency_cdf(c) for c in ("light", "heavy")}
+        per_type = {}
+        for k, qt in enumerate(mx.types):
+            ts = srv.type_stats(k)
+            per_type[qt.name] = {"weight": qt.weight, "heavy": qt.heavy, **ts}
         srv.close()
-        out = {k: st[k] for k in ("qps", "p50_ms", "p99_ms", "light_p99_ms", "heavy_p99_ms", "mean_batch", "failed")}
+        out = {k: st[k] for k in ("qps", "p50_ms", "p99_ms", "light_p50_ms", "light_p99_ms", "heavy_p50_ms",
+                                  "heavy_p99_ms", "mean_batch", "failed")}
         out["_cdf"] = cdf
+        out["_per_type"] = per_type
         return out
 
     # capacity of the baseline: every request present at t=0
     cap0 = run(0, stats_plans, 0.0)["qps"]
-    out = {"config": f"{n_req} requests: 95% light constant-start (1..4 patterns), 5% heavy type-index (4..6 patterns), "
+    out = {"config": f"{n_req} requests of the weighted mix {mx.path.parent.name}/{mx.path.name} "
+                     f"({mx.n_light} light templates: constant starts of 1..4 patterns; "
+                     f"{len(mx.types) - mx.n_light} heavy type-index queries of 4..6 patterns; "
+                     f"{100.0 * sum(t.weight for t in mx.types if not t.heavy) / sum(mx.weights):.0f}% light by weight), "
                      f"Poisson arrivals, {layout.n_entities} entities, {heavy_workers} heavy workers",
+           "mix": [{"type": t.name, "weight": t.weight, "heavy": t.heavy} for t in mx.types],
            "baseline_capacity_qps": cap0,
            "plan_us": {"statistics": t_stats * 1e6, "learned_batched": t_learned * 1e6},
            "heavy_plans_checked": {"plans": checked, "bindings_differ": mismatched}, "sweep": []}
@@ -755,11 +973,15 @@ def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2)
                        "ratio": (best["qps"] / base["qps"]) if best else None,
                        # the reference Logger's 25-point CDF (ms) of light and heavy requests
                        "cdf_rates": W.Server.CDF_RATES,
-                       "baseline_cdf_ms": base["_cdf"], "batched_cdf_ms": best["_cdf"] if best else None}
+                       "baseline_cdf_ms": base["_cdf"], "batched_cdf_ms": best["_cdf"] if best else None,
+                       # per query type, as the reference Logger reports a mix (core/logger.hpp:182-305)
+                       "baseline_per_type": base["_per_type"],
+                       "batched_per_type": best["_per_type"] if best else None}
     for row in out["sweep"]:
         for t in (row["query_at_a_time_stats"], row["batched_learned"]):
             if t:
                 t.pop("_cdf", None)
+                t.pop("_per_type", None)
     return out
 
 

@@ -42,7 +42,9 @@ enum {
     WK_ETIMEDOUT = -3,  /* a bounded device-side wait gave up               */
     WK_EDEVICE   = -4,  /* CUDA runtime error (no device, launch failure)   */
     WK_ENOSTORE  = -5,  /* no store has been built/attached to the context  */
-    WK_EOVERFLOW = -6   /* a result exceeded a stated capacity               */
+    WK_EOVERFLOW = -6,  /* a result exceeded a stated capacity               */
+    WK_ECANCELED = -7,  /* a server request was cancelled before it ran      */
+    WK_EREJECTED = -8   /* a server request was refused at admission         */
 };
 
 enum { WK_DIR_IN = 0, WK_DIR_OUT = 1 };
@@ -98,8 +100,11 @@ int         wk_device_count(int *count);
  */
 int wk_store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o,
                    int64_t n_triples, int32_t num_ids);
-/* As wk_store_build, with the per-predicate sorts of the triples -- by (s, o)
- * and by (o, s) -- done on the context's device (a radix sort); the image is
+/* As wk_store_build, with the whole build on the context's device: the
+ * checks, the sorts of the triples by (s, o) and by (o, s), deduplication,
+ * list cutting, index lists, dense offsets and neighbour arrays, presence
+ * bitmaps and bucket insertion (wk_build.cu); the host does per-id
+ * arithmetic only and receives the finished image.  The image is
  * byte-identical to wk_store_build's.  Needs a device context and n < 2^32 - 1. */
 int wk_store_build_device(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o,
                           int64_t n, int32_t num_ids);
@@ -124,6 +129,10 @@ typedef struct {
     int64_t cache_bytes_loaded;
     int64_t dense_dirs;      /* (id, direction) pairs stored as dense offsets */
                              /* arrays instead of hashed keys                 */
+    int64_t cache_requests;  /* segment lookups by ops and prefetches, paged  */
+    int64_t cache_hits;      /* ... of which found the segment resident       */
+    int64_t cache_compactions; /* times the pool was compacted (free bytes    */
+                             /* enough for a segment but split into ranges)   */
 } wk_store_info;
 int wk_store_get_info(wk_ctx *ctx, wk_store_info *info);
 
@@ -138,6 +147,23 @@ int wk_store_get_edges(wk_ctx *ctx, int64_t vid, int32_t pid, int32_t dir,
  * per id; for class ids the member count is returned in `subjects`. */
 int wk_store_pred_stats(wk_ctx *ctx, int32_t id, int64_t *triples, int64_t *subjects,
                         int64_t *objects);
+
+/* How one id's segment is laid out (this library's own HBM format; the
+ * reference keeps every key in GStore's buckets, core/gstore.hpp:102-187):
+ * per direction (index = WK_DIR_IN / WK_DIR_OUT), whether its vertex keys are
+ * a dense offsets array, whether every vertex list holds at most one
+ * neighbour (functional: a dense functional direction also keeps the
+ * neighbour per id), and whether a hashed direction has a presence bitmap. */
+typedef struct {
+    int64_t keys;            /* keys of the id, hashed and dense               */
+    int64_t edges;           /* int32 entries of its edge segment             */
+    int32_t main_buckets, overflow_buckets;
+    int32_t dense[2], functional[2], bitmap[2];
+    int32_t max_degree[2];   /* longest vertex list (index lists excluded)    */
+    int64_t device_bytes;    /* bytes the segment takes on the device (its    */
+                             /* buckets, offsets arrays and edges, 256 B apart)*/
+} wk_seg_layout;
+int wk_store_seg_layout(wk_ctx *ctx, int32_t id, wk_seg_layout *out);
 
 /* --------------------------------------------------- per-pattern ops
  * Counterparts of RCache::{known_to_unknown, known_to_known, known_to_const,
@@ -168,12 +194,14 @@ int wk_const_to_unknown(wk_ctx *ctx, wk_history *h, int64_t start, int32_t direc
  * WK_EINVAL); *out_rows receives the output row count
  * (also when the output does not fit: WK_EOVERFLOW).  The call allocates
  * nothing: its scratch is one fixed device array inside the library (about
- * 2.1 MB, held by every GPU that loads the library until exit).  Limits: at
- * most 262,144 input rows per call; the output is bounded by out_capacity;
- * needs a resident (unpaged) store.  Every call shares that array, so calls
- * that overlap on the GPU race; the first call on a device looks the array up
- * and should precede any stream capture.  Returns after the output is
- * written. */
+ * 2.1 MB), which wk_ctx_create loads on the context's device -- with the
+ * kernels this call launches -- and looks up, so no call loads a module or
+ * takes device memory; the array stays on that GPU until the process exits.
+ * Limits: at most 262,144 input rows per call; the output is bounded by
+ * out_capacity; needs a resident (unpaged) store.  Every call on a device
+ * shares that array, so calls that overlap on the GPU race.  A context must
+ * not outlive a reset of its device (the address it looked up would be
+ * stale).  Returns after the output is written. */
 int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int64_t rows, int32_t cols,
                                 int64_t start, int32_t direction, int32_t predict,
                                 int32_t *out, int64_t out_capacity, int64_t *out_rows);
@@ -305,6 +333,11 @@ typedef struct {
     int32_t batch_window_us;      /* a light batch launches once its oldest request
                                      has waited this long, or it is full (0: as
                                      soon as a batch object is free)             */
+    int32_t pad;
+    int64_t max_request_bytes;    /* admission cap: a request whose projected
+                                     history bytes exceed it is refused at
+                                     submission (status WK_EREJECTED, no device
+                                     work); 0 = no cap                            */
 } wk_server_config;
 
 typedef struct {
@@ -315,6 +348,8 @@ typedef struct {
     double  p50_ms, p99_ms, light_p50_ms, light_p99_ms, heavy_p50_ms, heavy_p99_ms;
                                   /* percentiles by the reference Logger's rule:
                                      sorted latencies, element floor(n q)         */
+    int64_t rejected, cancelled;  /* refused at admission / cancelled before they
+                                     ran (neither counts as completed)            */
 } wk_server_stats;
 
 typedef struct wk_server wk_server;
@@ -327,6 +362,32 @@ int     wk_server_drain(wk_server *s, double timeout_s);
 int     wk_server_result(wk_server *s, int64_t id, int64_t *rows, int32_t *cols, int32_t *host, int64_t cap,
                          double *latency_s, int32_t *status);
 int     wk_server_get_stats(wk_server *s, wk_server_stats *out);
+/* A request tagged with its query type: the index of the template it was
+ * instantiated from in a weighted mix, as the reference's batch driver tags
+ * each request (core/proxy.hpp:360-410, Logger::start_record).  The class
+ * (light or heavy) still follows the request's shape. */
+int64_t wk_server_submit_typed(wk_server *s, const int64_t *cmd_chains, int32_t n_patterns, double arrival_s,
+                               int32_t type);
+/* Per-type statistics of the completed requests of one type, by the
+ * reference Logger's rule (core/logger.hpp:182-305: per-type sorted
+ * latencies, median element n / 2, 99th element floor(0.99 n), the 25-point
+ * CDF); qps is the type's completed requests over the server's span. */
+typedef struct {
+    int64_t completed, failed;
+    double  qps, p50_ms, p99_ms;
+    double  cdf_ms[25];
+} wk_type_stats;
+int     wk_server_type_stats(wk_server *s, int32_t type, wk_type_stats *out);
+/* Cancel a request that has not started: it completes at once with status
+ * WK_ECANCELED and no device work.  WK_EINVAL when it is already running or
+ * finished (its result stands). */
+int     wk_server_cancel(wk_server *s, int64_t id);
+/* Host-side fault injection: the next n device-buffer reservations of
+ * worker context `worker` (0.. the server's workers; -1 the context that
+ * re-runs overflowed light requests) fail with WK_ENOMEM exactly as a failed
+ * cudaMalloc would, before any kernel of the op is launched.  The request
+ * that meets it fails with WK_ENOMEM; every other request is unaffected. */
+int     wk_server_inject_alloc_failure(wk_server *s, int32_t worker, int32_t n);
 /* Latency CDF of the completed requests (cls 0 all, 1 light, 2 heavy): the
  * reference Logger's 25 points (core/logger.hpp print_cdf), at rates 0.01,
  * 0.05 .. 0.95 by 0.05 and 0.96 .. 1.00 by 0.01, into out_ms[WK_CDF_POINTS]. */
@@ -354,6 +415,10 @@ int wk_last_op_stats(wk_ctx *ctx, wk_op_stats *st);
 int wk_query_op_stats(wk_ctx *ctx, wk_op_stats *st, int32_t cap, int32_t *n);
 int64_t wk_kernel_launches(wk_ctx *ctx);   /* cumulative kernel launches */
 int wk_sync(wk_ctx *ctx);
+/* Host-side fault injection: the context's next n device-buffer reservations
+ * (history and op scratch) fail with WK_ENOMEM as a failed cudaMalloc would.
+ * For testing the callers' error paths; no device state is touched. */
+int wk_ctx_inject_alloc_failure(wk_ctx *ctx, int32_t n);
 /* ------------------------------------------------------- the planner
  * Statistics-based plan of a BGP: Planner::generate_plan
  * (core/planner.hpp:927-1028) over the statistics of

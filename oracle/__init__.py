@@ -22,7 +22,10 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libwkref.so"
-REF_SRC = Path(os.environ.get("WK_REFERENCE_DIR", "/root/reference"))
+# The reference sources, for the harness that pins the restatement.  Only the
+# environment names them: without WK_REFERENCE_DIR the harness is not built
+# and the tests that need it skip.
+REF_SRC = Path(os.environ["WK_REFERENCE_DIR"]) if os.environ.get("WK_REFERENCE_DIR") else None
 
 _I32P = C.POINTER(C.c_int32)
 _I64P = C.POINTER(C.c_int64)
@@ -35,7 +38,7 @@ class orc_table(C.Structure):
 def build(with_ref: bool = True) -> None:
     """Compile the C restatement, and the reference harness when the sources exist."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
-    if with_ref and (REF_SRC / "core" / "gstore.hpp").exists():
+    if with_ref and REF_SRC is not None and (REF_SRC / "core" / "gstore.hpp").exists():
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_SRC}"], check=True)
 
 
@@ -69,6 +72,8 @@ def _load():
         lib.orc_table_set.restype = C.c_int
         lib.orc_table_set.argtypes = [C.POINTER(orc_table), _I32P, C.c_int64, C.c_int32]
         lib.orc_pred_stats.argtypes = [C.c_void_p, C.c_int32, _I64P, _I64P, _I64P]
+        lib.orc_rows_digest.restype = C.c_uint64
+        lib.orc_rows_digest.argtypes = [_I32P, C.c_int64, C.c_int32, C.c_int32]
         _lib = lib
     return _lib
 
@@ -290,6 +295,16 @@ class RefStore:
             self.close()
         except Exception:
             pass
+
+
+def rows_digest(table: np.ndarray, nthreads: int = 1) -> tuple[int, int]:
+    """(rows, order-independent digest) of a 2-D int32 table: equal for two
+    tables holding the same rows in any order (wk_oracle.c, orc_rows_digest)."""
+    t = np.ascontiguousarray(table, np.int32)
+    if t.ndim != 2 or t.shape[0] == 0:
+        return (0, 0)
+    d = _load().orc_rows_digest(t.ctypes.data_as(_I32P), t.shape[0], t.shape[1], max(1, nthreads))
+    return (int(t.shape[0]), int(d))
 
 
 def canonical(table: np.ndarray) -> np.ndarray:

@@ -495,13 +495,16 @@ typedef struct {
     const int64_t *cmd;
     int32_t npat;
     orc_table t;
+    int64_t *rows;   /* rows of this thread's table after every step */
     int rc;
 } mt_job;
 
 static void *mt_run(void *arg) {
     mt_job *j = (mt_job *)arg;
-    for (int32_t i = 1; i < j->npat && j->rc == 0; ++i)
+    for (int32_t i = 1; i < j->npat && j->rc == 0; ++i) {
         j->rc = orc_step(j->st, &j->t, 0, j->cmd[i * 4], j->cmd[i * 4 + 1], j->cmd[i * 4 + 2], j->cmd[i * 4 + 3], NULL);
+        j->rows[i] = j->t.rows;
+    }
     return NULL;
 }
 
@@ -521,11 +524,13 @@ int orc_execute(const orc_store *st, const int64_t *cmd, int32_t npat, int32_t n
     /* strided split of the first step's rows (core/engine.hpp:243-245) */
     mt_job *jobs = (mt_job *)calloc((size_t)nthreads, sizeof(mt_job));
     pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
-    if (!jobs || !th) { free(jobs); free(th); return -1; }
+    int64_t *trows = (int64_t *)calloc((size_t)nthreads * (size_t)npat, sizeof(int64_t));
+    if (!jobs || !th || !trows) { free(jobs); free(th); free(trows); return -1; }
     const int32_t C = out->cols;
     for (int32_t tdx = 0; tdx < nthreads; ++tdx) {
         mt_job *j = &jobs[tdx];
         j->st = st; j->cmd = cmd; j->npat = npat;
+        j->rows = trows + (size_t)tdx * (size_t)npat;
         int64_t nr = out->rows > tdx ? (out->rows - tdx + nthreads - 1) / nthreads : 0;
         j->t.data = (int32_t *)malloc((size_t)(nr * C + 1) * sizeof(int32_t));
         j->t.cols = C;
@@ -554,8 +559,74 @@ int orc_execute(const orc_store *st, const int64_t *cmd, int32_t npat, int32_t n
             at += jobs[tdx].t.rows * cols;
         }
     }
+    /* the row count after every step is the sum over the threads' tables */
+    if (!rc && step_rows)
+        for (int32_t i = 1; i < npat; ++i) {
+            int64_t r = 0;
+            for (int32_t tdx = 0; tdx < nthreads; ++tdx) r += jobs[tdx].rows[i];
+            step_rows[i] = r;
+        }
     for (int32_t tdx = 0; tdx < nthreads; ++tdx) orc_table_free(&jobs[tdx].t);
     free(jobs);
     free(th);
+    free(trows);
     return rc ? -1 : 0;
+}
+
+/* ------------------------------------------------------ table digests */
+/* Order-independent digest of a table: the sum (mod 2^64) over rows of a
+ * 64-bit hash of the row's values in column order.  Two tables with the same
+ * rows in any order have the same digest; the test code compares results of
+ * the strided multi-thread split and of index starts (whose order the
+ * reference leaves to racing loader threads) this way, at sizes where a
+ * canonical sort would take minutes. */
+static inline uint64_t row_hash(const int32_t *r, int32_t cols) {
+    uint64_t h = 0x243f6a8885a308d3ull ^ (uint64_t)cols;
+    for (int32_t c = 0; c < cols; ++c) h = dmix(h + ((uint64_t)(uint32_t)r[c] | ((uint64_t)(c + 1) << 32)));
+    return h;
+}
+
+typedef struct {
+    const int32_t *data;
+    int64_t r0, r1;
+    int32_t cols;
+    uint64_t sum;
+} dg_job;
+
+static void *dg_run(void *arg) {
+    dg_job *j = (dg_job *)arg;
+    uint64_t s = 0;
+    for (int64_t i = j->r0; i < j->r1; ++i) s += row_hash(j->data + i * j->cols, j->cols);
+    j->sum = s;
+    return NULL;
+}
+
+uint64_t orc_rows_digest(const int32_t *data, int64_t rows, int32_t cols, int32_t nthreads) {
+    if (rows <= 0 || cols <= 0) return 0;
+    if (nthreads < 1) nthreads = 1;
+    if ((int64_t)nthreads > rows / 4096 + 1) nthreads = (int32_t)(rows / 4096 + 1);
+    dg_job *jobs = (dg_job *)calloc((size_t)nthreads, sizeof(dg_job));
+    pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!jobs || !th) {
+        free(jobs);
+        free(th);
+        dg_job one = {data, 0, rows, cols, 0};
+        dg_run(&one);
+        return one.sum;
+    }
+    for (int32_t t = 0; t < nthreads; ++t) {
+        jobs[t].data = data;
+        jobs[t].cols = cols;
+        jobs[t].r0 = rows * t / nthreads;
+        jobs[t].r1 = rows * (t + 1) / nthreads;
+        pthread_create(&th[t], NULL, dg_run, &jobs[t]);
+    }
+    uint64_t s = 0;
+    for (int32_t t = 0; t < nthreads; ++t) {
+        pthread_join(th[t], NULL);
+        s += jobs[t].sum;
+    }
+    free(jobs);
+    free(th);
+    return s;
 }

@@ -48,11 +48,14 @@ int orc_step(const orc_store *st, orc_table *t, int is_first, int64_t start, int
 /* Whole query; nthreads > 1 splits the first step's rows by stride like
  * Engine::index_to_unknown (core/engine.hpp:243-245) and concatenates the
  * per-thread results.  step_rows (may be NULL) receives the row count after
- * every step (single-thread runs only). */
+ * every step (summed over the threads' tables when nthreads > 1). */
 int orc_execute(const orc_store *st, const int64_t *cmd, int32_t npat, int32_t nthreads, orc_table *out,
                 int64_t *step_rows);
 
 void orc_table_free(orc_table *t);
+/* Order-independent digest of a rows x cols table (sum over rows of a hash of
+ * each row), computed on nthreads threads. */
+uint64_t orc_rows_digest(const int32_t *data, int64_t rows, int32_t cols, int32_t nthreads);
 /* replace t's contents with a copy of src (rows x cols) */
 int orc_table_set(orc_table *t, const int32_t *src, int64_t rows, int32_t cols);
 

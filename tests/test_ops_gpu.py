@@ -105,6 +105,37 @@ def test_k2k_k2c_random_histories(gpu_small, small_graph, small_oracle, R, C):
         assert np.array_equal(got.reshape(exp.shape), exp), const
 
 
+@pytest.mark.parametrize("R", [1, 33, 4097, 60_000])
+def test_k2k_k2c_on_a_functional_direction(gpu_small, small_graph, small_oracle, R):
+    """rdf:type OUT is dense and functional: its membership test reads the
+    neighbour array once.  Rows mix real (entity, class) pairs, wrong classes,
+    absent vertices and index keys (0, looked up in the hash table)."""
+    g, s, p, o = small_graph
+    rng = np.random.default_rng(R)
+    m = p == W.TYPE_ID
+    es, eo = s[m], o[m]
+    idx = rng.integers(0, len(es), size=R)
+    h = np.stack([es[idx], eo[idx], es[rng.integers(0, len(es), size=R)]], 1).astype(np.int32)
+    wrong = rng.random(R) < 0.4
+    h[wrong, 1] = 17 + rng.integers(0, 10, size=wrong.sum())
+    h[rng.random(R) < 0.05, 0] = W.VID_BASE + 50_000_000
+    h[rng.random(R) < 0.02, 0] = 0
+    for (start, end) in ((-1, -2), (-3, -2)):
+        req = W.Request([])
+        gpu_small.upload_history(req, h)
+        gpu_small.known_to_known(req, start, W.OUT, W.TYPE_ID, end)
+        got = gpu_small.download(req)
+        exp, _ = small_oracle.step(h, False, start, W.TYPE_ID, W.OUT, end)
+        assert np.array_equal(got.reshape(exp.shape), exp), (start, end)
+    for const in (17, 21, 5):
+        req = W.Request([])
+        gpu_small.upload_history(req, h)
+        gpu_small.known_to_const(req, -1, W.OUT, W.TYPE_ID, const)
+        got = gpu_small.download(req)
+        exp, _ = small_oracle.step(h, False, -1, W.TYPE_ID, W.OUT, const)
+        assert np.array_equal(got.reshape(exp.shape), exp), const
+
+
 def test_index_and_const_starts(gpu_small, small_graph, small_oracle):
     g, s, p, o = small_graph
     for idx, d in ((17, W.IN), (20, W.IN), (2, W.IN), (2, W.OUT), (16, W.OUT)):
@@ -199,6 +230,43 @@ def test_paged_segment_cache_gives_same_rows(small_graph, small_oracle, golden_s
     assert info["cache_loads"] > 0 and info["cache_evictions"] > 0
 
 
+def test_fragmented_segment_cache_compacts(small_graph, small_oracle):
+    """A pool whose free bytes would hold a segment but whose free ranges do
+    not (the current step's segment, kept resident, splits them) is compacted
+    instead of refusing the segment (the reference pages fixed frames,
+    core/shard_manager.hpp:78-128; here a segment is one range, moved down).
+
+    Budget 5 MiB; segments 2, 3 and 6 (about 1.6 MB each) are loaded in that
+    order, then a query steps through 3 and prefetches the type segment (2.4
+    MB): evicting 2 and 6 frees 3.6 MB in two ranges of at most 2.0 MB around
+    3, which is protected."""
+    g, s, p, o = small_graph
+    host = W.RCache(device=-1)
+    host.build_store(s, p, o, g.num_ids)
+    size = {pid: host.seg_layout(pid)["device_bytes"] for pid in (1, 2, 3, 6)}
+    budget = 5 << 20
+    assert size[2] + size[3] + size[6] <= budget < size[2] + size[3] + size[6] + size[1]
+    assert max(size[2], size[6] + budget - size[2] - size[3] - size[6]) < size[1] <= budget - size[3]
+    rc = W.RCache(device=0, cache_budget_mb=5, enable_prefetch=True)
+    rc.build_store_graph(g)
+    for pid in (2, 3, 6):                       # one-pattern queries: no prefetch, one segment each
+        c = int(s[p == pid][0])
+        req, _ = rc.execute([c, pid, W.OUT, -1])
+        assert np.array_equal(req.result_table.reshape(-1), small_oracle.get_edges(c, pid, W.OUT))
+    c = int(s[p == 3][0])
+    q = [c, 3, W.OUT, -1, -1, W.TYPE_ID, W.OUT, -2]
+    req, rows = rc.execute(q)
+    exp, erows = small_oracle.execute(q)
+    assert list(rows) == list(erows) and np.array_equal(req.result_table, exp)
+    info = rc.store_info()
+    assert info["cache_compactions"] >= 1 and info["cache_evictions"] >= 2
+    assert info["cache_hits"] < info["cache_requests"]
+    # every segment still answers after the move
+    for pid in (3, 1):
+        req, _ = rc.execute([c, pid, W.OUT, -1])
+        assert np.array_equal(req.result_table.reshape(-1), small_oracle.get_edges(c, pid, W.OUT))
+
+
 def test_kernel_launch_count_and_timing(gpu_small, golden_small):
     before = gpu_small.kernel_launches()
     gpu_small.enable_timing(True)
@@ -272,10 +340,11 @@ def test_query_op_stats_cover_every_pattern(gpu_small, golden_small):
     assert stats[0]["kind"] == 3 and all(s["kind"] in (0, 1, 2) for s in stats[1:])
 
 
-@pytest.mark.parametrize("which", ["small", "hub", "dups"])
+@pytest.mark.parametrize("which", ["small", "hub", "dups", "classpred"])
 def test_device_sorted_build_gives_the_same_image(lib_built, small_graph, which):
-    """wk_store_build_device sorts the triples on the GPU; the image (buckets,
-    edges, offsets arrays, metadata) must be byte-identical to the host build's."""
+    """wk_store_build_device builds the image on the GPU (sorts, lists,
+    dense arrays, bitmaps, bucket insertion); the image (buckets, edges,
+    offsets arrays, metadata) must be byte-identical to the host build's."""
     if which == "small":
         g, s, p, o = small_graph
         nid = g.num_ids
@@ -287,12 +356,43 @@ def test_device_sorted_build_gives_the_same_image(lib_built, small_graph, which)
             s, p, o = (np.concatenate([x, x[k]]) for x in (s, p, o))
             perm = rng.permutation(len(s))
             s, p, o = s[perm], p[perm], o[perm]
+        if which == "classpred":   # id 5 is a class and a predicate: two [0|5|IN] index keys
+            rng = np.random.default_rng(9)
+            m = 5000
+            s = np.concatenate([s, W.VID_BASE + rng.integers(0, 20_000, m)]).astype(np.int32)
+            p = np.concatenate([p, np.full(m, 5)]).astype(np.int32)
+            o = np.concatenate([o, W.VID_BASE + rng.integers(0, 20_000, m)]).astype(np.int32)
     a = W.RCache(device=0)
     a.build_store(s, p, o, nid)
     b = W.RCache(device=0)
-    b.build_store(s, p, o, nid, sort_on_device=True)
+    b.build_store(s, p, o, nid, on_device=True)
     assert a.store_digest() == b.store_digest()
     assert a.store_info()["num_keys"] == b.store_info()["num_keys"]
+
+
+@pytest.mark.parametrize("bad", ["predicate", "subject", "class", "object"])
+def test_device_build_refuses_bad_triples_as_the_host_does(lib_built, bad):
+    s, p, o, nid = _hub_graph()
+    s, p, o = s.copy(), p.copy(), o.copy()
+    i = int(np.flatnonzero(p == W.TYPE_ID)[7]) if bad == "class" else 1234
+    if bad == "predicate":
+        p[i] = nid + 1
+    elif bad == "subject":
+        s[i] = 5
+    elif bad == "class":
+        o[i] = nid + 3
+    else:
+        o[i] = -7
+    p[i + 5] = 0   # a later bad triple: the first one is reported
+    msgs = []
+    for dev in (False, True):
+        rc = W.RCache(device=0)
+        with pytest.raises(W.WkError) as e:
+            rc.build_store(s, p, o, nid, on_device=dev)
+        assert e.value.status == W.WK_EINVAL
+        msgs.append(str(e.value))
+        rc.close()
+    assert msgs[0] == msgs[1]
 
 
 def test_k2u_over_256_groups(lib_built):

@@ -118,3 +118,34 @@ def test_logger_rule_restatement():
     assert logger_ref.at_rate(lats, 0.01) == 1.0
     r = logger_ref.cdf_rates()
     assert len(r) == 25 and r[0] == 0.01 and abs(r[19] - 0.95) < 1e-12 and abs(r[-1] - 1.0) < 1e-12
+
+
+def test_rows_digest_is_order_free_and_sensitive(lib_built):
+    """The order-independent table digest that compares results at benchmark
+    sizes: any row order gives the same value; a changed value, a swapped
+    column pair or a dropped row does not."""
+    rng = np.random.default_rng(4)
+    t = rng.integers(W.VID_BASE, W.VID_BASE + 5000, size=(50_000, 5), dtype=np.int64).astype(np.int32)
+    base = oracle.rows_digest(t, 1)
+    assert oracle.rows_digest(t[rng.permutation(len(t))], 8) == base
+    assert oracle.rows_digest(t, 3) == base
+    u = t.copy()
+    u[777, 2] += 1
+    assert oracle.rows_digest(u)[1] != base[1]
+    v = t.copy()
+    v[10, [1, 3]] = v[10, [3, 1]]
+    assert v[10, 1] == v[10, 3] or oracle.rows_digest(v)[1] != base[1]
+    assert oracle.rows_digest(t[:-1]) != base
+    assert oracle.rows_digest(np.zeros((0, 5), np.int32)) == (0, 0)
+
+
+def test_multithread_execute_gives_single_thread_rows(small_graph, small_oracle):
+    """The strided split of the CPU baseline (core/engine.hpp:243-245) returns
+    the single-thread run's rows in another order, and the same per-step row
+    counts."""
+    g, s, p, o = small_graph
+    for name, q in workloads.small_queries(s, p, o):
+        a, ra = small_oracle.execute(q, nthreads=1)
+        b, rb = small_oracle.execute(q, nthreads=5)
+        assert list(ra) == list(rb), name
+        assert oracle.rows_digest(a) == oracle.rows_digest(b), name

@@ -54,7 +54,16 @@ def _history(s, R, C, seed):
     return h
 
 
-@pytest.mark.parametrize("R,C,pid,d", [(70_001, 3, 2, W.OUT), (MAX_ROWS, 2, 5, W.IN)])
+def _free_device_bytes():
+    torch = pytest.importorskip("torch")
+    return torch.cuda.mem_get_info(0)[0]
+
+
+# (input rows, columns, predicate, direction): output widths 3, 4, 8 (the
+# widest specialised expansion) and 10 (the generic one with scalar stores);
+# the maximum row count; a small call whose output ends inside a 16 B group
+@pytest.mark.parametrize("R,C,pid,d", [(70_001, 3, 2, W.OUT), (MAX_ROWS, 2, 5, W.IN), (4_099, 7, 3, W.OUT),
+                                       (3_001, 9, 4, W.IN), (5, 2, 2, W.OUT)])
 def test_noalloc_matches_existing_op_twice(setup, R, C, pid, d):
     g, s, rc, out_owner = setup
     cap = 16 << 20
@@ -66,8 +75,12 @@ def test_noalloc_matches_existing_op_twice(setup, R, C, pid, d):
         req = W.Request([])
         rc.upload_history(req, h)
         in_ptr = req.hist.data
+        rc.sync()
+        free0 = _free_device_bytes()
         st, nrows = _noalloc(rc, in_ptr, R, C, -1 - (call % C), d, pid, out_ptr, cap)
         assert st == W.WK_OK, W.load_library().wk_last_error()
+        # the call took no device memory (no allocation, no module load)
+        assert _free_device_bytes() == free0
         got = _download(out_owner, out_ptr, nrows, C + 1)
         rc.known_to_unknown(req, -1 - (call % C), d, pid)      # the ordinary entry point
         exp = rc.download(req)

@@ -25,6 +25,7 @@ _PKG = Path(__file__).resolve().parent
 _LIB_PATH = _PKG / "libwkgpu.so"
 
 WK_OK, WK_EINVAL, WK_ENOMEM, WK_ETIMEDOUT, WK_EDEVICE, WK_ENOSTORE, WK_EOVERFLOW = 0, -1, -2, -3, -4, -5, -6
+WK_ECANCELED, WK_EREJECTED = -7, -8
 IN, OUT = 0, 1
 PREDICATE_ID, TYPE_ID = 0, 1
 VID_BASE = 1 << 17
@@ -49,7 +50,14 @@ class wk_store_info(C.Structure):
     _fields_ = [("num_keys", C.c_int64), ("num_edges", C.c_int64), ("key_bytes", C.c_int64),
                 ("edge_bytes", C.c_int64), ("overflow_buckets", C.c_int64), ("device_bytes", C.c_int64),
                 ("num_ids", C.c_int32), ("paged", C.c_int32), ("cache_loads", C.c_int64),
-                ("cache_evictions", C.c_int64), ("cache_bytes_loaded", C.c_int64), ("dense_dirs", C.c_int64)]
+                ("cache_evictions", C.c_int64), ("cache_bytes_loaded", C.c_int64), ("dense_dirs", C.c_int64),
+                ("cache_requests", C.c_int64), ("cache_hits", C.c_int64), ("cache_compactions", C.c_int64)]
+
+
+class wk_seg_layout(C.Structure):
+    _fields_ = [("keys", C.c_int64), ("edges", C.c_int64), ("main_buckets", C.c_int32),
+                ("overflow_buckets", C.c_int32), ("dense", C.c_int32 * 2), ("functional", C.c_int32 * 2),
+                ("bitmap", C.c_int32 * 2), ("max_degree", C.c_int32 * 2), ("device_bytes", C.c_int64)]
 
 
 class wk_op_stats(C.Structure):
@@ -60,14 +68,21 @@ class wk_op_stats(C.Structure):
 class wk_server_config(C.Structure):
     _fields_ = [("mode", C.c_int32), ("max_batch", C.c_int32), ("max_steps", C.c_int32), ("heavy_workers", C.c_int32),
                 ("batch_capacity_ints", C.c_int64), ("light_budget_bytes", C.c_int64), ("plan", C.c_int32),
-                ("keep_results", C.c_int32), ("batch_window_us", C.c_int32)]
+                ("keep_results", C.c_int32), ("batch_window_us", C.c_int32), ("pad", C.c_int32),
+                ("max_request_bytes", C.c_int64)]
 
 
 class wk_server_stats(C.Structure):
     _fields_ = [("completed", C.c_int64), ("light", C.c_int64), ("heavy", C.c_int64), ("failed", C.c_int64),
                 ("batches", C.c_int64), ("mean_batch", C.c_double), ("span_s", C.c_double), ("qps", C.c_double),
                 ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("light_p50_ms", C.c_double),
-                ("light_p99_ms", C.c_double), ("heavy_p50_ms", C.c_double), ("heavy_p99_ms", C.c_double)]
+                ("light_p99_ms", C.c_double), ("heavy_p50_ms", C.c_double), ("heavy_p99_ms", C.c_double),
+                ("rejected", C.c_int64), ("cancelled", C.c_int64)]
+
+
+class wk_type_stats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("failed", C.c_int64), ("qps", C.c_double), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("cdf_ms", C.c_double * 25)]
 
 
 class wk_pred_group(C.Structure):
@@ -139,6 +154,11 @@ _SIGS = {
     "wk_server_get_stats": (C.c_int, [_P, C.POINTER(wk_server_stats)]),
     "wk_server_latency_cdf": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double)]),
     "wk_server_destroy": (C.c_int, [_P]),
+    "wk_server_submit_typed": (C.c_int64, [_P, _I64P, C.c_int32, C.c_double, C.c_int32]),
+    "wk_server_type_stats": (C.c_int, [_P, C.c_int32, C.POINTER(wk_type_stats)]),
+    "wk_server_cancel": (C.c_int, [_P, C.c_int64]),
+    "wk_server_inject_alloc_failure": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "wk_ctx_inject_alloc_failure": (C.c_int, [_P, C.c_int32]),
     "wk_mlp_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(_P)]),
     "wk_mlp_destroy": (C.c_int, [_P]),
     "wk_mlp_num_params": (C.c_int64, [_P]),
@@ -160,6 +180,7 @@ _SIGS = {
     "wk_timer_end": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "wk_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_P)]),
     "wk_host_free": (C.c_int, [_P]),
+    "wk_store_seg_layout": (C.c_int, [_P, C.c_int32, C.POINTER(wk_seg_layout)]),
     "wk_graph_generate": (C.c_int, [C.POINTER(wk_graph_spec), C.c_int32, C.POINTER(_P)]),
     "wk_graph_size": (C.c_int64, [_P]),
     "wk_graph_num_ids": (C.c_int32, [_P]),
@@ -172,10 +193,32 @@ _SIGS = {
 }
 
 _lib = None
+_gen = None
+_GEN_LIB_PATH = _PKG / "libwkgen.so"
+_GEN_SIGS = {k: _SIGS[k] for k in ("wk_graph_generate", "wk_graph_size", "wk_graph_num_ids", "wk_graph_first_class",
+                                   "wk_graph_s", "wk_graph_p", "wk_graph_o", "wk_graph_free", "wk_last_error")}
 
 
 def lib_path() -> Path:
     return _LIB_PATH
+
+
+def load_gen_library():
+    """Load libwkgen.so, the seeded graph generator alone (host code, no CUDA),
+    so that a process that only needs a graph -- the CPU baseline -- does not
+    map the GPU library."""
+    global _gen
+    if _gen is not None:
+        return _gen
+    if not _GEN_LIB_PATH.exists():
+        raise ImportError(f"{_GEN_LIB_PATH} is missing: build it with `python -m wukonggpu_gb300.build`")
+    lib = C.CDLL(str(_GEN_LIB_PATH))
+    for name, (res, args) in _GEN_SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _gen = lib
+    return lib
 
 
 def load_library():
@@ -256,9 +299,11 @@ class Graph:
     """A seeded synthetic ID-form RDF graph (owned by the library)."""
 
     def __init__(self, spec: wk_graph_spec, n_threads: int = 0):
-        lib = load_library()
+        lib = load_gen_library()
         h = _P()
-        _check(lib.wk_graph_generate(C.byref(spec), n_threads, C.byref(h)))
+        st = lib.wk_graph_generate(C.byref(spec), n_threads, C.byref(h))
+        if st != WK_OK:
+            raise WkError(st, lib.wk_last_error().decode(errors="replace"))
         self._h = h
         self.spec = spec
         self.n = lib.wk_graph_size(h)
@@ -267,7 +312,7 @@ class Graph:
 
     def arrays(self):
         """(s, p, o) as numpy views into library memory (valid while the graph lives)."""
-        lib = load_library()
+        lib = load_gen_library()
         out = []
         for f in (lib.wk_graph_s, lib.wk_graph_p, lib.wk_graph_o):
             ptr = f(self._h)
@@ -276,7 +321,7 @@ class Graph:
 
     def close(self):
         if getattr(self, "_h", None):
-            load_library().wk_graph_free(self._h)
+            load_gen_library().wk_graph_free(self._h)
             self._h = None
 
     def __del__(self):
@@ -330,13 +375,13 @@ class RCache:
         self._h = h
 
     # -- store
-    def build_store(self, s, p, o, num_ids: int, sort_on_device: bool = False):
-        """Build the store from ID-form triples; sort_on_device runs the
-        per-predicate sorts on the GPU (same image)."""
+    def build_store(self, s, p, o, num_ids: int, on_device: bool = False):
+        """Build the store from ID-form triples; on_device builds the whole
+        image on the GPU (wk_store_build_device; the same image)."""
         s = np.ascontiguousarray(s, np.int32)
         p = np.ascontiguousarray(p, np.int32)
         o = np.ascontiguousarray(o, np.int32)
-        f = load_library().wk_store_build_device if sort_on_device else load_library().wk_store_build
+        f = load_library().wk_store_build_device if on_device else load_library().wk_store_build
         _check(f(self._h, _i32(s), _i32(p), _i32(o), len(s), num_ids))
 
     def store_digest(self) -> int:
@@ -345,7 +390,9 @@ class RCache:
         return d.value
 
     def build_store_graph(self, g: Graph):
-        _check(load_library().wk_store_build_graph(self._h, g._h))
+        """The store of a generated graph, from its arrays in place (no copies)."""
+        s, p, o = g.arrays()
+        _check(load_library().wk_store_build(self._h, _i32(s), _i32(p), _i32(o), len(s), g.num_ids))
 
     def share_store(self, owner: "RCache"):
         _check(load_library().wk_ctx_share_store(self._h, owner._h))
@@ -362,6 +409,14 @@ class RCache:
         out = np.zeros(max(deg.value, 1), np.int32)
         _check(lib.wk_store_get_edges(self._h, vid, pid, d, _i32(out), deg.value, C.byref(deg)))
         return out[:deg.value]
+
+    def seg_layout(self, pid: int) -> dict:
+        """The layout decisions of one id's segment (wk_store_seg_layout)."""
+        x = wk_seg_layout()
+        _check(load_library().wk_store_seg_layout(self._h, pid, C.byref(x)))
+        return {"keys": x.keys, "edges": x.edges, "main_buckets": x.main_buckets,
+                "overflow_buckets": x.overflow_buckets, "dense": list(x.dense), "functional": list(x.functional),
+                "bitmap": list(x.bitmap), "max_degree": list(x.max_degree), "device_bytes": x.device_bytes}
 
     def pred_stats(self, pid: int):
         t, s, o = C.c_int64(), C.c_int64(), C.c_int64()
@@ -431,6 +486,10 @@ class RCache:
         out = np.zeros(4, np.int64)
         _check(load_library().wk_stat_get(self._h, which, a, b, out.ctypes.data_as(_I64P)))
         return [int(x) for x in out] if which == 4 else int(out[0])
+
+    def inject_alloc_failure(self, n: int):
+        """The next n device-buffer reservations fail with WK_ENOMEM (host-side injection)."""
+        _check(load_library().wk_ctx_inject_alloc_failure(self._h, n))
 
     def set_row_limit(self, max_rows: int):
         """Cap on k2u output rows (0 = none); larger steps fail with WK_EOVERFLOW."""
@@ -689,12 +748,36 @@ class Server:
         self._h = h
         self.cfg = cfg
 
-    def submit(self, cmd_chains, arrival_s: float = 0.0) -> int:
+    def submit(self, cmd_chains, arrival_s: float = 0.0, qtype: int = -1) -> int:
+        """Queue a request arriving `arrival_s` after start; `qtype` tags it with
+        its template's index in a weighted mix (per-type statistics)."""
         cc = np.asarray(cmd_chains, np.int64)
-        rid = load_library().wk_server_submit(self._h, cc.ctypes.data_as(_I64P), len(cc) // 4, arrival_s)
+        rid = load_library().wk_server_submit_typed(self._h, cc.ctypes.data_as(_I64P), len(cc) // 4, arrival_s,
+                                                    qtype)
         if rid < 0:
             _check(int(rid))
         return rid
+
+    def finished(self, rid: int) -> bool:
+        """Whether the request has completed (run, failed, refused or cancelled)."""
+        rows, cols = C.c_int64(), C.c_int32()
+        return load_library().wk_server_result(self._h, rid, C.byref(rows), C.byref(cols), None, 0, None,
+                                               None) == WK_OK
+
+    def cancel(self, rid: int) -> bool:
+        """Cancel a request that has not started; False when it already runs or finished."""
+        return load_library().wk_server_cancel(self._h, rid) == WK_OK
+
+    def type_stats(self, qtype: int) -> dict:
+        """The reference Logger's statistics of one request type."""
+        st = wk_type_stats()
+        _check(load_library().wk_server_type_stats(self._h, qtype, C.byref(st)))
+        return {"completed": st.completed, "failed": st.failed, "qps": st.qps, "p50_ms": st.p50_ms,
+                "p99_ms": st.p99_ms, "cdf_ms": list(st.cdf_ms)}
+
+    def inject_alloc_failure(self, worker: int, n: int):
+        """The next n buffer reservations of a worker context fail with WK_ENOMEM (host-side injection)."""
+        _check(load_library().wk_server_inject_alloc_failure(self._h, worker, n))
 
     def start(self):
         _check(load_library().wk_server_start(self._h))

@@ -18,6 +18,10 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libwkgpu.so"
+# the seeded graph generator alone (host code, no CUDA): the CPU baseline loads
+# it to make its graph without mapping the GPU library
+GEN_LIB = PKG / "libwkgen.so"
+GEN_SRCS = ("wk_gen.cpp", "wk_error.cpp")
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -71,8 +75,16 @@ def build(verbose: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    gen_objs = [BUILD / (n + ".o") for n in GEN_SRCS]
+    if not GEN_LIB.exists() or GEN_LIB.stat().st_mtime < max(o.stat().st_mtime for o in gen_objs):
+        tmp = GEN_LIB.with_suffix(".so.tmp")
+        cmd = ["g++", "-shared", "-o", str(tmp), *map(str, gen_objs), "-lpthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, GEN_LIB)
     if verbose:
-        print(f"built {LIB}")
+        print(f"built {LIB} and {GEN_LIB.name}")
     return LIB
 
 

@@ -163,16 +163,10 @@ struct Stats;   // planner statistics (wk_planner.cpp)
 Stats *build_stats(const HostStore &hs);
 void free_stats(Stats *s);
 
-// A device sort for the build: given the largest vertex id and predicate,
-// fills keys[k] (hi << 32 | lo) and pids[k] with all n triples sorted by
-// (predicate, hi, lo), order 0 (s, o) and order 1 (o, s).
-using SortTriples = std::function<int(uint32_t max_vid, uint32_t max_pid, std::vector<uint64_t> (&keys)[2],
-                                      std::vector<uint32_t> (&pids)[2])>;
-
-// The store image from ID-form triples; the per-predicate sorts run on the
-// host, or through device_sort when given (the image is the same either way).
+// The store image from ID-form triples, built on the host (wk_store.cpp);
+// wk_build.cu builds the same image on the device.
 int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
-                     int32_t num_ids, HostStore **out, const SortTriples *device_sort = nullptr);
+                     int32_t num_ids, HostStore **out);
 
 // Device view of one predicate segment (passed to kernels by value).
 struct PredView {

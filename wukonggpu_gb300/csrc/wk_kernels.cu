@@ -352,8 +352,8 @@ __device__ __forceinline__ SliceLoc locate_slice(unsigned long long k, const uns
 }
 
 // -------------------------------------------------------------- k2u expand
-// last row i in [0, n) with pos[i] <= j; pos is non-decreasing with pos[0] = 0,
-// so for j below the block's total that row has a non-empty list
+// last entry k in [0, n) with pos[k] <= j; pos is non-decreasing with pos[0] =
+// 0 (n >= 1), so for j below the block's total that entry's list covers j
 __device__ __forceinline__ int row_of(const uint32_t *pos, int n, uint32_t j) {
     int lo = 0, hi = n - 1;
     while (lo < hi) {
@@ -364,52 +364,64 @@ __device__ __forceinline__ int row_of(const uint32_t *pos, int n, uint32_t j) {
     return lo;
 }
 
+// The block's input rows whose list is not empty, compacted in order:
+// entry k is block row row[k], its first output row pos[k] (block-local), its
+// list offset minus pos[k] in erel[k] (modulo 2^32: erel + j is the entry
+// index of output row j), and pos[n] = the block's total.  A sparse direction
+// leaves most rows empty, so searches and walks over the entries skip them.
+struct ExpandRows {
+    uint32_t pos[kRowsPerBlock + 1];
+    uint32_t erel[kRowsPerBlock];
+    uint16_t row[kRowsPerBlock];
+    int n;
+};
+
 // One group of 4 output rows.  Rows are counted locally from P - lead, the
 // 16 B-aligned row at or before the block's first output row P (lead =
 // P mod 4); local row u is block row j = u - lead, valid for lead <= u < span
-// (span = lead + the block's count, below 2^31 + 4).  Block row j copies
-// input row i (the one whose list covers j) and appends entry j - pos[i] of
-// its list.  A whole group is W 16 B stores (4 rows of W words); the first and
-// last group of a block may be partial.
+// (span = lead + the block's count, below 2^31 + 4).  Block row j copies the
+// input row of the entry k whose list covers j and appends entry j - pos[k]
+// of that list.  A whole group is W 16 B stores (4 rows of W words); the
+// first and last group of a block may be partial.
 template <int W>
-__device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint32_t span, const uint32_t *pos,
-                                                const uint32_t *erel, int n, const int32_t *__restrict__ rows,
-                                                const int32_t *__restrict__ edges, int32_t *__restrict__ obase) {
+__device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint32_t span, const ExpandRows &er_,
+                                                const int32_t *__restrict__ rows, const int32_t *__restrict__ edges,
+                                                int32_t *__restrict__ obase) {
     constexpr int C = W - 1;
-    int i = row_of(pos, n, u >= lead ? u - lead : 0u);
-    uint32_t nxt = pos[i + 1];
+    int k = row_of(er_.pos, er_.n, u >= lead ? u - lead : 0u);
+    uint32_t nxt = er_.pos[k + 1];
     int32_t v[4 * W];
-    int ip = -1;       // input row of the previous output row of the group, if valid
-    uint32_t er = 0;   // erel[ip]
+    int kp = -1;       // entry of the previous output row of the group, if valid
+    uint32_t er = 0;   // erel[kp]
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const uint32_t uq = u + (uint32_t)q;
         if (uq >= lead && uq < span) {
             const uint32_t j = uq - lead;
-            while (j >= nxt) nxt = pos[++i + 1];
-            if (q > 0 && i == ip) {
+            while (j >= nxt) nxt = er_.pos[++k + 1];   // one step per list boundary
+            if (q > 0 && k == kp) {
                 // the same input row as the previous output row: copied from registers
 #pragma unroll
                 for (int c = 0; c < C; ++c) v[q * W + c] = v[(q - 1) * W + c];
             } else {
-                const int32_t *src = rows + i * C;
+                const int32_t *src = rows + (int)er_.row[k] * C;
 #pragma unroll
                 for (int c = 0; c < C; ++c) v[q * W + c] = __ldg(src + c);
-                er = erel[i];
+                er = er_.erel[k];
             }
             v[q * W + C] = __ldg(edges + (er + j));
-            ip = i;
+            kp = k;
         } else {
 #pragma unroll
             for (int c = 0; c < W; ++c) v[q * W + c] = 0;
-            ip = -1;
+            kp = -1;
         }
     }
     int32_t *g = obase + (size_t)u * W;
     if (u >= lead && u + 4u <= span) {
 #pragma unroll
-        for (int k = 0; k < W; ++k)
-            reinterpret_cast<int4 *>(g)[k] = make_int4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        for (int k2 = 0; k2 < W; ++k2)
+            reinterpret_cast<int4 *>(g)[k2] = make_int4(v[4 * k2], v[4 * k2 + 1], v[4 * k2 + 2], v[4 * k2 + 3]);
     } else {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -442,9 +454,8 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
                   int64_t ngroups, int64_t nblk, const __grid_constant__ GroupTable gt, int32_t *__restrict__ out) {
     constexpr int kRPT = kRowsPerBlock / kThreads;
     static_assert(kRPT == 4, "4 input rows per thread");
-    __shared__ uint32_t pos[kRowsPerBlock + 1];
-    __shared__ uint32_t erel[kRowsPerBlock];   // a row's list offset minus its first output row
-    __shared__ uint32_t s_w[kThreads / 32];
+    __shared__ ExpandRows xr;
+    __shared__ uint32_t s_w[2][kThreads / 32];
     const int C = W >= 2 ? W - 1 : C_rt;
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
 
@@ -456,7 +467,8 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
     const int64_t r0 = b * kRowsPerBlock;
     const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
 
-    // 2. the block's degrees and edge offsets, 4 rows per thread; local exclusive scan
+    // 2. the block's degrees and edge offsets, 4 rows per thread; local
+    //    exclusive scans of the degrees and of the non-empty rows
     const int q0 = t * kRPT;
     uint32_t d[kRPT], o[kRPT];
     if (q0 + kRPT <= n) {
@@ -472,25 +484,33 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
         }
     }
     const uint32_t ls = d[0] + d[1] + d[2] + d[3];
-    uint32_t is = ls;
+    const uint32_t lc = (d[0] != 0u) + (d[1] != 0u) + (d[2] != 0u) + (d[3] != 0u);
+    uint32_t is = ls, ic = lc;
 #pragma unroll
     for (int sh = 1; sh < 32; sh <<= 1) {
-        const uint32_t x = __shfl_up_sync(FULL, is, sh);
-        if (lane >= sh) is += x;
+        const uint32_t x = __shfl_up_sync(FULL, is, sh), y = __shfl_up_sync(FULL, ic, sh);
+        if (lane >= sh) { is += x; ic += y; }
     }
-    if (lane == 31) s_w[wid] = is;
+    if (lane == 31) { s_w[0][wid] = is; s_w[1][wid] = ic; }
     __syncthreads();
-    uint32_t e = is - ls;
+    uint32_t e = is - ls, kk = ic - lc;
 #pragma unroll
     for (int w = 0; w < kThreads / 32; ++w)
-        if (w < wid) e += s_w[w];
+        if (w < wid) { e += s_w[0][w]; kk += s_w[1][w]; }
 #pragma unroll
     for (int q = 0; q < kRPT; ++q) {
-        pos[q0 + q] = e;
-        erel[q0 + q] = o[q] - e;   // modulo 2^32: erel + j is the entry's index
-        e += d[q];
+        if (d[q]) {
+            xr.pos[kk] = e;
+            xr.erel[kk] = o[q] - e;   // modulo 2^32: erel + j is the entry's index
+            xr.row[kk] = (uint16_t)(q0 + q);
+            ++kk;
+            e += d[q];
+        }
     }
-    if (t == kThreads - 1) pos[kRowsPerBlock] = e;   // the block's total; rows >= n have no list
+    if (t == kThreads - 1) {   // the block's totals; rows >= n have no list
+        xr.pos[kk] = e;
+        xr.n = (int)kk;
+    }
     __syncthreads();
     const unsigned long long P = loc.P;
     const uint32_t T = loc.T;
@@ -503,18 +523,18 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
         const uint32_t u1 = u0 >= span ? u0 : (span - u0 < (uint32_t)kSliceRows ? span : u0 + (uint32_t)kSliceRows);
         int32_t *obase = out + (P - lead) * W;
         for (uint32_t u = u0 + 4u * (uint32_t)t; u < u1; u += 4u * kThreads)
-            k2u_write_group<W>(u, lead, span, pos, erel, n, hblk, edges, obase);
+            k2u_write_group<W>(u, lead, span, xr, hblk, edges, obase);
     } else {
         const int Wd = C + 1;
         int32_t *oblk = out + P * Wd;
         const uint32_t j0 = slice * (uint32_t)kSliceRows;
         const uint32_t j1 = j0 >= T ? j0 : (T - j0 < (uint32_t)kSliceRows ? T : j0 + (uint32_t)kSliceRows);
         for (uint32_t j = j0 + (uint32_t)t; j < j1; j += kThreads) {
-            const int i = row_of(pos, n, j);
+            const int k = row_of(xr.pos, xr.n, j);
             int32_t *dst = oblk + (size_t)j * Wd;
-            const int32_t *src = hblk + (int64_t)i * C;
+            const int32_t *src = hblk + (int64_t)xr.row[k] * C;
             for (int c = 0; c < C; ++c) dst[c] = __ldg(src + c);
-            dst[C] = __ldg(edges + (erel[i] + j));
+            dst[C] = __ldg(edges + (xr.erel[k] + j));
         }
     }
 }
@@ -622,7 +642,27 @@ __device__ __forceinline__ bool list_contains(const int32_t *__restrict__ e, uin
     return f;
 }
 
-// totals[0] += adjacency entries a linear scan would touch, totals[1] += rows kept
+// The general lookup of the filter probe: probe_warp (runs of equal keys
+// probed once) where every lane takes it; in the NB kernel only a lane with an
+// index key (a start value of 0) gets here, alone, and looks itself up.
+template <bool NB>
+__device__ __forceinline__ void probe_view_or_warp(const PredView &pv, int32_t vid, uint32_t dir, uint32_t &o,
+                                                   uint32_t &d, int *err) {
+    if constexpr (NB) {
+        o = 0u;
+        d = vid >= 0 ? probe_view(pv, (uint32_t)vid, dir, &o, err) : 0u;
+    } else {
+        probe_warp(pv, vid, dir, o, d, err);
+    }
+}
+
+// totals[0] += adjacency entries a linear scan would touch, totals[1] += rows kept.
+// NB: the direction is dense and functional, so its neighbour array answers a
+// membership test with one 4 B read (the list holds that neighbour or
+// nothing; a linear scan touches 1 entry or none); a start value of 0 (an
+// index key, hashed) takes the general path.  All rounds' reads are issued
+// before any is used.
+template <bool NB>
 __global__ void __launch_bounds__(kThreads)
 filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, int ecol,
                     int32_t end_const, uint32_t dir, PredView pv,
@@ -639,18 +679,33 @@ filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol
     }
     unsigned int my_nz = 0;
     unsigned long long my_scan = 0;
+    int32_t g[kRounds];   // NB: the neighbour, or -1 (none, or not looked up here)
+    if constexpr (NB) {
+        const int32_t *nba = dir ? pv.nb[1] : pv.nb[0];
+        const uint32_t vmin = dir ? pv.vmin[1] : pv.vmin[0], dn = dir ? pv.dn[1] : pv.dn[0];
+#pragma unroll
+        for (int rd = 0; rd < kRounds; ++rd) {
+            const uint32_t x = (uint32_t)v[rd] - vmin;   // wraps above dn below vmin
+            g[rd] = (v[rd] > 0 && x < dn) ? __ldg(nba + x) : -1;
+        }
+    }
 #pragma unroll
     for (int rd = 0; rd < kRounds; ++rd) {
         const int64_t row0 = wrow0 + rd * 32;
         if (row0 >= R) break;   // warp-uniform
         const int64_t r = row0 + lane;
-        uint32_t o, d;
-        probe_warp(pv, v[rd], dir, o, d, err);
         bool found = false;
-        if (r < R && d > 0u) {
-            uint32_t sc = 0;
-            found = list_contains(pv.edges + o, d, tg[rd], &sc);
-            my_scan += sc;
+        if (NB && v[rd] != 0) {
+            found = r < R && g[rd] >= 0 && g[rd] == tg[rd];
+            my_scan += (r < R && g[rd] >= 0) ? 1u : 0u;
+        } else {
+            uint32_t o, d;
+            probe_view_or_warp<NB>(pv, v[rd], dir, o, d, err);
+            if (r < R && d > 0u) {
+                uint32_t sc = 0;
+                found = list_contains(pv.edges + o, d, tg[rd], &sc);
+                my_scan += sc;
+            }
         }
         const uint32_t m = __ballot_sync(FULL, found);
         if (lane == 0) {
@@ -720,6 +775,104 @@ filter_write_kernel(const int32_t *__restrict__ hist, int64_t R, int C, const ui
     }
 }
 
+// One CTA per block of input rows, for tables of C <= 8 columns: the kept
+// rows are staged in shared memory, then the block's output words [P C,
+// (P + nb) C) stream out as aligned 16 B stores (P the block's look-back
+// prefix, nb its kept rows).  When at least a quarter of the block's rows are
+// kept the whole block is read with 16 B loads and the kept rows picked from
+// shared memory; otherwise each kept row is gathered alone.
+template <int C>
+__global__ void __launch_bounds__(kThreads)
+filter_write_vec_kernel(const int32_t *__restrict__ hist, int64_t R, const uint32_t *__restrict__ mask,
+                        const unsigned int *__restrict__ blk_nz, unsigned long long *flags, int32_t *__restrict__ out) {
+    __shared__ int sel[kRowsPerBlock];
+    __shared__ unsigned int wbase[kRowsPerBlock / 32 + 1];
+    __shared__ unsigned long long s_P;
+    __shared__ __align__(16) int32_t rows[kRowsPerBlock * C];
+    constexpr int kPer = kRowsPerBlock / kThreads;   // 4 rows per thread
+    const int64_t b = blockIdx.x;
+    const unsigned int nb = blk_nz[b];
+    if (nb == 0u) return;   // successors add this block's count (0) as they walk past
+    const int64_t r0 = b * kRowsPerBlock;
+    const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
+    const int64_t nwords_mask = (R + 31) >> 5;
+    const int t = threadIdx.x;
+    if (t < 32) {
+        const int64_t wi = (r0 >> 5) + t;
+        const uint32_t m = wi < nwords_mask ? mask[wi] : 0u;
+        unsigned int c = __popc(m), inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned int v = __shfl_up_sync(FULL, inc, o);
+            if (t >= o) inc += v;
+        }
+        wbase[t] = inc - c;
+        if (t == 31) wbase[32] = inc;
+        const unsigned long long P = lookback_prefix(blk_nz, flags, b);
+        if (t == 0) {
+            st_flag(flags + b, kPrefixReady | (P + nb));
+            s_P = P;
+        }
+    }
+    __syncthreads();
+    {
+        const int wi = (t * kPer) >> 5, bit0 = (t * kPer) & 31;
+        const int64_t mwi = (r0 >> 5) + wi;
+        const uint32_t m = mwi < nwords_mask ? mask[mwi] : 0u;
+        unsigned int pos = wbase[wi] + __popc(m & ((1u << bit0) - 1u));
+#pragma unroll
+        for (int q = 0; q < kPer; ++q)
+            if (m & (1u << (bit0 + q))) sel[pos++] = t * kPer + q;
+    }
+    const int32_t *src = hist + r0 * C;
+    const bool whole = 4u * nb >= (unsigned int)n;   // the same in every thread
+    if (whole) {
+        // the block's n C words; 16 B loads when the block starts on a 16 B boundary
+        const int words = n * C;
+        if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+            for (int i = t; 4 * i < words; i += kThreads) {
+                if (4 * i + 4 <= words) {
+                    reinterpret_cast<int4 *>(rows)[i] = __ldg(reinterpret_cast<const int4 *>(src) + i);
+                } else {
+                    for (int k = 4 * i; k < words; ++k) rows[k] = __ldg(src + k);
+                }
+            }
+        } else {
+            for (int k = t; k < words; k += kThreads) rows[k] = __ldg(src + k);
+        }
+    }
+    __syncthreads();   // sel (and the whole block) complete
+    if (!whole) {
+        for (int j = t; j < (int)nb; j += kThreads) {
+            const int32_t *sr = src + sel[j] * C;
+#pragma unroll
+            for (int c = 0; c < C; ++c) rows[j * C + c] = __ldg(sr + c);
+        }
+        __syncthreads();
+    }
+    // output words [P C, (P + nb) C): int4 stores aligned to 16 B of out
+    const unsigned long long P = s_P;
+    const uint32_t lead = (uint32_t)((P * C) & 3ull), words = nb * C;
+    int32_t *g = out + (P * C - lead);
+    for (uint32_t i = (uint32_t)t; 4u * i < lead + words; i += kThreads) {
+        int32_t v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t kk = 4u * i + j - lead;   // wraps above `words` before the lead
+            v[j] = kk < words ? (whole ? rows[sel[kk / C] * C + kk % C] : rows[kk]) : 0;
+        }
+        if (4u * i >= lead && 4u * i + 4u <= lead + words) {
+            reinterpret_cast<int4 *>(g)[i] = make_int4(v[0], v[1], v[2], v[3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t kk = 4u * i + j - lead;
+                if (kk < words) g[4u * i + j] = v[j];
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------- list copy
 __global__ void copy_list_kernel(const int32_t *__restrict__ src, int64_t n, int32_t *__restrict__ dst) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -732,17 +885,11 @@ static inline unsigned int nblocks_rows(int64_t R) {
 }
 
 void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums,
-                      int *err, bool func, unsigned long long *clear, int64_t nclear, cudaStream_t st) {
+                      int *err, bool func, unsigned long long *clear, int64_t nclear, int sms, cudaStream_t st) {
     const bool dense = (dir ? pv.rp[1] : pv.rp[0]) != nullptr;
     const unsigned int nb = nblocks_rows(R);
     // two blocks per CTA once the op has enough blocks to fill the GPU with half as many CTAs
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms < 1) sms = 1;
-    }
+    if (sms < 1) sms = 1;
     const bool pair = dense && nb >= 16u * (unsigned int)sms;
 #define WK_COUNT(F, D, B) \
     k2u_count_kernel<F, D, B><<<(nb + B - 1) / B, kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, \
@@ -805,16 +952,59 @@ void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edg
 #undef WK_EXPAND
 }
 
+// Load every k2u count and expansion kernel now (with lazy module loading a
+// kernel's code is otherwise loaded, and device memory taken for it, at its
+// first launch).
+int preload_k2u_kernels() {
+    cudaFuncAttributes a;
+    cudaError_t e = cudaSuccess;
+    auto get = [&](const void *f) {
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, f);
+    };
+    get((const void *)k2u_count_kernel<false, false, 1>);
+    get((const void *)k2u_count_kernel<false, true, 1>);
+    get((const void *)k2u_count_kernel<false, true, 2>);
+    get((const void *)k2u_count_kernel<true, false, 1>);
+    get((const void *)k2u_count_kernel<true, true, 1>);
+    get((const void *)k2u_count_kernel<true, true, 2>);
+    get((const void *)k2u_expand_kernel<0>);
+    get((const void *)k2u_expand_kernel<2>);
+    get((const void *)k2u_expand_kernel<3>);
+    get((const void *)k2u_expand_kernel<4>);
+    get((const void *)k2u_expand_kernel<5>);
+    get((const void *)k2u_expand_kernel<6>);
+    get((const void *)k2u_expand_kernel<7>);
+    get((const void *)k2u_expand_kernel<8>);
+    return (int)e;
+}
+
 void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ecol, int32_t end_const,
                          uint32_t dir, PredView pv, uint32_t *mask, unsigned int *blk_nz,
                          unsigned long long *flags, unsigned long long *totals, int *err, cudaStream_t st) {
-    filter_probe_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv, mask,
-                                                              blk_nz, flags, totals, err);
+    if ((dir ? pv.nb[1] : pv.nb[0]) != nullptr)
+        filter_probe_kernel<true><<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv,
+                                                                        mask, blk_nz, flags, totals, err);
+    else
+        filter_probe_kernel<false><<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv,
+                                                                         mask, blk_nz, flags, totals, err);
 }
 
 void launch_filter_write(const int32_t *hist, int64_t R, int C, const uint32_t *mask, const unsigned int *blk_nz,
                          unsigned long long *flags, int32_t *out, cudaStream_t st) {
-    filter_write_kernel<<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, mask, blk_nz, flags, out);
+    const unsigned int g = nblocks_rows(R);
+#define WK_FWRITE(CC) filter_write_vec_kernel<CC><<<g, kThreads, 0, st>>>(hist, R, mask, blk_nz, flags, out)
+    switch (C) {
+        case 1: WK_FWRITE(1); break;
+        case 2: WK_FWRITE(2); break;
+        case 3: WK_FWRITE(3); break;
+        case 4: WK_FWRITE(4); break;
+        case 5: WK_FWRITE(5); break;
+        case 6: WK_FWRITE(6); break;
+        case 7: WK_FWRITE(7); break;
+        case 8: WK_FWRITE(8); break;
+        default: filter_write_kernel<<<g, kThreads, 0, st>>>(hist, R, C, mask, blk_nz, flags, out); break;
+    }
+#undef WK_FWRITE
 }
 
 void launch_copy_list(const int32_t *src, int64_t n, int32_t *dst, cudaStream_t st) {

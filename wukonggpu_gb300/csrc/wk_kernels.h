@@ -36,8 +36,14 @@ struct GroupTable {
 // neighbour as int32 (-1 when there is none) for launch_k2u_expand_func; err
 // bit 3 when a row's list had more than one entry (an index key), which the
 // functional expansion cannot write.
-void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg, uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums,
-                      int *err, bool func, unsigned long long *clear, int64_t nclear, cudaStream_t st);
+// sms: the device's SM count (two input blocks per CTA once an op has 16 per SM).
+void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t dir, PredView pv, uint32_t *deg,
+                      uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums, int *err, bool func,
+                      unsigned long long *clear, int64_t nclear, int sms, cudaStream_t st);
+
+// Load every k2u count and expansion kernel on the current device (they load
+// lazily, at first launch, otherwise); returns a cudaError_t.
+int preload_k2u_kernels();
 
 // k2u pass 2 of a functional direction (2 <= C + 1 <= 8): the matched rows
 // with their neighbour appended, compacted in order; one CTA per non-empty

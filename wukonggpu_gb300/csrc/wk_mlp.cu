@@ -196,10 +196,12 @@ struct wk_mlp {
     int32_t *pids = nullptr;
     int64_t step = 0;
     int64_t kernels = 0;
-    int *d_err = nullptr;        // device flag of the tensor-core GEMM (bit 2: a wait ran out)
+    int *d_err = nullptr;        // device flag of the tensor-core GEMM (bit 2: a wait ran out,
+                                 // bit 3: work left in flight, TMEM kept)
     int *h_err = nullptr;        // pinned mirror
     int status = 0;              // a host-side GEMM failure since the last check
     int sms = 152;               // multiprocessors of the device (GEMM tile width choice)
+    bool broken = false;         // a GEMM left work in flight: no further GEMM is launched
 };
 
 namespace {
@@ -227,6 +229,12 @@ void refresh_bf16(wk_mlp *m, cudaStream_t s) {
 // these products are small, and more CTAs means more copies and products in flight.
 void gemm(wk_mlp *m, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N,
           int K, const float *bias, cudaStream_t s) {
+    if (m->broken) {
+        if (!m->status)
+            m->status = set_error(WK_EDEVICE, "estimator: an earlier tensor-core GEMM left work in flight; "
+                                              "destroy the estimator");
+        return;
+    }
     if (M <= 0 || K <= 0 || N <= 0 || N % 64 || ldc % 4 || ((uintptr_t)C & 15u) || ((uintptr_t)bias & 15u)) {
         if (!m->status) m->status = set_error(WK_EINVAL, "estimator GEMM: shape or alignment (M %d, N %d, K %d)", M, N, K);
         return;
@@ -259,8 +267,16 @@ int check_status(wk_mlp *m, cudaStream_t s, const char *what) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, what);
     if (*m->h_err) {
+        const int f = *m->h_err;
         *m->h_err = 0;
         cudaMemsetAsync(m->d_err, 0, sizeof(int), s);
+        if (f & 8) {
+            // copies or products may still be in flight and their CTA kept its
+            // TMEM: the estimator launches no further GEMM
+            m->broken = true;
+            return set_error(WK_EDEVICE, "%s: a tensor-core GEMM wait ran out with work in flight; "
+                                         "destroy the estimator", what);
+        }
         return set_error(WK_ETIMEDOUT, "%s: a tensor-core GEMM wait ran out", what);
     }
     return WK_OK;

@@ -13,18 +13,20 @@
 //   - at most kMaxRows input rows per call (262,144); a larger call is
 //     rejected with WK_EINVAL before any device work; the output is bounded
 //     only by the caller's capacity (WK_EOVERFLOW, with the row count);
-//   - the array (about 2.1 MB) is held by every GPU that loads the library
-//     until the process exits;
+//   - the array (about 2.1 MB) is loaded on a device, and its address looked
+//     up, when a context is made for that device (wk_ctx_create calls
+//     noalloc_prepare), together with the kernels this entry point launches:
+//     with lazy module loading both would otherwise be loaded -- and device
+//     memory taken -- inside the first call.  The array then stays on that
+//     GPU until the process exits;
 //   - every call shares it and it keeps the last call's contents: the fields
 //     that must start at zero (error flags and group sums) are cleared at the
 //     start of each call, everything else is fully written before it is read.
 //     Calls that overlap on the GPU (from several host threads or several
 //     contexts' streams at once) race on the array and must not be issued;
-//   - the device address of the array is looked up once per device, on the
-//     first call made with that device current (cudaGetSymbolAddress); make
-//     that first call before any stream capture begins.
+//   - a context keeps the address it looked up; it must not be used after a
+//     reset of its device.
 #include <cstdint>
-#include <mutex>
 
 #include "wk_runtime.h"
 
@@ -44,27 +46,19 @@ constexpr size_t kScratchBytes = al(kOffBlkSum + 8 * kMaxBlocks);
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-std::mutex g_mu;
-void *g_addr[256] = {nullptr};   // per device ordinal
-
-// the array's device address for `device` (which must be current)
-int scratch_address(int device, unsigned char **out) {
-    if (device < 0 || device >= 256) return wk::set_error(WK_EINVAL, "noalloc: device ordinal %d", device);
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[device]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return wk::cuda_fail(e == cudaSuccess ? cudaErrorInvalidSymbol : e,
-                                                         "noalloc: cudaGetSymbolAddress");
-        g_addr[device] = p;
-    }
-    *out = static_cast<unsigned char *>(g_addr[device]);
-    return WK_OK;
-}
-
 }  // namespace
 
 using namespace wk;
+
+int wk::noalloc_prepare(unsigned char **scratch) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return cuda_fail(e == cudaSuccess ? cudaErrorInvalidSymbol : e,
+                                                 "noalloc: cudaGetSymbolAddress");
+    if ((e = (cudaError_t)dev::preload_k2u_kernels()) != cudaSuccess) return cuda_fail(e, "noalloc: kernel load");
+    *scratch = static_cast<unsigned char *>(p);
+    return WK_OK;
+}
 
 extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int64_t rows, int32_t cols,
                                            int64_t start, int32_t direction, int32_t predict, int32_t *out,
@@ -90,9 +84,8 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     if (rows == 0) return WK_OK;
-    unsigned char *sc = nullptr;
-    int st = scratch_address(ctx->device, &sc);
-    if (st) return st;
+    unsigned char *sc = ctx->noalloc_scratch;   // looked up when the context was made
+    if (!sc) return set_error(WK_EDEVICE, "known_to_unknown_noalloc: the context has no scratch address");
     int *err = reinterpret_cast<int *>(sc + kOffFlags);
     unsigned long long *gsum = reinterpret_cast<unsigned long long *>(sc + kOffFlags) + 2;
     uint32_t *deg = reinterpret_cast<uint32_t *>(sc + kOffDeg);
@@ -105,7 +98,7 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     if ((e = cudaMemsetAsync(sc + kOffFlags, 0, 32, s)) != cudaSuccess) return cuda_fail(e, "noalloc: clear flags");
     // kMaxRows input rows are one group: its two sums are the op's totals
     dev::launch_k2u_count(hist, rows, cols, scol, (uint32_t)direction, pv, deg, off, blk_sum, gsum, err, false,
-                          nullptr, 0, s);
+                          nullptr, 0, ctx->sms, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: count launch");
     ctx->launches += 1;
     if ((e = cudaMemcpyAsync(ctx->h_scal, sc + kOffFlags, 32, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
@@ -118,17 +111,21 @@ extern "C" int wk_known_to_unknown_noalloc(wk_ctx *ctx, const int32_t *hist, int
     if (ctx->h_scal[0] & 2ull)
         return set_error(WK_EOVERFLOW, "known_to_unknown_noalloc: 1024 consecutive input rows expand to 2^31 rows or more");
     if (R_out == 0) return WK_OK;
-    if (R_out * (cols + 1) > out_capacity)
+    // R_out * (cols + 1) > out_capacity, without forming a product that could overflow
+    const int64_t width = (int64_t)cols + 1;
+    if (R_out > out_capacity / width)
         return set_error(WK_EOVERFLOW,
-                         "known_to_unknown_noalloc: output needs %lld int32 elements, capacity is %lld "
+                         "known_to_unknown_noalloc: output needs %lld rows of %lld int32 elements, capacity is %lld "
                          "(*out_rows holds the row count)",
-                         (long long)(R_out * (cols + 1)), (long long)out_capacity);
+                         (long long)R_out, (long long)width, (long long)out_capacity);
     dev::GroupTable gt;
     gt.n = 1;
     gt.out[0] = 0ull;
     gt.sl[0] = 0u;
     gt.out[1] = ctx->h_scal[2];
-    gt.sl[1] = (unsigned int)ctx->h_scal[3];   // at most 256 blocks' slices
+    // the slices of at most 256 blocks: each block has ceil((count + 3) / 8192)
+    // of them with count below 2^31, so fewer than 2^26 in all
+    gt.sl[1] = (unsigned int)ctx->h_scal[3];
     dev::launch_k2u_expand(hist, rows, cols, pv.edges, deg, off, blk_sum, gsum, gt, ctx->h_scal[3], out, s);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "noalloc: expand launch");
     ctx->launches += 1;

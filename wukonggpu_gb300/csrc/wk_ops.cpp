@@ -172,6 +172,16 @@ int wk::reserve_op_scratch(wk_ctx *ctx, int64_t rows) {
 
 namespace {
 
+// An op's device-buffer reservation.  A context given injected allocation
+// failures (wk_ctx_inject_alloc_failure) fails its next ones with WK_ENOMEM
+// here, as a failed cudaMalloc inside DevBuf::reserve would.
+int take(wk_ctx *ctx, DevBuf &b, size_t bytes) {
+    if (ctx->inject_alloc_fail.load(std::memory_order_relaxed) > 0 &&
+        ctx->inject_alloc_fail.fetch_sub(1, std::memory_order_relaxed) > 0)
+        return set_error(WK_ENOMEM, "cudaMalloc: out of memory (injected allocation failure)");
+    return b.reserve(bytes);
+}
+
 // zero the op totals (dscal[1..3]) before a first pass accumulates into them
 int clear_totals(wk_ctx *ctx) {
     cudaError_t e = cudaMemsetAsync(ctx->dscal.as<unsigned long long>() + 1, 0, 24, ctx->stream);
@@ -191,7 +201,7 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     if (st) return st;
     DevBuf &ob = out_buf(ctx, h);
     if (R == 0) {
-        if ((st = ob.reserve(16))) return st;
+        if ((st = take(ctx, ob, 16))) return st;
         h->data = ob.as<int32_t>();
         h->size = 0;
         h->col_num = C + 1;
@@ -200,8 +210,8 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     }
     const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
     const int64_t groups = (nblk + (1 << dev::kGroupShift) - 1) >> dev::kGroupShift;
-    if ((st = ctx->deg.reserve((size_t)R * 4)) || (st = ctx->off.reserve((size_t)R * 4)) ||
-        (st = ctx->blk_sum.reserve((size_t)nblk * 8)) || (st = reserve_gsum(ctx, groups)))
+    if ((st = take(ctx, ctx->deg, (size_t)R * 4)) || (st = take(ctx, ctx->off, (size_t)R * 4)) ||
+        (st = take(ctx, ctx->blk_sum, (size_t)nblk * 8)) || (st = reserve_gsum(ctx, groups)))
         return st;
     // a functional direction (at most one neighbour per vertex) expands as a
     // compaction; if a row hits an index list (vertex 0) the op reruns unspecialised
@@ -214,7 +224,7 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         if ((st = clk.begin())) return st;
         dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
                               ctx->blk_sum.as<unsigned long long>(), gs + 2, reinterpret_cast<int *>(gs), func,
-                              gsum_buffer(ctx, par ^ 1), 2 + 2 * ctx->gs_used[par ^ 1], ctx->stream);
+                              gsum_buffer(ctx, par ^ 1), 2 + 2 * ctx->gs_used[par ^ 1], ctx->sms, ctx->stream);
         if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;
         ctx->gs_par = par ^ 1;
         ctx->gs_used[par ^ 1] = 0;
@@ -255,9 +265,9 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     ctx->last.rows_out = R_out;
     ctx->last.alg_bytes = 4 * R * C + 16 * R + 4 * R_out + 4 * R_out * (C + 1);
     if (R_out == 0) {
-        if ((st = ob.reserve(16))) return st;
+        if ((st = take(ctx, ob, 16))) return st;
     } else {
-        if ((st = ob.reserve((size_t)R_out * (C + 1) * 4))) return st;
+        if ((st = take(ctx, ob, (size_t)R_out * (C + 1) * 4))) return st;
         if ((st = clk.begin())) return st;
         if (func)
             dev::launch_k2u_expand_func(h->data, R, C, ctx->deg.as<int32_t>(), ctx->blk_sum.as<unsigned long long>(),
@@ -294,15 +304,15 @@ int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const,
     if (st) return st;
     DevBuf &ob = out_buf(ctx, h);
     if (R == 0) {
-        if ((st = ob.reserve(16))) return st;
+        if ((st = take(ctx, ob, 16))) return st;
         h->data = ob.as<int32_t>();
         h->size = 0;
         h->step++;
         return WK_OK;
     }
     const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
-    if ((st = ctx->mask.reserve((size_t)((R + 31) / 32) * 4)) || (st = ctx->blk_nz.reserve((size_t)nblk * 4)) ||
-        (st = ctx->lb_flags.reserve((size_t)nblk * 8)) || (st = ob.reserve((size_t)R * C * 4)) ||
+    if ((st = take(ctx, ctx->mask, (size_t)((R + 31) / 32) * 4)) || (st = take(ctx, ctx->blk_nz, (size_t)nblk * 4)) ||
+        (st = take(ctx, ctx->lb_flags, (size_t)nblk * 8)) || (st = take(ctx, ob, (size_t)R * C * 4)) ||
         (st = clear_totals(ctx)))
         return st;
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
@@ -339,7 +349,7 @@ int op_list(wk_ctx *ctx, wk_history *h, uint64_t vid, uint32_t pid, uint32_t dir
     const uint64_t deg = hs.lookup(vid, pid, dir, &e);
     DevBuf &ob = out_buf(ctx, h);
     int st;
-    if ((st = ob.reserve((size_t)deg * 4 + 16))) return st;
+    if ((st = take(ctx, ob, (size_t)deg * 4 + 16))) return st;
     if (deg) {
         PredView pv;
         if ((st = ensure_seg(ctx, (int)pid, &pv))) return st;
@@ -483,6 +493,12 @@ extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history
     }
     ctx->protect.clear();
     return st;
+}
+
+extern "C" int wk_ctx_inject_alloc_failure(wk_ctx *ctx, int32_t n) {
+    if (!ctx || n < 0) return set_error(WK_EINVAL, "wk_ctx_inject_alloc_failure: bad arguments");
+    ctx->inject_alloc_fail.store(n);
+    return WK_OK;
 }
 
 extern "C" int wk_set_row_limit(wk_ctx *ctx, int64_t max_rows) {

@@ -14,16 +14,6 @@
 
 namespace wk {
 
-static thread_local char g_err[512] = "";
-
-int set_error(int status, const char *fmt, ...) {
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(g_err, sizeof(g_err), fmt, ap);
-    va_end(ap);
-    return status;
-}
-
 int cuda_fail(cudaError_t e, const char *what) {
     cudaGetLastError();
     return set_error(e == cudaErrorMemoryAllocation ? WK_ENOMEM : WK_EDEVICE, "%s: %s (%d)", what,
@@ -136,6 +126,58 @@ void DeviceStore::pool_free(uint64_t off, uint64_t n) {
     }
 }
 
+uint64_t DeviceStore::pool_free_bytes() const {
+    uint64_t f = 0;
+    for (auto &x : free_list) f += x.second;
+    return f;
+}
+
+// Slide every resident segment down to the lowest offsets, in offset order,
+// so that the free space becomes one range at the top of the pool.  Used when
+// the pool's free bytes would hold a segment but no single free range does
+// (segments kept resident, such as the current step's and the prefetched
+// one, can split the free space).  Both streams are drained first, so no
+// kernel or copy uses a segment while it moves; a move copies forward in
+// chunks no longer than the distance moved, so no chunk overwrites bytes not
+// yet copied.  The views of moved segments are updated.
+int DeviceStore::compact(cudaStream_t use_st, cudaStream_t copy_st) {
+    cudaError_t e;
+    if ((e = cudaStreamSynchronize(copy_st)) != cudaSuccess || (e = cudaStreamSynchronize(use_st)) != cudaSuccess)
+        return cuda_fail(e, "segment cache compaction (drain)");
+    std::vector<int> ids;
+    for (int v = 1; v <= hs->num_ids; ++v)
+        if (res[(size_t)v].resident && res[(size_t)v].bytes) ids.push_back(v);
+    std::sort(ids.begin(), ids.end(), [&](int a, int b) { return res[(size_t)a].off < res[(size_t)b].off; });
+    char *base = static_cast<char *>(pool);
+    uint64_t at = 0;
+    for (int v : ids) {
+        Resident &x = res[(size_t)v];
+        if (x.off != at) {
+            const uint64_t dist = x.off - at;   // > 0: segments never overlap and are visited in order
+            for (uint64_t done = 0; done < x.bytes;) {
+                const uint64_t c = std::min(dist, x.bytes - done);
+                if ((e = cudaMemcpyAsync(base + at + done, base + x.off + done, c, cudaMemcpyDeviceToDevice,
+                                         use_st)) != cudaSuccess)
+                    return cuda_fail(e, "segment cache compaction (move)");
+                done += c;
+            }
+            x.off = at;
+            const PredSeg &sg = hs->segs[(size_t)v];
+            char *sb = base + at;
+            char *rb = sb + align256(sg.bucket_bytes());
+            char *eb = rb + align256(sg.rowptr_bytes());
+            views[(size_t)v] = make_view(sg, reinterpret_cast<const Bucket *>(sb), reinterpret_cast<const uint32_t *>(rb),
+                                         reinterpret_cast<const int32_t *>(eb));
+        }
+        at += x.bytes;
+    }
+    if ((e = cudaStreamSynchronize(use_st)) != cudaSuccess) return cuda_fail(e, "segment cache compaction (sync)");
+    free_list.clear();
+    if (at < pool_bytes) free_list[at] = pool_bytes - at;
+    ++compactions;
+    return WK_OK;
+}
+
 // Make segment `id` resident (ShardManager::load_predicate,
 // core/shard_manager.hpp:473-555).  Eviction takes the least recently used
 // segment that is not protected (the reference evicts non-query predicates
@@ -145,7 +187,9 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
     if (!pool) return WK_OK;
     Resident &r = res[(size_t)id];
     ++clock;
+    ++requests;
     if (r.resident) {
+        ++hits;
         r.last_use = clock;
         if (r.ev && copy_st != use_st) {
             cudaError_t e = cudaStreamWaitEvent(use_st, r.ev, 0);
@@ -161,6 +205,12 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
                          (unsigned long long)need, (unsigned long long)pool_bytes);
     uint64_t off = 0;
     while (!pool_alloc(need, &off)) {
+        // free bytes enough but split into ranges: compact rather than evict
+        if (pool_free_bytes() >= need) {
+            int st = compact(use_st, copy_st);
+            if (st) return st;
+            continue;
+        }
         int victim = -1;
         uint64_t oldest = ~0ull;
         for (int v = 1; v <= hs->num_ids; ++v) {
@@ -169,15 +219,12 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
             if (std::find(protect.begin(), protect.end(), v) != protect.end()) continue;
             if (x.last_use < oldest) { oldest = x.last_use; victim = v; }
         }
-        if (victim < 0) {
-            uint64_t free_total = 0;
-            for (auto &f : free_list) free_total += f.second;
+        if (victim < 0)
             return set_error(WK_ENOMEM,
                              "segment cache: cannot fit id %d (%llu bytes) beside the protected segments "
-                             "(%llu bytes free in %zu ranges; the budget must hold the largest segments a "
-                             "query step and its prefetch use at once)",
-                             id, (unsigned long long)need, (unsigned long long)free_total, free_list.size());
-        }
+                             "(%llu bytes free; the budget must hold the largest segments a query step and "
+                             "its prefetch use at once)",
+                             id, (unsigned long long)need, (unsigned long long)pool_free_bytes());
         Resident &x = res[(size_t)victim];
         pool_free(x.off, x.bytes);
         x.resident = false;
@@ -254,21 +301,6 @@ extern "C" void wk_config_default(wk_config *cfg) {
     cfg->enable_prefetch = 1;
 }
 
-extern "C" const char *wk_last_error(void) { return g_err; }
-
-extern "C" const char *wk_status_str(int s) {
-    switch (s) {
-        case WK_OK: return "ok";
-        case WK_EINVAL: return "invalid argument";
-        case WK_ENOMEM: return "out of memory";
-        case WK_ETIMEDOUT: return "timed out";
-        case WK_EDEVICE: return "device error";
-        case WK_ENOSTORE: return "no store";
-        case WK_EOVERFLOW: return "overflow";
-        default: return "unknown status";
-    }
-}
-
 extern "C" int wk_device_count(int *count) {
     if (!count) return set_error(WK_EINVAL, "wk_device_count: null");
     int n = 0;
@@ -308,6 +340,12 @@ extern "C" int wk_ctx_create(const wk_config *cfg_in, wk_ctx **out) {
         delete ctx;
         return r;
     }
+    if ((e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device)) != cudaSuccess) {
+        int r = cuda_fail(e, "wk_ctx_create: SM count");
+        delete ctx;
+        return r;
+    }
+    if ((st = wk::noalloc_prepare(&ctx->noalloc_scratch)) != WK_OK) { delete ctx; return st; }
     if ((st = ctx->dscal.reserve(4096)) != WK_OK) { delete ctx; return st; }
     if ((e = cudaMemset(ctx->dscal.ptr, 0, 4096)) != cudaSuccess) { int r = cuda_fail(e, "wk_ctx_create"); delete ctx; return r; }
     const int64_t hc = cfg.history_capacity > 0 ? cfg.history_capacity : (16ll << 20);
@@ -330,9 +368,8 @@ extern "C" int wk_sync(wk_ctx *ctx) {
 }
 
 namespace wk {
-int device_sort_triples(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
-                        uint32_t max_vid, uint32_t max_pid, std::vector<uint64_t> (&keys)[2],
-                        std::vector<uint32_t> (&pids)[2]);
+int build_store_device(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o, int64_t n, int32_t num_ids,
+                       HostStore **out);
 }
 
 static int store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
@@ -340,12 +377,10 @@ static int store_build(wk_ctx *ctx, const int32_t *s, const int32_t *p, const in
     int st;
     if (ctx->device >= 0 && (st = make_current(ctx))) return st;
     HostStore *hs = nullptr;
-    if (on_device) {
-        const SortTriples sorter = [&](uint32_t max_vid, uint32_t max_pid, std::vector<uint64_t> (&keys)[2],
-                                       std::vector<uint32_t> (&pids)[2]) {
-            return device_sort_triples(ctx, s, p, o, n, max_vid, max_pid, keys, pids);
-        };
-        st = build_host_store(s, p, o, n, num_ids, &hs, &sorter);
+    if (on_device && n > 0) {
+        if (n < 0 || !s || !p || !o || num_ids < 1 || num_ids >= WK_VID_BASE)
+            return set_error(WK_EINVAL, "store build: bad arguments (n=%lld, num_ids=%d)", (long long)n, num_ids);
+        st = build_store_device(ctx, s, p, o, n, num_ids, &hs);
     } else {
         st = build_host_store(s, p, o, n, num_ids, &hs);
     }
@@ -414,6 +449,9 @@ extern "C" int wk_store_get_info(wk_ctx *ctx, wk_store_info *info) {
     info->cache_loads = ctx->store->loads;
     info->cache_evictions = ctx->store->evictions;
     info->cache_bytes_loaded = (int64_t)ctx->store->bytes_loaded;
+    info->cache_requests = ctx->store->requests;
+    info->cache_hits = ctx->store->hits;
+    info->cache_compactions = ctx->store->compactions;
     info->dense_dirs = 0;
     for (int id = 1; id <= hs->num_ids; ++id)
         info->dense_dirs += (hs->segs[(size_t)id].dn[0] ? 1 : 0) + (hs->segs[(size_t)id].dn[1] ? 1 : 0);
@@ -441,6 +479,27 @@ extern "C" int wk_store_pred_stats(wk_ctx *ctx, int32_t id, int64_t *triples, in
     *triples = sg.triples;
     *subjects = sg.subjects;
     *objects = sg.objects;
+    return WK_OK;
+}
+
+extern "C" int wk_store_seg_layout(wk_ctx *ctx, int32_t id, wk_seg_layout *out) {
+    if (!ctx || !out) return set_error(WK_EINVAL, "wk_store_seg_layout: null");
+    if (!ctx->store) return set_error(WK_ENOSTORE, "wk_store_seg_layout: no store");
+    const HostStore *hs = ctx->store->hs.get();
+    if (id < 1 || id > hs->num_ids) return set_error(WK_EINVAL, "wk_store_seg_layout: id %d out of range", id);
+    const PredSeg &sg = hs->segs[(size_t)id];
+    std::memset(out, 0, sizeof(*out));
+    out->keys = (int64_t)sg.nkeys;
+    out->edges = (int64_t)sg.nedges;
+    out->main_buckets = (int32_t)sg.nmain;
+    out->overflow_buckets = (int32_t)sg.nover;
+    for (int d = 0; d < 2; ++d) {
+        out->dense[d] = sg.dn[d] ? 1 : 0;
+        out->functional[d] = sg.maxdeg[d] <= 1u ? 1 : 0;
+        out->bitmap[d] = sg.bn[d] ? 1 : 0;
+        out->max_degree[d] = (int32_t)sg.maxdeg[d];
+    }
+    out->device_bytes = (int64_t)ctx->store->seg_bytes(id);
     return WK_OK;
 }
 

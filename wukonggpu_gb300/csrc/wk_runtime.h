@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <climits>
 #include <map>
 #include <memory>
@@ -15,10 +16,15 @@ namespace wk {
 
 int cuda_fail(cudaError_t e, const char *what);
 
-// growable device buffer (grows by 1.5x, never shrinks)
+// growable device buffer (grows by 1.5x, never shrinks); freed when it goes
+// out of scope (the device it was allocated on must be current then)
 struct DevBuf {
     void *ptr = nullptr;
     size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
     int reserve(size_t nbytes);
     void release();
     template <class T> T *as() const { return static_cast<T *>(ptr); }
@@ -47,7 +53,7 @@ struct DeviceStore {
     uint64_t pool_bytes = 0, clock = 0;
     std::map<uint64_t, uint64_t> free_list;   // offset -> size
     std::vector<Resident> res;
-    int64_t loads = 0, evictions = 0;
+    int64_t loads = 0, evictions = 0, requests = 0, hits = 0, compactions = 0;
     uint64_t bytes_loaded = 0;
 
     ~DeviceStore();
@@ -56,6 +62,8 @@ struct DeviceStore {
     uint64_t seg_bytes(int id) const;
     bool pool_alloc(uint64_t need, uint64_t *off);
     void pool_free(uint64_t off, uint64_t n);
+    uint64_t pool_free_bytes() const;
+    int compact(cudaStream_t use_st, cudaStream_t copy_st);
     int ensure(int id, const std::vector<int> &protect, cudaStream_t copy_st, cudaStream_t use_st,
                cudaEvent_t use_ready);
 };
@@ -64,6 +72,7 @@ struct DeviceStore {
 
 struct wk_ctx {
     int device = 0;                  // -1: host-only context (store image, statistics, planner)
+    int sms = 0;                     // the device's SM count
     wk_config cfg{};
     cudaStream_t stream = nullptr;   // op stream
     cudaStream_t side = nullptr;     // segment prefetch stream
@@ -100,10 +109,22 @@ struct wk_ctx {
     // query-level state (segment cache protection / prefetch)
     std::vector<int> protect;
 
+    // injected allocation failures still to come (wk_ctx_inject_alloc_failure)
+    std::atomic<int> inject_alloc_fail{0};
+
+    // the no-allocation entry point's scratch array on this device, resolved
+    // when the context is made (wk_noalloc.cu)
+    unsigned char *noalloc_scratch = nullptr;
+
     ~wk_ctx();
 };
 
 namespace wk {
+// The device address of the no-allocation entry point's scratch array on the
+// current device, after loading the kernels that entry point launches, so
+// that no later call loads a module or takes device memory (wk_noalloc.cu).
+int noalloc_prepare(unsigned char **scratch);
+
 // Reserve a context's per-op scratch (per-row degree/offset/mask, per-block
 // counts and look-back words) for steps of up to `rows` input rows.
 int reserve_op_scratch(wk_ctx *ctx, int64_t rows);

@@ -62,9 +62,11 @@ struct Req {
     std::vector<int64_t> cmd;
     int npat = 0;
     double arrival = 0.0;
-    bool heavy = false;
+    bool heavy = false;      // the request's class, by shape (the same in both modes)
+    int32_t type = -1;       // the template it was made from (wk_server_submit_typed)
     double proj_bytes = 0.0;
-    std::atomic<int> state{0};   // 0 waiting, 1 running, 2 done, 3 failed
+    // 0 waiting, 1 running, 2 done, 3 failed, 4 refused at admission, 5 cancelled
+    std::atomic<int> state{0};
     int status = 0;
     std::vector<int32_t> result;
     int64_t rows = 0;
@@ -100,13 +102,15 @@ struct wk_server {
     wk_batch *batch[2] = {nullptr, nullptr};
     int32_t *h_res = nullptr;           // pinned download buffer of a batch
     std::deque<std::unique_ptr<Req>> all;
-    std::deque<Req *> light_q, heavy_q;
+    std::deque<Req *> light_q;          // light requests waiting for a batch (mode 1)
+    std::deque<Req *> single_q;         // requests the workers run one at a time
     std::mutex mu;
     std::condition_variable cv;
     std::vector<std::thread> threads;
     clk::time_point t0;
     std::atomic<bool> started{false}, stopping{false};
     std::atomic<int64_t> done_count{0}, failed{0}, batches{0}, batched_reqs{0}, device_launches{0};
+    std::atomic<int64_t> rejected{0}, cancelled{0};
     int64_t submitted = 0;
 
     double now() const { return std::chrono::duration<double>(clk::now() - t0).count(); }
@@ -395,11 +399,17 @@ extern "C" int wk_server_create(wk_ctx *ctx, const wk_server_config *cfg, wk_ser
 }
 
 extern "C" int64_t wk_server_submit(wk_server *s, const int64_t *cmd, int32_t npat, double arrival_s) {
+    return wk_server_submit_typed(s, cmd, npat, arrival_s, -1);
+}
+
+extern "C" int64_t wk_server_submit_typed(wk_server *s, const int64_t *cmd, int32_t npat, double arrival_s,
+                                          int32_t type) {
     if (!s || !cmd || npat < 1 || npat > 16) return set_error(WK_EINVAL, "wk_server_submit: bad arguments");
     std::unique_ptr<Req> r(new Req());
     r->cmd.assign(cmd, cmd + (size_t)npat * 4);
     r->npat = npat;
     r->arrival = arrival_s;
+    r->type = type;
     bool empty = false;
     if (s->cfg.plan) {
         std::vector<int64_t> out((size_t)(npat + 2) * 4);
@@ -413,15 +423,27 @@ extern "C" int64_t wk_server_submit(wk_server *s, const int64_t *cmd, int32_t np
             }
         }
     }
-    // light: a constant start the batch accepts; index starts stay heavy
-    r->heavy = s->cfg.mode == 0 || r->cmd[0] < WK_VID_BASE ||
+    // the class, by shape in both modes: light is a constant start the batch
+    // accepts, heavy everything else (index starts, longer queries); where it
+    // runs is separate -- mode 0 runs every request on the single worker
+    r->heavy = r->cmd[0] < WK_VID_BASE ||
                !batch_compatible(r->cmd, r->npat, s->cfg.max_steps, s->ctx->store->hs->num_ids);
     r->proj_bytes = projected_bytes(s->ctx, r->cmd, r->npat);
+    // admission by projected history bytes: a request over the cap is refused
+    const bool refuse = s->cfg.max_request_bytes > 0 && r->proj_bytes > (double)s->cfg.max_request_bytes;
     Req *raw = r.get();
     std::lock_guard<std::mutex> lk(s->mu);
     r->id = (int64_t)s->all.size();
     s->all.push_back(std::move(r));
     s->submitted++;
+    if (refuse) {
+        raw->status = WK_EREJECTED;
+        raw->done_t = raw->arrival;
+        raw->state.store(4);
+        s->rejected++;
+        s->done_count++;
+        return raw->id;
+    }
     if (empty) {
         raw->rows = 0;
         raw->cols = 0;
@@ -431,7 +453,7 @@ extern "C" int64_t wk_server_submit(wk_server *s, const int64_t *cmd, int32_t np
         s->done_count++;
         return raw->id;
     }
-    auto &q = raw->heavy ? s->heavy_q : s->light_q;
+    auto &q = (s->cfg.mode == 0 || raw->heavy) ? s->single_q : s->light_q;
     auto it = std::upper_bound(q.begin(), q.end(), raw, [](Req *a, Req *b) { return a->arrival < b->arrival; });
     q.insert(it, raw);
     s->cv.notify_all();
@@ -443,10 +465,10 @@ extern "C" int wk_server_start(wk_server *s) {
     if (s->started.exchange(true)) return set_error(WK_EINVAL, "wk_server_start: already started");
     s->t0 = clk::now();
     if (s->cfg.mode == 0) {
-        s->threads.emplace_back(single_loop, s, s->workers[0], &s->heavy_q);
+        s->threads.emplace_back(single_loop, s, s->workers[0], &s->single_q);
     } else {
         s->threads.emplace_back(batch_loop, s);
-        for (wk_ctx *w : s->workers) s->threads.emplace_back(single_loop, s, w, &s->heavy_q);
+        for (wk_ctx *w : s->workers) s->threads.emplace_back(single_loop, s, w, &s->single_q);
     }
     return WK_OK;
 }
@@ -493,7 +515,8 @@ extern "C" int wk_server_get_stats(wk_server *s, wk_server_stats *out) {
     {
         std::lock_guard<std::mutex> lk(s->mu);
         for (auto &r : s->all) {
-            if (r->state.load() < 2) continue;
+            const int stt = r->state.load();
+            if (stt != 2 && stt != 3) continue;   // waiting, running, refused or cancelled
             const double lat = r->done_t - r->arrival;
             all.push_back(lat);
             (r->heavy ? heavy : light).push_back(lat);
@@ -515,7 +538,65 @@ extern "C" int wk_server_get_stats(wk_server *s, wk_server_stats *out) {
     out->light_p99_ms = pct(light, 0.99) * 1e3;
     out->heavy_p50_ms = pct(heavy, 0.50) * 1e3;
     out->heavy_p99_ms = pct(heavy, 0.99) * 1e3;
+    out->rejected = s->rejected.load();
+    out->cancelled = s->cancelled.load();
     return WK_OK;
+}
+
+extern "C" int wk_server_type_stats(wk_server *s, int32_t type, wk_type_stats *out) {
+    if (!s || !out) return set_error(WK_EINVAL, "wk_server_type_stats: null");
+    std::memset(out, 0, sizeof(*out));
+    std::vector<double> v;
+    double first = 1e300, last = 0.0;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto &r : s->all) {
+            const int stt = r->state.load();
+            if (stt != 2 && stt != 3) continue;
+            first = std::min(first, r->arrival);
+            last = std::max(last, r->done_t);
+            if (r->type != type) continue;
+            v.push_back(r->done_t - r->arrival);
+            if (stt == 3) out->failed++;
+        }
+    }
+    std::sort(v.begin(), v.end());
+    out->completed = (int64_t)v.size();
+    out->qps = last > first ? (double)v.size() / (last - first) : 0.0;
+    out->p50_ms = rank_at(v, 0.50) * 1e3;
+    out->p99_ms = rank_at(v, 0.99) * 1e3;
+    for (int k = 0; k < WK_CDF_POINTS; ++k) out->cdf_ms[k] = rank_at(v, cdf_rate(k)) * 1e3;
+    return WK_OK;
+}
+
+extern "C" int wk_server_cancel(wk_server *s, int64_t id) {
+    if (!s) return set_error(WK_EINVAL, "wk_server_cancel: null");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (id < 0 || id >= (int64_t)s->all.size()) return set_error(WK_EINVAL, "wk_server_cancel: id %lld", (long long)id);
+    Req *r = s->all[(size_t)id].get();
+    // a request still in a queue has not started: the loops take requests
+    // out of their queue under this lock before they run them
+    for (std::deque<Req *> *q : {&s->light_q, &s->single_q}) {
+        auto it = std::find(q->begin(), q->end(), r);
+        if (it == q->end()) continue;
+        q->erase(it);
+        r->status = WK_ECANCELED;
+        r->done_t = s->started.load() ? s->now() : r->arrival;
+        r->state.store(5);
+        s->cancelled++;
+        s->done_count++;
+        s->cv.notify_all();
+        return WK_OK;
+    }
+    return set_error(WK_EINVAL, "wk_server_cancel: request %lld is running or finished", (long long)id);
+}
+
+extern "C" int wk_server_inject_alloc_failure(wk_server *s, int32_t worker, int32_t n) {
+    if (!s || n < 0 || worker < -1 || worker >= (int32_t)s->workers.size())
+        return set_error(WK_EINVAL, "wk_server_inject_alloc_failure: bad arguments");
+    wk_ctx *c = worker < 0 ? s->solo : s->workers[(size_t)worker];
+    if (!c) return set_error(WK_EINVAL, "wk_server_inject_alloc_failure: no such context in this mode");
+    return wk_ctx_inject_alloc_failure(c, n);
 }
 
 extern "C" int wk_server_latency_cdf(wk_server *s, int32_t cls, double *out_ms) {
@@ -524,7 +605,8 @@ extern "C" int wk_server_latency_cdf(wk_server *s, int32_t cls, double *out_ms) 
     {
         std::lock_guard<std::mutex> lk(s->mu);
         for (auto &r : s->all) {
-            if (r->state.load() < 2) continue;
+            const int stt = r->state.load();
+            if (stt != 2 && stt != 3) continue;
             if (cls == 1 && r->heavy) continue;
             if (cls == 2 && !r->heavy) continue;
             v.push_back(r->done_t - r->arrival);

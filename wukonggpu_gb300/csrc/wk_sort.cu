@@ -205,68 +205,65 @@ int bits_of(uint64_t v) {
 
 }  // namespace sortdev
 
-// Sort the n triples by (predicate, hi, lo) for both orders on the device of
-// ctx; the results come back as host arrays (key = hi << 32 | lo and the
-// predicate of each pair), duplicates included.
-int device_sort_triples(wk_ctx *ctx, const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
-                        uint32_t max_vid, uint32_t max_pid, std::vector<uint64_t> (&keys)[2],
-                        std::vector<uint32_t> (&pids)[2]) {
+// Exclusive scan of m uint32 values in place on stream st (the sum of all m
+// must stay below 2^32); scratch receives the block sums.
+int scan_u32_device(uint32_t *x, int64_t m, DevBuf &scratch, cudaStream_t st, int64_t *launches) {
     using namespace sortdev;
-    for (int k = 0; k < 2; ++k) {
-        keys[k].assign((size_t)n, 0ull);
-        pids[k].assign((size_t)n, 0u);
-    }
-    if (n == 0) return WK_OK;
-    cudaStream_t st = ctx->stream;
+    if (m <= 0) return WK_OK;
+    const int64_t nb = (m + kScanBlock - 1) / kScanBlock;
+    int rc = scratch.reserve((size_t)nb * 4);
+    if (rc) return rc;
+    scan_sums_kernel<<<(unsigned int)nb, kThreads, 0, st>>>(x, m, scratch.as<uint32_t>());
+    scan_top_kernel<<<1, kThreads, 0, st>>>(scratch.as<uint32_t>(), nb);
+    scan_apply_kernel<<<(unsigned int)nb, kThreads, 0, st>>>(x, m, scratch.as<uint32_t>());
+    if (launches) *launches += 3;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "device scan");
+}
+
+// Stable LSD radix sort of n (key, id) pairs on stream st by (id, key): the
+// key's 8-bit digits at the given bit offsets (0..56), then the id's digits
+// up to id_bits.  key/id hold the input and receive the result; key_tmp and
+// id_tmp are ping-pong buffers of the same sizes.
+int sort_pairs_device(uint64_t *key, uint32_t *id, uint64_t *key_tmp, uint32_t *id_tmp, int64_t n,
+                      const std::vector<int> &key_shifts, int id_bits, cudaStream_t st, int64_t *launches) {
+    using namespace sortdev;
+    if (n <= 1) return WK_OK;
     const int64_t ntiles = (n + kTile - 1) / kTile;
     const int64_t m = ntiles * kBins;
-    const int64_t nb = (m + kScanBlock - 1) / kScanBlock;
-    DevBuf tri, kb[2], pb[2], cnt, bs;
+    DevBuf cnt, bs;
     int rc;
-    if ((rc = tri.reserve((size_t)n * 12)) || (rc = kb[0].reserve((size_t)n * 8)) || (rc = kb[1].reserve((size_t)n * 8)) ||
-        (rc = pb[0].reserve((size_t)n * 4)) || (rc = pb[1].reserve((size_t)n * 4)) ||
-        (rc = cnt.reserve((size_t)m * 4)) || (rc = bs.reserve((size_t)nb * 4))) {
-        tri.release(); kb[0].release(); kb[1].release(); pb[0].release(); pb[1].release(); cnt.release(); bs.release();
-        return rc;
-    }
-    int32_t *ds = tri.as<int32_t>(), *dp = ds + n, *dobj = dp + n;
-    cudaError_t e = cudaSuccess;
-    if ((e = cudaMemcpyAsync(ds, s, (size_t)n * 4, cudaMemcpyHostToDevice, st)) == cudaSuccess &&
-        (e = cudaMemcpyAsync(dp, p, (size_t)n * 4, cudaMemcpyHostToDevice, st)) == cudaSuccess)
-        e = cudaMemcpyAsync(dobj, o, (size_t)n * 4, cudaMemcpyHostToDevice, st);
-    // digit passes: lo, hi (both below max_vid), then the predicate
-    std::vector<int> shifts;
-    const int vb = bits_of(max_vid), pb_bits = bits_of(max_pid);
-    for (int sh = 0; sh < vb; sh += 8) shifts.push_back(sh);
-    for (int sh = 0; sh < vb; sh += 8) shifts.push_back(32 + sh);
-    for (int sh = 0; sh < pb_bits; sh += 8) shifts.push_back(64 + sh);
+    if ((rc = cnt.reserve((size_t)m * 4))) return rc;
+    std::vector<int> shifts(key_shifts);
+    for (int sh = 0; sh < id_bits; sh += 8) shifts.push_back(64 + sh);
+    uint64_t *kb[2] = {key, key_tmp};
+    uint32_t *pb[2] = {id, id_tmp};
+    int cur = 0;
     const unsigned int gt = (unsigned int)ntiles;
-    for (int order = 0; order < 2 && e == cudaSuccess; ++order) {
-        pack_kernel<<<1024, 256, 0, st>>>(ds, dp, dobj, n, order, kb[0].as<uint64_t>(), pb[0].as<uint32_t>());
-        int cur = 0;
-        for (int sh : shifts) {
-            hist_kernel<<<gt, kThreads, 0, st>>>(kb[cur].as<uint64_t>(), pb[cur].as<uint32_t>(), n, sh,
-                                                 cnt.as<uint32_t>(), ntiles);
-            scan_sums_kernel<<<(unsigned int)nb, kThreads, 0, st>>>(cnt.as<uint32_t>(), m, bs.as<uint32_t>());
-            scan_top_kernel<<<1, kThreads, 0, st>>>(bs.as<uint32_t>(), nb);
-            scan_apply_kernel<<<(unsigned int)nb, kThreads, 0, st>>>(cnt.as<uint32_t>(), m, bs.as<uint32_t>());
-            scatter_kernel<<<gt, kThreads, 0, st>>>(kb[cur].as<uint64_t>(), pb[cur].as<uint32_t>(), n, sh,
-                                                    cnt.as<uint32_t>(), ntiles, kb[1 - cur].as<uint64_t>(),
-                                                    pb[1 - cur].as<uint32_t>());
-            ctx->launches += 5;
-            cur = 1 - cur;
-        }
-        ctx->launches += 1;
-        if ((e = cudaGetLastError()) != cudaSuccess) break;
-        if ((e = cudaMemcpyAsync(keys[order].data(), kb[cur].ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, st)) !=
-                cudaSuccess ||
-            (e = cudaMemcpyAsync(pids[order].data(), pb[cur].ptr, (size_t)n * 4, cudaMemcpyDeviceToHost, st)) !=
-                cudaSuccess)
-            break;
-        e = cudaStreamSynchronize(st);
+    for (int sh : shifts) {
+        hist_kernel<<<gt, kThreads, 0, st>>>(kb[cur], pb[cur], n, sh, cnt.as<uint32_t>(), ntiles);
+        if ((rc = scan_u32_device(cnt.as<uint32_t>(), m, bs, st, launches))) return rc;
+        scatter_kernel<<<gt, kThreads, 0, st>>>(kb[cur], pb[cur], n, sh, cnt.as<uint32_t>(), ntiles, kb[1 - cur],
+                                                pb[1 - cur]);
+        if (launches) *launches += 2;
+        cur = 1 - cur;
     }
-    tri.release(); kb[0].release(); kb[1].release(); pb[0].release(); pb[1].release(); cnt.release(); bs.release();
-    return e == cudaSuccess ? WK_OK : cuda_fail(e, "store build: device sort");
+    cudaError_t e = cudaSuccess;
+    if (cur == 1) {   // the result is in the tmp buffers: move it back
+        if ((e = cudaMemcpyAsync(key, key_tmp, (size_t)n * 8, cudaMemcpyDeviceToDevice, st)) == cudaSuccess)
+            e = cudaMemcpyAsync(id, id_tmp, (size_t)n * 4, cudaMemcpyDeviceToDevice, st);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e == cudaSuccess ? WK_OK : cuda_fail(e, "device sort");
 }
+
+// Pack the triples of one order (0: s << 32 | o, 1: o << 32 | s) with their
+// predicates, from device copies of s, p, o.
+void pack_triples_device(const int32_t *s, const int32_t *p, const int32_t *o, int64_t n, int order, uint64_t *key,
+                         uint32_t *pid, cudaStream_t st) {
+    sortdev::pack_kernel<<<1024, 256, 0, st>>>(s, p, o, n, order, key, pid);
+}
+
+int radix_bits(uint64_t v) { return sortdev::bits_of(v); }
 
 }  // namespace wk

@@ -284,14 +284,12 @@ void parallel_for(size_t n, F f) {
 }  // namespace
 
 int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64_t n,
-                     int32_t num_ids, HostStore **out, const SortTriples *device_sort) {
+                     int32_t num_ids, HostStore **out) {
     if (n < 0 || (n > 0 && (!s || !p || !o)) || num_ids < 1 || num_ids >= WK_VID_BASE)
         return set_error(WK_EINVAL, "store build: bad arguments (n=%lld, num_ids=%d)", (long long)n, num_ids);
     // validate and bucket triples by predicate (counting sort)
     std::vector<int64_t> cnt((size_t)num_ids + 2, 0);
-    uint32_t max_vid = 0;
     for (int64_t i = 0; i < n; ++i) {
-        max_vid = std::max(max_vid, (uint32_t)std::max(s[i], o[i]));
         int32_t pi = p[i];
         if (pi < 1 || pi > num_ids)
             return set_error(WK_EINVAL, "store build: triple %lld has predicate %d outside [1,%d]",
@@ -311,17 +309,9 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
     }
     std::vector<int64_t> start((size_t)num_ids + 2, 0);
     for (int32_t i = 1; i <= num_ids + 1; ++i) start[(size_t)i] = start[(size_t)i - 1] + cnt[(size_t)i - 1];
-    // Either the triples sorted by (p, s, o) and (p, o, s) on the device
-    // (order k in keys[k], each id's run at [start[id], start[id + 1])), or the
-    // host's counting sort by p, whose runs emit_groups sorts per id.
-    std::vector<uint64_t> keys[2];
-    std::vector<uint32_t> kpid[2];
-    std::vector<uint64_t> so;       // host path: packed s<<32|o, grouped by p
-    if (device_sort) {
-        int st = (*device_sort)(max_vid, (uint32_t)num_ids, keys, kpid);
-        if (st) return st;
-    } else {
-        so.resize((size_t)n);
+    // a counting sort by p, whose runs emit_groups sorts per id
+    std::vector<uint64_t> so((size_t)n);   // packed s<<32|o, grouped by p
+    {
         std::vector<int64_t> at(start);
         for (int64_t i = 0; i < n; ++i)
             so[(size_t)at[(size_t)p[i]]++] = ((uint64_t)(uint32_t)s[i] << 32) | (uint32_t)o[i];
@@ -333,19 +323,12 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
     {
         const int64_t a = start[WK_TYPE_ID], b = start[WK_TYPE_ID + 1];
         std::vector<uint64_t> cs;
-        if (device_sort) {
-            sb[WK_TYPE_ID].triples = (int64_t)emit_sorted(keys[0].data() + a, (size_t)(b - a), WK_DIR_OUT,
-                                                          sb[WK_TYPE_ID], nullptr);
-            cs.assign(keys[1].begin() + a, keys[1].begin() + b);   // (class, s), sorted
-            cs.erase(std::unique(cs.begin(), cs.end()), cs.end());
-        } else {
-            std::vector<uint64_t> out_pairs(so.begin() + a, so.begin() + b);
-            emit_groups(out_pairs, WK_DIR_OUT, sb[WK_TYPE_ID], nullptr);
-            sb[WK_TYPE_ID].triples = (int64_t)out_pairs.size();
-            cs.reserve(out_pairs.size());
-            for (uint64_t x : out_pairs) cs.push_back(((x & 0xffffffffull) << 32) | (x >> 32));
-            std::sort(cs.begin(), cs.end());
-        }
+        std::vector<uint64_t> out_pairs(so.begin() + a, so.begin() + b);
+        emit_groups(out_pairs, WK_DIR_OUT, sb[WK_TYPE_ID], nullptr);
+        sb[WK_TYPE_ID].triples = (int64_t)out_pairs.size();
+        cs.reserve(out_pairs.size());
+        for (uint64_t x : out_pairs) cs.push_back(((x & 0xffffffffull) << 32) | (x >> 32));
+        std::sort(cs.begin(), cs.end());
         sb[WK_TYPE_ID].subjects = (int64_t)sb[WK_TYPE_ID].keys.size();
         for (uint64_t x : cs) class_members[(size_t)(x >> 32)].push_back((int32_t)(uint32_t)x);
     }
@@ -355,17 +338,11 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         SegBuild &b = sb[id];
         if (id != WK_TYPE_ID && cnt[id] > 0) {
             std::vector<int32_t> subjects, objects;
-            if (device_sort) {
-                const size_t a0 = (size_t)start[id], len = (size_t)(start[id + 1] - start[id]);
-                b.triples = (int64_t)emit_sorted(keys[0].data() + a0, len, WK_DIR_OUT, b, &subjects);
-                emit_sorted(keys[1].data() + a0, len, WK_DIR_IN, b, &objects);
-            } else {
-                std::vector<uint64_t> pairs(so.begin() + start[id], so.begin() + start[id + 1]);
-                emit_groups(pairs, WK_DIR_OUT, b, &subjects);
-                b.triples = (int64_t)pairs.size();
-                for (auto &x : pairs) x = ((x & 0xffffffffull) << 32) | (x >> 32);
-                emit_groups(pairs, WK_DIR_IN, b, &objects);
-            }
+            std::vector<uint64_t> pairs(so.begin() + start[id], so.begin() + start[id + 1]);
+            emit_groups(pairs, WK_DIR_OUT, b, &subjects);
+            b.triples = (int64_t)pairs.size();
+            for (auto &x : pairs) x = ((x & 0xffffffffull) << 32) | (x >> 32);
+            emit_groups(pairs, WK_DIR_IN, b, &objects);
             add_index(WK_DIR_IN, subjects, b);    // [0|p|IN]  subjects of p
             add_index(WK_DIR_OUT, objects, b);    // [0|p|OUT] objects of p
             b.subjects = (int64_t)subjects.size();
@@ -378,10 +355,6 @@ int build_host_store(const int32_t *s, const int32_t *p, const int32_t *o, int64
         }
     });
     std::vector<uint64_t>().swap(so);
-    for (int k = 0; k < 2; ++k) {
-        std::vector<uint64_t>().swap(keys[k]);
-        std::vector<uint32_t>().swap(kpid[k]);
-    }
     parallel_for((size_t)num_ids + 1, [&](size_t id) {
         if (id) split_dense(sb[id]);
     });

@@ -16,9 +16,14 @@
 //     32-column chunks with tcgen05.ld, stages each chunk in shared memory (the
 //     pipeline stages are free by then) and writes it out as whole rows of
 //     float4 with the bias added, so a store instruction covers 4 rows x 128 B.
-// Every mbarrier wait is bounded; a wait that runs out sets bit 2 of *err,
-// waits (bounded) for the copies and products already issued, frees TMEM and
-// returns.
+// Every mbarrier wait is bounded.  A wait that runs out sets bit 2 of *err and
+// stops the pipeline: the producer waits (bounded) for the copies it issued
+// and the issuer for the last commit of the products it issued.  If those
+// drain waits also run out, work may still be in flight, so the CTA sets bit
+// 3 as well and exits without freeing its TMEM columns -- a unit still
+// writing them must not find them given to another CTA.  The host then
+// refuses every later call on the estimator (the TMEM and the device state
+// are no longer trusted); nothing is reused.
 #pragma once
 
 #include <cstdint>
@@ -95,6 +100,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     __shared__ uint32_t s_tmem;
     __shared__ __align__(8) uint64_t s_full[kStages], s_empty[kStages];
     __shared__ volatile int s_fail;
+    __shared__ volatile int s_inflight;   // a drain wait ran out: copies or products may be in flight
     // 128 B swizzle: stage bases 1024 B aligned
     unsigned char *sm = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -107,6 +113,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     }
     if (t == 0) {
         s_fail = 0;
+        s_inflight = 0;
         for (int i = 0; i < kStages; ++i) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_full[i])));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_empty[i])));
@@ -135,7 +142,11 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         }
         // every copy in flight lands before the CTA can leave (immediate when all were consumed)
         for (int j = issued > kStages ? issued - kStages : 0; j < issued; ++j)
-            mbar_wait(smem_u32(&s_full[j % kStages]), (uint32_t)((j / kStages) & 1));
+            if (!mbar_wait(smem_u32(&s_full[j % kStages]), (uint32_t)((j / kStages) & 1))) {
+                s_fail = 1;
+                s_inflight = 1;
+                break;
+            }
     } else if (t == 32) {
         int committed = 0;
         for (int sl = 0; sl < nslab; ++sl) {
@@ -161,7 +172,10 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         // the last commit covers every product issued: they complete before TMEM is read or freed
         if (committed > 0) {
             const int c = committed - 1;
-            if (!mbar_wait(smem_u32(&s_empty[c % kStages]), (uint32_t)((c / kStages) & 1))) s_fail = 1;
+            if (!mbar_wait(smem_u32(&s_empty[c % kStages]), (uint32_t)((c / kStages) & 1))) {
+                s_fail = 1;
+                s_inflight = 1;
+            }
         }
     }
     __syncthreads();
@@ -192,11 +206,12 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             __syncwarp();
         }
     } else if (s_fail && t == 0) {
-        atomicOr(err, 4);
+        atomicOr(err, s_inflight ? (4 | 8) : 4);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) {
+    // products still in flight may write these columns: they stay allocated
+    if (warp == 0 && !s_inflight) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN));
     }

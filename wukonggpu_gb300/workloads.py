@@ -131,6 +131,27 @@ def scale_queries(per_shape: int = 5):
     return out
 
 
+def scale_filter_queries():
+    """The single-query-scale shapes closed by checks: cycles back to a bound
+    column (known_to_known) and constant objects (known_to_const), each keeping
+    a fraction of its rows (1e4..1e7 input rows per check on the 100M graph)."""
+    C = SQ_FIRST_CLASS
+    f, z, m = SQ_FUNC, SQ_ZIPF, SQ_M2O
+    return [
+        # ?x type C . ?x m1 ?h . ?h m1^-1 ?y . ?y m2 ?h (k2k: the co-member's other hub is ?h)
+        ("k2k_hub_cycle", [C, TYPE_ID, IN, -1, -1, m[0], OUT, -2, -2, m[0], IN, -3, -3, m[1], OUT, -2]),
+        # ?x type C . ?x z1^-1 ?y . ?y m3 ?h . ?x m3 ?h (k2k: a star closed on a shared hub)
+        ("k2k_shared_hub", [C + 1, TYPE_ID, IN, -1, -1, z[0], IN, -2, -2, m[2], OUT, -3, -1, m[2], OUT, -3]),
+        # ?x type C . ?x m1 ?h . ?h m1^-1 ?y . ?y f1 ?a . ?x f1 ?a (k2k on a functional predicate)
+        ("k2k_functional", [C, TYPE_ID, IN, -1, -1, m[0], OUT, -2, -2, m[0], IN, -3, -3, f[0], OUT, -4,
+                            -1, f[0], OUT, -4]),
+        # ?x type C . ?x z2 ?y . ?y type C' (k2c on another class)
+        ("k2c_other_class", [C + 3, TYPE_ID, IN, -1, -1, z[1], OUT, -2, -2, TYPE_ID, OUT, C + 4]),
+        # ?x type C . ?x m1 ?h . ?h m1^-1 ?y . ?y type C (k2c: co-members of the same class)
+        ("k2c_same_class", [C + 5, TYPE_ID, IN, -1, -1, m[3], OUT, -2, -2, m[3], IN, -3, -3, TYPE_ID, OUT, C + 5]),
+    ]
+
+
 # ---------------------------------------------------------- random BGPs
 def random_bgps(s, p, o, n: int, seed: int, min_pat: int = 2, max_pat: int = 6, first_class: int | None = None,
                 n_classes: int = 0, const_frac: float = 0.4):
