@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--one-query", type=int, default=-1,
                     help="run query N of the mix once, op by op, print each op's stats and exit "
                          "(a fixed launch sequence for ncu captures)")
+    ap.add_argument("--one-query-group", default="mix", choices=["mix", "filter"],
+                    help="the query group --one-query takes query N from: the headline mix or the filter group")
     ap.add_argument("--e2e-contexts", type=int, default=4,
                     help="contexts (one host thread each) that share the store in the end-to-end pass")
     ap.add_argument("--parity-serving-scale", type=float, default=0.05,
@@ -385,7 +387,8 @@ def run_one_query(args):
     g = W.Graph(W.spec_single_query(scale=args.scale))
     rc = W.RCache(device=0)
     rc.build_store_graph(g)
-    name, q = workloads.scale_queries()[args.one_query]
+    group = workloads.scale_queries() if args.one_query_group == "mix" else workloads.scale_filter_queries()
+    name, q = group[args.one_query]
     rc.enable_timing(True)
     req = W.Request(q)
     for i in range(len(q) // 4):

@@ -214,6 +214,28 @@ int wk_history_upload(wk_ctx *ctx, wk_history *h, const int32_t *host, int64_t s
 int wk_history_download(wk_ctx *ctx, const wk_history *h, int32_t *host, int64_t cap);
 void wk_history_init(wk_history *h);
 
+/* ------------------------------------------------------ fork-join across ranks
+ * Split a table by the rank that owns each row's start vertex, the device
+ * side of a fork-join step (RCache::generate_sub_query, core/rcache.hpp:
+ * 964-1030, with calc_dispatched_position / history_dispatch,
+ * core/gpu_hash.cu:698-790).  `start` is the bound variable of the next
+ * pattern (column -start-1); a row goes to part value % nparts
+ * (mymath::hash_mod, utils/mymath.hpp:55-59; values are vertex ids, >= 0).
+ * On return *out holds the parts one after another, each in the input's
+ * row order, in the ping-pong partner of the input's buffer, and
+ * part_rows[0..nparts) their row counts.  1 <= nparts <= 256; fewer than
+ * 2^32 - 1 rows.  `out` may be `in`. */
+int wk_history_partition(wk_ctx *ctx, const wk_history *in, int64_t start, int32_t nparts,
+                         int64_t *part_rows, wk_history *out);
+
+/* Device-to-device transfers for a collective's buffers: copy the table of
+ * *h to `dst` (cap int32 elements; WK_EINVAL when smaller than h->size), and
+ * make *h a table of `size` elements in `col_num` columns copied from
+ * `src`, in the context's first history buffer (h->step is kept).  Both
+ * return after the copy is complete. */
+int wk_history_to_device(wk_ctx *ctx, const wk_history *h, int32_t *dst, int64_t cap);
+int wk_history_from_device(wk_ctx *ctx, wk_history *h, const int32_t *src, int64_t size, int32_t col_num);
+
 /* ------------------------------------------------------ whole query
  * Execute every pattern of `cmd_chains` (n_patterns x {start, pid, dir, end},
  * core/query.hpp:68) with the step dispatch of GPU_Engine::execute_one_step

@@ -44,6 +44,7 @@ def test_gradients_match_cpu_oracle(gpu_small, M):
             continue
         cos = float(x @ y / (np.linalg.norm(x) * ny + 1e-30))
         rel = float(np.linalg.norm(x - y) / ny)
+        print(f"gradient block {name} M={M}: cos {cos:.6f} rel {rel:.5f}")
         assert cos > 0.999 and rel < 0.05, (name, cos, rel)
 
 

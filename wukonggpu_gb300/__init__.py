@@ -123,6 +123,10 @@ _SIGS = {
     "wk_history_upload": (C.c_int, [_P, C.POINTER(wk_history), _I32P, C.c_int64, C.c_int32]),
     "wk_history_download": (C.c_int, [_P, C.POINTER(wk_history), _I32P, C.c_int64]),
     "wk_history_init": (None, [C.POINTER(wk_history)]),
+    "wk_history_partition": (C.c_int, [_P, C.POINTER(wk_history), C.c_int64, C.c_int32, _I64P,
+                                       C.POINTER(wk_history)]),
+    "wk_history_to_device": (C.c_int, [_P, C.POINTER(wk_history), _P, C.c_int64]),
+    "wk_history_from_device": (C.c_int, [_P, C.POINTER(wk_history), _P, C.c_int64, C.c_int32]),
     "wk_execute": (C.c_int, [_P, _I64P, C.c_int32, C.POINTER(wk_history), _I64P]),
     "wk_enable_timing": (C.c_int, [_P, C.c_int]),
     "wk_last_op_stats": (C.c_int, [_P, C.POINTER(wk_op_stats)]),
@@ -443,6 +447,26 @@ class RCache:
         t = np.ascontiguousarray(table, np.int32)
         cols = t.shape[1] if t.ndim == 2 else 1
         _check(load_library().wk_history_upload(self._h, C.byref(req.hist), _i32(t.reshape(-1)), t.size, cols))
+
+    # -- fork-join across ranks
+    def partition(self, req: Request, start: int, nparts: int) -> np.ndarray:
+        """Split req's table by owner rank (value of variable `start` modulo
+        nparts) on the device; req then holds the parts one after another and
+        the return value their row counts (wk_history_partition)."""
+        counts = np.zeros(nparts, np.int64)
+        out = wk_history()
+        _check(load_library().wk_history_partition(self._h, C.byref(req.hist), start, nparts,
+                                                    counts.ctypes.data_as(_I64P), C.byref(out)))
+        req.hist = out
+        return counts
+
+    def to_device(self, req: Request, dst_ptr: int, cap: int):
+        """Copy req's table to device memory at dst_ptr (cap int32 elements)."""
+        _check(load_library().wk_history_to_device(self._h, C.byref(req.hist), C.c_void_p(dst_ptr), cap))
+
+    def from_device(self, req: Request, src_ptr: int, size: int, cols: int):
+        """Make req's table the `size` int32 elements at device address src_ptr."""
+        _check(load_library().wk_history_from_device(self._h, C.byref(req.hist), C.c_void_p(src_ptr), size, cols))
 
     def download(self, req: Request, into: "PinnedBuffer | None" = None) -> np.ndarray:
         h = req.hist

@@ -723,153 +723,157 @@ filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol
 }
 
 // ----------------------------------------------------------- filter write
-// One CTA per block of input rows: the kept rows, in order, go to the output
-// rows that start at the block's look-back prefix.
+// A write CTA takes kWriteBlocks consecutive blocks of input rows: it loads
+// their kept-row counts at once and writes the non-empty blocks in order, so
+// a filter that keeps few rows costs one CTA per kWriteBlocks blocks rather
+// than one per block, and a block's look-back mostly finds its predecessor
+// published by the same CTA.
+constexpr int kWriteBlocks = 8;
+
+struct FilterSel {
+    int sel[kRowsPerBlock];                      // the block's kept rows, in order
+    unsigned int wbase[kRowsPerBlock / 32 + 1];
+    unsigned long long P;                        // the block's output prefix
+};
+
+// the kept rows of block b (nb of them) in order, and the block's prefix
+// (published for its successors); ends with the CTA synchronised
+__device__ __forceinline__ void filter_select(int64_t b, unsigned int nb, int64_t R, const uint32_t *__restrict__ mask,
+                                              const unsigned int *__restrict__ blk_nz, unsigned long long *flags,
+                                              FilterSel &fs) {
+    constexpr int kPer = kRowsPerBlock / kThreads;   // 4 rows per thread
+    const int64_t r0 = b * kRowsPerBlock;
+    const int64_t nwords_mask = (R + 31) >> 5;
+    const int t = threadIdx.x;
+    if (t < 32) {
+        const int64_t wi = (r0 >> 5) + t;
+        const uint32_t m = wi < nwords_mask ? mask[wi] : 0u;
+        unsigned int c = __popc(m), inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned int v = __shfl_up_sync(FULL, inc, o);
+            if (t >= o) inc += v;
+        }
+        fs.wbase[t] = inc - c;
+        if (t == 31) fs.wbase[32] = inc;
+        const unsigned long long P = lookback_prefix(blk_nz, flags, b);
+        if (t == 0) {
+            st_flag(flags + b, kPrefixReady | (P + nb));
+            fs.P = P;
+        }
+    }
+    __syncthreads();
+    {
+        const int wi = (t * kPer) >> 5, bit0 = (t * kPer) & 31;
+        const int64_t mwi = (r0 >> 5) + wi;
+        const uint32_t m = mwi < nwords_mask ? mask[mwi] : 0u;
+        unsigned int pos = fs.wbase[wi] + __popc(m & ((1u << bit0) - 1u));
+#pragma unroll
+        for (int q = 0; q < kPer; ++q)
+            if (m & (1u << (bit0 + q))) fs.sel[pos++] = t * kPer + q;
+    }
+    __syncthreads();
+}
+
+// Any width: each kept row copied word by word to the rows that start at the
+// block's look-back prefix.
 __global__ void __launch_bounds__(kThreads)
 filter_write_kernel(const int32_t *__restrict__ hist, int64_t R, int C, const uint32_t *__restrict__ mask,
                     const unsigned int *__restrict__ blk_nz, unsigned long long *flags,
                     int32_t *__restrict__ out) {
-    __shared__ int sel[kRowsPerBlock];
-    __shared__ unsigned int wbase[kRowsPerBlock / 32 + 1];
-    __shared__ unsigned long long s_P;
-    constexpr int kPer = kRowsPerBlock / kThreads;   // 4 rows per thread
-    const int64_t b = blockIdx.x;
-    const unsigned int nb = blk_nz[b];
-    if (nb == 0u) return;   // successors add this block's count (0) as they walk past
-    const int64_t r0 = b * kRowsPerBlock;
-    const int64_t nwords_mask = (R + 31) >> 5;
+    __shared__ FilterSel fs;
+    __shared__ unsigned int s_nz[kWriteBlocks];
+    const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
+    const int64_t bb = (int64_t)blockIdx.x * kWriteBlocks;
     const int t = threadIdx.x;
-    if (t < 32) {
-        const int64_t wi = (r0 >> 5) + t;
-        const uint32_t m = wi < nwords_mask ? mask[wi] : 0u;
-        unsigned int c = __popc(m), inc = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned int v = __shfl_up_sync(FULL, inc, o);
-            if (t >= o) inc += v;
-        }
-        wbase[t] = inc - c;
-        if (t == 31) wbase[32] = inc;
-        const unsigned long long P = lookback_prefix(blk_nz, flags, b);
-        if (t == 0) {
-            st_flag(flags + b, kPrefixReady | (P + nb));
-            s_P = P;
-        }
-    }
+    if (t < kWriteBlocks) s_nz[t] = bb + t < nblk ? blk_nz[bb + t] : 0u;
     __syncthreads();
-    {
-        const int wi = (t * kPer) >> 5, bit0 = (t * kPer) & 31;
-        const int64_t mwi = (r0 >> 5) + wi;
-        const uint32_t m = mwi < nwords_mask ? mask[mwi] : 0u;
-        unsigned int pos = wbase[wi] + __popc(m & ((1u << bit0) - 1u));
-#pragma unroll
-        for (int q = 0; q < kPer; ++q)
-            if (m & (1u << (bit0 + q))) sel[pos++] = t * kPer + q;
-    }
-    __syncthreads();
-    int32_t *dst = out + (int64_t)s_P * C;
-    for (int j = t; j < (int)nb; j += kThreads) {
-        const int32_t *src = hist + (r0 + sel[j]) * C;
-        int32_t *d = dst + (int64_t)j * C;
-        for (int c = 0; c < C; ++c) d[c] = __ldg(src + c);
+    for (int k = 0; k < kWriteBlocks; ++k) {
+        const unsigned int nb = s_nz[k];
+        if (nb == 0u) continue;   // successors add this block's count (0) as they walk past
+        const int64_t b = bb + k, r0 = b * kRowsPerBlock;
+        filter_select(b, nb, R, mask, blk_nz, flags, fs);
+        int32_t *dst = out + (int64_t)fs.P * C;
+        for (int j = t; j < (int)nb; j += kThreads) {
+            const int32_t *src = hist + (r0 + fs.sel[j]) * C;
+            int32_t *d = dst + (int64_t)j * C;
+            for (int c = 0; c < C; ++c) d[c] = __ldg(src + c);
+        }
+        __syncthreads();   // fs is reused by the next block
     }
 }
 
-// One CTA per block of input rows, for tables of C <= 8 columns: the kept
-// rows are staged in shared memory, then the block's output words [P C,
-// (P + nb) C) stream out as aligned 16 B stores (P the block's look-back
-// prefix, nb its kept rows).  When at least a quarter of the block's rows are
-// kept the whole block is read with 16 B loads and the kept rows picked from
-// shared memory; otherwise each kept row is gathered alone.
+// Tables of C <= 8 columns: a block's kept rows are staged in shared memory,
+// then its output words [P C, (P + nb) C) stream out as aligned 16 B stores
+// (P the block's look-back prefix, nb its kept rows).  When at least a
+// quarter of the block's rows are kept the whole block is read with 16 B
+// loads and the kept rows picked from shared memory; otherwise each kept row
+// is gathered alone.
 template <int C>
 __global__ void __launch_bounds__(kThreads)
 filter_write_vec_kernel(const int32_t *__restrict__ hist, int64_t R, const uint32_t *__restrict__ mask,
                         const unsigned int *__restrict__ blk_nz, unsigned long long *flags, int32_t *__restrict__ out) {
-    __shared__ int sel[kRowsPerBlock];
-    __shared__ unsigned int wbase[kRowsPerBlock / 32 + 1];
-    __shared__ unsigned long long s_P;
+    __shared__ FilterSel fs;
+    __shared__ unsigned int s_nz[kWriteBlocks];
     __shared__ __align__(16) int32_t rows[kRowsPerBlock * C];
-    constexpr int kPer = kRowsPerBlock / kThreads;   // 4 rows per thread
-    const int64_t b = blockIdx.x;
-    const unsigned int nb = blk_nz[b];
-    if (nb == 0u) return;   // successors add this block's count (0) as they walk past
-    const int64_t r0 = b * kRowsPerBlock;
-    const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
-    const int64_t nwords_mask = (R + 31) >> 5;
+    const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
+    const int64_t bb = (int64_t)blockIdx.x * kWriteBlocks;
     const int t = threadIdx.x;
-    if (t < 32) {
-        const int64_t wi = (r0 >> 5) + t;
-        const uint32_t m = wi < nwords_mask ? mask[wi] : 0u;
-        unsigned int c = __popc(m), inc = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned int v = __shfl_up_sync(FULL, inc, o);
-            if (t >= o) inc += v;
-        }
-        wbase[t] = inc - c;
-        if (t == 31) wbase[32] = inc;
-        const unsigned long long P = lookback_prefix(blk_nz, flags, b);
-        if (t == 0) {
-            st_flag(flags + b, kPrefixReady | (P + nb));
-            s_P = P;
-        }
-    }
+    if (t < kWriteBlocks) s_nz[t] = bb + t < nblk ? blk_nz[bb + t] : 0u;
     __syncthreads();
-    {
-        const int wi = (t * kPer) >> 5, bit0 = (t * kPer) & 31;
-        const int64_t mwi = (r0 >> 5) + wi;
-        const uint32_t m = mwi < nwords_mask ? mask[mwi] : 0u;
-        unsigned int pos = wbase[wi] + __popc(m & ((1u << bit0) - 1u));
-#pragma unroll
-        for (int q = 0; q < kPer; ++q)
-            if (m & (1u << (bit0 + q))) sel[pos++] = t * kPer + q;
-    }
-    const int32_t *src = hist + r0 * C;
-    const bool whole = 4u * nb >= (unsigned int)n;   // the same in every thread
-    if (whole) {
-        // the block's n C words; 16 B loads when the block starts on a 16 B boundary
-        const int words = n * C;
-        if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
-            for (int i = t; 4 * i < words; i += kThreads) {
-                if (4 * i + 4 <= words) {
-                    reinterpret_cast<int4 *>(rows)[i] = __ldg(reinterpret_cast<const int4 *>(src) + i);
-                } else {
-                    for (int k = 4 * i; k < words; ++k) rows[k] = __ldg(src + k);
+    for (int kb = 0; kb < kWriteBlocks; ++kb) {
+        const unsigned int nb = s_nz[kb];
+        if (nb == 0u) continue;   // successors add this block's count (0) as they walk past
+        const int64_t b = bb + kb, r0 = b * kRowsPerBlock;
+        const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
+        const int32_t *src = hist + r0 * C;
+        const bool whole = 4u * nb >= (unsigned int)n;   // the same in every thread
+        if (whole) {
+            // the block's n C words; 16 B loads when the block starts on a 16 B boundary
+            const int words = n * C;
+            if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+                for (int i = t; 4 * i < words; i += kThreads) {
+                    if (4 * i + 4 <= words) {
+                        reinterpret_cast<int4 *>(rows)[i] = __ldg(reinterpret_cast<const int4 *>(src) + i);
+                    } else {
+                        for (int k = 4 * i; k < words; ++k) rows[k] = __ldg(src + k);
+                    }
                 }
+            } else {
+                for (int k = t; k < words; k += kThreads) rows[k] = __ldg(src + k);
             }
-        } else {
-            for (int k = t; k < words; k += kThreads) rows[k] = __ldg(src + k);
         }
-    }
-    __syncthreads();   // sel (and the whole block) complete
-    if (!whole) {
-        for (int j = t; j < (int)nb; j += kThreads) {
-            const int32_t *sr = src + sel[j] * C;
+        filter_select(b, nb, R, mask, blk_nz, flags, fs);   // also completes the staging above
+        if (!whole) {
+            for (int j = t; j < (int)nb; j += kThreads) {
+                const int32_t *sr = src + fs.sel[j] * C;
 #pragma unroll
-            for (int c = 0; c < C; ++c) rows[j * C + c] = __ldg(sr + c);
+                for (int c = 0; c < C; ++c) rows[j * C + c] = __ldg(sr + c);
+            }
+            __syncthreads();
         }
-        __syncthreads();
-    }
-    // output words [P C, (P + nb) C): int4 stores aligned to 16 B of out
-    const unsigned long long P = s_P;
-    const uint32_t lead = (uint32_t)((P * C) & 3ull), words = nb * C;
-    int32_t *g = out + (P * C - lead);
-    for (uint32_t i = (uint32_t)t; 4u * i < lead + words; i += kThreads) {
-        int32_t v[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t kk = 4u * i + j - lead;   // wraps above `words` before the lead
-            v[j] = kk < words ? (whole ? rows[sel[kk / C] * C + kk % C] : rows[kk]) : 0;
-        }
-        if (4u * i >= lead && 4u * i + 4u <= lead + words) {
-            reinterpret_cast<int4 *>(g)[i] = make_int4(v[0], v[1], v[2], v[3]);
-        } else {
+        // output words [P C, (P + nb) C): int4 stores aligned to 16 B of out
+        const unsigned long long P = fs.P;
+        const uint32_t lead = (uint32_t)((P * C) & 3ull), words = nb * C;
+        int32_t *g = out + (P * C - lead);
+        for (uint32_t i = (uint32_t)t; 4u * i < lead + words; i += kThreads) {
+            int32_t v[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const uint32_t kk = 4u * i + j - lead;
-                if (kk < words) g[4u * i + j] = v[j];
+                const uint32_t kk = 4u * i + j - lead;   // wraps above `words` before the lead
+                v[j] = kk < words ? (whole ? rows[fs.sel[kk / C] * C + kk % C] : rows[kk]) : 0;
+            }
+            if (4u * i >= lead && 4u * i + 4u <= lead + words) {
+                reinterpret_cast<int4 *>(g)[i] = make_int4(v[0], v[1], v[2], v[3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint32_t kk = 4u * i + j - lead;
+                    if (kk < words) g[4u * i + j] = v[j];
+                }
             }
         }
+        __syncthreads();   // rows and fs are reused by the next block
     }
 }
 
@@ -991,7 +995,7 @@ void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ec
 
 void launch_filter_write(const int32_t *hist, int64_t R, int C, const uint32_t *mask, const unsigned int *blk_nz,
                          unsigned long long *flags, int32_t *out, cudaStream_t st) {
-    const unsigned int g = nblocks_rows(R);
+    const unsigned int g = (nblocks_rows(R) + kWriteBlocks - 1) / kWriteBlocks;
 #define WK_FWRITE(CC) filter_write_vec_kernel<CC><<<g, kThreads, 0, st>>>(hist, R, mask, blk_nz, flags, out)
     switch (C) {
         case 1: WK_FWRITE(1); break;

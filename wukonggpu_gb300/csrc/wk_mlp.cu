@@ -35,6 +35,7 @@ constexpr int kX = kIn + kEmb;   // 80
 constexpr int kH = 256;
 constexpr int kOutPad = 64;   // output layer padded to one GEMM tile
 constexpr int kXPadN = 128;   // W1^T rows padded (dX GEMM has N = 80 -> 128)
+constexpr float kB1 = 0.9f, kB2 = 0.999f;   // Adam moment decay rates
 
 // ------------------------------------------------------------ elementwise
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
@@ -105,8 +106,9 @@ __global__ void colsum_kernel(const __nv_bfloat16 *__restrict__ Dt, int Mp, floa
     }
 }
 
-// loss = mean((y - t)^2) over real rows; dY (bf16, col 0, row-major and
-// transposed) = 2 (y - t) / M.  One block.
+// loss[0] = mean((y - t)^2) over real rows, also added into loss[1] (the
+// epoch's running sum); dY (bf16, col 0, row-major and transposed) =
+// 2 (y - t) / M.  One block.
 __global__ void loss_kernel(const float *__restrict__ Y, const float *__restrict__ tgt, int M, int Mp,
                             __nv_bfloat16 *__restrict__ dY, __nv_bfloat16 *__restrict__ dYt, float *__restrict__ loss) {
     float s = 0.f;
@@ -128,7 +130,11 @@ __global__ void loss_kernel(const float *__restrict__ Y, const float *__restrict
     if (threadIdx.x < 32) {
         s = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.f;
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (threadIdx.x == 0) *loss = s / (float)(M > 0 ? M : 1);
+        if (threadIdx.x == 0) {
+            const float l = s / (float)(M > 0 ? M : 1);
+            loss[0] = l;
+            loss[1] += l;
+        }
     }
 }
 
@@ -144,10 +150,14 @@ __global__ void emb_grad_kernel(const float *__restrict__ dX, int ldx, const int
     }
 }
 
-// Adam over fp32 master weights; g, m, v, w all of length n
+// Adam over fp32 master weights; g, m, v, w all of length n.  The bias
+// corrections (1 - b1^t, 1 - b2^t) of this step are cbias[*bidx], so that a
+// captured step reads the current ones when it is replayed.
 __global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
-                            float *__restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float c1,
-                            float c2) {
+                            float *__restrict__ v, int64_t n, float lr, float b1, float b2, float eps,
+                            const float2 *__restrict__ cbias, const int *__restrict__ bidx) {
+    const float2 c = cbias[*bidx];
+    const float c1 = c.x, c2 = c.y;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float gi = g[i];
         const float mi = b1 * m[i] + (1.f - b1) * gi;
@@ -157,6 +167,28 @@ __global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g, 
         w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
     }
 }
+
+// Batch *bidx of an epoch: rows order[*bidx * batch + i], i < M, of the
+// device-resident samples into the step's input buffers.
+__global__ void gather_batch_kernel(const float *__restrict__ all_feats, const int32_t *__restrict__ all_pids,
+                                    const float *__restrict__ all_tgt, const int64_t *__restrict__ order,
+                                    const int *__restrict__ bidx, int batch, int M, float *__restrict__ feats,
+                                    int32_t *__restrict__ pids, float *__restrict__ tgt) {
+    const int64_t b0 = (int64_t)(*bidx) * batch;
+    const int64_t n = (int64_t)M * kIn;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = (int)(i / kIn), c = (int)(i % kIn);
+        const int64_t j = order[b0 + r];
+        feats[i] = all_feats[j * kIn + c];
+        if (c == 0) {
+            pids[r] = all_pids[j];
+            tgt[r] = all_tgt[j];
+        }
+    }
+}
+
+// the next batch of the epoch
+__global__ void bump_kernel(int *bidx) { ++*bidx; }
 
 // bf16 copies of a weight matrix W [rows x cols] (fp32): row-major into Wb
 // (ld = ldb, zero padded) and transposed into Wt (ld = ldt)
@@ -194,6 +226,9 @@ struct wk_mlp {
                   *dyt = nullptr;
     float *z[4] = {}, *dh = nullptr, *dx = nullptr, *feats = nullptr, *tgt = nullptr, *loss = nullptr;
     int32_t *pids = nullptr;
+    int *bidx = nullptr;         // the batch of the epoch a training step takes
+    float2 *cbias = nullptr;     // Adam bias corrections of an epoch's steps
+    int64_t cbias_cap = 0;
     int64_t step = 0;
     int64_t kernels = 0;
     int *d_err = nullptr;        // device flag of the tensor-core GEMM (bit 2: a wait ran out,
@@ -337,10 +372,8 @@ void backward_step(wk_mlp *m, int M, float lr, bool update, cudaStream_t s) {
     emb_grad_kernel<<<nblk((int64_t)M * kEmb), 256, 0, s>>>(m->dx, kXPadN, m->pids, M, m->n_ids, g + m->off_emb);
     m->kernels += 3;
     if (update) {
-        ++m->step;
-        const float b1 = 0.9f, b2 = 0.999f;
-        const float c1 = 1.f - std::pow(b1, (float)m->step), c2 = 1.f - std::pow(b2, (float)m->step);
-        adam_kernel<<<nblk(m->n_params), 256, 0, s>>>(m->params, g, m->m1, m->m2, m->n_params, lr, b1, b2, 1e-8f, c1, c2);
+        adam_kernel<<<nblk(m->n_params), 256, 0, s>>>(m->params, g, m->m1, m->m2, m->n_params, lr, kB1, kB2, 1e-8f,
+                                                      m->cbias, m->bidx);
         refresh_bf16(m, s);
         m->kernels++;
     }
@@ -373,6 +406,8 @@ void free_mlp(wk_mlp *m) {
     cudaFree(m->x0); cudaFree(m->x0t); cudaFree(m->dz); cudaFree(m->dzt); cudaFree(m->dy); cudaFree(m->dyt);
     cudaFree(m->dh); cudaFree(m->dx); cudaFree(m->feats); cudaFree(m->tgt); cudaFree(m->loss); cudaFree(m->pids);
     cudaFree(m->d_err);
+    cudaFree(m->bidx);
+    cudaFree(m->cbias);
     if (m->h_err) cudaFreeHost(m->h_err);
     delete m;
 }
@@ -415,7 +450,7 @@ extern "C" int wk_mlp_create(wk_ctx *ctx, int32_t n_ids, int32_t max_batch, uint
          cudaMalloc(&m->dx, 4 * std::max(Mp * (size_t)kXPadN, (size_t)kH * kXPadN)) == cudaSuccess &&
          cudaMalloc(&m->feats, 4 * Mp * kIn) == cudaSuccess && cudaMalloc(&m->tgt, 4 * Mp) == cudaSuccess &&
          cudaMalloc(&m->loss, 16) == cudaSuccess && cudaMalloc(&m->pids, 4 * Mp) == cudaSuccess &&
-         cudaMalloc(&m->d_err, sizeof(int)) == cudaSuccess &&
+         cudaMalloc(&m->d_err, sizeof(int)) == cudaSuccess && cudaMalloc(&m->bidx, sizeof(int)) == cudaSuccess &&
          cudaHostAlloc((void **)&m->h_err, sizeof(int), 0) == cudaSuccess &&
          cudaFuncSetAttribute(tc::gemm_tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)tc::smem_bytes(64)) == cudaSuccess &&
@@ -450,6 +485,8 @@ extern "C" int wk_mlp_create(wk_ctx *ctx, int32_t n_ids, int32_t max_batch, uint
     if (e == cudaSuccess) e = cudaMemsetAsync(m->dy, 0, 2 * Mp * kOutPad, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->dyt, 0, 2 * Mp * kOutPad, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(m->d_err, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->bidx, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->loss, 0, 16, s);
     if (m->h_err) *m->h_err = 0;
     if (e != cudaSuccess) { int r = cuda_fail(e, "wk_mlp_create init"); free_mlp(m); return r; }
     refresh_bf16(m, s);
@@ -505,49 +542,111 @@ extern "C" int wk_mlp_gradients(wk_mlp *m, const float *feats, const int32_t *pi
 // Mini-batch training: `epochs` passes over n samples in batches of `batch`
 // (sample order shuffled with `seed`), Adam with learning rate lr.  Returns
 // the mean loss of the last epoch.
+//
+// The samples are uploaded once and stay on the device; every step gathers
+// its batch there by the epoch's order.  A step of a full batch is the same
+// launch sequence every time (its batch index and Adam bias corrections are
+// read from device memory), so the second full batch is captured as a CUDA
+// graph and every later one replays it: one launch instead of about forty.
+// A shorter last batch runs as plain launches.  The host reads the device
+// once per epoch (the loss sum and the GEMM status).
 extern "C" int wk_mlp_train(wk_mlp *m, const float *feats, const int32_t *pids, const float *tgt, int64_t n,
                             int32_t epochs, int32_t batch, float lr, uint64_t seed, float *last_loss) {
     if (!m || !feats || !pids || !tgt || n < 1 || epochs < 1 || batch < 1 || batch > m->cap_m)
         return set_error(WK_EINVAL, "wk_mlp_train: bad arguments");
-    cudaSetDevice(m->ctx->device);
+    cudaError_t e = cudaSetDevice(m->ctx->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     cudaStream_t s = m->ctx->stream;
+    const int64_t nb = (n + batch - 1) / batch, nfull = n / batch;
+    const int tail = (int)(n - nfull * batch);
+    DevBuf d_feats, d_pids, d_tgt, d_order;
+    int st;
+    if ((st = d_feats.reserve(sizeof(float) * (size_t)n * kIn)) || (st = d_pids.reserve(sizeof(int32_t) * (size_t)n)) ||
+        (st = d_tgt.reserve(sizeof(float) * (size_t)n)) || (st = d_order.reserve(sizeof(int64_t) * (size_t)n)))
+        return st;
+    if (nb > m->cbias_cap) {
+        cudaFree(m->cbias);
+        m->cbias = nullptr;
+        m->cbias_cap = 0;
+        if ((e = cudaMalloc(&m->cbias, sizeof(float2) * (size_t)nb)) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(WK_ENOMEM, "wk_mlp_train: bias-correction table");
+        }
+        m->cbias_cap = nb;
+    }
+    if ((e = cudaMemcpyAsync(d_feats.ptr, feats, sizeof(float) * (size_t)n * kIn, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(d_pids.ptr, pids, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, s)) ||
+        (e = cudaMemcpyAsync(d_tgt.ptr, tgt, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, s)))
+        return cuda_fail(e, "wk_mlp_train upload");
     std::vector<int64_t> order((size_t)n);
     for (int64_t i = 0; i < n; ++i) order[(size_t)i] = i;
+    std::vector<float2> cb((size_t)nb);
     std::mt19937_64 rng(seed);
-    std::vector<float> bf((size_t)batch * kIn), bt((size_t)batch);
-    std::vector<int32_t> bp((size_t)batch);
     float *h_loss = nullptr;
-    if (cudaHostAlloc((void **)&h_loss, 4, 0) != cudaSuccess) return set_error(WK_ENOMEM, "wk_mlp_train: pinned");
+    if (cudaHostAlloc((void **)&h_loss, 8, 0) != cudaSuccess) return set_error(WK_ENOMEM, "wk_mlp_train: pinned");
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t graph_kernels = 0;
+    auto one_step = [&](int M) {
+        gather_batch_kernel<<<nblk((int64_t)M * kIn), 256, 0, s>>>(d_feats.as<float>(), d_pids.as<int32_t>(),
+                                                                   d_tgt.as<float>(), d_order.as<int64_t>(), m->bidx,
+                                                                   batch, M, m->feats, m->pids, m->tgt);
+        forward(m, M, s);
+        add_out_bias_kernel<<<nblk(M), 256, 0, s>>>(m->z[3], m->params + m->off_b[3], M);
+        backward_step(m, M, lr, true, s);
+        bump_kernel<<<1, 1, 0, s>>>(m->bidx);
+        m->kernels += 4;   // gather, output bias, Adam, bump
+    };
+    auto finish = [&](int rc) {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamSynchronize(s);   // the pinned loss and the device samples may still be in use
+        cudaFreeHost(h_loss);
+        m->ctx->launches += m->kernels;
+        m->kernels = 0;
+        return rc;
+    };
     double ep_loss = 0.0;
     for (int ep = 0; ep < epochs; ++ep) {
         std::shuffle(order.begin(), order.end(), rng);
-        double tot = 0.0;
-        int64_t nb = 0;
-        for (int64_t b0 = 0; b0 < n; b0 += batch) {
-            const int M = (int)std::min<int64_t>(batch, n - b0);
-            for (int i = 0; i < M; ++i) {
-                const int64_t j = order[(size_t)(b0 + i)];
-                std::memcpy(&bf[(size_t)i * kIn], feats + j * kIn, sizeof(float) * kIn);
-                bp[(size_t)i] = pids[j];
-                bt[(size_t)i] = tgt[j];
-            }
-            int st = upload(m, bf.data(), bp.data(), bt.data(), M, s);
-            if (st) { cudaFreeHost(h_loss); return st; }
-            forward(m, M, s);
-            add_out_bias_kernel<<<nblk(M), 256, 0, s>>>(m->z[3], m->params + m->off_b[3], M);
-            backward_step(m, M, lr, true, s);
-            cudaMemcpyAsync(h_loss, m->loss, 4, cudaMemcpyDeviceToHost, s);
-            if ((st = check_status(m, s, "wk_mlp_train"))) { cudaFreeHost(h_loss); return st; }
-            tot += *h_loss;
-            ++nb;
+        // Adam step t = step + k + 1 for batch k of this epoch
+        for (int64_t k = 0; k < nb; ++k) {
+            const float t = (float)(m->step + k + 1);
+            cb[(size_t)k] = make_float2(1.f - std::pow(kB1, t), 1.f - std::pow(kB2, t));
         }
-        ep_loss = tot / (double)(nb ? nb : 1);
+        if ((e = cudaMemcpyAsync(d_order.ptr, order.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemcpyAsync(m->cbias, cb.data(), sizeof(float2) * (size_t)nb, cudaMemcpyHostToDevice, s)) ||
+            (e = cudaMemsetAsync(m->bidx, 0, sizeof(int), s)) || (e = cudaMemsetAsync(m->loss + 1, 0, sizeof(float), s)))
+            return finish(cuda_fail(e, "wk_mlp_train epoch"));
+        for (int64_t k = 0; k < nfull; ++k) {
+            if (exec) {
+                if ((e = cudaGraphLaunch(exec, s)) != cudaSuccess) return finish(cuda_fail(e, "wk_mlp_train replay"));
+                m->kernels += graph_kernels;
+            } else if (k == 0 && ep == 0) {
+                one_step(batch);
+            } else {
+                const int64_t k0 = m->kernels;
+                if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+                    return finish(cuda_fail(e, "wk_mlp_train capture"));
+                one_step(batch);
+                e = cudaStreamEndCapture(s, &graph);
+                graph_kernels = m->kernels - k0;
+                m->kernels = k0;
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+                if (e != cudaSuccess) return finish(cuda_fail(e, "wk_mlp_train graph"));
+                if ((e = cudaGraphLaunch(exec, s)) != cudaSuccess) return finish(cuda_fail(e, "wk_mlp_train replay"));
+                m->kernels += graph_kernels;
+            }
+        }
+        if (tail) one_step(tail);
+        m->step += nb;
+        if ((e = cudaMemcpyAsync(h_loss, m->loss, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return finish(cuda_fail(e, "wk_mlp_train loss"));
+        if ((st = check_status(m, s, "wk_mlp_train"))) return finish(st);
+        ep_loss = (double)h_loss[1] / (double)nb;
     }
-    cudaFreeHost(h_loss);
-    m->ctx->launches += m->kernels;
-    m->kernels = 0;
     if (last_loss) *last_loss = (float)ep_loss;
-    return WK_OK;
+    return finish(WK_OK);
 }
 
 // Predictions (log(1 + rows)) for n samples, in chunks of the batch capacity.

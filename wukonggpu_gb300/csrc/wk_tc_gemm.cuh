@@ -230,7 +230,8 @@ inline EncodeTiledFn encode_fn() {
     if (!fn) {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        // the entry point as CUDA 12.0 introduced it (its signature has not changed since)
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
             fn = (EncodeTiledFn)p;
     }
