@@ -507,8 +507,14 @@ def run_gb300(args, dist):
                 "peak_source": peak_kind, "kernel": "k2u op (count + expand kernels)",
                 "timing": "per-kernel CUDA events on the op stream, a second pass over the timed steps",
                 "alg_bytes_per_launch": per_launch, "k2u_share_of_op_time": k2u_ms / all_ms if all_ms else None,
+                # the expansion kernel alone: its output rows and list entries ...
                 "expand_kernel_gbs": (sum(4 * op["rows_out"] * (op["cols_in"] + 2) for op in k2u)
                                       / (write_ms / 1000.0) / 1e9) if write_ms else None,
+                # ... and with the input rows it copies (4 R C), the op's bytes split
+                # between the kernels: the count keeps the 16 B probe per row
+                "expand_kernel_gbs_incl_rows": (sum(4 * op["rows_in"] * op["cols_in"]
+                                                    + 4 * op["rows_out"] * (op["cols_in"] + 2) for op in k2u)
+                                                / (write_ms / 1000.0) / 1e9) if write_ms else None,
                 "expand_share_of_k2u_time": write_ms / k2u_ms if k2u_ms else None}
 
     # ---- the filter group: the same shapes closed by known_to_known /

@@ -278,7 +278,13 @@ int wk_batch_download(wk_batch *b, int32_t *host, int64_t cap, int64_t *total_in
  * whole warp instead of one thread. */
 int wk_batch_set_tuning(wk_batch *b, int32_t blocks_per_sm, int32_t rows_per_warp, int32_t split_ints);
 int wk_batch_get_tuning(wk_batch *b, int32_t *blocks_per_sm, int32_t *rows_per_warp, int32_t *split_ints);
-/* Autotuner: time every candidate launch shape on these queries and keep the fastest. */
+/* Step form: 0 = three kernels per step (count, scan, write); 1 = one
+ * cooperative persistent kernel per step whose blocks meet at two bounded
+ * grid barriers (a wait that runs out fails the batch with WK_ETIMEDOUT).
+ * wk_batch_get_fused returns the current form. */
+int wk_batch_set_fused(wk_batch *b, int32_t fused);
+int wk_batch_get_fused(wk_batch *b);
+/* Autotuner: time every candidate step form and launch shape on these queries and keep the fastest. */
 int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
                       int32_t reps, double *best_ms);
 int64_t wk_batch_kernel_launches(wk_batch *b);

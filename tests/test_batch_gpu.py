@@ -25,11 +25,32 @@ def _check(tables, queries, orc):
         assert got.shape == exp.shape and np.array_equal(got, exp), q
 
 
-def test_batch_matches_oracle_graph_and_plain(gpu_small, small_oracle, light):
+@pytest.mark.parametrize("fused", [False, True])
+def test_batch_matches_oracle_graph_and_plain(gpu_small, small_oracle, light, fused):
+    """Both step forms: three kernels per step, or one cooperative kernel
+    whose blocks meet at grid barriers."""
     b = W.Batch(gpu_small, max_queries=1024, max_steps=4, capacity_ints=1 << 24)
+    b.set_fused(fused)
+    assert b.fused() == fused
     for use_graph in (False, True):
+        k0 = b.kernel_launches()
         nq = b.run(light, use_graph=use_graph)
         _check(b.download(nq), light, small_oracle)
+        assert b.kernel_launches() - k0 == 1 + (1 if fused else 3) * 4
+    for bps, rows, split in ((2, 32, 16), (8, 128, 256)):   # 8 blocks/SM: clamped to what fits at once
+        b.set_tuning(bps, rows, split)
+        nq = b.run(light[:300])
+        _check(b.download(nq), light[:300], small_oracle)
+
+
+def test_fused_batch_capacity_overflow_is_reported(gpu_small, light):
+    """The scan inside the one-kernel step finds the overflow; every block
+    leaves after the barrier and later steps do nothing."""
+    b = W.Batch(gpu_small, max_queries=1024, max_steps=4, capacity_ints=4096)
+    b.set_fused(True)
+    with pytest.raises(W.WkError) as e:
+        b.run(light)
+    assert e.value.status == W.WK_EOVERFLOW
 
 
 def test_graph_replay_with_new_batches(gpu_small, small_oracle, small_graph):

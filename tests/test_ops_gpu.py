@@ -75,8 +75,8 @@ def test_k2u_random_histories(gpu_small, small_graph, small_oracle, R, C):
         assert got.shape == exp.shape and np.array_equal(got, exp), (pid, d, scol)
 
 
-@pytest.mark.parametrize("R", [1, 33, 1025, 50_000])
-@pytest.mark.parametrize("C", [2, 5])
+@pytest.mark.parametrize("R", [1, 33, 1025, 50_000, 700_001])   # 700,001 rows: 684 blocks in 3 groups of 256
+@pytest.mark.parametrize("C", [2, 5, 11])
 def test_k2k_k2c_random_histories(gpu_small, small_graph, small_oracle, R, C):
     g, s, p, o = small_graph
     rng = np.random.default_rng(R + 13 * C)
@@ -105,7 +105,7 @@ def test_k2k_k2c_random_histories(gpu_small, small_graph, small_oracle, R, C):
         assert np.array_equal(got.reshape(exp.shape), exp), const
 
 
-@pytest.mark.parametrize("R", [1, 33, 4097, 60_000])
+@pytest.mark.parametrize("R", [1, 33, 4097, 60_000, 600_000])
 def test_k2k_k2c_on_a_functional_direction(gpu_small, small_graph, small_oracle, R):
     """rdf:type OUT is dense and functional: its membership test reads the
     neighbour array once.  Rows mix real (entity, class) pairs, wrong classes,

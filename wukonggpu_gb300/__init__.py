@@ -146,6 +146,8 @@ _SIGS = {
     "wk_batch_download": (C.c_int, [_P, _I32P, C.c_int64, _I64P]),
     "wk_batch_set_tuning": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "wk_batch_get_tuning": (C.c_int, [_P, _I32P, _I32P, _I32P]),
+    "wk_batch_set_fused": (C.c_int, [_P, C.c_int32]),
+    "wk_batch_get_fused": (C.c_int, [_P]),
     "wk_batch_autotune": (C.c_int, [_P, _I64P, _I32P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "wk_batch_kernel_launches": (C.c_int64, [_P]),
     "wk_server_config_default": (None, [C.POINTER(wk_server_config)]),
@@ -610,6 +612,13 @@ class Batch:
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
         _check(load_library().wk_batch_get_tuning(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
+
+    def set_fused(self, fused: bool):
+        """One cooperative kernel per step (True) or three kernels (False)."""
+        _check(load_library().wk_batch_set_fused(self._h, 1 if fused else 0))
+
+    def fused(self) -> bool:
+        return load_library().wk_batch_get_fused(self._h) == 1
 
     def autotune(self, queries, reps: int = 3) -> float:
         cmd, npat = self.pack(queries)

@@ -22,10 +22,14 @@
 //                 written at out_int_off[q] + pos_in_q * width; rows whose
 //                 output exceeds `split` ints are written warp-cooperatively,
 //                 the rest thread-per-row
-// Every size lives in device memory and every grid is persistent, so the
-// launch sequence of a batch never depends on its data: it is captured once
-// into a CUDA graph and replayed for each new batch.  Each query's rows come
-// out in exactly the order the query produces alone.
+// The three phases run either as three kernels per step or as one
+// cooperative persistent kernel per step (batch_step_kernel) whose blocks
+// meet at two grid barriers -- after the count and after the scan, which
+// block 0 runs -- each wait bounded; the autotuner picks the faster.  Every
+// size lives in device memory and every grid is persistent, so the launch
+// sequence of a batch never depends on its data: it is captured once into a
+// CUDA graph and replayed for each new batch.  Each query's rows come out in
+// exactly the order the query produces alone.
 #include <algorithm>
 #include <cstring>
 #include <unordered_map>
@@ -49,7 +53,11 @@ struct BatchTune {
     int blocks_per_sm;   // persistent grid = SMs x blocks_per_sm
     int rounds;          // rows per warp per tile = 32 * rounds
     int split;           // output ints above which a row is written by a whole warp
+    int fused;           // 1: one cooperative kernel per step; 0: count, scan and write kernels
 };
+
+constexpr int kErrBarrier = 1 << 4;         // flags[0]: a grid-barrier wait ran out
+constexpr long kBarrierIters = 1l << 24;    // polls of a grid-barrier wait (about 1 s with the back-off)
 
 constexpr int kBT = 256;                    // threads per block
 constexpr int kMaxQ = 4096;                 // queries per batch (shared-memory row offsets)
@@ -91,12 +99,8 @@ struct StepIO {
     int Q;
 };
 
-__global__ void __launch_bounds__(kBT)
-batch_count_kernel(StepIO io, int rounds) {
-    extern __shared__ int64_t s_off[];   // Q + 1
-    if (io.flags[1]) return;
-    for (int i = threadIdx.x; i <= io.Q; i += blockDim.x) s_off[i] = io.in_row_off[i];
-    __syncthreads();
+// count: per (query, row) output counts, per-tile and per-query sums
+__device__ __forceinline__ void count_phase(const StepIO &io, int rounds, const int64_t *s_off) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tile_rows = (kBT / 32) * 32 * rounds;
     const int64_t total = s_off[io.Q];
@@ -160,18 +164,27 @@ batch_count_kernel(StepIO io, int rounds) {
     }
 }
 
-// One block: tile prefix sums, per-query output layout, capacity check.
-__global__ void __launch_bounds__(1024)
-batch_scan_kernel(StepIO io, int rounds) {
-    __shared__ unsigned long long ws[32], wi[32];
+__global__ void __launch_bounds__(kBT)
+batch_count_kernel(StepIO io, int rounds) {
+    extern __shared__ int64_t s_off[];   // Q + 1
     if (io.flags[1]) return;
+    for (int i = threadIdx.x; i <= io.Q; i += blockDim.x) s_off[i] = io.in_row_off[i];
+    __syncthreads();
+    count_phase(io, rounds, s_off);
+}
+
+// One block (any multiple of 32 threads up to 1024): tile prefix sums,
+// per-query output layout, capacity check.
+__device__ __forceinline__ void scan_phase(const StepIO &io, int rounds) {
+    __shared__ unsigned long long ws[32], wi[32];
+    const int nt = blockDim.x, nw = nt >> 5;
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
     const int tile_rows = (kBT / 32) * 32 * rounds;
     const int64_t total = io.in_row_off[io.Q];
     const int64_t n = (total + tile_rows - 1) / tile_rows;
     // (1) exclusive scan of the tile sums, in place
     {
-        const int64_t per = (n + 1023) / 1024, a = (int64_t)t * per, b = a + per < n ? a + per : n;
+        const int64_t per = (n + nt - 1) / nt, a = (int64_t)t * per, b = a + per < n ? a + per : n;
         unsigned long long ls = 0ull;
         for (int64_t i = a; i < b; ++i) ls += io.tile_sum[i];
         unsigned long long is = ls;
@@ -179,7 +192,7 @@ batch_scan_kernel(StepIO io, int rounds) {
         if (lane == 31) ws[wid] = is;
         __syncthreads();
         if (wid == 0) {
-            unsigned long long x = ws[lane];
+            unsigned long long x = lane < nw ? ws[lane] : 0ull;
             for (int o = 1; o < 32; o <<= 1) { const unsigned long long v = __shfl_up_sync(FULL, x, o); if (lane >= o) x += v; }
             ws[lane] = x;
         }
@@ -188,9 +201,9 @@ batch_scan_kernel(StepIO io, int rounds) {
         for (int64_t i = a; i < b; ++i) { const unsigned long long v = io.tile_sum[i]; io.tile_sum[i] = es; es += v; }
         __syncthreads();
     }
-    // (2) per-query output rows and ints (Q <= 4096: four per thread)
+    // (2) per-query output rows and ints (Q <= 4096: four per thread of 1024)
     {
-        const int Q = io.Q, per = (Q + 1023) / 1024, a = t * per, b = a + per < Q ? a + per : Q;
+        const int Q = io.Q, per = (Q + nt - 1) / nt, a = t * per, b = a + per < Q ? a + per : Q;
         unsigned long long lr = 0ull, li = 0ull;
         for (int q = a; q < b; ++q) {
             const StepDesc d = io.desc[q];
@@ -206,7 +219,7 @@ batch_scan_kernel(StepIO io, int rounds) {
         if (lane == 31) { ws[wid] = ir; wi[wid] = ii; }
         __syncthreads();
         if (wid == 0) {
-            unsigned long long x = ws[lane], y = wi[lane];
+            unsigned long long x = lane < nw ? ws[lane] : 0ull, y = lane < nw ? wi[lane] : 0ull;
             for (int o = 1; o < 32; o <<= 1) {
                 const unsigned long long v = __shfl_up_sync(FULL, x, o), u = __shfl_up_sync(FULL, y, o);
                 if (lane >= o) { x += v; y += u; }
@@ -228,24 +241,25 @@ batch_scan_kernel(StepIO io, int rounds) {
             er += r;
             ei += r * (unsigned long long)w;
         }
-        if (t == 1023) {
+        if (t == nt - 1) {
             io.out_row_off[Q] = (int64_t)er;
             if ((int64_t)er > io.cap_rows || (int64_t)ei > io.cap_ints) io.flags[1] = 1;
         }
     }
 }
 
+__global__ void __launch_bounds__(1024)
+batch_scan_kernel(StepIO io, int rounds) {
+    if (io.flags[1]) return;
+    scan_phase(io, rounds);
+}
+
 // Per tile: block scan of the counts, then write.  Rows with more than
 // `split` output ints are queued and written by whole warps.
-__global__ void __launch_bounds__(kBT)
-batch_write_kernel(StepIO io, int rounds, int split) {
-    extern __shared__ int64_t s_off[];   // Q+1 input row offsets
+__device__ __forceinline__ void write_phase(const StepIO &io, int rounds, int split, const int64_t *s_off) {
     __shared__ unsigned long long s_w[kBT / 32];
     __shared__ int s_nq;
     __shared__ int s_big[kBT * 8];       // queued rows (local index), rounds <= 8
-    if (io.flags[1]) return;
-    for (int i = threadIdx.x; i <= io.Q; i += blockDim.x) s_off[i] = io.in_row_off[i];
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tile_rows = kBT * rounds;
     const int64_t total = s_off[io.Q];
@@ -325,6 +339,77 @@ batch_write_kernel(StepIO io, int rounds, int split) {
     }
 }
 
+__global__ void __launch_bounds__(kBT)
+batch_write_kernel(StepIO io, int rounds, int split) {
+    extern __shared__ int64_t s_off[];   // Q+1 input row offsets
+    if (io.flags[1]) return;
+    for (int i = threadIdx.x; i <= io.Q; i += blockDim.x) s_off[i] = io.in_row_off[i];
+    __syncthreads();
+    write_phase(io, rounds, split, s_off);
+}
+
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier of a cooperative launch: bar[0] counts arrivals, bar[1] is the
+// generation.  The block arriving last resets the count and advances the
+// generation; the others poll the generation with a back-off,
+// at most kBarrierIters times -- a wait that runs out sets kErrBarrier and
+// returns false in every thread of the block (the caller then leaves; every
+// other block's wait ends the same way, so the launch ends).
+__device__ __forceinline__ bool grid_barrier(unsigned int *bar, int *flags) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int gen = ld_acquire(bar + 1);
+        __threadfence();   // this block's writes before its arrival
+        int ok = 1;
+        if (atomicAdd(bar, 1u) + 1u == gridDim.x) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            st_release(bar + 1, gen + 1u);
+        } else {
+            long it = 0;
+            while (ld_acquire(bar + 1) == gen) {
+                if (++it > kBarrierIters) {
+                    ok = 0;
+                    atomicOr(flags, kErrBarrier);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// One step in one cooperative launch: count, barrier, scan (block 0),
+// barrier, write.  Launched with at most as many blocks as fit on the device
+// at once (the cooperative launch refuses more).
+__global__ void __launch_bounds__(kBT)
+batch_step_kernel(StepIO io, int rounds, int split, unsigned int *bar) {
+    extern __shared__ int64_t s_off[];   // Q + 1 input row offsets
+    if (io.flags[1]) return;             // set before the launch: the same in every block
+    for (int i = threadIdx.x; i <= io.Q; i += blockDim.x) s_off[i] = io.in_row_off[i];
+    __syncthreads();
+    count_phase(io, rounds, s_off);
+    if (!grid_barrier(bar, io.flags)) return;
+    if (blockIdx.x == 0) scan_phase(io, rounds);
+    if (!grid_barrier(bar, io.flags)) return;
+    if (*(volatile int *)(io.flags + 1)) return;   // this step's scan found the batch over capacity
+    write_phase(io, rounds, split, s_off);
+}
+
 // step-0 layout: every query has one virtual row and no columns
 __global__ void batch_init_kernel(int Q, int64_t *row_off, int64_t *int_off, int32_t *cols,
                                   unsigned long long *q_rows, int *flags) {
@@ -348,7 +433,7 @@ struct wk_batch {
     int32_t max_q = 0, max_steps = 0;
     int64_t cap_ints = 0, cap_rows = 0;
     int sms = 0;
-    BatchTune tune{4, 4, 64};
+    BatchTune tune{4, 4, 64, 0};
     // device
     PredView *d_pvs = nullptr;
     StepDesc *d_desc = nullptr;             // [max_steps][max_q]
@@ -358,6 +443,7 @@ struct wk_batch {
     uint32_t *d_cnt = nullptr, *d_off = nullptr;
     unsigned long long *d_tile = nullptr, *d_qrows = nullptr;
     int *d_flags = nullptr;
+    unsigned int *d_bar = nullptr;          // grid barrier of the one-kernel steps (count, generation)
     // host (pinned)
     StepDesc *h_desc = nullptr;
     int64_t *h_layout = nullptr;            // row_off (Q+1), int_off (Q), cols as int64 (Q)
@@ -366,7 +452,7 @@ struct wk_batch {
     // executable graphs by batch size (a serving loop's batch sizes vary from
     // batch to batch; each size is captured once), all for graph_tune
     std::unordered_map<int, cudaGraphExec_t> graphs;
-    BatchTune graph_tune{0, 0, 0};
+    BatchTune graph_tune{0, 0, 0, 0};
     cudaGraphExec_t gexec = nullptr;   // the last one launched
     int32_t last_q = 0;
     int final_buf = 0;
@@ -401,6 +487,7 @@ void free_batch(wk_batch *b) {
     cudaFree(b->d_pvs); cudaFree(b->d_desc);
     for (int i = 0; i < 2; ++i) { cudaFree(b->d_row_off[i]); cudaFree(b->d_int_off[i]); cudaFree(b->d_cols[i]); cudaFree(b->d_hist[i]); }
     cudaFree(b->d_cnt); cudaFree(b->d_off); cudaFree(b->d_tile); cudaFree(b->d_qrows); cudaFree(b->d_flags);
+    cudaFree(b->d_bar);
     if (b->h_desc) cudaFreeHost(b->h_desc);
     if (b->h_layout) cudaFreeHost(b->h_layout);
     if (b->h_flags) cudaFreeHost(b->h_flags);
@@ -431,7 +518,13 @@ StepIO make_io(wk_batch *b, int s, int Q) {
     return io;
 }
 
-// the whole batch: descriptor upload, layout init, max_steps x (count, scan, write)
+// kernels of one batch: the layout init, then per step three kernels or one
+int64_t batch_kernels(const wk_batch *b, const BatchTune &t) {
+    return 1 + (t.fused ? 1 : 3) * (int64_t)b->max_steps;
+}
+
+// the whole batch: descriptor upload, layout init, max_steps x (count, scan,
+// write) as three kernels or as one cooperative kernel
 int enqueue(wk_batch *b, int Q, const BatchTune &t, cudaStream_t st) {
     // the Q descriptors of each step (step s's start at s * max_q)
     for (int s = 0; s < b->max_steps; ++s) {
@@ -449,15 +542,42 @@ int enqueue(wk_batch *b, int Q, const BatchTune &t, cudaStream_t st) {
     const int64_t full = (int64_t)b->sms * t.blocks_per_sm;
     const unsigned grid = (unsigned)std::min<int64_t>(full, std::max<int64_t>(b->sms / 4, 2 * (int64_t)Q));
     const size_t sm_off = sizeof(int64_t) * (size_t)(Q + 1);
-    for (int s = 0; s < b->max_steps; ++s) {
-        StepIO io = make_io(b, s, Q);
-        batch_count_kernel<<<grid, kBT, sm_off, st>>>(io, t.rounds);
-        batch_scan_kernel<<<1, 1024, 0, st>>>(io, t.rounds);
-        batch_write_kernel<<<grid, kBT, sm_off, st>>>(io, t.rounds, t.split);
+    if (t.fused) {
+        // every block of a cooperative launch must be resident at once
+        int occ = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_step_kernel, kBT, sm_off);
+        if (e != cudaSuccess) return cuda_fail(e, "batch step occupancy");
+        if (occ < 1) return set_error(WK_EDEVICE, "batch step kernel: no block fits on an SM");
+        const unsigned gf = (unsigned)std::min<int64_t>(grid, (int64_t)occ * b->sms);
+        // the barrier words start at zero in every batch (a wait that ran out leaves them unbalanced)
+        if ((e = cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned int), st)) != cudaSuccess)
+            return cuda_fail(e, "batch barrier reset");
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(gf);
+        cfg.blockDim = dim3(kBT);
+        cfg.dynamicSmemBytes = sm_off;
+        cfg.stream = st;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        for (int s = 0; s < b->max_steps; ++s) {
+            StepIO io = make_io(b, s, Q);
+            if ((e = cudaLaunchKernelEx(&cfg, batch_step_kernel, io, t.rounds, t.split, b->d_bar)) != cudaSuccess)
+                return cuda_fail(e, "batch step launch");
+        }
+    } else {
+        for (int s = 0; s < b->max_steps; ++s) {
+            StepIO io = make_io(b, s, Q);
+            batch_count_kernel<<<grid, kBT, sm_off, st>>>(io, t.rounds);
+            batch_scan_kernel<<<1, 1024, 0, st>>>(io, t.rounds);
+            batch_write_kernel<<<grid, kBT, sm_off, st>>>(io, t.rounds, t.split);
+        }
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "batch launch");
-    b->kernels += 1 + 3 * (int64_t)b->max_steps;
+    b->kernels += batch_kernels(b, t);
     return WK_OK;
 }
 
@@ -489,6 +609,7 @@ extern "C" int wk_batch_create(wk_ctx *ctx, int32_t max_queries, int32_t max_ste
               cudaMalloc(&b->d_tile, 8 * (size_t)tiles) == cudaSuccess &&
               cudaMalloc(&b->d_qrows, 8 * (size_t)max_queries) == cudaSuccess &&
               cudaMalloc(&b->d_flags, 64) == cudaSuccess &&
+              cudaMalloc(&b->d_bar, 2 * sizeof(unsigned int)) == cudaSuccess &&
               cudaHostAlloc((void **)&b->h_desc, sizeof(StepDesc) * (size_t)max_queries * max_steps, 0) == cudaSuccess &&
               cudaHostAlloc((void **)&b->h_layout, 8 * (size_t)(3 * max_queries + 1), 0) == cudaSuccess &&
               cudaHostAlloc((void **)&b->h_flags, 64, 0) == cudaSuccess &&
@@ -506,6 +627,7 @@ extern "C" int wk_batch_create(wk_ctx *ctx, int32_t max_queries, int32_t max_ste
     }
     e = cudaMemcpy(b->d_pvs, ctx->store->views.data(), sizeof(PredView) * npv, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_flags, 0, 64);
+    if (e == cudaSuccess) e = cudaMemset(b->d_bar, 0, 2 * sizeof(unsigned int));
     if (e != cudaSuccess) { int r = cuda_fail(e, "wk_batch_create"); free_batch(b); return r; }
     *out = b;
     return WK_OK;
@@ -520,9 +642,17 @@ extern "C" int wk_batch_set_tuning(wk_batch *b, int32_t blocks_per_sm, int32_t r
     if (!b || blocks_per_sm < 1 || blocks_per_sm > 16 || rows_per_warp < 32 || rows_per_warp > 256 ||
         rows_per_warp % 32 || split_ints < 1)
         return set_error(WK_EINVAL, "wk_batch_set_tuning: blocks/SM 1..16, rows/warp 32..256 (x32), split >= 1");
-    b->tune = BatchTune{blocks_per_sm, rows_per_warp / 32, split_ints};
+    b->tune = BatchTune{blocks_per_sm, rows_per_warp / 32, split_ints, b->tune.fused};
     return WK_OK;
 }
+
+extern "C" int wk_batch_set_fused(wk_batch *b, int32_t fused) {
+    if (!b || (fused != 0 && fused != 1)) return set_error(WK_EINVAL, "wk_batch_set_fused: 0 or 1");
+    b->tune.fused = fused;
+    return WK_OK;
+}
+
+extern "C" int wk_batch_get_fused(wk_batch *b) { return b ? b->tune.fused : 0; }
 
 extern "C" int wk_batch_get_tuning(wk_batch *b, int32_t *blocks_per_sm, int32_t *rows_per_warp, int32_t *split_ints) {
     if (!b || !blocks_per_sm || !rows_per_warp || !split_ints) return set_error(WK_EINVAL, "wk_batch_get_tuning: null");
@@ -613,15 +743,15 @@ extern "C" int wk_batch_launch(wk_batch *b, const int64_t *cmd_chains, const int
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return cuda_fail(e, "batch graph instantiate");
             it = b->graphs.emplace(nq, ge).first;
-            b->kernels -= 1 + 3 * (int64_t)b->max_steps;   // capture does not launch
+            b->kernels -= batch_kernels(b, b->tune);   // capture does not launch
         }
         b->gexec = it->second;
         if ((e = cudaGraphLaunch(b->gexec, s)) != cudaSuccess) return cuda_fail(e, "batch graph launch");
-        b->kernels += 1 + 3 * (int64_t)b->max_steps;
+        b->kernels += batch_kernels(b, b->tune);
     } else {
         if ((st = enqueue(b, nq, b->tune, s))) return st;
     }
-    ctx->launches += 1 + 3 * (int64_t)b->max_steps;
+    ctx->launches += batch_kernels(b, b->tune);
     b->last_q = nq;
     b->final_buf = b->max_steps & 1;
     // layout of the final tables + flags, then the completion event
@@ -648,6 +778,8 @@ extern "C" int wk_batch_wait(wk_batch *b) {
     if (e != cudaSuccess) return cuda_fail(e, "batch wait");
     if (b->h_flags[1]) return set_error(WK_EOVERFLOW, "wk_batch: a step exceeded the batch capacity of %lld ints",
                                         (long long)b->cap_ints);
+    if (b->h_flags[0] & kErrBarrier)
+        return set_error(WK_ETIMEDOUT, "wk_batch: a grid-barrier wait of the one-kernel step ran out");
     if (b->h_flags[0]) return set_error(WK_EDEVICE, "wk_batch: corrupt overflow chain in the store");
     return WK_OK;
 }
@@ -684,9 +816,11 @@ extern "C" int wk_batch_download(wk_batch *b, int32_t *host, int64_t cap, int64_
     return WK_OK;
 }
 
-// Autotuner: time the batch with every candidate (blocks/SM, rows/warp,
-// split) on the given queries (CUDA events, best of `reps` after a warm run)
-// and keep the fastest.  Writes the chosen triple and its time.
+// Autotuner: time the batch with every candidate (three kernels or one per
+// step, blocks/SM, rows/warp, split) on the given queries (CUDA events, best
+// of `reps` after a warm run) and keep the fastest.  A one-kernel candidate
+// the device refuses (its cooperative launch, or its capture into a graph) is
+// skipped.  Writes the chosen candidate's time.
 extern "C" int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
                                  int32_t reps, double *best_ms) {
     if (!b || reps < 1) return set_error(WK_EINVAL, "wk_batch_autotune: bad arguments");
@@ -698,11 +832,16 @@ extern "C" int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const i
         return set_error(WK_EDEVICE, "wk_batch_autotune: events");
     double best = 1e30;
     BatchTune keep = b->tune;
+    for (int fu = 0; fu < 2; ++fu)
     for (int bl : kBlocks)
         for (int rw : kRows)
             for (int sp : kSplit) {
-                b->tune = BatchTune{bl, rw / 32, sp};
+                b->tune = BatchTune{bl, rw / 32, sp, fu};
                 int st = wk_batch_run(b, cmd_chains, n_patterns, nq, 1);   // builds the graph
+                if (st && fu && st != WK_EOVERFLOW && st != WK_ETIMEDOUT) {
+                    cudaGetLastError();
+                    continue;
+                }
                 if (st) { cudaEventDestroy(e0); cudaEventDestroy(e1); b->tune = keep; return st; }
                 double tbest = 1e30;
                 for (int r = 0; r < reps; ++r) {

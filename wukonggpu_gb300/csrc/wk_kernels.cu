@@ -56,47 +56,6 @@ __device__ __forceinline__ void block_sum2(unsigned long long &a, unsigned int &
     }
 }
 
-// ------------------------------------------------------------- look-back
-constexpr unsigned long long kPrefixReady = 1ull << 63;
-
-__device__ __forceinline__ unsigned long long ld_flag(const unsigned long long *p) {
-    unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_flag(unsigned long long *p, unsigned long long v) {
-    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
-// Exclusive output prefix of block b: the sum of agg[0..b).  flags[k] is
-// kPrefixReady | (inclusive prefix of block k) once block k has published it,
-// else 0 (cleared by the op's first kernel).  Called by one full warp, which
-// reads 32 predecessors per step and stops at the nearest published one.  It
-// never waits on another block, so it ends after at most b / 32 steps.
-template <typename A>
-__device__ __forceinline__ unsigned long long lookback_prefix(const A *__restrict__ agg,
-                                                              const unsigned long long *flags, int64_t b) {
-    const int lane = threadIdx.x & 31;
-    unsigned long long acc = 0;
-    for (int64_t i = b - 1; i >= 0; i -= 32) {
-        const int64_t k = i - lane;
-        unsigned long long f = 0ull, a = 0ull;
-        if (k >= 0) {
-            f = ld_flag(flags + k);
-            a = (unsigned long long)agg[k];
-        }
-        const unsigned ready = __ballot_sync(FULL, (f & kPrefixReady) != 0ull);
-        if (ready) {
-            const int L = __ffs(ready) - 1;   // nearest published predecessor
-            acc += warp_sum(lane < L ? a : (lane == L ? (f & ~kPrefixReady) : 0ull));
-            return acc;
-        }
-        acc += warp_sum(a);
-    }
-    return acc;
-}
-
 // --------------------------------------------------------------- k2u count
 // A block's output rows are written by slices_of(count) expansion CTAs (none
 // for an empty block), so a block that holds hub rows is spread over many
@@ -663,12 +622,17 @@ __device__ __forceinline__ void probe_view_or_warp(const PredView &pv, int32_t v
 // index key, hashed) takes the general path.  All rounds' reads are issued
 // before any is used.
 template <bool NB>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 6)
 filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, int ecol,
                     int32_t end_const, uint32_t dir, PredView pv,
                     uint32_t *__restrict__ mask, unsigned int *__restrict__ blk_nz,
-                    unsigned long long *__restrict__ flags, unsigned long long *__restrict__ totals, int *err) {
+                    unsigned long long *__restrict__ group_sums, unsigned long long *__restrict__ clear,
+                    int64_t nclear, unsigned long long *__restrict__ totals, int *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // the other sums buffer, read by the previous op's write or expansion, is
+    // cleared for the next op (a few hundred words at most)
+    for (int64_t w = (int64_t)blockIdx.x * kThreads + threadIdx.x; w < nclear; w += (int64_t)gridDim.x * kThreads)
+        clear[w] = 0ull;
     const int64_t wrow0 = (int64_t)blockIdx.x * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
     int32_t v[kRounds], tg[kRounds];
 #pragma unroll
@@ -716,164 +680,98 @@ filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol
     block_sum2(my_scan, my_nz);
     if (threadIdx.x == 0) {
         blk_nz[blockIdx.x] = my_nz;
-        flags[blockIdx.x] = 0ull;
         if (my_scan) atomicAdd(totals, my_scan);
-        if (my_nz) atomicAdd(totals + 1, (unsigned long long)my_nz);
+        if (my_nz) {
+            atomicAdd(totals + 1, (unsigned long long)my_nz);
+            atomicAdd(group_sums + 2 * (blockIdx.x >> kGroupShift), (unsigned long long)my_nz);
+        }
     }
 }
 
 // ----------------------------------------------------------- filter write
-// A write CTA takes kWriteBlocks consecutive blocks of input rows: it loads
-// their kept-row counts at once and writes the non-empty blocks in order, so
-// a filter that keeps few rows costs one CTA per kWriteBlocks blocks rather
-// than one per block, and a block's look-back mostly finds its predecessor
-// published by the same CTA.
-constexpr int kWriteBlocks = 8;
+// A write CTA takes kWriteBlocks consecutive blocks of input rows, one per
+// warp, all in one group of 2^kGroupShift blocks.  Their output prefixes need
+// no look-back and no wait: the probe kernel added every block's kept-row
+// count into its group's sum, so the prefix of the CTA's first block is the
+// sum of the group sums before its group and of the block counts before it in
+// the group -- one CTA reduction -- and warp w adds the counts of the CTA's
+// blocks before its own.  Each warp then writes its block alone: the kept
+// rows' positions from the block's 32 mask words (one per lane, a warp scan
+// of their popcounts), then the block's output words [P C, (P + nb) C) as
+// aligned 16 B stores where whole, each word gathered from its kept row (the
+// block's rows stay in L1 and L2 while the warp copies them).
+constexpr int kWriteBlocks = kThreads / 32;
+static_assert(((1 << kGroupShift) % kWriteBlocks) == 0, "a write CTA's blocks share a group");
 
-struct FilterSel {
-    int sel[kRowsPerBlock];                      // the block's kept rows, in order
-    unsigned int wbase[kRowsPerBlock / 32 + 1];
-    unsigned long long P;                        // the block's output prefix
-};
-
-// the kept rows of block b (nb of them) in order, and the block's prefix
-// (published for its successors); ends with the CTA synchronised
-__device__ __forceinline__ void filter_select(int64_t b, unsigned int nb, int64_t R, const uint32_t *__restrict__ mask,
-                                              const unsigned int *__restrict__ blk_nz, unsigned long long *flags,
-                                              FilterSel &fs) {
-    constexpr int kPer = kRowsPerBlock / kThreads;   // 4 rows per thread
-    const int64_t r0 = b * kRowsPerBlock;
-    const int64_t nwords_mask = (R + 31) >> 5;
-    const int t = threadIdx.x;
-    if (t < 32) {
-        const int64_t wi = (r0 >> 5) + t;
-        const uint32_t m = wi < nwords_mask ? mask[wi] : 0u;
-        unsigned int c = __popc(m), inc = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned int v = __shfl_up_sync(FULL, inc, o);
-            if (t >= o) inc += v;
-        }
-        fs.wbase[t] = inc - c;
-        if (t == 31) fs.wbase[32] = inc;
-        const unsigned long long P = lookback_prefix(blk_nz, flags, b);
-        if (t == 0) {
-            st_flag(flags + b, kPrefixReady | (P + nb));
-            fs.P = P;
-        }
-    }
-    __syncthreads();
-    {
-        const int wi = (t * kPer) >> 5, bit0 = (t * kPer) & 31;
-        const int64_t mwi = (r0 >> 5) + wi;
-        const uint32_t m = mwi < nwords_mask ? mask[mwi] : 0u;
-        unsigned int pos = fs.wbase[wi] + __popc(m & ((1u << bit0) - 1u));
-#pragma unroll
-        for (int q = 0; q < kPer; ++q)
-            if (m & (1u << (bit0 + q))) fs.sel[pos++] = t * kPer + q;
-    }
-    __syncthreads();
-}
-
-// Any width: each kept row copied word by word to the rows that start at the
-// block's look-back prefix.
+template <int CT>   // the columns, or 0 for any (C_rt)
 __global__ void __launch_bounds__(kThreads)
-filter_write_kernel(const int32_t *__restrict__ hist, int64_t R, int C, const uint32_t *__restrict__ mask,
-                    const unsigned int *__restrict__ blk_nz, unsigned long long *flags,
+filter_write_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const uint32_t *__restrict__ mask,
+                    const unsigned int *__restrict__ blk_nz, const unsigned long long *__restrict__ group_sums,
                     int32_t *__restrict__ out) {
-    __shared__ FilterSel fs;
+    __shared__ uint16_t sel[kWriteBlocks][kRowsPerBlock];   // each warp's kept rows, in order
+    __shared__ unsigned long long s_part[kThreads / 32];
     __shared__ unsigned int s_nz[kWriteBlocks];
+    const int C = CT > 0 ? CT : C_rt;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
-    const int64_t bb = (int64_t)blockIdx.x * kWriteBlocks;
-    const int t = threadIdx.x;
-    if (t < kWriteBlocks) s_nz[t] = bb + t < nblk ? blk_nz[bb + t] : 0u;
-    __syncthreads();
-    for (int k = 0; k < kWriteBlocks; ++k) {
-        const unsigned int nb = s_nz[k];
-        if (nb == 0u) continue;   // successors add this block's count (0) as they walk past
-        const int64_t b = bb + k, r0 = b * kRowsPerBlock;
-        filter_select(b, nb, R, mask, blk_nz, flags, fs);
-        int32_t *dst = out + (int64_t)fs.P * C;
-        for (int j = t; j < (int)nb; j += kThreads) {
-            const int32_t *src = hist + (r0 + fs.sel[j]) * C;
-            int32_t *d = dst + (int64_t)j * C;
-            for (int c = 0; c < C; ++c) d[c] = __ldg(src + c);
-        }
-        __syncthreads();   // fs is reused by the next block
-    }
-}
+    const int64_t b0 = (int64_t)blockIdx.x * kWriteBlocks;
+    const int64_t g = b0 >> kGroupShift;
 
-// Tables of C <= 8 columns: a block's kept rows are staged in shared memory,
-// then its output words [P C, (P + nb) C) stream out as aligned 16 B stores
-// (P the block's look-back prefix, nb its kept rows).  When at least a
-// quarter of the block's rows are kept the whole block is read with 16 B
-// loads and the kept rows picked from shared memory; otherwise each kept row
-// is gathered alone.
-template <int C>
-__global__ void __launch_bounds__(kThreads)
-filter_write_vec_kernel(const int32_t *__restrict__ hist, int64_t R, const uint32_t *__restrict__ mask,
-                        const unsigned int *__restrict__ blk_nz, unsigned long long *flags, int32_t *__restrict__ out) {
-    __shared__ FilterSel fs;
-    __shared__ unsigned int s_nz[kWriteBlocks];
-    __shared__ __align__(16) int32_t rows[kRowsPerBlock * C];
-    const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
-    const int64_t bb = (int64_t)blockIdx.x * kWriteBlocks;
-    const int t = threadIdx.x;
-    if (t < kWriteBlocks) s_nz[t] = bb + t < nblk ? blk_nz[bb + t] : 0u;
+    // 1. the prefix of block b0, and the CTA's blocks' counts
+    unsigned long long x = 0ull;
+    for (int64_t i = t; i < g; i += kThreads) x += group_sums[2 * i];
+    for (int64_t i = (g << kGroupShift) + t; i < b0; i += kThreads) x += blk_nz[i];
+    if (t < kWriteBlocks) s_nz[t] = b0 + t < nblk ? blk_nz[b0 + t] : 0u;
+    x = warp_sum(x);
+    if (lane == 0) s_part[w] = x;
     __syncthreads();
-    for (int kb = 0; kb < kWriteBlocks; ++kb) {
-        const unsigned int nb = s_nz[kb];
-        if (nb == 0u) continue;   // successors add this block's count (0) as they walk past
-        const int64_t b = bb + kb, r0 = b * kRowsPerBlock;
-        const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
-        const int32_t *src = hist + r0 * C;
-        const bool whole = 4u * nb >= (unsigned int)n;   // the same in every thread
-        if (whole) {
-            // the block's n C words; 16 B loads when the block starts on a 16 B boundary
-            const int words = n * C;
-            if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
-                for (int i = t; 4 * i < words; i += kThreads) {
-                    if (4 * i + 4 <= words) {
-                        reinterpret_cast<int4 *>(rows)[i] = __ldg(reinterpret_cast<const int4 *>(src) + i);
-                    } else {
-                        for (int k = 4 * i; k < words; ++k) rows[k] = __ldg(src + k);
-                    }
-                }
-            } else {
-                for (int k = t; k < words; k += kThreads) rows[k] = __ldg(src + k);
-            }
-        }
-        filter_select(b, nb, R, mask, blk_nz, flags, fs);   // also completes the staging above
-        if (!whole) {
-            for (int j = t; j < (int)nb; j += kThreads) {
-                const int32_t *sr = src + fs.sel[j] * C;
+    unsigned long long P = 0ull;
 #pragma unroll
-                for (int c = 0; c < C; ++c) rows[j * C + c] = __ldg(sr + c);
-            }
-            __syncthreads();
+    for (int i = 0; i < kThreads / 32; ++i) P += s_part[i];
+    for (int i = 0; i < w; ++i) P += s_nz[i];
+    const unsigned int nb = s_nz[w];
+    if (nb == 0u) return;   // the warp's block keeps nothing (or lies past the table)
+
+    // 2. the block's kept rows, in order
+    const int64_t b = b0 + w, r0 = b * kRowsPerBlock;
+    const int64_t wi = (r0 >> 5) + lane, nwords = (R + 31) >> 5;
+    uint32_t m = wi < nwords ? mask[wi] : 0u;   // bits past R are 0
+    const unsigned int c = __popc(m);
+    unsigned int pos = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int v = __shfl_up_sync(FULL, pos, o);
+        if (lane >= o) pos += v;
+    }
+    pos -= c;
+    uint16_t *ws = sel[w];
+    while (m) {
+        ws[pos++] = (uint16_t)(lane * 32 + __ffs(m) - 1);
+        m &= m - 1u;
+    }
+    __syncwarp();
+
+    // 3. output words [P C, (P + nb) C) as int4 stores aligned to 16 B of out
+    const int32_t *hb = hist + r0 * C;
+    const uint32_t words = nb * (uint32_t)C;
+    const uint32_t lead = (uint32_t)((P * (unsigned long long)C) & 3ull);
+    int32_t *gout = out + (P * (unsigned long long)C - lead);
+    for (uint32_t u = (uint32_t)lane; 4u * u < lead + words; u += 32u) {
+        int32_t v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t kk = 4u * u + (uint32_t)j - lead;   // wraps above `words` before the lead
+            v[j] = kk < words ? __ldg(hb + (int)ws[kk / (uint32_t)C] * C + (int)(kk % (uint32_t)C)) : 0;
         }
-        // output words [P C, (P + nb) C): int4 stores aligned to 16 B of out
-        const unsigned long long P = fs.P;
-        const uint32_t lead = (uint32_t)((P * C) & 3ull), words = nb * C;
-        int32_t *g = out + (P * C - lead);
-        for (uint32_t i = (uint32_t)t; 4u * i < lead + words; i += kThreads) {
-            int32_t v[4];
+        if (4u * u >= lead && 4u * u + 4u <= lead + words) {
+            reinterpret_cast<int4 *>(gout)[u] = make_int4(v[0], v[1], v[2], v[3]);
+        } else {
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const uint32_t kk = 4u * i + j - lead;   // wraps above `words` before the lead
-                v[j] = kk < words ? (whole ? rows[fs.sel[kk / C] * C + kk % C] : rows[kk]) : 0;
-            }
-            if (4u * i >= lead && 4u * i + 4u <= lead + words) {
-                reinterpret_cast<int4 *>(g)[i] = make_int4(v[0], v[1], v[2], v[3]);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const uint32_t kk = 4u * i + j - lead;
-                    if (kk < words) g[4u * i + j] = v[j];
-                }
+                const uint32_t kk = 4u * u + (uint32_t)j - lead;
+                if (kk < words) gout[4u * u + j] = v[j];
             }
         }
-        __syncthreads();   // rows and fs are reused by the next block
     }
 }
 
@@ -984,19 +882,22 @@ int preload_k2u_kernels() {
 
 void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ecol, int32_t end_const,
                          uint32_t dir, PredView pv, uint32_t *mask, unsigned int *blk_nz,
-                         unsigned long long *flags, unsigned long long *totals, int *err, cudaStream_t st) {
+                         unsigned long long *group_sums, unsigned long long *clear, int64_t nclear,
+                         unsigned long long *totals, int *err, cudaStream_t st) {
     if ((dir ? pv.nb[1] : pv.nb[0]) != nullptr)
         filter_probe_kernel<true><<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv,
-                                                                        mask, blk_nz, flags, totals, err);
+                                                                        mask, blk_nz, group_sums, clear, nclear,
+                                                                        totals, err);
     else
         filter_probe_kernel<false><<<nblocks_rows(R), kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv,
-                                                                         mask, blk_nz, flags, totals, err);
+                                                                         mask, blk_nz, group_sums, clear, nclear,
+                                                                         totals, err);
 }
 
 void launch_filter_write(const int32_t *hist, int64_t R, int C, const uint32_t *mask, const unsigned int *blk_nz,
-                         unsigned long long *flags, int32_t *out, cudaStream_t st) {
+                         const unsigned long long *group_sums, int32_t *out, cudaStream_t st) {
     const unsigned int g = (nblocks_rows(R) + kWriteBlocks - 1) / kWriteBlocks;
-#define WK_FWRITE(CC) filter_write_vec_kernel<CC><<<g, kThreads, 0, st>>>(hist, R, mask, blk_nz, flags, out)
+#define WK_FWRITE(CC) filter_write_kernel<CC><<<g, kThreads, 0, st>>>(hist, R, C, mask, blk_nz, group_sums, out)
     switch (C) {
         case 1: WK_FWRITE(1); break;
         case 2: WK_FWRITE(2); break;
@@ -1006,7 +907,7 @@ void launch_filter_write(const int32_t *hist, int64_t R, int C, const uint32_t *
         case 6: WK_FWRITE(6); break;
         case 7: WK_FWRITE(7); break;
         case 8: WK_FWRITE(8); break;
-        default: filter_write_kernel<<<g, kThreads, 0, st>>>(hist, R, C, mask, blk_nz, flags, out); break;
+        default: WK_FWRITE(0); break;
     }
 #undef WK_FWRITE
 }

@@ -61,16 +61,19 @@ void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edg
                        const GroupTable &gt, unsigned long long slices, int32_t *out, cudaStream_t st);
 
 // k2k/k2c pass 1: probe + membership of the end value; per-row ballot masks,
-// per-block kept-row counts, flags cleared; totals[0] += adjacency entries a
-// linear scan touches, totals[1] += kept rows.
+// per-block kept-row counts, each added into its group's sum (group_sums[2 g],
+// 2^kGroupShift blocks a group, zero on entry); totals[0] += adjacency entries
+// a linear scan touches, totals[1] += kept rows.  The nclear words at `clear`
+// (the other sums buffer) are zeroed.
 // ecol >= 0: end is column ecol (k2k); ecol < 0: end is the constant `end_const` (k2c).
 void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ecol, int32_t end_const,
                          uint32_t dir, PredView pv, uint32_t *mask, unsigned int *blk_nz,
-                         unsigned long long *flags, unsigned long long *totals, int *err, cudaStream_t st);
+                         unsigned long long *group_sums, unsigned long long *clear, int64_t nclear,
+                         unsigned long long *totals, int *err, cudaStream_t st);
 
 // k2k/k2c pass 2: copy the kept rows in order (out holds up to R rows of C columns).
 void launch_filter_write(const int32_t *hist, int64_t R, int C, const uint32_t *mask, const unsigned int *blk_nz,
-                         unsigned long long *flags, int32_t *out, cudaStream_t st);
+                         const unsigned long long *group_sums, int32_t *out, cudaStream_t st);
 
 // Copy an adjacency list (index or constant start) into a one-column table.
 void launch_copy_list(const int32_t *src, int64_t n, int32_t *dst, cudaStream_t st);

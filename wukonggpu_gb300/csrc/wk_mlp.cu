@@ -14,7 +14,11 @@
 // product (X . W^T), for the input gradient (dZ . W, with W^T kept as a BF16
 // copy) and for the weight gradient (dZ^T . X, with the transposed
 // activations written by the forward pass).  Dimensions are padded: M and N
-// to multiples of 64, K to multiples of 16; padding is zero.
+// to multiples of 64, K to multiples of 16; padding is zero.  The hidden
+// layers' activation runs in the GEMM's epilogue: the forward product writes
+// GELU(Z) in bf16 (row-major and transposed) beside Z, and the input-gradient
+// product of the layer above writes dZ = dH * GELU'(Z) with the bias
+// gradient (its column sums), so dH itself is never stored.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -38,11 +42,6 @@ constexpr int kXPadN = 128;   // W1^T rows padded (dX GEMM has N = 80 -> 128)
 constexpr float kB1 = 0.9f, kB2 = 0.999f;   // Adam moment decay rates
 
 // ------------------------------------------------------------ elementwise
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_grad(float x) {
-    return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
-}
-
 // X0 [Mp x 80] bf16 = [feats | emb[pid]] for real rows, 0 for padding
 __global__ void build_input_kernel(const float *__restrict__ feats, const int32_t *__restrict__ pids, int M, int Mp,
                                    const float *__restrict__ emb, int n_ids, __nv_bfloat16 *__restrict__ X0,
@@ -62,31 +61,6 @@ __global__ void build_input_kernel(const float *__restrict__ feats, const int32_
         const __nv_bfloat16 bv = __float2bfloat16(v);
         X0[i] = bv;
         X0t[(size_t)c * Mp + r] = bv;
-    }
-}
-
-// H = GELU(Z) as bf16, row-major and transposed; rows >= M are zero
-__global__ void gelu_fwd_kernel(const float *__restrict__ Z, int M, int Mp, int N, __nv_bfloat16 *__restrict__ H,
-                                __nv_bfloat16 *__restrict__ Ht) {
-    const int64_t n = (int64_t)Mp * N;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int r = (int)(i / N), c = (int)(i % N);
-        const __nv_bfloat16 h = __float2bfloat16(r < M ? gelu(Z[i]) : 0.f);
-        H[i] = h;
-        Ht[(size_t)c * Mp + r] = h;
-    }
-}
-
-// dZ = dH * GELU'(Z) as bf16 (row-major and transposed), and db = column sums
-__global__ void gelu_bwd_kernel(const float *__restrict__ dH, const float *__restrict__ Z, int M, int Mp, int N,
-                                __nv_bfloat16 *__restrict__ dZ, __nv_bfloat16 *__restrict__ dZt) {
-    const int64_t n = (int64_t)Mp * N;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int r = (int)(i / N), c = (int)(i % N);
-        const float v = r < M ? dH[i] * gelu_grad(Z[i]) : 0.f;
-        const __nv_bfloat16 b = __float2bfloat16(v);
-        dZ[i] = b;
-        dZt[(size_t)c * Mp + r] = b;
     }
 }
 
@@ -222,9 +196,10 @@ struct wk_mlp {
     // bf16 weights (row-major, padded) and transposes
     __nv_bfloat16 *wb[4] = {}, *wt[4] = {};
     // activations (capacity cap_m)
-    __nv_bfloat16 *x0 = nullptr, *x0t = nullptr, *h[3] = {}, *ht[3] = {}, *dz = nullptr, *dzt = nullptr, *dy = nullptr,
+    // dz / dzt: two buffers, the layer whose weight gradient is taken and the one below it
+    __nv_bfloat16 *x0 = nullptr, *x0t = nullptr, *h[3] = {}, *ht[3] = {}, *dz[2] = {}, *dzt[2] = {}, *dy = nullptr,
                   *dyt = nullptr;
-    float *z[4] = {}, *dh = nullptr, *dx = nullptr, *feats = nullptr, *tgt = nullptr, *loss = nullptr;
+    float *z[4] = {}, *dx = nullptr, *feats = nullptr, *tgt = nullptr, *loss = nullptr;
     int32_t *pids = nullptr;
     int *bidx = nullptr;         // the batch of the epoch a training step takes
     float2 *cbias = nullptr;     // Adam bias corrections of an epoch's steps
@@ -259,18 +234,22 @@ void refresh_bf16(wk_mlp *m, cudaStream_t s) {
     m->kernels += 4;
 }
 
-// C = A . B^T (+ bias) on the tensor cores (wk_tc_gemm.cuh); N is a multiple of 64.
-// The tile width is the widest that still gives a full wave of CTAs, else 64:
-// these products are small, and more CTAs means more copies and products in flight.
+// C = A . B^T (+ bias) on the tensor cores (wk_tc_gemm.cuh), with the
+// epilogue EPI; N is a multiple of 64.  The tile width is the widest that still
+// gives a full wave of CTAs, else 64: these products are small, and more CTAs
+// means more copies and products in flight.
+template <int EPI = tc::kEpiStore>
 void gemm(wk_mlp *m, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N,
-          int K, const float *bias, cudaStream_t s) {
+          int K, const float *bias, cudaStream_t s, const tc::EpiArgs &ea = tc::EpiArgs()) {
     if (m->broken) {
         if (!m->status)
             m->status = set_error(WK_EDEVICE, "estimator: an earlier tensor-core GEMM left work in flight; "
                                               "destroy the estimator");
         return;
     }
-    if (M <= 0 || K <= 0 || N <= 0 || N % 64 || ldc % 4 || ((uintptr_t)C & 15u) || ((uintptr_t)bias & 15u)) {
+    if (M <= 0 || K <= 0 || N <= 0 || N % 64 || ldc % 4 || ((uintptr_t)C & 15u) || ((uintptr_t)bias & 15u) ||
+        (EPI != tc::kEpiStore && (((uintptr_t)ea.h & 15u) || ea.ldh % 8 || !ea.ht || ea.m_store > M)) ||
+        (EPI == tc::kEpiGeluBwd && (((uintptr_t)ea.z & 15u) || ea.ldz % 4 || !ea.colsum))) {
         if (!m->status) m->status = set_error(WK_EINVAL, "estimator GEMM: shape or alignment (M %d, N %d, K %d)", M, N, K);
         return;
     }
@@ -284,11 +263,48 @@ void gemm(wk_mlp *m, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, in
     }
     const dim3 grid((unsigned)mt, (unsigned)(N / bn));
     switch (bn) {
-        case 64: tc::gemm_tc_kernel<64><<<grid, tc::kThreads, tc::smem_bytes(64), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
-        case 128: tc::gemm_tc_kernel<128><<<grid, tc::kThreads, tc::smem_bytes(128), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
-        default: tc::gemm_tc_kernel<256><<<grid, tc::kThreads, tc::smem_bytes(256), s>>>(ta, tb, C, ldc, M, K, bias, m->d_err); break;
+        case 64:
+            tc::gemm_tc_kernel<64, EPI><<<grid, tc::kThreads, tc::smem_bytes(64), s>>>(ta, tb, C, ldc, M, K, bias,
+                                                                                       m->d_err, ea);
+            break;
+        case 128:
+            tc::gemm_tc_kernel<128, EPI><<<grid, tc::kThreads, tc::smem_bytes(128), s>>>(ta, tb, C, ldc, M, K, bias,
+                                                                                         m->d_err, ea);
+            break;
+        default:
+            tc::gemm_tc_kernel<256, EPI><<<grid, tc::kThreads, tc::smem_bytes(256), s>>>(ta, tb, C, ldc, M, K, bias,
+                                                                                         m->d_err, ea);
+            break;
     }
     m->kernels++;
+}
+
+// the epilogue operands of a hidden layer's activation: h / ht written for
+// rows below Mp, values for rows below M
+tc::EpiArgs act_args(int M, int Mp, __nv_bfloat16 *h, __nv_bfloat16 *ht, const float *z = nullptr,
+                     float *colsum = nullptr) {
+    tc::EpiArgs ea;
+    ea.m_real = M;
+    ea.m_store = Mp;
+    ea.h = h;
+    ea.ldh = kH;
+    ea.ht = ht;
+    ea.ldt = Mp;
+    ea.z = z;
+    ea.ldz = kH;
+    ea.colsum = colsum;
+    return ea;
+}
+
+template <int BN, int EPI>
+bool set_gemm_smem() {
+    return cudaFuncSetAttribute(tc::gemm_tc_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tc::smem_bytes(BN)) == cudaSuccess;
+}
+
+template <int EPI>
+bool set_gemm_smem_all() {
+    return set_gemm_smem<64, EPI>() && set_gemm_smem<128, EPI>() && set_gemm_smem<256, EPI>();
 }
 
 // the status of the work queued since the last check: a host-side failure, a
@@ -325,14 +341,15 @@ void forward(wk_mlp *m, int M, cudaStream_t s) {
     const __nv_bfloat16 *in = m->x0;
     int kin = kX;
     for (int l = 0; l < 3; ++l) {
-        gemm(m, in, kin, m->wb[l], kin, m->z[l], kH, Mp, kH, kin, m->params + m->off_b[l], s);
-        gelu_fwd_kernel<<<nblk((int64_t)Mp * kH), 256, 0, s>>>(m->z[l], M, Mp, kH, m->h[l], m->ht[l]);
+        // Z_l = X W_l^T + b_l, and H_l = GELU(Z_l) from the epilogue
+        gemm<tc::kEpiGeluFwd>(m, in, kin, m->wb[l], kin, m->z[l], kH, Mp, kH, kin, m->params + m->off_b[l], s,
+                              act_args(M, Mp, m->h[l], m->ht[l]));
         in = m->h[l];
         kin = kH;
     }
     gemm(m, in, kH, m->wb[3], kH, m->z[3], kOutPad, Mp, kOutPad, kH, nullptr, s);
     // output bias (layer 4 has one real output): added in the loss / predict read
-    m->kernels += 4;
+    m->kernels += 1;
 }
 
 // loss + backward + Adam on M rows (targets uploaded)
@@ -342,32 +359,39 @@ void backward_step(wk_mlp *m, int M, float lr, bool update, cudaStream_t s) {
     cudaMemsetAsync(g, 0, sizeof(float) * (size_t)m->n_params, s);
     // dY: y includes the output bias
     loss_kernel<<<1, 1024, 0, s>>>(m->z[3], m->tgt, M, Mp, m->dy, m->dyt, m->loss);
-    // layer 4: dW4 = dY^T . H3 (B = H3^T [256 x Mp]); db4 = sum dY; dH3 = dY . W4 (B = W4^T [256 x 64])
+    // layer 4: dW4 = dY^T . H3 (B = H3^T [256 x Mp]); db4 = sum dY; dZ3 = (dY . W4) * GELU'(Z3)
+    // (B = W4^T [256 x 64]) with db3 from the same epilogue
+    int cur = 0;
     {
         float *dw4 = g + m->off_w[3];   // [1 x 256] real, GEMM writes [64 x 256]
         gemm(m, m->dyt, Mp, m->ht[2], Mp, m->dx /*scratch [64 x 256]*/, kH, kOutPad, kH, Mp, nullptr, s);
         cudaMemcpyAsync(dw4, m->dx, sizeof(float) * kH, cudaMemcpyDeviceToDevice, s);   // row 0
         colsum_kernel<<<1, 256, 0, s>>>(m->dyt, Mp, g + m->off_b[3]);
-        gemm(m, m->dy, kOutPad, m->wt[3], kOutPad, m->dh, kH, Mp, kH, kOutPad, nullptr, s);
+        gemm<tc::kEpiGeluBwd>(m, m->dy, kOutPad, m->wt[3], kOutPad, nullptr, kH, Mp, kH, kOutPad, nullptr, s,
+                              act_args(M, Mp, m->dz[cur], m->dzt[cur], m->z[2], g + m->off_b[2]));
     }
     for (int l = 2; l >= 0; --l) {
-        gelu_bwd_kernel<<<nblk((int64_t)Mp * kH), 256, 0, s>>>(m->dh, m->z[l], M, Mp, kH, m->dz, m->dzt);
+        // dZ_l is in dz[cur] / dzt[cur], db_l already summed
         const __nv_bfloat16 *inT = (l == 0) ? m->x0t : m->ht[l - 1];
         const int kin = (l == 0) ? kX : kH;
         // dW_l [256 x kin] = dZ^T [256 x Mp] . (X^T [kin x Mp])^T ; N = kin must be a multiple of 64
         if (kin % 64 == 0) {
-            gemm(m, m->dzt, Mp, inT, Mp, g + m->off_w[l], kin, kH, kin, Mp, nullptr, s);
+            gemm(m, m->dzt[cur], Mp, inT, Mp, g + m->off_w[l], kin, kH, kin, Mp, nullptr, s);
         } else {
             // layer 0: kin = 80 -> compute into scratch [256 x 128] then copy the first 80 columns
-            gemm(m, m->dzt, Mp, inT, Mp, m->dx, kXPadN, kH, kXPadN, Mp, nullptr, s);
+            gemm(m, m->dzt[cur], Mp, inT, Mp, m->dx, kXPadN, kH, kXPadN, Mp, nullptr, s);
             cudaMemcpy2DAsync(g + m->off_w[0], sizeof(float) * kX, m->dx, sizeof(float) * kXPadN, sizeof(float) * kX,
                               kH, cudaMemcpyDeviceToDevice, s);
         }
-        colsum_kernel<<<kH, 256, 0, s>>>(m->dzt, Mp, g + m->off_b[l]);
-        // dH_{l-1} = dZ . W_l  (B = W_l^T [kin(pad) x 256])
-        if (l > 0) gemm(m, m->dz, kH, m->wt[l], kH, m->dh, kH, Mp, kH, kH, nullptr, s);
-        else gemm(m, m->dz, kH, m->wt[0], kH, m->dx, kXPadN, Mp, kXPadN, kH, nullptr, s);
-        m->kernels += 2;
+        // dZ_{l-1} = (dZ_l . W_l) * GELU'(Z_{l-1}) (B = W_l^T [256 x 256]), with db_{l-1};
+        // layer 0: dX = dZ_0 . W_0 (B = W_0^T [128 x 256]) for the embedding gradient
+        if (l > 0) {
+            gemm<tc::kEpiGeluBwd>(m, m->dz[cur], kH, m->wt[l], kH, nullptr, kH, Mp, kH, kH, nullptr, s,
+                                  act_args(M, Mp, m->dz[1 - cur], m->dzt[1 - cur], m->z[l - 1], g + m->off_b[l - 1]));
+            cur = 1 - cur;
+        } else {
+            gemm(m, m->dz[cur], kH, m->wt[0], kH, m->dx, kXPadN, Mp, kXPadN, kH, nullptr, s);
+        }
     }
     emb_grad_kernel<<<nblk((int64_t)M * kEmb), 256, 0, s>>>(m->dx, kXPadN, m->pids, M, m->n_ids, g + m->off_emb);
     m->kernels += 3;
@@ -403,8 +427,9 @@ void free_mlp(wk_mlp *m) {
     cudaFree(m->m2);
     for (int l = 0; l < 4; ++l) { cudaFree(m->wb[l]); cudaFree(m->wt[l]); cudaFree(m->z[l]); }
     for (int l = 0; l < 3; ++l) { cudaFree(m->h[l]); cudaFree(m->ht[l]); }
-    cudaFree(m->x0); cudaFree(m->x0t); cudaFree(m->dz); cudaFree(m->dzt); cudaFree(m->dy); cudaFree(m->dyt);
-    cudaFree(m->dh); cudaFree(m->dx); cudaFree(m->feats); cudaFree(m->tgt); cudaFree(m->loss); cudaFree(m->pids);
+    cudaFree(m->x0); cudaFree(m->x0t); cudaFree(m->dy); cudaFree(m->dyt);
+    for (int i = 0; i < 2; ++i) { cudaFree(m->dz[i]); cudaFree(m->dzt[i]); }
+    cudaFree(m->dx); cudaFree(m->feats); cudaFree(m->tgt); cudaFree(m->loss); cudaFree(m->pids);
     cudaFree(m->d_err);
     cudaFree(m->bidx);
     cudaFree(m->cbias);
@@ -444,20 +469,16 @@ extern "C" int wk_mlp_create(wk_ctx *ctx, int32_t n_ids, int32_t max_batch, uint
         ok = cudaMalloc(&m->h[l], 2 * Mp * kH) == cudaSuccess && cudaMalloc(&m->ht[l], 2 * Mp * kH) == cudaSuccess;
     // X0^T has kXPadN rows: the layer-0 weight-gradient product pads N = 80 to 128 and reads rows 80..127 (zero)
     ok = ok && cudaMalloc(&m->x0, 2 * Mp * kX) == cudaSuccess && cudaMalloc(&m->x0t, 2 * Mp * kXPadN) == cudaSuccess &&
-         cudaMalloc(&m->dz, 2 * Mp * kH) == cudaSuccess && cudaMalloc(&m->dzt, 2 * Mp * kH) == cudaSuccess &&
+         cudaMalloc(&m->dz[0], 2 * Mp * kH) == cudaSuccess && cudaMalloc(&m->dzt[0], 2 * Mp * kH) == cudaSuccess &&
+         cudaMalloc(&m->dz[1], 2 * Mp * kH) == cudaSuccess && cudaMalloc(&m->dzt[1], 2 * Mp * kH) == cudaSuccess &&
          cudaMalloc(&m->dy, 2 * Mp * kOutPad) == cudaSuccess && cudaMalloc(&m->dyt, 2 * Mp * kOutPad) == cudaSuccess &&
-         cudaMalloc(&m->dh, 4 * Mp * kH) == cudaSuccess &&
          cudaMalloc(&m->dx, 4 * std::max(Mp * (size_t)kXPadN, (size_t)kH * kXPadN)) == cudaSuccess &&
          cudaMalloc(&m->feats, 4 * Mp * kIn) == cudaSuccess && cudaMalloc(&m->tgt, 4 * Mp) == cudaSuccess &&
          cudaMalloc(&m->loss, 16) == cudaSuccess && cudaMalloc(&m->pids, 4 * Mp) == cudaSuccess &&
          cudaMalloc(&m->d_err, sizeof(int)) == cudaSuccess && cudaMalloc(&m->bidx, sizeof(int)) == cudaSuccess &&
          cudaHostAlloc((void **)&m->h_err, sizeof(int), 0) == cudaSuccess &&
-         cudaFuncSetAttribute(tc::gemm_tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tc::smem_bytes(64)) == cudaSuccess &&
-         cudaFuncSetAttribute(tc::gemm_tc_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tc::smem_bytes(128)) == cudaSuccess &&
-         cudaFuncSetAttribute(tc::gemm_tc_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tc::smem_bytes(256)) == cudaSuccess;
+         set_gemm_smem_all<tc::kEpiStore>() && set_gemm_smem_all<tc::kEpiGeluFwd>() &&
+         set_gemm_smem_all<tc::kEpiGeluBwd>();
     if (!ok) {
         cudaGetLastError();
         free_mlp(m);

@@ -164,7 +164,7 @@ int wk::reserve_op_scratch(wk_ctx *ctx, int64_t rows) {
     int st;
     if ((st = ctx->deg.reserve((size_t)rows * 4)) || (st = ctx->off.reserve((size_t)rows * 4)) ||
         (st = ctx->mask.reserve((size_t)((rows + 31) / 32) * 4)) || (st = ctx->blk_sum.reserve((size_t)nblk * 8)) ||
-        (st = ctx->blk_nz.reserve((size_t)nblk * 4)) || (st = ctx->lb_flags.reserve((size_t)(nblk + 1) * 16)) ||
+        (st = ctx->blk_nz.reserve((size_t)nblk * 4)) ||
         (st = reserve_gsum(ctx, (nblk + (1 << dev::kGroupShift) - 1) >> dev::kGroupShift)))
         return st;
     return WK_OK;
@@ -311,19 +311,27 @@ int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const,
         return WK_OK;
     }
     const int64_t nblk = (R + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock;
+    const int64_t groups = (nblk + (1 << dev::kGroupShift) - 1) >> dev::kGroupShift;
     if ((st = take(ctx, ctx->mask, (size_t)((R + 31) / 32) * 4)) || (st = take(ctx, ctx->blk_nz, (size_t)nblk * 4)) ||
-        (st = take(ctx, ctx->lb_flags, (size_t)nblk * 8)) || (st = take(ctx, ob, (size_t)R * C * 4)) ||
-        (st = clear_totals(ctx)))
+        (st = reserve_gsum(ctx, groups)) || (st = take(ctx, ob, (size_t)R * C * 4)) || (st = clear_totals(ctx)))
         return st;
     unsigned long long *tot = ctx->dscal.as<unsigned long long>() + 1;
     int *err = ctx->dscal.as<int>();
+    // the block counts' group sums go to one of the two sums buffers k2u uses,
+    // and the probe clears the other
+    const int par = ctx->gs_par;
+    unsigned long long *gs = gsum_buffer(ctx, par) + 2;
     if ((st = clk.begin())) return st;
     dev::launch_filter_probe(h->data, R, C, scol, ecol, end_const, dir, pv, ctx->mask.as<uint32_t>(),
-                             ctx->blk_nz.as<unsigned int>(), ctx->lb_flags.as<unsigned long long>(), tot, err,
-                             ctx->stream);
-    if ((st = launch_check("filter probe")) || (st = clk.end(true)) || (st = clk.begin())) return st;
-    dev::launch_filter_write(h->data, R, C, ctx->mask.as<uint32_t>(), ctx->blk_nz.as<unsigned int>(),
-                             ctx->lb_flags.as<unsigned long long>(), ob.as<int32_t>(), ctx->stream);
+                             ctx->blk_nz.as<unsigned int>(), gs, gsum_buffer(ctx, par ^ 1),
+                             2 + 2 * ctx->gs_used[par ^ 1], tot, err, ctx->stream);
+    if ((st = launch_check("filter probe"))) return st;
+    ctx->gs_par = par ^ 1;
+    ctx->gs_used[par ^ 1] = 0;
+    ctx->gs_used[par] = groups;
+    if ((st = clk.end(true)) || (st = clk.begin())) return st;
+    dev::launch_filter_write(h->data, R, C, ctx->mask.as<uint32_t>(), ctx->blk_nz.as<unsigned int>(), gs,
+                             ob.as<int32_t>(), ctx->stream);
     if ((st = launch_check("filter write")) || (st = clk.end(false))) return st;
     int errf = 0;
     if ((st = read_totals(ctx, &errf))) return st;

@@ -284,7 +284,7 @@ wk_ctx::~wk_ctx() {
     if (stream) cudaStreamSynchronize(stream);
     for (auto &b : hbuf) b.release();
     deg.release(); off.release(); mask.release(); blk_sum.release(); blk_nz.release();
-    lb_flags.release(); dscal.release();
+    dscal.release();
     if (h_scal) cudaFreeHost(h_scal);
     if (h_gs) cudaFreeHost(h_gs);
     for (auto &e : tev) cudaEventDestroy(e);

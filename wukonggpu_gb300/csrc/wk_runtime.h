@@ -82,7 +82,6 @@ struct wk_ctx {
     wk::DevBuf hbuf[2];              // ping-pong history buffers (core/rcache.hpp:87-88)
     // scratch of the two-pass ops
     wk::DevBuf deg, off, mask, blk_sum, blk_nz;
-    wk::DevBuf lb_flags;             // filter look-back words
     // k2u: two alternating sums buffers, each a 16 B header (the op's error
     // flags) and 16 B per group of 256 input blocks; a count kernel adds into
     // one and clears the other for the next op

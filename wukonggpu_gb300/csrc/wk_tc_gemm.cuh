@@ -13,9 +13,16 @@
 //     tcgen05.mma (kind::f16, 128 x BN x 16 each) from shared-memory
 //     descriptors and commits them to the stage's "empty" mbarrier;
 //   - after the last commit, warp w reads TMEM lanes 32w..32w+31 (rows) in
-//     32-column chunks with tcgen05.ld, stages each chunk in shared memory (the
-//     pipeline stages are free by then) and writes it out as whole rows of
-//     float4 with the bias added, so a store instruction covers 4 rows x 128 B.
+//     32-column chunks with tcgen05.ld and runs the epilogue the template
+//     names (EpiArgs):
+//       kEpiStore:   C = acc (+ bias), staged in shared memory (the pipeline
+//                    stages are free by then) and written as whole rows of
+//                    float4, so a store instruction covers 4 rows x 128 B;
+//       kEpiGeluFwd: the same C (the pre-activation Z), and H = GELU(Z) in
+//                    bf16, row-major and transposed (zero for rows >= m_real);
+//       kEpiGeluBwd: dZ = acc * GELU'(Z) in bf16, row-major and transposed
+//                    (zero for rows >= m_real), and the column sums of the
+//                    rounded dZ added into colsum[] -- C is not written.
 // Every mbarrier wait is bounded.  A wait that runs out sets bit 2 of *err and
 // stops the pipeline: the producer waits (bounded) for the copies it issued
 // and the issuer for the last commit of the products it issued.  If those
@@ -41,6 +48,29 @@ constexpr int kStages = 4;
 constexpr int kThreads = 128;
 constexpr int kEpiPitch = 36;       // floats per staged output row: rows 16 B apart modulo 128 B
 constexpr long kWaitIters = 1l << 22;
+
+enum { kEpiStore = 0, kEpiGeluFwd = 1, kEpiGeluBwd = 2 };
+
+// The epilogue's extra operands (unused by kEpiStore).  Rows below m_store get
+// h / ht written (row-major with ld ldh, transposed with ld ldt); rows below
+// m_real carry values, the rest zeros.
+struct EpiArgs {
+    int m_real = 0, m_store = 0;
+    __nv_bfloat16 *h = nullptr;
+    int ldh = 0;
+    __nv_bfloat16 *ht = nullptr;
+    int ldt = 0;
+    const float *z = nullptr;   // kEpiGeluBwd: the layer's pre-activation (ld ldz)
+    int ldz = 0;
+    float *colsum = nullptr;    // kEpiGeluBwd: column sums of dZ are added here
+};
+
+// The estimator's activation, exact GELU: x Phi(x), and its derivative
+// Phi(x) + x phi(x) (Phi, phi the standard normal CDF and density).
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -88,11 +118,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// C must be 16 B aligned with ldc a multiple of 4, and bias (if any) 16 B aligned.
-template <int BN>
+// C must be 16 B aligned with ldc a multiple of 4, and bias (if any) 16 B
+// aligned; h (and z) 16 B aligned with ldh (ldz) a multiple of 8 (4).
+template <int BN, int EPI>
 __global__ void __launch_bounds__(kThreads)
 gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-               float *__restrict__ C, int ldc, int M, int K, const float *__restrict__ bias, int *err) {
+               float *__restrict__ C, int ldc, int M, int K, const float *__restrict__ bias, int *err,
+               const EpiArgs ea) {
     static_assert(BN == 64 || BN == 128 || BN == 256, "tile width: an MMA N and a TMEM allocation");
     constexpr uint32_t kABytes = kTM * 128, kBBytes = BN * 128, kStage = kABytes + kBBytes;
     static_assert(4 * 32 * kEpiPitch * 4 <= kStage, "the output staging fits in stage 0");
@@ -184,26 +216,77 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         // every copy landed and every product ran: stage 0 is free for the output rows
         float *stg = reinterpret_cast<float *>(sm) + warp * 32 * kEpiPitch;
         const int q = lane & 7;
+        const int myrow = m0 + warp * 32 + lane;   // the row of this lane's TMEM lane
         for (int c0 = 0; c0 < BN; c0 += 32) {
             uint32_t r[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+            const int cb = n0 + c0;   // the chunk's first column
             float4 *mine = reinterpret_cast<float4 *>(stg + lane * kEpiPitch);
+            if constexpr (EPI != kEpiGeluBwd) {
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
-                mine[i] = make_float4(__uint_as_float(r[4 * i]), __uint_as_float(r[4 * i + 1]),
-                                      __uint_as_float(r[4 * i + 2]), __uint_as_float(r[4 * i + 3]));
-            __syncwarp();
-            const int col = n0 + c0 + q * 4;
-            const float4 bv = bias ? *reinterpret_cast<const float4 *>(bias + col) : make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int i = 0; i < 8; ++i)
+                    mine[i] = make_float4(__uint_as_float(r[4 * i]), __uint_as_float(r[4 * i + 1]),
+                                          __uint_as_float(r[4 * i + 2]), __uint_as_float(r[4 * i + 3]));
+                __syncwarp();
+                const int col = cb + q * 4;
+                const float4 bv = bias ? *reinterpret_cast<const float4 *>(bias + col) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int rr = i * 4 + (lane >> 3);
-                const int row = m0 + warp * 32 + rr;
-                float4 v = *reinterpret_cast<const float4 *>(stg + rr * kEpiPitch + q * 4);
-                v.x += bv.x; v.y += bv.y; v.z += bv.z; v.w += bv.w;
-                if (row < M) *reinterpret_cast<float4 *>(C + (size_t)row * ldc + col) = v;
+                for (int i = 0; i < 8; ++i) {
+                    const int rr = i * 4 + (lane >> 3);
+                    const int row = m0 + warp * 32 + rr;
+                    float4 v = *reinterpret_cast<const float4 *>(stg + rr * kEpiPitch + q * 4);
+                    v.x += bv.x; v.y += bv.y; v.z += bv.z; v.w += bv.w;
+                    if (row < M) *reinterpret_cast<float4 *>(C + (size_t)row * ldc + col) = v;
+                }
+                __syncwarp();
             }
-            __syncwarp();
+            if constexpr (EPI == kEpiGeluFwd || EPI == kEpiGeluBwd) {
+                // this lane's row of the chunk: 32 values in bf16
+                __nv_bfloat16 hv[32];
+                if constexpr (EPI == kEpiGeluFwd) {
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) {
+                        const float zv = __uint_as_float(r[i]) + (bias ? bias[cb + i] : 0.f);
+                        hv[i] = __float2bfloat16(myrow < ea.m_real ? gelu(zv) : 0.f);
+                    }
+                } else {
+                    float zr[32] = {};
+                    if (myrow < ea.m_real) {
+                        const float4 *zp = reinterpret_cast<const float4 *>(ea.z + (size_t)myrow * ea.ldz + cb);
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const float4 z4 = zp[i];
+                            zr[4 * i] = z4.x; zr[4 * i + 1] = z4.y; zr[4 * i + 2] = z4.z; zr[4 * i + 3] = z4.w;
+                        }
+                    }
+#pragma unroll
+                    for (int i = 0; i < 32; ++i)
+                        hv[i] = __float2bfloat16(myrow < ea.m_real ? __uint_as_float(r[i]) * gelu_grad(zr[i]) : 0.f);
+                    // column sums of the rounded values: rows staged in shared memory, lane i sums column i
+                    float *mrow = stg + lane * kEpiPitch;
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) mrow[i] = __bfloat162float(hv[i]);
+                    __syncwarp();
+                    float cs = 0.f;
+#pragma unroll 8
+                    for (int rr = 0; rr < 32; ++rr) cs += stg[rr * kEpiPitch + lane];
+                    if (cs != 0.f) atomicAdd(ea.colsum + cb + lane, cs);
+                    __syncwarp();
+                }
+                if (myrow < ea.m_store) {
+                    // element 2k at the lower address: the low half of word k
+                    uint32_t w[16];
+#pragma unroll
+                    for (int k = 0; k < 16; ++k)
+                        w[k] = (uint32_t)__bfloat16_as_ushort(hv[2 * k]) |
+                               ((uint32_t)__bfloat16_as_ushort(hv[2 * k + 1]) << 16);
+                    uint4 *hp = reinterpret_cast<uint4 *>(ea.h + (size_t)myrow * ea.ldh + cb);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) hp[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) ea.ht[(size_t)(cb + i) * ea.ldt + myrow] = hv[i];
+                }
+            }
         }
     } else if (s_fail && t == 0) {
         atomicOr(err, s_inflight ? (4 | 8) : 4);
