@@ -434,3 +434,25 @@ def test_k2u_over_256_groups(lib_built):
         rc.known_to_unknown(req, -1, W.OUT, pid)
         got = rc.download(req)
         assert got.shape == exp.shape and np.array_equal(got, exp), pid
+
+
+@pytest.mark.parametrize("with_index_key", [False, True])
+def test_functional_k2u_in_chunks(gpu_small, small_graph, small_oracle, with_index_key):
+    """A functional op whose history passes 96 MB runs its count and expansion
+    chunk by chunk (12 groups of 262,144 rows a chunk at 4 columns: three
+    chunks here, the last one ragged).  An index key among the rows makes the
+    whole op rerun unspecialised after the chunks."""
+    g, s, p, o = small_graph
+    rng = np.random.default_rng(5)
+    ents = np.unique(s[p == W.TYPE_ID])
+    R, C = 7_000_001, 4
+    h = rng.choice(ents, size=(R, C)).astype(np.int32)
+    h[rng.random(R) < 0.2, 1] = W.VID_BASE + 90_000_000   # no type: the row is dropped
+    if with_index_key:
+        h[4_500_017, 1] = 0
+    req = W.Request([])
+    gpu_small.upload_history(req, h)
+    gpu_small.known_to_unknown(req, -2, W.OUT, W.TYPE_ID)
+    got = gpu_small.download(req)
+    exp, _ = small_oracle.step(h, False, -2, W.TYPE_ID, W.OUT, -C - 1)
+    assert got.shape == exp.shape and np.array_equal(got, exp)

@@ -167,11 +167,14 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
                 if constexpr (FUNC) {
                     reinterpret_cast<int32_t *>(deg)[r] = d ? __ldg(pv.edges + o) : -1;
                     if (d > 1u) atomicOr(err, 8);   // an index list: the op reruns unspecialised
+                    // at most one output row per input row, so a block's output never
+                    // exceeds its rows even before the rerun
+                    my_sum[rd / kRounds] += d ? 1u : 0u;
                 } else {
                     deg[r] = d;
                     off[r] = o;
+                    my_sum[rd / kRounds] += d;
                 }
-                my_sum[rd / kRounds] += d;
             }
         }
     }
@@ -507,21 +510,49 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
 // (rows kPitch words apart, an odd pitch so the 32 lanes' rows fall in 32
 // banks), and the CTA then streams the block's output words to HBM as
 // aligned int4 stores.
-template <int W>
+//
+// DIRECT (an op run in chunks of whole groups, each chunk's count then its
+// expansion, so the expansion finds the chunk's history rows in L2): CTA k
+// takes block b_first + k of the chunk, empty or not, and its output prefix
+// is the sum of the group sums before its group and of the block counts
+// before it in the group -- counts that this and the earlier chunks' count
+// kernels finished -- with no table from the host.
+template <int W, bool DIRECT>
 __global__ void __launch_bounds__(kThreads)
 k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_t *__restrict__ nbr,
                        const unsigned long long *__restrict__ blk_sum,
                        const unsigned long long *__restrict__ group_sums, int64_t ngroups, int64_t nblk,
-                       const __grid_constant__ GroupTable gt, int32_t *__restrict__ out) {
+                       const __grid_constant__ GroupTable gt, int64_t b_first, int32_t *__restrict__ out) {
     constexpr int C = W - 1;
     constexpr int kPitch = W | 1;
     __shared__ int32_t rows[kRowsPerBlock * kPitch];
     __shared__ uint32_t s_w[kThreads / 32];
+    __shared__ unsigned long long s_p[kThreads / 32];
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
 
     // the block (every non-empty block has one slice)
-    const SliceLoc loc = locate_slice(blockIdx.x, blk_sum, group_sums, ngroups, nblk, gt);
-    if (loc.b < 0) return;   // the same in every thread
+    SliceLoc loc;
+    if constexpr (DIRECT) {
+        loc.b = b_first + blockIdx.x;
+        if (loc.b >= nblk) return;
+        const unsigned long long tb = blk_sum[loc.b];
+        if (tb == 0ull) return;   // the same in every thread
+        const int64_t g = loc.b >> kGroupShift;
+        unsigned long long x = 0ull;
+        for (int64_t i = t; i < g; i += kThreads) x += group_sums[2 * i];
+        for (int64_t i = (g << kGroupShift) + t; i < loc.b; i += kThreads) x += blk_sum[i];
+        x = warp_sum(x);
+        if (lane == 0) s_p[wid] = x;
+        __syncthreads();
+        loc.P = 0ull;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) loc.P += s_p[w];
+        loc.T = (uint32_t)tb;
+        loc.slice = 0u;
+    } else {
+        loc = locate_slice(blockIdx.x, blk_sum, group_sums, ngroups, nblk, gt);
+        if (loc.b < 0) return;   // the same in every thread
+    }
     const int64_t b = loc.b;
     const int64_t r0 = b * kRowsPerBlock;
     const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
@@ -818,7 +849,30 @@ void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t
     const int64_t ng = (nblk + (1 << kGroupShift) - 1) >> kGroupShift;
     const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND_F(WC) \
-    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, group_sums, ng, nblk, gt, out)
+    k2u_expand_func_kernel<WC, false><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, group_sums, ng, nblk, gt, 0, out)
+    switch (C + 1) {
+        case 2: WK_EXPAND_F(2); break;
+        case 3: WK_EXPAND_F(3); break;
+        case 4: WK_EXPAND_F(4); break;
+        case 5: WK_EXPAND_F(5); break;
+        case 6: WK_EXPAND_F(6); break;
+        case 7: WK_EXPAND_F(7); break;
+        default: WK_EXPAND_F(8); break;
+    }
+#undef WK_EXPAND_F
+}
+
+void launch_k2u_expand_func_chunk(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
+                                  const unsigned long long *blk_sum, const unsigned long long *group_sums,
+                                  int64_t b_first, int64_t b_count, int32_t *out, cudaStream_t st) {
+    if (b_count <= 0) return;
+    const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
+    const int64_t ng = (nblk + (1 << kGroupShift) - 1) >> kGroupShift;
+    GroupTable gt;
+    gt.n = 0;
+    const unsigned int g = (unsigned int)b_count;
+#define WK_EXPAND_F(WC) \
+    k2u_expand_func_kernel<WC, true><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, group_sums, ng, nblk, gt, b_first, out)
     switch (C + 1) {
         case 2: WK_EXPAND_F(2); break;
         case 3: WK_EXPAND_F(3); break;
