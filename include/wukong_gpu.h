@@ -271,6 +271,9 @@ int wk_batch_ready(wk_batch *b);
 int wk_batch_wait(wk_batch *b);
 /* Result of query q of the last run: rows, columns and its int32 offset in the packed result. */
 int wk_batch_result(wk_batch *b, int32_t q, int64_t *rows, int32_t *cols, int64_t *int_offset);
+/* The results of all nq queries of the last run at once (nq must be its
+ * query count): rows, columns and int32 offsets, one entry per query. */
+int wk_batch_layouts(wk_batch *b, int32_t nq, int64_t *rows, int32_t *cols, int64_t *int_offsets);
 /* Copy the packed results of the last run to host memory (host may be NULL to get the size). */
 int wk_batch_download(wk_batch *b, int32_t *host, int64_t cap, int64_t *total_ints);
 /* Launch shape of the step kernels: persistent blocks per SM, input rows per

@@ -16,6 +16,7 @@ There is no CPU fallback: if the library is missing every entry point raises.
 from __future__ import annotations
 
 import ctypes as C
+import itertools
 import os
 from pathlib import Path
 
@@ -147,6 +148,7 @@ _SIGS = {
     "wk_batch_set_tuning": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "wk_batch_get_tuning": (C.c_int, [_P, _I32P, _I32P, _I32P]),
     "wk_batch_set_fused": (C.c_int, [_P, C.c_int32]),
+    "wk_batch_layouts": (C.c_int, [_P, C.c_int32, _I64P, _I32P, _I64P]),
     "wk_batch_get_fused": (C.c_int, [_P]),
     "wk_batch_autotune": (C.c_int, [_P, _I64P, _I32P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "wk_batch_kernel_launches": (C.c_int64, [_P]),
@@ -578,8 +580,8 @@ class Batch:
 
     @staticmethod
     def pack(queries):
-        cmd = np.asarray([x for q in queries for x in q], np.int64)
-        npat = np.asarray([len(q) // 4 for q in queries], np.int32)
+        npat = np.fromiter((len(q) >> 2 for q in queries), np.int32, len(queries))
+        cmd = np.fromiter(itertools.chain.from_iterable(queries), np.int64, 4 * int(npat.sum()))
         return cmd, npat
 
     def run(self, queries, use_graph: bool = True, packed=None):
@@ -598,11 +600,14 @@ class Batch:
         else:
             buf = np.zeros(max(tot.value, 1), np.int32)
         _check(lib.wk_batch_download(self._h, buf.ctypes.data_as(_I32P), buf.size, C.byref(tot)))
-        out = []
-        rows, cols, off = C.c_int64(), C.c_int32(), C.c_int64()
-        for q in range(nq):
-            _check(lib.wk_batch_result(self._h, q, C.byref(rows), C.byref(cols), C.byref(off)))
-            out.append(buf[off.value:off.value + rows.value * cols.value].reshape(rows.value, max(cols.value, 1)))
+        rows = np.empty(nq, np.int64)
+        cols = np.empty(nq, np.int32)
+        offs = np.empty(nq, np.int64)
+        _check(lib.wk_batch_layouts(self._h, nq, rows.ctypes.data_as(_I64P), cols.ctypes.data_as(_I32P),
+                                    offs.ctypes.data_as(_I64P)))
+        width = np.maximum(cols, 1).tolist()
+        ends = (offs + rows * cols).tolist()
+        out = [buf[a:e].reshape(-1, w) for a, e, w in zip(offs.tolist(), ends, width)]
         return out
 
     def set_tuning(self, blocks_per_sm: int, rows_per_warp: int, split_ints: int):

@@ -800,6 +800,18 @@ extern "C" int wk_batch_result(wk_batch *b, int32_t q, int64_t *rows, int32_t *c
     return WK_OK;
 }
 
+extern "C" int wk_batch_layouts(wk_batch *b, int32_t nq, int64_t *rows, int32_t *cols, int64_t *int_offsets) {
+    if (!b || nq != b->last_q || (nq > 0 && (!rows || !cols || !int_offsets)))
+        return set_error(WK_EINVAL, "wk_batch_layouts: bad arguments (the last run had %d queries)", b ? b->last_q : 0);
+    const int32_t *c = reinterpret_cast<const int32_t *>(b->h_layout + 2 * nq + 1);
+    for (int q = 0; q < nq; ++q) {
+        rows[q] = b->h_layout[q + 1] - b->h_layout[q];
+        cols[q] = c[q];
+        int_offsets[q] = b->h_layout[nq + 1 + q];
+    }
+    return WK_OK;
+}
+
 extern "C" int wk_batch_download(wk_batch *b, int32_t *host, int64_t cap, int64_t *total_ints) {
     if (!b || !total_ints) return set_error(WK_EINVAL, "wk_batch_download: null");
     const int nq = b->last_q;
