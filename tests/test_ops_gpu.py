@@ -438,11 +438,10 @@ def test_k2u_over_256_groups(lib_built):
 
 
 @pytest.mark.parametrize("with_index_key", [False, True])
-def test_functional_k2u_in_chunks(gpu_small, small_graph, small_oracle, with_index_key):
-    """A functional op whose history passes 96 MB runs its count and expansion
-    chunk by chunk (12 groups of 262,144 rows a chunk at 4 columns: three
-    chunks here, the last one ragged).  An index key among the rows makes the
-    whole op rerun unspecialised after the chunks."""
+def test_large_functional_k2u(gpu_small, small_graph, small_oracle, with_index_key):
+    """A functional op over a 112 MB history (7,000,001 rows: 27 groups, the
+    last one ragged), once as the compaction and once with an index key among
+    its rows, which makes the op rerun unspecialised."""
     g, s, p, o = small_graph
     rng = np.random.default_rng(5)
     ents = np.unique(s[p == W.TYPE_ID])

@@ -510,49 +510,21 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
 // (rows kPitch words apart, an odd pitch so the 32 lanes' rows fall in 32
 // banks), and the CTA then streams the block's output words to HBM as
 // aligned int4 stores.
-//
-// DIRECT (an op run in chunks of whole groups, each chunk's count then its
-// expansion, so the expansion finds the chunk's history rows in L2): CTA k
-// takes block b_first + k of the chunk, empty or not, and its output prefix
-// is the sum of the group sums before its group and of the block counts
-// before it in the group -- counts that this and the earlier chunks' count
-// kernels finished -- with no table from the host.
-template <int W, bool DIRECT>
+template <int W>
 __global__ void __launch_bounds__(kThreads)
 k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_t *__restrict__ nbr,
                        const unsigned long long *__restrict__ blk_sum,
                        const unsigned long long *__restrict__ group_sums, int64_t ngroups, int64_t nblk,
-                       const __grid_constant__ GroupTable gt, int64_t b_first, int32_t *__restrict__ out) {
+                       const __grid_constant__ GroupTable gt, int32_t *__restrict__ out) {
     constexpr int C = W - 1;
     constexpr int kPitch = W | 1;
     __shared__ int32_t rows[kRowsPerBlock * kPitch];
     __shared__ uint32_t s_w[kThreads / 32];
-    __shared__ unsigned long long s_p[kThreads / 32];
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
 
     // the block (every non-empty block has one slice)
-    SliceLoc loc;
-    if constexpr (DIRECT) {
-        loc.b = b_first + blockIdx.x;
-        if (loc.b >= nblk) return;
-        const unsigned long long tb = blk_sum[loc.b];
-        if (tb == 0ull) return;   // the same in every thread
-        const int64_t g = loc.b >> kGroupShift;
-        unsigned long long x = 0ull;
-        for (int64_t i = t; i < g; i += kThreads) x += group_sums[2 * i];
-        for (int64_t i = (g << kGroupShift) + t; i < loc.b; i += kThreads) x += blk_sum[i];
-        x = warp_sum(x);
-        if (lane == 0) s_p[wid] = x;
-        __syncthreads();
-        loc.P = 0ull;
-#pragma unroll
-        for (int w = 0; w < kThreads / 32; ++w) loc.P += s_p[w];
-        loc.T = (uint32_t)tb;
-        loc.slice = 0u;
-    } else {
-        loc = locate_slice(blockIdx.x, blk_sum, group_sums, ngroups, nblk, gt);
-        if (loc.b < 0) return;   // the same in every thread
-    }
+    const SliceLoc loc = locate_slice(blockIdx.x, blk_sum, group_sums, ngroups, nblk, gt);
+    if (loc.b < 0) return;   // the same in every thread
     const int64_t b = loc.b;
     const int64_t r0 = b * kRowsPerBlock;
     const int n = (int)((R - r0) < kRowsPerBlock ? (R - r0) : kRowsPerBlock);
@@ -652,11 +624,10 @@ __device__ __forceinline__ void probe_view_or_warp(const PredView &pv, int32_t v
 // nothing; a linear scan touches 1 entry or none); a start value of 0 (an
 // index key, hashed) takes the general path.  All rounds' reads are issued
 // before any is used.
-// BPC blocks of input rows per CTA: 2 for a large op on a dense functional
-// direction (each lane then keeps eight rows' loads in flight and a CTA's
-// fixed costs are shared by 2048 rows), 1 otherwise.
+// BPC blocks of input rows per CTA (1 as launched: two blocks per CTA, with
+// eight rounds of loads in flight per lane, took 48 registers and ran slower).
 template <bool NB, int BPC>
-__global__ void __launch_bounds__(kThreads, BPC == 2 ? 5 : 6)
+__global__ void __launch_bounds__(kThreads, 6)
 filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, int ecol,
                     int32_t end_const, uint32_t dir, PredView pv,
                     uint32_t *__restrict__ mask, unsigned int *__restrict__ blk_nz,
@@ -879,30 +850,7 @@ void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t
     const int64_t ng = (nblk + (1 << kGroupShift) - 1) >> kGroupShift;
     const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND_F(WC) \
-    k2u_expand_func_kernel<WC, false><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, group_sums, ng, nblk, gt, 0, out)
-    switch (C + 1) {
-        case 2: WK_EXPAND_F(2); break;
-        case 3: WK_EXPAND_F(3); break;
-        case 4: WK_EXPAND_F(4); break;
-        case 5: WK_EXPAND_F(5); break;
-        case 6: WK_EXPAND_F(6); break;
-        case 7: WK_EXPAND_F(7); break;
-        default: WK_EXPAND_F(8); break;
-    }
-#undef WK_EXPAND_F
-}
-
-void launch_k2u_expand_func_chunk(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
-                                  const unsigned long long *blk_sum, const unsigned long long *group_sums,
-                                  int64_t b_first, int64_t b_count, int32_t *out, cudaStream_t st) {
-    if (b_count <= 0) return;
-    const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
-    const int64_t ng = (nblk + (1 << kGroupShift) - 1) >> kGroupShift;
-    GroupTable gt;
-    gt.n = 0;
-    const unsigned int g = (unsigned int)b_count;
-#define WK_EXPAND_F(WC) \
-    k2u_expand_func_kernel<WC, true><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, group_sums, ng, nblk, gt, b_first, out)
+    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, group_sums, ng, nblk, gt, out)
     switch (C + 1) {
         case 2: WK_EXPAND_F(2); break;
         case 3: WK_EXPAND_F(3); break;
@@ -974,13 +922,8 @@ void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ec
     filter_probe_kernel<NBV, B><<<(nb + B - 1) / B, kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv, \
                                                                        mask, blk_nz, group_sums, clear, nclear, \
                                                                        totals, err)
-    if ((dir ? pv.nb[1] : pv.nb[0]) != nullptr) {
-        // two blocks per CTA once the op has enough blocks to fill the GPU with half as many CTAs
-        if (nb >= 16u * (unsigned int)sms) WK_PROBE(true, 2);
-        else WK_PROBE(true, 1);
-    } else {
-        WK_PROBE(false, 1);
-    }
+    if ((dir ? pv.nb[1] : pv.nb[0]) != nullptr) WK_PROBE(true, 1);
+    else WK_PROBE(false, 1);
 #undef WK_PROBE
 }
 

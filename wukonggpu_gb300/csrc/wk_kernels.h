@@ -51,14 +51,6 @@ int preload_k2u_kernels();
 void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
                             const unsigned long long *blk_sum, const unsigned long long *group_sums,
                             const GroupTable &gt, unsigned long long slices, int32_t *out, cudaStream_t st);
-// The same for blocks [b_first, b_first + b_count) of the table, one CTA per
-// block: each finds its output prefix from the group sums and block counts
-// already on the device (the chunks of an op run in order, each chunk's count
-// before its expansion), so no host table is needed.
-void launch_k2u_expand_func_chunk(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
-                                  const unsigned long long *blk_sum, const unsigned long long *group_sums,
-                                  int64_t b_first, int64_t b_count, int32_t *out, cudaStream_t st);
-
 // k2u pass 2: one CTA per slice (slices = the op's total from the group sums)
 // finds its block from blk_sum and the group sums and writes its rows
 // (row || neighbour) of the block's output; out holds the op's output rows

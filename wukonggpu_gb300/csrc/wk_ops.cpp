@@ -193,10 +193,6 @@ int clear_totals(wk_ctx *ctx) {
     return e == cudaSuccess ? WK_OK : cuda_fail(e, "clear totals");
 }
 
-// History bytes per chunk of a large functional k2u (well inside the 129 MB L2,
-// beside the neighbour array and the output stream).
-constexpr int64_t kFuncChunkBytes = 48ll << 20;
-
 // two-pass k2u (count -> host adds up the group sums -> expand)
 int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     const int C = h->col_num;
@@ -227,66 +223,6 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     bool func = pv.func[dir] != 0u && C + 1 <= 8;
     int errf = 0;
     unsigned long long *gs = nullptr;
-    // A functional op whose history does not fit in L2 runs in chunks of whole
-    // groups, each chunk's count then its expansion, so the expansion reads the
-    // chunk's history rows from L2 instead of DRAM.  Its output (at most one row
-    // per input row) is sized by the input, so the chunks need no host
-    // synchronisation; the host reads the totals once at the end.
-    const int64_t chunk_groups =
-        std::max<int64_t>(1, kFuncChunkBytes / ((int64_t)C * 4 << (dev::kGroupShift + 10)));
-    if (func && R * C * 4 >= 2 * kFuncChunkBytes && groups > chunk_groups) {
-        const int64_t chunk_blocks = chunk_groups << dev::kGroupShift, chunk_rows = chunk_blocks * dev::kRowsPerBlock;
-        if ((st = take(ctx, ob, (size_t)R * (C + 1) * 4))) return st;
-        const int par = ctx->gs_par;
-        gs = gsum_buffer(ctx, par);
-        for (int64_t r0 = 0, b0 = 0; r0 < R; r0 += chunk_rows, b0 += chunk_blocks) {
-            const int64_t rc = std::min(chunk_rows, R - r0);
-            if ((st = clk.begin())) return st;
-            dev::launch_k2u_count(h->data + r0 * C, rc, C, scol, dir, pv, ctx->deg.as<uint32_t>() + r0,
-                                  ctx->off.as<uint32_t>() + r0, ctx->blk_sum.as<unsigned long long>() + b0,
-                                  gs + 2 + 2 * (b0 >> dev::kGroupShift), reinterpret_cast<int *>(gs), true,
-                                  gsum_buffer(ctx, par ^ 1), r0 == 0 ? 2 + 2 * ctx->gs_used[par ^ 1] : 0, ctx->sms,
-                                  ctx->stream);
-            if ((st = launch_check("k2u count")) || (st = clk.end(false)) || (st = clk.begin())) return st;
-            dev::launch_k2u_expand_func_chunk(h->data, R, C, ctx->deg.as<int32_t>(),
-                                              ctx->blk_sum.as<unsigned long long>(), gs + 2, b0,
-                                              (rc + dev::kRowsPerBlock - 1) / dev::kRowsPerBlock, ob.as<int32_t>(),
-                                              ctx->stream);
-            if ((st = launch_check("k2u expand")) || (st = clk.end(true))) return st;
-        }
-        ctx->gs_par = par ^ 1;
-        ctx->gs_used[par ^ 1] = 0;
-        ctx->gs_used[par] = groups;
-        cudaError_t e = cudaMemcpyAsync(ctx->h_gs, gs, (size_t)(16 + 16 * groups), cudaMemcpyDeviceToHost,
-                                        ctx->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "k2u: group sums readback");
-        if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(e, "op sync");
-        errf = (int)(ctx->h_gs[0] & 0xffffffffull);
-        if (!(errf & 8)) {
-            if (errf & 1)
-                return set_error(WK_EDEVICE,
-                                 "probe found an overflow chain longer than the segment's overflow area (corrupt store)");
-            unsigned long long rows_out = 0ull;
-            for (int64_t g = 0; g < groups; ++g) rows_out += ctx->h_gs[2 + 2 * g];
-            const int64_t R_out = (int64_t)rows_out;
-            if (R_out > ctx->row_limit)
-                return set_error(WK_EOVERFLOW, "k2u: %lld output rows exceed the context's row limit %lld",
-                                 (long long)R_out, (long long)ctx->row_limit);
-            clk.finish();
-            ctx->last.rows_out = R_out;
-            ctx->last.alg_bytes = 4 * R * C + 16 * R + 4 * R_out + 4 * R_out * (C + 1);
-            h->data = ob.as<int32_t>();
-            h->size = R_out * (C + 1);
-            h->col_num = C + 1;
-            h->step++;
-            return WK_OK;
-        }
-        func = false;   // an index list: the whole op reruns unspecialised, into the other sums buffer
-        clk = OpClock(ctx);
-        ctx->last.kind = KIND_K2U;
-        ctx->last.rows_in = R;
-        ctx->last.cols_in = C;
-    }
     for (;;) {
         const int par = ctx->gs_par;
         gs = gsum_buffer(ctx, par);
