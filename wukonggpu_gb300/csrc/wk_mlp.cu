@@ -236,8 +236,8 @@ void refresh_bf16(wk_mlp *m, cudaStream_t s) {
 
 // C = A . B^T (+ bias) on the tensor cores (wk_tc_gemm.cuh), with the
 // epilogue EPI; N is a multiple of 64.  The tile width is the widest that still
-// gives a full wave of CTAs, else 64: these products are small, and more CTAs
-// means more copies and products in flight.
+// gives a full wave of CTAs, else 32: these products are small, and more CTAs
+// means more copies and products in flight and more warps for the epilogue.
 template <int EPI = tc::kEpiStore>
 void gemm(wk_mlp *m, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, float *C, int ldc, int M, int N,
           int K, const float *bias, cudaStream_t s, const tc::EpiArgs &ea = tc::EpiArgs()) {
@@ -254,7 +254,10 @@ void gemm(wk_mlp *m, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, in
         return;
     }
     const int mt = (M + tc::kTM - 1) / tc::kTM;
-    const int bn = (N % 256 == 0 && mt * (N / 256) >= m->sms) ? 256 : (N % 128 == 0 && mt * (N / 128) >= m->sms) ? 128 : 64;
+    const int bn = (N % 256 == 0 && mt * (N / 256) >= m->sms)   ? 256
+                   : (N % 128 == 0 && mt * (N / 128) >= m->sms) ? 128
+                   : (mt * (N / 64) >= m->sms)                  ? 64
+                                                                : 32;
     CUtensorMap ta, tb;
     if (!tc::make_map(&ta, A, (uint64_t)M, (uint64_t)K, (uint64_t)lda, tc::kTM) ||
         !tc::make_map(&tb, B, (uint64_t)N, (uint64_t)K, (uint64_t)ldb, (uint32_t)bn)) {
@@ -263,6 +266,10 @@ void gemm(wk_mlp *m, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, in
     }
     const dim3 grid((unsigned)mt, (unsigned)(N / bn));
     switch (bn) {
+        case 32:
+            tc::gemm_tc_kernel<32, EPI><<<grid, tc::kThreads, tc::smem_bytes(32), s>>>(ta, tb, C, ldc, M, K, bias,
+                                                                                       m->d_err, ea);
+            break;
         case 64:
             tc::gemm_tc_kernel<64, EPI><<<grid, tc::kThreads, tc::smem_bytes(64), s>>>(ta, tb, C, ldc, M, K, bias,
                                                                                        m->d_err, ea);
@@ -304,7 +311,8 @@ bool set_gemm_smem() {
 
 template <int EPI>
 bool set_gemm_smem_all() {
-    return set_gemm_smem<64, EPI>() && set_gemm_smem<128, EPI>() && set_gemm_smem<256, EPI>();
+    return set_gemm_smem<32, EPI>() && set_gemm_smem<64, EPI>() && set_gemm_smem<128, EPI>() &&
+           set_gemm_smem<256, EPI>();
 }
 
 // the status of the work queued since the last check: a host-side failure, a

@@ -2,8 +2,8 @@
 // C[M x N] fp32 = A[M x K] . B[N x K]^T (+ bias[n]), A and B bf16 row-major
 // (K contiguous), FP32 accumulation in tensor memory (TMEM).
 //
-// One CTA of 4 warps computes a 128 x BN tile (BN = 64, 128 or 256: one MMA
-// shape); the grid is M tiles x N / BN.  K is walked in slabs of 64 bf16 -- one
+// One CTA of 4 warps computes a 128 x BN tile (BN = 32, 64, 128 or 256: one
+// MMA shape); the grid is M tiles x N / BN.  K is walked in slabs of 64 bf16 -- one
 // 128-byte row of the 128 B swizzle -- through kStages shared-memory stages:
 //   - thread 0 (the producer) loads each slab's A box (64 x 128) and B box
 //     (64 x BN) with TMA (cp.async.bulk.tensor.2d, 128 B swizzle; rows past M
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(kThreads)
 gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                float *__restrict__ C, int ldc, int M, int K, const float *__restrict__ bias, int *err,
                const EpiArgs ea) {
-    static_assert(BN == 64 || BN == 128 || BN == 256, "tile width: an MMA N and a TMEM allocation");
+    static_assert(BN == 32 || BN == 64 || BN == 128 || BN == 256, "tile width: an MMA N and a TMEM allocation");
     constexpr uint32_t kABytes = kTM * 128, kBBytes = BN * 128, kStage = kABytes + kBBytes;
     static_assert(4 * 32 * kEpiPitch * 4 <= kStage, "the output staging fits in stage 0");
     extern __shared__ unsigned char smem_raw[];
