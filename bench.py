@@ -568,16 +568,24 @@ def run_gb300(args, dist):
     d2h_gbs = d2h_bandwidth(rc, pins[0], maxrows)
     work = [q for _ in range(args.steps) for _, q in queries]
     moved = [[0, 0] for _ in range(nctx)]
+    import threading
+    next_item = iter(range(len(work)))
+    take_lock = threading.Lock()
 
     def worker(k):
-        for i in range(k, len(work), nctx):
+        # each context takes the next query when it is free, so no context sits
+        # on a queue of large results while the others have finished
+        while True:
+            with take_lock:
+                i = next(next_item, None)
+            if i is None:
+                return
             cc = np.asarray(work[i], np.int64)
             moved[k][0] += cc.nbytes
             req, _ = ctxs[k].execute(cc.tolist(), download=False)
             out = ctxs[k].download(req, into=pins[k])
             moved[k][1] += out.nbytes
 
-    import threading
     dist.barrier()
     t0 = time.perf_counter()
     th = [threading.Thread(target=worker, args=(k,)) for k in range(nctx)]

@@ -45,7 +45,9 @@ def test_gradients_match_cpu_oracle(gpu_small, M):
         cos = float(x @ y / (np.linalg.norm(x) * ny + 1e-30))
         rel = float(np.linalg.norm(x - y) / ny)
         print(f"gradient block {name} M={M}: cos {cos:.6f} rel {rel:.5f}")
-        assert cos > 0.999 and rel < 0.05, (name, cos, rel)
+        # the largest relative error seen on a GB300 is 0.00052 (the same BF16
+        # roundings; FP32 sums in a different order): a tenfold margin
+        assert cos > 0.99999 and rel < 0.005, (name, cos, rel)
 
 
 def test_training_fits_a_function(gpu_small):
