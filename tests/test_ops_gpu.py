@@ -105,7 +105,7 @@ def test_k2k_k2c_random_histories(gpu_small, small_graph, small_oracle, R, C):
         assert np.array_equal(got.reshape(exp.shape), exp), const
 
 
-# 2,599,000 rows: 2,539 blocks, enough for two blocks per probe CTA, the last CTA with one
+# 2,599,000 rows: 2,539 blocks in 10 groups, the last block ragged
 @pytest.mark.parametrize("R", [1, 33, 4097, 60_000, 600_000, 2_599_000])
 def test_k2k_k2c_on_a_functional_direction(gpu_small, small_graph, small_oracle, R):
     """rdf:type OUT is dense and functional: its membership test reads the

@@ -624,52 +624,45 @@ __device__ __forceinline__ void probe_view_or_warp(const PredView &pv, int32_t v
 // nothing; a linear scan touches 1 entry or none); a start value of 0 (an
 // index key, hashed) takes the general path.  All rounds' reads are issued
 // before any is used.
-// BPC blocks of input rows per CTA (1 as launched: two blocks per CTA, with
-// eight rounds of loads in flight per lane, took 48 registers and ran slower).
-template <bool NB, int BPC>
+// One CTA per block of input rows (two blocks per CTA, with eight rounds of
+// loads in flight per lane, took 48 registers and ran slower).
+template <bool NB>
 __global__ void __launch_bounds__(kThreads, 6)
 filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, int ecol,
                     int32_t end_const, uint32_t dir, PredView pv,
                     uint32_t *__restrict__ mask, unsigned int *__restrict__ blk_nz,
                     unsigned long long *__restrict__ group_sums, unsigned long long *__restrict__ clear,
                     int64_t nclear, unsigned long long *__restrict__ totals, int *err) {
-    constexpr int NR = kRounds * BPC;   // rounds of 32 rows per warp
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // the other sums buffer, read by the previous op's write or expansion, is
     // cleared for the next op (a few hundred words at most)
     for (int64_t w = (int64_t)blockIdx.x * kThreads + threadIdx.x; w < nclear; w += (int64_t)gridDim.x * kThreads)
         clear[w] = 0ull;
-    const int64_t b0 = (int64_t)blockIdx.x * BPC;
-    const int64_t nblk = (R + kRowsPerBlock - 1) / kRowsPerBlock;
-    // round rd: block b0 + rd / kRounds, the warp's rows 32 (rd % kRounds) + lane
-    auto row_at = [&](int rd) -> int64_t {
-        return (b0 + rd / kRounds) * kRowsPerBlock + (int64_t)warp * (kRounds * 32) + (rd % kRounds) * 32 + lane;
-    };
-    int32_t v[NR], tg[NR];
+    const int64_t b = blockIdx.x;
+    const int64_t wrow0 = b * kRowsPerBlock + (int64_t)warp * (kRounds * 32);
+    int32_t v[kRounds], tg[kRounds];
 #pragma unroll
-    for (int rd = 0; rd < NR; ++rd) {
-        const int64_t r = row_at(rd);
+    for (int rd = 0; rd < kRounds; ++rd) {
+        const int64_t r = wrow0 + rd * 32 + lane;
         v[rd] = r < R ? __ldg(hist + r * C + scol) : -1;
         tg[rd] = (r < R && ecol >= 0) ? __ldg(hist + r * C + ecol) : end_const;
     }
-    unsigned int my_nz[BPC];   // kept rows per block (lane 0)
-#pragma unroll
-    for (int j = 0; j < BPC; ++j) my_nz[j] = 0u;
+    unsigned int my_nz = 0u;   // kept rows (lane 0)
     unsigned long long my_scan = 0;
-    int32_t g[NR];   // NB: the neighbour, or -1 (none, or not looked up here)
+    int32_t g[kRounds];   // NB: the neighbour, or -1 (none, or not looked up here)
     if constexpr (NB) {
         const int32_t *nba = dir ? pv.nb[1] : pv.nb[0];
         const uint32_t vmin = dir ? pv.vmin[1] : pv.vmin[0], dn = dir ? pv.dn[1] : pv.dn[0];
 #pragma unroll
-        for (int rd = 0; rd < NR; ++rd) {
+        for (int rd = 0; rd < kRounds; ++rd) {
             const uint32_t x = (uint32_t)v[rd] - vmin;   // wraps above dn below vmin
             g[rd] = (v[rd] > 0 && x < dn) ? __ldg(nba + x) : -1;
         }
     }
 #pragma unroll
-    for (int rd = 0; rd < NR; ++rd) {
-        const int64_t r = row_at(rd), row0 = r - lane;
-        if (row0 >= R) break;   // warp-uniform; rows grow with rd
+    for (int rd = 0; rd < kRounds; ++rd) {
+        const int64_t row0 = wrow0 + rd * 32, r = row0 + lane;
+        if (row0 >= R) break;   // warp-uniform
         bool found = false;
         if (NB && v[rd] != 0) {
             found = r < R && g[rd] >= 0 && g[rd] == tg[rd];
@@ -686,37 +679,17 @@ filter_probe_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol
         const uint32_t m = __ballot_sync(FULL, found);
         if (lane == 0) {
             mask[row0 >> 5] = m;
-            my_nz[rd / kRounds] += __popc(m);
+            my_nz += __popc(m);
         }
     }
-    __shared__ unsigned int s_nz[BPC][kThreads / 32];
-    __shared__ unsigned long long s_sc[kThreads / 32];
-    my_scan = warp_sum(my_scan);
-    if (lane == 0) {
-#pragma unroll
-        for (int j = 0; j < BPC; ++j) s_nz[j][warp] = my_nz[j];
-        s_sc[warp] = my_scan;
-    }
-    __syncthreads();
-    if (threadIdx.x < BPC) {
-        const int j = threadIdx.x;
-        const int64_t b = b0 + j;
-        unsigned int nz = 0u;
-#pragma unroll
-        for (int w = 0; w < kThreads / 32; ++w) nz += s_nz[j][w];
-        if (b < nblk) {
-            blk_nz[b] = nz;
-            if (nz) {
-                atomicAdd(totals + 1, (unsigned long long)nz);
-                atomicAdd(group_sums + 2 * (b >> kGroupShift), (unsigned long long)nz);
-            }
-        }
-    }
+    block_sum2(my_scan, my_nz);
     if (threadIdx.x == 0) {
-        unsigned long long sc = 0ull;
-#pragma unroll
-        for (int w = 0; w < kThreads / 32; ++w) sc += s_sc[w];
-        if (sc) atomicAdd(totals, sc);
+        blk_nz[b] = my_nz;
+        if (my_scan) atomicAdd(totals, my_scan);
+        if (my_nz) {
+            atomicAdd(totals + 1, (unsigned long long)my_nz);
+            atomicAdd(group_sums + 2 * (b >> kGroupShift), (unsigned long long)my_nz);
+        }
     }
 }
 
@@ -915,15 +888,13 @@ int preload_k2u_kernels() {
 void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ecol, int32_t end_const,
                          uint32_t dir, PredView pv, uint32_t *mask, unsigned int *blk_nz,
                          unsigned long long *group_sums, unsigned long long *clear, int64_t nclear,
-                         unsigned long long *totals, int *err, int sms, cudaStream_t st) {
+                         unsigned long long *totals, int *err, cudaStream_t st) {
     const unsigned int nb = nblocks_rows(R);
-    if (sms < 1) sms = 1;
-#define WK_PROBE(NBV, B) \
-    filter_probe_kernel<NBV, B><<<(nb + B - 1) / B, kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv, \
-                                                                       mask, blk_nz, group_sums, clear, nclear, \
-                                                                       totals, err)
-    if ((dir ? pv.nb[1] : pv.nb[0]) != nullptr) WK_PROBE(true, 1);
-    else WK_PROBE(false, 1);
+#define WK_PROBE(NBV) \
+    filter_probe_kernel<NBV><<<nb, kThreads, 0, st>>>(hist, R, C, scol, ecol, end_const, dir, pv, mask, blk_nz, \
+                                                      group_sums, clear, nclear, totals, err)
+    if ((dir ? pv.nb[1] : pv.nb[0]) != nullptr) WK_PROBE(true);
+    else WK_PROBE(false);
 #undef WK_PROBE
 }
 

@@ -68,7 +68,7 @@ void launch_k2u_expand(const int32_t *hist, int64_t R, int C, const int32_t *edg
 void launch_filter_probe(const int32_t *hist, int64_t R, int C, int scol, int ecol, int32_t end_const,
                          uint32_t dir, PredView pv, uint32_t *mask, unsigned int *blk_nz,
                          unsigned long long *group_sums, unsigned long long *clear, int64_t nclear,
-                         unsigned long long *totals, int *err, int sms, cudaStream_t st);
+                         unsigned long long *totals, int *err, cudaStream_t st);
 
 // k2k/k2c pass 2: copy the kept rows in order (out holds up to R rows of C columns).
 void launch_filter_write(const int32_t *hist, int64_t R, int C, const uint32_t *mask, const unsigned int *blk_nz,

@@ -329,7 +329,7 @@ int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const,
     if ((st = clk.begin())) return st;
     dev::launch_filter_probe(h->data, R, C, scol, ecol, end_const, dir, pv, ctx->mask.as<uint32_t>(),
                              ctx->blk_nz.as<unsigned int>(), gs, gsum_buffer(ctx, par ^ 1),
-                             2 + 2 * ctx->gs_used[par ^ 1], tot, err, ctx->sms, ctx->stream);
+                             2 + 2 * ctx->gs_used[par ^ 1], tot, err, ctx->stream);
     if ((st = launch_check("filter probe"))) return st;
     ctx->gs_par = par ^ 1;
     ctx->gs_used[par ^ 1] = 0;
