@@ -459,7 +459,9 @@ def run_gb300(args, dist):
             rc.timer_begin()
             rc.execute(q, download=False)
             lat.append(rc.timer_end())
-            op_log.extend(rc.query_op_stats())
+            for j, op in enumerate(rc.query_op_stats()):
+                op["pos"] = j   # the op's pattern within its query
+                op_log.append(op)
 
     # ---- headline: whole queries through wk_execute, device time from query-level events
     rc.enable_timing(False)
@@ -516,6 +518,19 @@ def run_gb300(args, dist):
                                                     + 4 * op["rows_out"] * (op["cols_in"] + 2) for op in k2u)
                                                 / (write_ms / 1000.0) / 1e9) if write_ms else None,
                 "expand_share_of_k2u_time": write_ms / k2u_ms if k2u_ms else None}
+
+    # ---- GB/s and latency per op: every op of the per-kernel pass, by its
+    # pattern's position in the query and its kind
+    kind_names = {0: "k2u", 1: "k2k", 2: "k2c", 3: "index", 4: "const"}
+    per_op = []
+    for key in sorted({(op["pos"], op["kind"]) for op in op_log}):
+        ops = [op for op in op_log if (op["pos"], op["kind"]) == key]
+        ms = sum(op["ms"] for op in ops)
+        per_op.append({"pattern": key[0], "kind": kind_names.get(key[1], str(key[1])), "ops": len(ops),
+                       "rows_in_mean": float(np.mean([op["rows_in"] for op in ops])),
+                       "rows_out_mean": float(np.mean([op["rows_out"] for op in ops])),
+                       "ms_mean": ms / len(ops),
+                       "gbs": sum(op["alg_bytes"] for op in ops) / (ms / 1000.0) / 1e9 if ms > 0 else None})
 
     # ---- the filter group: the same shapes closed by known_to_known /
     # known_to_const checks (not part of the headline mix), for the filter
@@ -652,6 +667,7 @@ def run_gb300(args, dist):
                              for sh in sorted({n.split("/")[0] for n, _ in queries})},
             "roofline": roofline,
             "roofline_filter": roofline_filter,
+            "per_op": per_op,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": h2d // args.steps,
                     "d2h_bytes_per_step": d2h // args.steps, "contexts": nctx,
