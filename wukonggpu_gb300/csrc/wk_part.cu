@@ -114,8 +114,9 @@ extern "C" int wk_history_partition(wk_ctx *ctx, const wk_history *in, int64_t s
     int st = ob.reserve((size_t)in->size * 4 + 16);
     if (st) return st;
     cudaStream_t s = ctx->stream;
-    DevBuf kb, kt, ib, it, bb;
-    if ((st = bb.reserve((size_t)(nparts + 1) * 8))) return st;
+    DevBuf &kb = ctx->part_key[0], &kt = ctx->part_key[1], &ib = ctx->part_id[0], &it = ctx->part_id[1];
+    DevBuf &bb = ctx->part_bound;
+    if ((st = bb.reserve((size_t)(kMaxParts + 1) * 8))) return st;
     if (R > 0) {
         if ((st = kb.reserve((size_t)R * 8)) || (st = kt.reserve((size_t)R * 8)) || (st = ib.reserve((size_t)R * 4)) ||
             (st = it.reserve((size_t)R * 4)))
