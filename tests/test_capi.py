@@ -49,6 +49,30 @@ def test_null_arguments_are_rejected(lib_built):
     assert b"null" in lib.wk_last_error()
 
 
+def test_new_entry_points_reject_bad_arguments(lib_built):
+    """The fork-join, batch and server entry points report bad arguments as
+    statuses, whatever the device (no call here reaches the GPU)."""
+    lib = W.load_library()
+    h = W.wk_history()
+    lib.wk_history_init(C.byref(h))
+    counts = np.zeros(4, np.int64)
+    p64 = counts.ctypes.data_as(C.POINTER(C.c_int64))
+    assert lib.wk_history_partition(None, C.byref(h), -1, 2, p64, C.byref(h)) == W.WK_EINVAL
+    assert lib.wk_history_to_device(None, C.byref(h), None, 0) == W.WK_EINVAL
+    assert lib.wk_history_from_device(None, C.byref(h), None, 0, 1) == W.WK_EINVAL
+    assert lib.wk_batch_set_fused(None, 1) == W.WK_EINVAL
+    assert lib.wk_batch_get_fused(None) == 0
+    assert lib.wk_batch_layouts(None, 1, None, None, None) == W.WK_EINVAL
+    assert lib.wk_server_cancel(None, 0) == W.WK_EINVAL
+    assert lib.wk_server_inject_alloc_failure(None, 0, 1) == W.WK_EINVAL
+    assert lib.wk_ctx_inject_alloc_failure(None, 1) == W.WK_EINVAL
+    # a host-only context refuses device work with WK_EDEVICE
+    rc = W.RCache(device=-1)
+    assert lib.wk_history_partition(rc._h, C.byref(h), -1, 2, p64, C.byref(h)) == W.WK_EDEVICE
+    assert lib.wk_history_to_device(rc._h, C.byref(h), None, 0) == W.WK_EDEVICE
+    rc.close()
+
+
 def test_no_device_is_an_error_not_a_fallback(lib_built):
     if W.device_count() > 0:
         pytest.skip("a CUDA device is present")
