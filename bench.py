@@ -66,8 +66,9 @@ def parse():
     ap.add_argument("--serving-scale", type=float, default=1.0,
                     help="entity scale of the serving section's own graph (1.0 = 20M entities, 1e9 triples); "
                          "0 serves on the single-query graph")
-    ap.add_argument("--heavy-workers", type=int, default=2,
-                    help="contexts running heavy requests in the serving loop")
+    ap.add_argument("--heavy-workers", type=int, default=3,
+                    help="contexts running heavy requests in the serving loop (2, 3, 4 and 6 measured; 3 serves "
+                         "the most at the baseline's p99)")
     ap.add_argument("--one-query", type=int, default=-1,
                     help="run query N of the mix once, op by op, print each op's stats and exit "
                          "(a fixed launch sequence for ncu captures)")
