@@ -326,24 +326,6 @@ __device__ __forceinline__ int row_of(const uint32_t *pos, int n, uint32_t j) {
     return lo;
 }
 
-// last entry k in [k0, n) with pos[k] <= j, given pos[k0] <= j: a galloping
-// search from k0 (1 read when j is still in k0's list, about 2 log2(d) reads
-// when it is d entries on)
-__device__ __forceinline__ int row_from(const uint32_t *pos, int n, int k0, uint32_t j) {
-    int lo = k0, step = 1;
-    while (lo + step < n && pos[lo + step] <= j) {
-        lo += step;
-        step <<= 1;
-    }
-    int hi = (lo + step < n ? lo + step : n) - 1;   // pos[hi + 1] > j, or hi = n - 1
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (pos[mid] <= j) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 // The block's input rows whose list is not empty, compacted in order:
 // entry k is block row row[k], its first output row pos[k] (block-local), its
 // list offset minus pos[k] in erel[k] (modulo 2^32: erel + j is the entry
@@ -362,16 +344,13 @@ struct ExpandRows {
 // (span = lead + the block's count, below 2^31 + 4).  Block row j copies the
 // input row of the entry k whose list covers j and appends entry j - pos[k]
 // of that list.  A whole group is W 16 B stores (4 rows of W words); the
-// first and last group of a block may be partial.  `hint` is an entry at or
-// before the group's first row's (the lane's previous group's), or -1; the
-// return value is the entry of the group's last row, the next group's hint.
+// first and last group of a block may be partial.
 template <int W>
-__device__ __forceinline__ int k2u_write_group(uint32_t u, uint32_t lead, uint32_t span, const ExpandRows &er_,
-                                               const int32_t *__restrict__ rows, const int32_t *__restrict__ edges,
-                                               int32_t *__restrict__ obase, int hint) {
+__device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint32_t span, const ExpandRows &er_,
+                                                const int32_t *__restrict__ rows, const int32_t *__restrict__ edges,
+                                                int32_t *__restrict__ obase) {
     constexpr int C = W - 1;
-    const uint32_t j0 = u >= lead ? u - lead : 0u;
-    int k = hint >= 0 ? row_from(er_.pos, er_.n, hint, j0) : row_of(er_.pos, er_.n, j0);
+    int k = row_of(er_.pos, er_.n, u >= lead ? u - lead : 0u);
     uint32_t nxt = er_.pos[k + 1];
     int32_t v[4 * W];
     int kp = -1;       // entry of the previous output row of the group, if valid
@@ -415,7 +394,6 @@ __device__ __forceinline__ int k2u_write_group(uint32_t u, uint32_t lead, uint32
             }
         }
     }
-    return k;
 }
 
 // One CTA per slice: CTA k writes local rows [k' kSliceRows, (k' + 1)
@@ -506,17 +484,8 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
         const uint32_t u0 = slice * (uint32_t)kSliceRows;
         const uint32_t u1 = u0 >= span ? u0 : (span - u0 < (uint32_t)kSliceRows ? span : u0 + (uint32_t)kSliceRows);
         int32_t *obase = out + (P - lead) * W;
-        // warp w takes a contiguous run of the slice's 128-row chunks, so a
-        // lane's next group is 128 rows on and its entry is found by a short
-        // galloping search from the lane's last one
-        constexpr uint32_t kChunk = 128u, kWarps = kThreads / 32;
-        const uint32_t nchunks = (u1 - u0 + kChunk - 1) / kChunk, per = (nchunks + kWarps - 1) / kWarps;
-        const uint32_t c0 = (uint32_t)wid * per, c1 = c0 + per < nchunks ? c0 + per : nchunks;
-        int hint = -1;
-        for (uint32_t c = c0; c < c1; ++c) {
-            const uint32_t u = u0 + c * kChunk + 4u * (uint32_t)lane;
-            if (u < u1) hint = k2u_write_group<W>(u, lead, span, xr, hblk, edges, obase, hint);
-        }
+        for (uint32_t u = u0 + 4u * (uint32_t)t; u < u1; u += 4u * kThreads)
+            k2u_write_group<W>(u, lead, span, xr, hblk, edges, obase);
     } else {
         const int Wd = C + 1;
         int32_t *oblk = out + P * Wd;
