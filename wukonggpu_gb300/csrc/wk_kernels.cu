@@ -352,40 +352,6 @@ __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint3
     constexpr int C = W - 1;
     int k = row_of(er_.pos, er_.n, u >= lead ? u - lead : 0u);
     uint32_t nxt = er_.pos[k + 1];
-    int32_t *g = obase + (size_t)u * W;
-    if (u >= lead && u + 4u <= span && u - lead + 4u <= nxt) {
-        // the whole group comes from one input row (a long list): the row is
-        // read once and its 4 list entries with one 16 B load, or two 8 B
-        // loads, where their address allows
-        const uint32_t j = u - lead;
-        const int32_t *src = rows + (int)er_.row[k] * C;
-        int32_t r[C > 0 ? C : 1];
-#pragma unroll
-        for (int c = 0; c < C; ++c) r[c] = __ldg(src + c);
-        const int32_t *ep = edges + (er_.erel[k] + j);
-        int32_t e[4];
-        if ((reinterpret_cast<uintptr_t>(ep) & 15u) == 0) {
-            const int4 x = __ldg(reinterpret_cast<const int4 *>(ep));
-            e[0] = x.x; e[1] = x.y; e[2] = x.z; e[3] = x.w;
-        } else if ((reinterpret_cast<uintptr_t>(ep) & 7u) == 0) {
-            const int2 x = __ldg(reinterpret_cast<const int2 *>(ep)), y = __ldg(reinterpret_cast<const int2 *>(ep) + 1);
-            e[0] = x.x; e[1] = x.y; e[2] = y.x; e[3] = y.y;
-        } else {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) e[q] = __ldg(ep + q);
-        }
-        int32_t v[4 * W];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-#pragma unroll
-            for (int c = 0; c < C; ++c) v[q * W + c] = r[c];
-            v[q * W + C] = e[q];
-        }
-#pragma unroll
-        for (int k2 = 0; k2 < W; ++k2)
-            reinterpret_cast<int4 *>(g)[k2] = make_int4(v[4 * k2], v[4 * k2 + 1], v[4 * k2 + 2], v[4 * k2 + 3]);
-        return;
-    }
     int32_t v[4 * W];
     int kp = -1;       // entry of the previous output row of the group, if valid
     uint32_t er = 0;   // erel[kp]
@@ -413,6 +379,7 @@ __device__ __forceinline__ void k2u_write_group(uint32_t u, uint32_t lead, uint3
             kp = -1;
         }
     }
+    int32_t *g = obase + (size_t)u * W;
     if (u >= lead && u + 4u <= span) {
 #pragma unroll
         for (int k2 = 0; k2 < W; ++k2)
