@@ -56,9 +56,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="entity-count scale of the graph (1.0 = 2M)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--sections", default="paged,batched,estimator,serving",
-                    help="extra sections after the headline: paged, batched, estimator, serving (comma list, or "
-                         "none)")
+    ap.add_argument("--sections", default="paged,batched,estimator,serving,partition",
+                    help="extra sections after the headline: paged, batched, estimator, serving, partition (comma "
+                         "list, or none)")
     ap.add_argument("--est-queries", type=int, default=200000,
                     help="random BGPs executed to train and test the estimator section's model")
     ap.add_argument("--serving-est-queries", type=int, default=4000,
@@ -626,6 +626,8 @@ def run_gb300(args, dist):
         est = None
         if "paged" in wanted:
             sections["paged"] = section_paged(g, queries, int(info["device_bytes"]), value, dist.local)
+        if "partition" in wanted:
+            sections["partition"] = section_partition(rc, peaks()[0])
         if "batched" in wanted:
             sections["batched"] = section_batched(rc, g)
             batch_sample = sections["batched"].pop("_sample")
@@ -724,6 +726,43 @@ def section_paged(g, queries, store_bytes: int, resident_qps: float, device: int
                 "vs_resident": (len(lat) / (sum(lat) / 1000.0)) / resident_qps if resident_qps else None})
             rc.close()
     return out
+
+
+def section_partition(rc, peak: float, rows: int = 1 << 24, cols: int = 4, nparts: int = 8, reps: int = 5):
+    """The fork-join split of a history table by owner (wk_history_partition,
+    the device side of RCache::generate_sub_query, core/rcache.hpp:964-1030):
+    a seeded table of `rows` x `cols` vertex ids resident in HBM, split by the
+    owner of column 0 (value % nparts).  Algorithmic bytes per split: the
+    table read and written once (8 R C).  GB/s is those bytes over the op's
+    device time (CUDA events on the library's stream, the bounds readback
+    included).  The first split is checked against a numpy stable split of
+    the same table: every row, in order."""
+    import wukonggpu_gb300 as W
+    rng = np.random.default_rng(17)
+    table = (W.VID_BASE + rng.integers(0, 2_000_000, size=(rows, cols))).astype(np.int32)
+    req = W.Request([])
+    rc.upload_history(req, table)
+    rc.sync()
+    rc.timer_begin()
+    counts = rc.partition(req, -1, nparts)
+    first_ms = rc.timer_end()
+    got = rc.download(req)
+    owner = table[:, 0].astype(np.uint32) % np.uint32(nparts)
+    order = np.argsort(owner, kind="stable")
+    exact = bool(np.array_equal(counts, np.bincount(owner, minlength=nparts)) and np.array_equal(got, table[order]))
+    del got, order
+    ms = []
+    for _ in range(reps):
+        rc.timer_begin()
+        rc.partition(req, -1, nparts)   # the table as split last time: the same work
+        ms.append(rc.timer_end())
+    alg = 8.0 * rows * cols
+    best = min(ms)
+    return {"config": f"{rows} rows x {cols} columns of vertex ids, split over {nparts} owners by column 0",
+            "rows": rows, "parts": nparts, "ms_first": first_ms, "ms": statistics.median(ms), "ms_best": best,
+            "alg_bytes": alg, "gbs": alg / (statistics.median(ms) / 1000.0) / 1e9,
+            "frac": alg / (statistics.median(ms) / 1000.0) / 1e9 / peak,
+            "rows_equal_numpy_stable_split": exact}
 
 
 def section_batched(rc, g, nq: int = 4096, reps: int = 5):

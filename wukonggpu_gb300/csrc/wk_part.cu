@@ -15,18 +15,25 @@
 // split is stable (a part keeps the rows in their input order), which gives
 // every part the same multiset of rows and a fixed order besides.
 //
-// Steps on the op stream: a key (owner << 32 | row) per row; one stable
-// radix pass on the owner byte (wk_sort.cu); a gather of the rows in key
-// order into the ping-pong partner of the input buffer; the parts' bounds by
-// a binary search per part over the sorted keys, read back once.
+// Steps on the op stream, a stable counting split in two passes over the
+// table:
+//   1. part_count: per tile of 2048 rows, the rows of each owner (warp
+//      match-any, one shared-memory add per owner and chunk of 32 rows);
+//   2. one exclusive scan of those counts laid out owner by owner, tile by
+//      tile: the global start of every (owner, tile) slot, so a part keeps
+//      its tiles, and the rows within a tile, in input order;
+//   3. part_scatter: each tile again, in order; a row's place in its part is
+//      its tile slot's start, plus the rows of that owner in the tile's
+//      earlier warps and earlier chunks, plus its rank among the lanes of its
+//      chunk with the same owner;
+//   4. the parts' bounds from the scanned slots, read back once.
 #include "wk_runtime.h"
 
 #include <algorithm>
 #include <vector>
 
 namespace wk {
-int sort_pairs_device(uint64_t *key, uint32_t *id, uint64_t *key_tmp, uint32_t *id_tmp, int64_t n,
-                      const std::vector<int> &key_shifts, int id_bits, cudaStream_t st, int64_t *launches);
+int scan_u32_device(uint32_t *x, int64_t m, DevBuf &scratch, cudaStream_t st, int64_t *launches);
 }
 
 using namespace wk;
@@ -34,60 +41,97 @@ using namespace wk;
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kMaxParts = 256;   // the owner is one radix digit
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxParts = 256;
+constexpr int kTile = 2048;                 // rows per CTA
+constexpr int kChunks = kTile / kThreads;   // chunks of 32 rows per warp
+#define FULL 0xffffffffu
 
-__global__ void owner_keys_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int col, uint32_t nparts,
-                                  uint64_t *__restrict__ key, uint32_t *__restrict__ id) {
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < R; r += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t owner = (uint32_t)__ldg(hist + r * C + col) % nparts;
-        key[r] = ((uint64_t)owner << 32) | (uint64_t)r;
-        id[r] = 0u;
-    }
+// the owner of row r, or ~0 past the table
+__device__ __forceinline__ uint32_t owner_of(const int32_t *__restrict__ hist, int64_t r, int64_t R, int C, int col,
+                                             uint32_t nparts) {
+    return r < R ? (uint32_t)__ldg(hist + r * C + col) % nparts : FULL;
 }
 
-// out row i = in row (low 32 bits of key[i])
-template <int C>
-__global__ void gather_rows_fixed_kernel(const int32_t *__restrict__ in, const uint64_t *__restrict__ key, int64_t R,
-                                         int32_t *__restrict__ out) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < R; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t src = (int64_t)(uint32_t)key[i];
+// row of chunk c of warp w in tile t
+__device__ __forceinline__ int64_t tile_row(int64_t t, int w, int c, int lane) {
+    return t * kTile + (int64_t)w * (kChunks * 32) + c * 32 + lane;
+}
+
+// cnt[p * ntiles + t] = rows of owner p in tile t
+__global__ void __launch_bounds__(kThreads)
+part_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int col, uint32_t nparts, int64_t ntiles,
+                  uint32_t *__restrict__ cnt) {
+    __shared__ uint32_t h[kMaxParts];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t p = threadIdx.x; p < nparts; p += kThreads) h[p] = 0u;
+    __syncthreads();
+    const int64_t t = blockIdx.x;
+#pragma unroll 4
+    for (int c = 0; c < kChunks; ++c) {
+        const uint32_t o = owner_of(hist, tile_row(t, w, c, lane), R, C, col, nparts);
+        const unsigned m = __match_any_sync(FULL, o);
+        if (o != FULL && lane == __ffs(m) - 1) atomicAdd(&h[o], (uint32_t)__popc(m));
+    }
+    __syncthreads();
+    for (uint32_t p = threadIdx.x; p < nparts; p += kThreads) cnt[(int64_t)p * ntiles + t] = h[p];
+}
+
+// rows of tile t to their places: start[p * ntiles + t] is where owner p's
+// rows of the tile begin (the scanned counts)
+__global__ void __launch_bounds__(kThreads)
+part_scatter_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int col, uint32_t nparts, int64_t ntiles,
+                    const uint32_t *__restrict__ start, int32_t *__restrict__ out) {
+    __shared__ uint32_t wc[kWarps][kMaxParts];   // per warp: its rows per owner, then its next place per owner
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t t = blockIdx.x;
+    for (uint32_t p = threadIdx.x; p < nparts; p += kThreads)
 #pragma unroll
-        for (int c = 0; c < C; ++c) out[i * C + c] = __ldg(in + src * C + c);
+        for (int x = 0; x < kWarps; ++x) wc[x][p] = 0u;
+    __syncthreads();
+    uint32_t own[kChunks];
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) {
+        const uint32_t o = owner_of(hist, tile_row(t, w, c, lane), R, C, col, nparts);
+        own[c] = o;
+        const unsigned m = __match_any_sync(FULL, o);
+        if (o != FULL && lane == __ffs(m) - 1) wc[w][o] += (uint32_t)__popc(m);   // this warp's row of wc only
+        __syncwarp();
     }
-}
-
-__global__ void gather_rows_kernel(const int32_t *__restrict__ in, const uint64_t *__restrict__ key, int64_t R, int C,
-                                   int32_t *__restrict__ out) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < R; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t src = (int64_t)(uint32_t)key[i];
-        for (int c = 0; c < C; ++c) out[i * C + c] = __ldg(in + src * C + c);
-    }
-}
-
-// bound[p] = the first sorted row whose owner is >= p, for p in [0, nparts]
-__global__ void part_bounds_kernel(const uint64_t *__restrict__ key, int64_t R, int nparts, int64_t *__restrict__ bound) {
-    for (int p = threadIdx.x; p <= nparts; p += blockDim.x) {
-        int64_t lo = 0, hi = R;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if ((int)(key[mid] >> 32) < p) lo = mid + 1;
-            else hi = mid;
+    __syncthreads();
+    // per owner: the tile's start, then the warps in order
+    for (uint32_t p = threadIdx.x; p < nparts; p += kThreads) {
+        uint32_t acc = start[(int64_t)p * ntiles + t];
+#pragma unroll
+        for (int x = 0; x < kWarps; ++x) {
+            const uint32_t n = wc[x][p];
+            wc[x][p] = acc;
+            acc += n;
         }
-        bound[p] = lo;
+    }
+    __syncthreads();
+    const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) {
+        const uint32_t o = own[c];
+        const unsigned m = __match_any_sync(FULL, o);
+        if (o != FULL) {
+            const uint32_t pos = wc[w][o] + (uint32_t)__popc(m & below);
+            const int32_t *src = hist + tile_row(t, w, c, lane) * C;
+            int32_t *dst = out + (int64_t)pos * C;
+            for (int k = 0; k < C; ++k) dst[k] = __ldg(src + k);
+        }
+        __syncwarp();
+        if (o != FULL && lane == __ffs(m) - 1) wc[w][o] += (uint32_t)__popc(m);
+        __syncwarp();
     }
 }
 
-int launch_gather(const int32_t *in, const uint64_t *key, int64_t R, int C, int32_t *out, unsigned int g,
-                  cudaStream_t st) {
-    switch (C) {
-    case 1: gather_rows_fixed_kernel<1><<<g, kThreads, 0, st>>>(in, key, R, out); break;
-    case 2: gather_rows_fixed_kernel<2><<<g, kThreads, 0, st>>>(in, key, R, out); break;
-    case 3: gather_rows_fixed_kernel<3><<<g, kThreads, 0, st>>>(in, key, R, out); break;
-    case 4: gather_rows_fixed_kernel<4><<<g, kThreads, 0, st>>>(in, key, R, out); break;
-    default: gather_rows_kernel<<<g, kThreads, 0, st>>>(in, key, R, C, out); break;
-    }
-    cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? WK_OK : cuda_fail(e, "partition gather");
+// bound[p] = the first row of part p, bound[nparts] = R
+__global__ void part_bounds_kernel(const uint32_t *__restrict__ start, int64_t ntiles, int64_t R, uint32_t nparts,
+                                   int64_t *__restrict__ bound) {
+    for (uint32_t p = threadIdx.x; p <= nparts; p += blockDim.x)
+        bound[p] = p < nparts ? (int64_t)start[(int64_t)p * ntiles] : R;
 }
 
 }  // namespace
@@ -114,29 +158,23 @@ extern "C" int wk_history_partition(wk_ctx *ctx, const wk_history *in, int64_t s
     int st = ob.reserve((size_t)in->size * 4 + 16);
     if (st) return st;
     cudaStream_t s = ctx->stream;
-    DevBuf &kb = ctx->part_key[0], &kt = ctx->part_key[1], &ib = ctx->part_id[0], &it = ctx->part_id[1];
-    DevBuf &bb = ctx->part_bound;
+    DevBuf &cb = ctx->part_cnt, &sb = ctx->part_scan, &bb = ctx->part_bound;
     if ((st = bb.reserve((size_t)(kMaxParts + 1) * 8))) return st;
-    if (R > 0) {
-        if ((st = kb.reserve((size_t)R * 8)) || (st = kt.reserve((size_t)R * 8)) || (st = ib.reserve((size_t)R * 4)) ||
-            (st = it.reserve((size_t)R * 4)))
-            return st;
-        const unsigned int g = (unsigned int)std::min<int64_t>((R + kThreads - 1) / kThreads, (int64_t)ctx->sms * 8);
-        owner_keys_kernel<<<g, kThreads, 0, s>>>(src, R, C, (int)(-start - 1), (uint32_t)nparts, kb.as<uint64_t>(),
-                                                  ib.as<uint32_t>());
-        ++ctx->launches;
-        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "partition keys");
-        if (nparts > 1 &&
-            (st = sort_pairs_device(kb.as<uint64_t>(), ib.as<uint32_t>(), kt.as<uint64_t>(), it.as<uint32_t>(), R,
-                                    std::vector<int>{32}, 0, s, &ctx->launches)))
-            return st;
-        if ((st = launch_gather(src, kb.as<uint64_t>(), R, C, ob.as<int32_t>(), g, s))) return st;
-        part_bounds_kernel<<<1, kThreads, 0, s>>>(kb.as<uint64_t>(), R, nparts, bb.as<int64_t>());
-        ctx->launches += 2;
-        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "partition bounds");
-    }
     std::vector<int64_t> bound((size_t)nparts + 1, 0);
     if (R > 0) {
+        const int64_t ntiles = (R + kTile - 1) / kTile, m = ntiles * nparts;
+        if ((st = cb.reserve((size_t)m * 4))) return st;
+        const int col = (int)(-start - 1);
+        part_count_kernel<<<(unsigned)ntiles, kThreads, 0, s>>>(src, R, C, col, (uint32_t)nparts, ntiles,
+                                                                cb.as<uint32_t>());
+        ++ctx->launches;
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "partition count");
+        if ((st = scan_u32_device(cb.as<uint32_t>(), m, sb, s, &ctx->launches))) return st;
+        part_scatter_kernel<<<(unsigned)ntiles, kThreads, 0, s>>>(src, R, C, col, (uint32_t)nparts, ntiles,
+                                                                  cb.as<uint32_t>(), ob.as<int32_t>());
+        part_bounds_kernel<<<1, kThreads, 0, s>>>(cb.as<uint32_t>(), ntiles, R, (uint32_t)nparts, bb.as<int64_t>());
+        ctx->launches += 2;
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "partition scatter");
         if ((e = cudaMemcpyAsync(bound.data(), bb.ptr, bound.size() * 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
             return cuda_fail(e, "partition bounds readback");
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "partition sync");

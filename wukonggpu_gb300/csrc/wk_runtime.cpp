@@ -285,8 +285,8 @@ wk_ctx::~wk_ctx() {
     for (auto &b : hbuf) b.release();
     deg.release(); off.release(); mask.release(); blk_sum.release(); blk_nz.release();
     dscal.release();
-    for (auto &b : part_key) b.release();
-    for (auto &b : part_id) b.release();
+    part_cnt.release();
+    part_scan.release();
     part_bound.release();
     if (h_scal) cudaFreeHost(h_scal);
     if (h_gs) cudaFreeHost(h_gs);

@@ -92,9 +92,9 @@ struct wk_ctx {
     unsigned long long *h_gs = nullptr;   // pinned copy of one buffer
     size_t h_gs_bytes = 0;
     wk::DevBuf dscal;                // [0] error flags, [8..32) totals
-    // wk_history_partition: sort keys and ids with their ping-pong partners,
-    // and the parts' bounds (grown on demand, kept for the next call)
-    wk::DevBuf part_key[2], part_id[2], part_bound;
+    // wk_history_partition: rows per (owner, tile) and their scan's block
+    // sums, and the parts' bounds (grown on demand, kept for the next call)
+    wk::DevBuf part_cnt, part_scan, part_bound;
     unsigned long long *h_scal = nullptr;   // pinned mirror of the totals
 
     // timing
