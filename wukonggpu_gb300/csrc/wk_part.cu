@@ -67,9 +67,12 @@ part_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int col, u
     for (uint32_t p = threadIdx.x; p < nparts; p += kThreads) h[p] = 0u;
     __syncthreads();
     const int64_t t = blockIdx.x;
-#pragma unroll 4
+    uint32_t own[kChunks];   // every load in flight before the first match
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) own[c] = owner_of(hist, tile_row(t, w, c, lane), R, C, col, nparts);
+#pragma unroll
     for (int c = 0; c < kChunks; ++c) {
-        const uint32_t o = owner_of(hist, tile_row(t, w, c, lane), R, C, col, nparts);
+        const uint32_t o = own[c];
         const unsigned m = __match_any_sync(FULL, o);
         if (o != FULL && lane == __ffs(m) - 1) atomicAdd(&h[o], (uint32_t)__popc(m));
     }
@@ -77,8 +80,24 @@ part_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int col, u
     for (uint32_t p = threadIdx.x; p < nparts; p += kThreads) cnt[(int64_t)p * ntiles + t] = h[p];
 }
 
+// one row of C ints (CT = C for 1, 2 and 4 columns: one vector load and
+// store; CT = 0 for any C)
+template <int CT>
+__device__ __forceinline__ void copy_row(const int32_t *__restrict__ src, int32_t *__restrict__ dst, int C) {
+    if constexpr (CT == 4) {
+        *reinterpret_cast<int4 *>(dst) = __ldg(reinterpret_cast<const int4 *>(src));
+    } else if constexpr (CT == 2) {
+        *reinterpret_cast<int2 *>(dst) = __ldg(reinterpret_cast<const int2 *>(src));
+    } else if constexpr (CT == 1) {
+        *dst = __ldg(src);
+    } else {
+        for (int k = 0; k < C; ++k) dst[k] = __ldg(src + k);
+    }
+}
+
 // rows of tile t to their places: start[p * ntiles + t] is where owner p's
 // rows of the tile begin (the scanned counts)
+template <int CT>
 __global__ void __launch_bounds__(kThreads)
 part_scatter_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int col, uint32_t nparts, int64_t ntiles,
                     const uint32_t *__restrict__ start, int32_t *__restrict__ out) {
@@ -89,11 +108,12 @@ part_scatter_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int col,
 #pragma unroll
         for (int x = 0; x < kWarps; ++x) wc[x][p] = 0u;
     __syncthreads();
-    uint32_t own[kChunks];
+    uint32_t own[kChunks];   // every load in flight before the first match
+#pragma unroll
+    for (int c = 0; c < kChunks; ++c) own[c] = owner_of(hist, tile_row(t, w, c, lane), R, C, col, nparts);
 #pragma unroll
     for (int c = 0; c < kChunks; ++c) {
-        const uint32_t o = owner_of(hist, tile_row(t, w, c, lane), R, C, col, nparts);
-        own[c] = o;
+        const uint32_t o = own[c];
         const unsigned m = __match_any_sync(FULL, o);
         if (o != FULL && lane == __ffs(m) - 1) wc[w][o] += (uint32_t)__popc(m);   // this warp's row of wc only
         __syncwarp();
@@ -117,9 +137,7 @@ part_scatter_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int col,
         const unsigned m = __match_any_sync(FULL, o);
         if (o != FULL) {
             const uint32_t pos = wc[w][o] + (uint32_t)__popc(m & below);
-            const int32_t *src = hist + tile_row(t, w, c, lane) * C;
-            int32_t *dst = out + (int64_t)pos * C;
-            for (int k = 0; k < C; ++k) dst[k] = __ldg(src + k);
+            copy_row<CT>(hist + tile_row(t, w, c, lane) * C, out + (int64_t)pos * C, C);
         }
         __syncwarp();
         if (o != FULL && lane == __ffs(m) - 1) wc[w][o] += (uint32_t)__popc(m);
@@ -170,8 +188,17 @@ extern "C" int wk_history_partition(wk_ctx *ctx, const wk_history *in, int64_t s
         ++ctx->launches;
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "partition count");
         if ((st = scan_u32_device(cb.as<uint32_t>(), m, sb, s, &ctx->launches))) return st;
-        part_scatter_kernel<<<(unsigned)ntiles, kThreads, 0, s>>>(src, R, C, col, (uint32_t)nparts, ntiles,
-                                                                  cb.as<uint32_t>(), ob.as<int32_t>());
+        // vector copies need 4 B x C aligned rows in both tables (the history
+        // buffers are 256 B aligned; a caller's table may not be)
+        const bool al = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(ob.ptr)) & 15u) == 0;
+#define WK_SCATTER(CT)                                                                                               \
+    part_scatter_kernel<CT><<<(unsigned)ntiles, kThreads, 0, s>>>(src, R, C, col, (uint32_t)nparts, ntiles, \
+                                                                      cb.as<uint32_t>(), ob.as<int32_t>())
+        if (al && C == 4) WK_SCATTER(4);
+        else if (al && C == 2) WK_SCATTER(2);
+        else if (C == 1) WK_SCATTER(1);
+        else WK_SCATTER(0);
+#undef WK_SCATTER
         part_bounds_kernel<<<1, kThreads, 0, s>>>(cb.as<uint32_t>(), ntiles, R, (uint32_t)nparts, bb.as<int64_t>());
         ctx->launches += 2;
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "partition scatter");
