@@ -782,10 +782,12 @@ def section_batched(rc, g, nq: int = 4096, reps: int = 5):
     queries = [q for q, r in zip(cand, sizes) if 1 <= r <= 10_000][:nq]
     best_ms = b.autotune(queries, reps=3)
     tune = b.tuning()
+    form_ms = b.autotune_forms()
     pinned = W.PinnedBuffer(1 << 26)
     rc.sync()
     # each timed batch packs its queries, runs the graph and reads every result back
     lat = []
+    k0 = b.kernel_launches()
     t0 = time.perf_counter()
     for _ in range(reps):
         a = time.perf_counter()
@@ -793,6 +795,7 @@ def section_batched(rc, g, nq: int = 4096, reps: int = 5):
         res = b.download(k, into=pinned)
         lat.append(time.perf_counter() - a)
     batched_s = time.perf_counter() - t0
+    launches_per_batch = (b.kernel_launches() - k0) / reps
     rows = [t.shape[0] for t in res]
     # the same queries one at a time, driven from C++: the request loop in
     # query-at-a-time mode with every request present at the start (its
@@ -815,11 +818,14 @@ def section_batched(rc, g, nq: int = 4096, reps: int = 5):
                       "final rows 1..1e4 (heavy-tailed)",
             "queries": len(queries), "rows_p50": float(np.median(rows)), "rows_max": int(max(rows)),
             "batched_qps": len(queries) * reps / batched_s, "batch_ms": float(np.median(lat) * 1e3),
-            "device_graph_ms": best_ms, "tuning": {"blocks_per_sm": tune[0], "rows_per_warp": tune[1], "split": tune[2]},
+            "device_graph_ms": best_ms,
+            "device_graph_ms_by_form": {"three_kernels_per_step": form_ms[0], "one_kernel_per_step": form_ms[1]},
+            "tuning": {"blocks_per_sm": tune[0], "rows_per_warp": tune[1], "split": tune[2],
+                       "one_kernel_per_step": b.fused()},
             "query_at_a_time_qps": len(queries) / single_s, "query_at_a_time": "wk_server mode 0 (C++), all present",
             "timed": "batched: pack + graph replay + download of every result per batch",
             "speedup": (len(queries) * reps / batched_s) / (len(queries) / single_s),
-            "same_as_alone_sample": bool(exact), "gpu_launches_per_batch": 1 + 3 * 4}
+            "same_as_alone_sample": bool(exact), "gpu_launches_per_batch": launches_per_batch}
 
 
 def _bindings_equal(oq, pa, ta, pb, tb):

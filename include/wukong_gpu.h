@@ -291,6 +291,10 @@ int wk_batch_get_fused(wk_batch *b);
 int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
                       int32_t reps, double *best_ms);
 int64_t wk_batch_kernel_launches(wk_batch *b);
+/* The last wk_batch_autotune's best time (ms) of each step form: three
+ * kernels per step, and one cooperative kernel per step; -1 where none of
+ * that form ran (the device refused it, or no autotune yet). */
+int wk_batch_autotune_forms(wk_batch *b, double *three_kernel_ms, double *one_kernel_ms);
 
 /* ------------------------------------------- learned cardinality estimator
  * An MLP (48 features + 32-d predicate embedding -> 3 x 256 GELU -> 1) that

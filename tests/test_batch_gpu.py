@@ -83,6 +83,10 @@ def test_tuning_and_autotune_keep_results(gpu_small, small_oracle, light):
         _check(b.download(nq), light[:300], small_oracle)
     ms = b.autotune(light, reps=2)
     assert ms > 0 and b.tuning()[0] in (2, 4, 8)
+    three, one = b.autotune_forms()        # each step form's best; the kept one is the faster
+    assert three is not None and one is not None
+    assert min(three, one) == pytest.approx(ms)
+    assert b.fused() == (one < three)
     nq = b.run(light)
     _check(b.download(nq), light, small_oracle)
 

@@ -149,6 +149,7 @@ _SIGS = {
     "wk_batch_get_tuning": (C.c_int, [_P, _I32P, _I32P, _I32P]),
     "wk_batch_set_fused": (C.c_int, [_P, C.c_int32]),
     "wk_batch_layouts": (C.c_int, [_P, C.c_int32, _I64P, _I32P, _I64P]),
+    "wk_batch_autotune_forms": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "wk_batch_get_fused": (C.c_int, [_P]),
     "wk_batch_autotune": (C.c_int, [_P, _I64P, _I32P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "wk_batch_kernel_launches": (C.c_int64, [_P]),
@@ -634,6 +635,13 @@ class Batch:
 
     def kernel_launches(self) -> int:
         return load_library().wk_batch_kernel_launches(self._h)
+
+    def autotune_forms(self):
+        """The last autotune's best ms for three kernels per step and for one
+        kernel per step (None where that form did not run)."""
+        a, b = C.c_double(), C.c_double()
+        _check(load_library().wk_batch_autotune_forms(self._h, C.byref(a), C.byref(b)))
+        return (a.value if a.value >= 0 else None), (b.value if b.value >= 0 else None)
 
     def close(self):
         if getattr(self, "_h", None):

@@ -456,6 +456,7 @@ struct wk_batch {
     cudaGraphExec_t gexec = nullptr;   // the last one launched
     int32_t last_q = 0;
     int final_buf = 0;
+    double form_best_ms[2] = {-1.0, -1.0};   // the last autotune's best per step form (-1: none ran)
     int64_t kernels = 0;
 };
 
@@ -844,6 +845,7 @@ extern "C" int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const i
         return set_error(WK_EDEVICE, "wk_batch_autotune: events");
     double best = 1e30;
     BatchTune keep = b->tune;
+    b->form_best_ms[0] = b->form_best_ms[1] = -1.0;
     for (int fu = 0; fu < 2; ++fu)
     for (int bl : kBlocks)
         for (int rw : kRows)
@@ -866,6 +868,7 @@ extern "C" int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const i
                     tbest = std::min(tbest, (double)ms);
                 }
                 if (tbest < best) { best = tbest; keep = b->tune; }
+                if (b->form_best_ms[fu] < 0.0 || tbest < b->form_best_ms[fu]) b->form_best_ms[fu] = tbest;
             }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -875,3 +878,10 @@ extern "C" int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const i
 }
 
 extern "C" int64_t wk_batch_kernel_launches(wk_batch *b) { return b ? b->kernels : 0; }
+
+extern "C" int wk_batch_autotune_forms(wk_batch *b, double *three_kernel_ms, double *one_kernel_ms) {
+    if (!b || !three_kernel_ms || !one_kernel_ms) return set_error(WK_EINVAL, "wk_batch_autotune_forms: null");
+    *three_kernel_ms = b->form_best_ms[0];
+    *one_kernel_ms = b->form_best_ms[1];
+    return WK_OK;
+}
