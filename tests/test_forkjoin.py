@@ -156,3 +156,49 @@ def test_gpu_executor_one_rank(small_graph, small_oracle, gpu_small):
             assert list(per_step) == list(erows), name
     finally:
         dist.destroy_process_group()
+
+
+def _gpu_rank_main(rank, world, port, queries, q):
+    """A rank with the GPU executor on the one GPU; tables cross ranks as host
+    tensors over gloo, so no rank's kernels wait on another's."""
+    import torch
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        g = W.Graph(W.spec_small())
+        rc = W.RCache(device=0)
+        rc.build_store_graph(g)
+        fj = D.ForkJoin(D.GpuExecutor(rc, torch, host_tables=True), dist)
+        out = []
+        for name, cmd in queries:
+            res, per_step = fj.execute(cmd)
+            out.append((name, oracle.rows_digest(res) if rank == 0 else None, per_step))
+        rc.close()
+        q.put((rank, out))
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_gpu_executors_on_two_ranks(small_graph, small_oracle):
+    """Two ranks, each with its own context and store replica on the GPU, run
+    the split, the exchange (gloo, host tensors) and the steps of every query;
+    the gathered rows equal the single-process result."""
+    g, s, p, o = small_graph
+    queries = workloads.small_queries(s, p, o)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_gpu_rank_main, args=(r, 2, port, queries, q)) for r in range(2)]
+    for pr in procs:
+        pr.start()
+    got = dict(q.get(timeout=600) for _ in range(2))
+    for pr in procs:
+        pr.join(timeout=60)
+        assert pr.exitcode == 0
+    for i, (name, cmd) in enumerate(queries):
+        exp, erows = small_oracle.execute(cmd)
+        assert got[0][i][1] == oracle.rows_digest(exp), name
+        for k in range(1, len(erows)):
+            assert got[0][i][2][k] + got[1][i][2][k] == erows[k], (name, k)

@@ -19,7 +19,10 @@ of a part keep their order, but the parts arrive in rank order, so a
 result equals the single-process one as a multiset of rows.
 
 An executor holds one rank's tables as flat int32 tensors with a column
-count; ``GpuExecutor`` runs the GPU ops of an ``RCache`` on CUDA tensors.
+count; ``GpuExecutor`` runs the GPU ops of an ``RCache`` on CUDA tensors, or,
+with ``host_tables=True``, keeps the tables in host memory between ops (for a
+group whose backend exchanges host tensors, such as gloo): each op uploads
+its table, runs on the device and brings the result back.
 """
 from __future__ import annotations
 
@@ -39,11 +42,12 @@ def _kind(pattern, cols: int) -> str:
 
 
 class GpuExecutor:
-    """One rank's ops on its GPU context; tables are CUDA int32 tensors."""
+    """One rank's ops on its GPU context; tables are CUDA int32 tensors, or
+    host int32 tensors with ``host_tables=True``."""
 
-    def __init__(self, rc, torch):
-        self.rc, self.torch = rc, torch
-        self.device = torch.device("cuda", torch.cuda.current_device())
+    def __init__(self, rc, torch, host_tables: bool = False):
+        self.rc, self.torch, self.host = rc, torch, host_tables
+        self.device = torch.device("cpu") if host_tables else torch.device("cuda", torch.cuda.current_device())
 
     def empty(self, n: int):
         return self.torch.empty(int(n), dtype=self.torch.int32, device=self.device)
@@ -52,12 +56,17 @@ class GpuExecutor:
         return self.torch.as_tensor(np.asarray(counts, np.int64), device=self.device)
 
     def _req(self, table, cols: int) -> Request:
-        self.torch.cuda.current_stream().synchronize()   # the collective's writes are on torch's stream
         req = Request([])
+        if self.host:
+            self.rc.upload_history(req, table.numpy().reshape(-1, cols))
+            return req
+        self.torch.cuda.current_stream().synchronize()   # the collective's writes are on torch's stream
         self.rc.from_device(req, table.data_ptr(), table.numel(), cols)
         return req
 
     def _table(self, req: Request):
+        if self.host:
+            return self.torch.from_numpy(np.ascontiguousarray(self.rc.download(req)).reshape(-1))
         t = self.empty(req.hist.size)
         self.torch.cuda.current_stream().synchronize()
         self.rc.to_device(req, t.data_ptr(), t.numel())
