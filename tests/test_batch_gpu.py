@@ -43,6 +43,15 @@ def test_batch_matches_oracle_graph_and_plain(gpu_small, small_oracle, light, fu
         _check(b.download(nq), light[:300], small_oracle)
 
 
+def test_fused_batch_of_one_query(gpu_small, small_oracle, light):
+    """The one-kernel step with the smallest grid: one query, one block."""
+    b = W.Batch(gpu_small, max_queries=1, max_steps=4, capacity_ints=1 << 22)
+    b.set_fused(True)
+    for i in (0, 7, 100):
+        b.run([light[i]])
+        _check(b.download(1), [light[i]], small_oracle)
+
+
 def test_fused_batch_capacity_overflow_is_reported(gpu_small, light):
     """The scan inside the one-kernel step finds the overflow; every block
     leaves after the barrier and later steps do nothing."""

@@ -113,7 +113,7 @@ def test_forkjoin_equals_single_process(world, small_graph, small_oracle):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("R,C,nparts", [(0, 2, 2), (1, 1, 3), (1000, 3, 2), (70001, 4, 7), (5000, 2, 256),
-                                         (300_001, 1, 8), (123_457, 9, 31)])
+                                         (300_001, 1, 8), (123_457, 9, 31), (1000, 2, 1)])
 def test_device_partition_is_a_stable_split(gpu_small, R, C, nparts):
     rng = np.random.default_rng(R + C + nparts)
     table = rng.integers(0, 1 << 30, size=(R, C), dtype=np.int64).astype(np.int32)
