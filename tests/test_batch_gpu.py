@@ -44,7 +44,8 @@ def test_batch_matches_oracle_graph_and_plain(gpu_small, small_oracle, light, fu
 
 
 def test_fused_batch_of_one_query(gpu_small, small_oracle, light):
-    """The one-kernel step with the smallest grid: one query, one block."""
+    """The one-kernel step on the smallest batch: one query, whose rows fill a
+    fraction of one tile while every block of the grid meets at the barriers."""
     b = W.Batch(gpu_small, max_queries=1, max_steps=4, capacity_ints=1 << 22)
     b.set_fused(True)
     for i in (0, 7, 100):
