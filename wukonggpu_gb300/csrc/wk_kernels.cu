@@ -124,8 +124,7 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
             for (int rd = 0; rd < NR; ++rd) {
                 const int64_t r = row_at(rd);
                 if (r < R) {
-                    // deg is null when the expansion repeats the lookup itself
-                    if (deg) reinterpret_cast<int32_t *>(deg)[r] = g[rd];
+                    reinterpret_cast<int32_t *>(deg)[r] = g[rd];
                     my_sum[rd / kRounds] += g[rd] >= 0 ? 1ull : 0ull;
                 }
             }
@@ -516,7 +515,7 @@ __global__ void __launch_bounds__(kThreads)
 k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_t *__restrict__ nbr,
                        const unsigned long long *__restrict__ blk_sum,
                        const unsigned long long *__restrict__ group_sums, int64_t ngroups, int64_t nblk,
-                       const __grid_constant__ GroupTable gt, const NbLookup lk, int32_t *__restrict__ out) {
+                       const __grid_constant__ GroupTable gt, int32_t *__restrict__ out) {
     constexpr int C = W - 1;
     constexpr int kPitch = W | 1;
     __shared__ int32_t rows[kRowsPerBlock * kPitch];
@@ -537,14 +536,7 @@ k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_
 #pragma unroll
     for (int ps = 0; ps < 4; ++ps) {
         const int r = wid * 128 + ps * 32 + lane;
-        if (lk.nba != nullptr) {
-            // a dense functional direction: the count kernel's lookup, repeated
-            const int32_t v = r < n ? __ldg(hist + (r0 + r) * C + lk.scol) : -1;
-            const uint32_t xv = (uint32_t)v - lk.vmin;   // wraps above dn below vmin
-            x[ps] = (v > 0 && xv < lk.dn) ? __ldg(lk.nba + xv) : -1;
-        } else {
-            x[ps] = r < n ? __ldg(nbr + r0 + r) : -1;
-        }
+        x[ps] = r < n ? __ldg(nbr + r0 + r) : -1;
         bm[ps] = __ballot_sync(FULL, x[ps] >= 0);
         wtot += __popc(bm[ps]);
     }
@@ -823,7 +815,7 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t 
 #undef WK_COUNT
 }
 
-void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr, const NbLookup &lk,
+void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
                             const unsigned long long *blk_sum, const unsigned long long *group_sums,
                             const GroupTable &gt, unsigned long long slices, int32_t *out, cudaStream_t st) {
     if (slices == 0ull) return;
@@ -831,7 +823,7 @@ void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t
     const int64_t ng = (nblk + (1 << kGroupShift) - 1) >> kGroupShift;
     const unsigned int g = (unsigned int)slices;
 #define WK_EXPAND_F(WC) \
-    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, group_sums, ng, nblk, gt, lk, out)
+    k2u_expand_func_kernel<WC><<<g, kThreads, 0, st>>>(hist, R, nbr, blk_sum, group_sums, ng, nblk, gt, out)
     switch (C + 1) {
         case 2: WK_EXPAND_F(2); break;
         case 3: WK_EXPAND_F(3); break;

@@ -48,16 +48,7 @@ int preload_k2u_kernels();
 // k2u pass 2 of a functional direction (2 <= C + 1 <= 8): the matched rows
 // with their neighbour appended, compacted in order; one CTA per non-empty
 // block (slices = the op's total from the group sums).
-// The neighbour lookup of a dense functional direction, for an expansion that
-// repeats it instead of reading each row's neighbour from the count kernel
-// (nba null: read nbr).
-struct NbLookup {
-    const int32_t *nba = nullptr;   // neighbour per id of [vmin, vmin + dn), or -1
-    uint32_t vmin = 0, dn = 0;
-    int scol = 0;                   // the start column
-};
-
-void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr, const NbLookup &lk,
+void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
                             const unsigned long long *blk_sum, const unsigned long long *group_sums,
                             const GroupTable &gt, unsigned long long slices, int32_t *out, cudaStream_t st);
 // k2u pass 2: one CTA per slice (slices = the op's total from the group sums)

@@ -193,10 +193,6 @@ int clear_totals(wk_ctx *ctx) {
     return e == cudaSuccess ? WK_OK : cuda_fail(e, "clear totals");
 }
 
-// A dense functional direction's expansion repeats the neighbour lookup
-// rather than reading the count kernel's per-row neighbour.
-constexpr bool kFuncLookupInExpand = true;
-
 // two-pass k2u (count -> host adds up the group sums -> expand)
 int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     const int C = h->col_num;
@@ -231,11 +227,7 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         const int par = ctx->gs_par;
         gs = gsum_buffer(ctx, par);
         if ((st = clk.begin())) return st;
-        // a dense functional direction's expansion repeats the count's neighbour
-        // lookup (one read of an array that stays in L2) instead of reading
-        // each row's neighbour back: the count writes none
-        const bool lookup = kFuncLookupInExpand && func && (dir ? pv.nb[1] : pv.nb[0]) != nullptr;
-        dev::launch_k2u_count(h->data, R, C, scol, dir, pv, lookup ? nullptr : ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
+        dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
                               ctx->blk_sum.as<unsigned long long>(), gs + 2, reinterpret_cast<int *>(gs), func,
                               gsum_buffer(ctx, par ^ 1), 2 + 2 * ctx->gs_used[par ^ 1], ctx->sms, ctx->stream);
         if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;
@@ -282,18 +274,9 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
     } else {
         if ((st = take(ctx, ob, (size_t)R_out * (C + 1) * 4))) return st;
         if ((st = clk.begin())) return st;
-        if (func) {
-            dev::NbLookup lk;
-            if (kFuncLookupInExpand && (dir ? pv.nb[1] : pv.nb[0]) != nullptr) {
-                lk.nba = dir ? pv.nb[1] : pv.nb[0];
-                lk.vmin = dir ? pv.vmin[1] : pv.vmin[0];
-                lk.dn = dir ? pv.dn[1] : pv.dn[0];
-                lk.scol = scol;
-            }
-            dev::launch_k2u_expand_func(h->data, R, C, ctx->deg.as<int32_t>(), lk,
-                                        ctx->blk_sum.as<unsigned long long>(), gs + 2, gt, slices, ob.as<int32_t>(),
-                                        ctx->stream);
-        }
+        if (func)
+            dev::launch_k2u_expand_func(h->data, R, C, ctx->deg.as<int32_t>(), ctx->blk_sum.as<unsigned long long>(),
+                                        gs + 2, gt, slices, ob.as<int32_t>(), ctx->stream);
         else
             dev::launch_k2u_expand(h->data, R, C, pv.edges, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
                                    ctx->blk_sum.as<unsigned long long>(), gs + 2, gt, slices, ob.as<int32_t>(),
