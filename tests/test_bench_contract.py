@@ -45,3 +45,8 @@ def test_gpu_arm_line(lib_built):
     assert e["value"] > 0 and e["h2d_bytes_per_step"] > 0 and e["d2h_bytes_per_step"] > 0
     assert {"sm_mhz", "sm_max_mhz", "reasons"} <= set(line["clocks"])
     assert line["per_op"] and all(op["ms_mean"] > 0 for op in line["per_op"])
+    # the reference arm names the same workload, config for config
+    ref = _run(["--impl", "reference", "--scale", "0.05", "--steps", "1", "--warmup", "3"], 900)
+    assert ref["config"] == line["config"]
+    assert (ref["metric"], ref["unit"], ref["higher_is_better"]) == (line["metric"], line["unit"],
+                                                                      line["higher_is_better"])
