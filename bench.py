@@ -821,7 +821,7 @@ def section_batched(rc, g, nq: int = 4096, reps: int = 5):
             "device_graph_ms": best_ms,
             "device_graph_ms_by_form": {"three_kernels_per_step": form_ms[0], "one_kernel_per_step": form_ms[1]},
             "tuning": {"blocks_per_sm": tune[0], "rows_per_warp": tune[1], "split": tune[2],
-                       "one_kernel_per_step": b.fused()},
+                       "one_kernel_per_step": b.fused(), "block_threads": b.block_threads()},
             "query_at_a_time_qps": len(queries) / single_s, "query_at_a_time": "wk_server mode 0 (C++), all present",
             "timed": "batched: pack + graph replay + download of every result per batch",
             "speedup": (len(queries) * reps / batched_s) / (len(queries) / single_s),

@@ -287,7 +287,11 @@ int wk_batch_get_tuning(wk_batch *b, int32_t *blocks_per_sm, int32_t *rows_per_w
  * wk_batch_get_fused returns the current form. */
 int wk_batch_set_fused(wk_batch *b, int32_t fused);
 int wk_batch_get_fused(wk_batch *b);
-/* Autotuner: time every candidate step form and launch shape on these queries and keep the fastest. */
+/* Threads per block of the step kernels: 128 or 256 (a tile is that many
+ * warps' rows).  wk_batch_get_block_threads returns the current value. */
+int wk_batch_set_block_threads(wk_batch *b, int32_t threads);
+int wk_batch_get_block_threads(wk_batch *b);
+/* Autotuner: time every candidate step form, block size and launch shape on these queries and keep the fastest. */
 int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
                       int32_t reps, double *best_ms);
 int64_t wk_batch_kernel_launches(wk_batch *b);

@@ -25,13 +25,16 @@ def _check(tables, queries, orc):
         assert got.shape == exp.shape and np.array_equal(got, exp), q
 
 
+@pytest.mark.parametrize("threads", [256, 128])
 @pytest.mark.parametrize("fused", [False, True])
-def test_batch_matches_oracle_graph_and_plain(gpu_small, small_oracle, light, fused):
-    """Both step forms: three kernels per step, or one cooperative kernel
-    whose blocks meet at grid barriers."""
+def test_batch_matches_oracle_graph_and_plain(gpu_small, small_oracle, light, fused, threads):
+    """Both step forms (three kernels per step, or one cooperative kernel
+    whose blocks meet at grid barriers) at both block sizes."""
     b = W.Batch(gpu_small, max_queries=1024, max_steps=4, capacity_ints=1 << 24)
     b.set_fused(fused)
     assert b.fused() == fused
+    b.set_block_threads(threads)
+    assert b.block_threads() == threads
     for use_graph in (False, True):
         k0 = b.kernel_launches()
         nq = b.run(light, use_graph=use_graph)
@@ -43,11 +46,13 @@ def test_batch_matches_oracle_graph_and_plain(gpu_small, small_oracle, light, fu
         _check(b.download(nq), light[:300], small_oracle)
 
 
-def test_fused_batch_of_one_query(gpu_small, small_oracle, light):
+@pytest.mark.parametrize("threads", [256, 128])
+def test_fused_batch_of_one_query(gpu_small, small_oracle, light, threads):
     """The one-kernel step on the smallest batch: one query, whose rows fill a
     fraction of one tile while every block of the grid meets at the barriers."""
     b = W.Batch(gpu_small, max_queries=1, max_steps=4, capacity_ints=1 << 22)
     b.set_fused(True)
+    b.set_block_threads(threads)
     for i in (0, 7, 100):
         b.run([light[i]])
         _check(b.download(1), [light[i]], small_oracle)
@@ -97,12 +102,14 @@ def test_tuning_and_autotune_keep_results(gpu_small, small_oracle, light):
     assert three is not None and one is not None
     assert min(three, one) == pytest.approx(ms)
     assert b.fused() == (one < three)
+    assert b.block_threads() in (128, 256)
     nq = b.run(light)
     _check(b.download(nq), light, small_oracle)
 
 
 def test_capacity_overflow_is_reported(gpu_small, light):
     b = W.Batch(gpu_small, max_queries=1024, max_steps=4, capacity_ints=4096)
+    b.set_block_threads(128)               # the tile sums are sized for the smaller tiles
     with pytest.raises(W.WkError) as e:
         b.run(light)
     assert e.value.status == W.WK_EOVERFLOW

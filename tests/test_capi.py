@@ -62,6 +62,8 @@ def test_new_entry_points_reject_bad_arguments(lib_built):
     assert lib.wk_history_from_device(None, C.byref(h), None, 0, 1) == W.WK_EINVAL
     assert lib.wk_batch_set_fused(None, 1) == W.WK_EINVAL
     assert lib.wk_batch_get_fused(None) == 0
+    assert lib.wk_batch_set_block_threads(None, 128) == W.WK_EINVAL
+    assert lib.wk_batch_get_block_threads(None) == 0
     assert lib.wk_batch_layouts(None, 1, None, None, None) == W.WK_EINVAL
     assert lib.wk_server_cancel(None, 0) == W.WK_EINVAL
     assert lib.wk_server_inject_alloc_failure(None, 0, 1) == W.WK_EINVAL

@@ -151,6 +151,8 @@ _SIGS = {
     "wk_batch_layouts": (C.c_int, [_P, C.c_int32, _I64P, _I32P, _I64P]),
     "wk_batch_autotune_forms": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "wk_batch_get_fused": (C.c_int, [_P]),
+    "wk_batch_set_block_threads": (C.c_int, [_P, C.c_int32]),
+    "wk_batch_get_block_threads": (C.c_int, [_P]),
     "wk_batch_autotune": (C.c_int, [_P, _I64P, _I32P, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "wk_batch_kernel_launches": (C.c_int64, [_P]),
     "wk_server_config_default": (None, [C.POINTER(wk_server_config)]),
@@ -625,6 +627,13 @@ class Batch:
 
     def fused(self) -> bool:
         return load_library().wk_batch_get_fused(self._h) == 1
+
+    def set_block_threads(self, threads: int):
+        """Threads per block of the step kernels: 128 or 256."""
+        _check(load_library().wk_batch_set_block_threads(self._h, threads))
+
+    def block_threads(self) -> int:
+        return load_library().wk_batch_get_block_threads(self._h)
 
     def autotune(self, queries, reps: int = 3) -> float:
         cmd, npat = self.pack(queries)

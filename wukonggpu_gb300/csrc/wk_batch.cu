@@ -54,12 +54,13 @@ struct BatchTune {
     int rounds;          // rows per warp per tile = 32 * rounds
     int split;           // output ints above which a row is written by a whole warp
     int fused;           // 1: one cooperative kernel per step; 0: count, scan and write kernels
+    int bt;              // threads per block of the step kernels: 128 or 256
 };
 
 constexpr int kErrBarrier = 1 << 4;         // flags[0]: a grid-barrier wait ran out
 constexpr long kBarrierIters = 1l << 24;    // polls of a grid-barrier wait (about 1 s with the back-off)
 
-constexpr int kBT = 256;                    // threads per block
+constexpr int kBTMin = 128;                 // the smaller of the two block sizes (128, 256 threads)
 constexpr int kMaxQ = 4096;                 // queries per batch (shared-memory row offsets)
 
 __device__ __forceinline__ int find_query(const int64_t *s_off, int Q, int64_t g) {
@@ -99,13 +100,15 @@ struct StepIO {
     int Q;
 };
 
-// count: per (query, row) output counts, per-tile and per-query sums
+// count: per (query, row) output counts, per-tile and per-query sums (BT
+// threads a block, a tile of BT x rounds rows)
+template <int BT>
 __device__ __forceinline__ void count_phase(const StepIO &io, int rounds, const int64_t *s_off) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tile_rows = (kBT / 32) * 32 * rounds;
+    const int tile_rows = (BT / 32) * 32 * rounds;
     const int64_t total = s_off[io.Q];
     const int64_t ntiles = (total + tile_rows - 1) / tile_rows;
-    __shared__ unsigned long long s_sum[kBT / 32];
+    __shared__ unsigned long long s_sum[BT / 32];
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         unsigned long long my = 0ull;
         for (int rd = 0; rd < rounds; ++rd) {
@@ -157,29 +160,31 @@ __device__ __forceinline__ void count_phase(const StepIO &io, int rounds, const 
         __syncthreads();
         if (threadIdx.x == 0) {
             unsigned long long t = 0ull;
-            for (int w = 0; w < kBT / 32; ++w) t += s_sum[w];
+            for (int w = 0; w < BT / 32; ++w) t += s_sum[w];
             io.tile_sum[tile] = t;
         }
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(kBT)
+template <int BT>
+__global__ void __launch_bounds__(BT)
 batch_count_kernel(StepIO io, int rounds) {
     extern __shared__ int64_t s_off[];   // Q + 1
     if (io.flags[1]) return;
     for (int i = threadIdx.x; i <= io.Q; i += blockDim.x) s_off[i] = io.in_row_off[i];
     __syncthreads();
-    count_phase(io, rounds, s_off);
+    count_phase<BT>(io, rounds, s_off);
 }
 
 // One block (any multiple of 32 threads up to 1024): tile prefix sums,
-// per-query output layout, capacity check.
+// per-query output layout, capacity check.  BT: the count's block size.
+template <int BT>
 __device__ __forceinline__ void scan_phase(const StepIO &io, int rounds) {
     __shared__ unsigned long long ws[32], wi[32];
     const int nt = blockDim.x, nw = nt >> 5;
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    const int tile_rows = (kBT / 32) * 32 * rounds;
+    const int tile_rows = (BT / 32) * 32 * rounds;
     const int64_t total = io.in_row_off[io.Q];
     const int64_t n = (total + tile_rows - 1) / tile_rows;
     // (1) exclusive scan of the tile sums, in place
@@ -248,20 +253,22 @@ __device__ __forceinline__ void scan_phase(const StepIO &io, int rounds) {
     }
 }
 
+template <int BT>
 __global__ void __launch_bounds__(1024)
 batch_scan_kernel(StepIO io, int rounds) {
     if (io.flags[1]) return;
-    scan_phase(io, rounds);
+    scan_phase<BT>(io, rounds);
 }
 
 // Per tile: block scan of the counts, then write.  Rows with more than
 // `split` output ints are queued and written by whole warps.
+template <int BT>
 __device__ __forceinline__ void write_phase(const StepIO &io, int rounds, int split, const int64_t *s_off) {
-    __shared__ unsigned long long s_w[kBT / 32];
+    __shared__ unsigned long long s_w[BT / 32];
     __shared__ int s_nq;
-    __shared__ int s_big[kBT * 8];       // queued rows (local index), rounds <= 8
+    __shared__ int s_big[BT * 8];        // queued rows (local index), rounds <= 8
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tile_rows = kBT * rounds;
+    const int tile_rows = BT * rounds;
     const int64_t total = s_off[io.Q];
     const int64_t ntiles = (total + tile_rows - 1) / tile_rows;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -308,7 +315,7 @@ __device__ __forceinline__ void write_phase(const StepIO &io, int rounds, int sp
         __syncthreads();
         // queued rows: one warp per row, lanes stride over the row's output ints
         const int nq = s_nq;
-        for (int i = warp; i < nq; i += kBT / 32) {
+        for (int i = warp; i < nq; i += BT / 32) {
             const int lr = s_big[i];
             const int64_t g = tile * tile_rows + lr;
             // output position of row g: tile base + counts of the rows before it in the tile
@@ -339,13 +346,14 @@ __device__ __forceinline__ void write_phase(const StepIO &io, int rounds, int sp
     }
 }
 
-__global__ void __launch_bounds__(kBT)
+template <int BT>
+__global__ void __launch_bounds__(BT)
 batch_write_kernel(StepIO io, int rounds, int split) {
     extern __shared__ int64_t s_off[];   // Q+1 input row offsets
     if (io.flags[1]) return;
     for (int i = threadIdx.x; i <= io.Q; i += blockDim.x) s_off[i] = io.in_row_off[i];
     __syncthreads();
-    write_phase(io, rounds, split, s_off);
+    write_phase<BT>(io, rounds, split, s_off);
 }
 
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
@@ -396,18 +404,19 @@ __device__ __forceinline__ bool grid_barrier(unsigned int *bar, int *flags) {
 // One step in one cooperative launch: count, barrier, scan (block 0),
 // barrier, write.  Launched with at most as many blocks as fit on the device
 // at once (the cooperative launch refuses more).
-__global__ void __launch_bounds__(kBT)
+template <int BT>
+__global__ void __launch_bounds__(BT)
 batch_step_kernel(StepIO io, int rounds, int split, unsigned int *bar) {
     extern __shared__ int64_t s_off[];   // Q + 1 input row offsets
     if (io.flags[1]) return;             // set before the launch: the same in every block
     for (int i = threadIdx.x; i <= io.Q; i += blockDim.x) s_off[i] = io.in_row_off[i];
     __syncthreads();
-    count_phase(io, rounds, s_off);
+    count_phase<BT>(io, rounds, s_off);
     if (!grid_barrier(bar, io.flags)) return;
-    if (blockIdx.x == 0) scan_phase(io, rounds);
+    if (blockIdx.x == 0) scan_phase<BT>(io, rounds);
     if (!grid_barrier(bar, io.flags)) return;
     if (*(volatile int *)(io.flags + 1)) return;   // this step's scan found the batch over capacity
-    write_phase(io, rounds, split, s_off);
+    write_phase<BT>(io, rounds, split, s_off);
 }
 
 // step-0 layout: every query has one virtual row and no columns
@@ -433,7 +442,7 @@ struct wk_batch {
     int32_t max_q = 0, max_steps = 0;
     int64_t cap_ints = 0, cap_rows = 0;
     int sms = 0;
-    BatchTune tune{4, 4, 64, 0};
+    BatchTune tune{4, 4, 64, 0, 256};
     // device
     PredView *d_pvs = nullptr;
     StepDesc *d_desc = nullptr;             // [max_steps][max_q]
@@ -452,7 +461,7 @@ struct wk_batch {
     // executable graphs by batch size (a serving loop's batch sizes vary from
     // batch to batch; each size is captured once), all for graph_tune
     std::unordered_map<int, cudaGraphExec_t> graphs;
-    BatchTune graph_tune{0, 0, 0, 0};
+    BatchTune graph_tune{0, 0, 0, 0, 0};
     cudaGraphExec_t gexec = nullptr;   // the last one launched
     int32_t last_q = 0;
     int final_buf = 0;
@@ -473,8 +482,10 @@ cudaError_t create_priority_stream(cudaStream_t *st) {
     return cudaStreamCreateWithPriority(st, cudaStreamNonBlocking, greatest);
 }
 
+// tiles of the smallest shape (kBTMin threads x rounds rows): the tile-sum
+// buffer holds any tuning's
 int64_t max_tiles(const wk_batch *b, int rounds) {
-    const int64_t tr = (int64_t)kBT * rounds;
+    const int64_t tr = (int64_t)kBTMin * rounds;
     return (b->cap_rows + tr - 1) / tr + 1;
 }
 
@@ -519,6 +530,46 @@ StepIO make_io(wk_batch *b, int s, int Q) {
     return io;
 }
 
+// the max_steps steps of a batch with BT-thread blocks: three kernels per
+// step, or one cooperative kernel
+template <int BT>
+int enqueue_steps(wk_batch *b, int Q, const BatchTune &t, unsigned grid, size_t sm_off, cudaStream_t st) {
+    if (t.fused) {
+        // every block of a cooperative launch must be resident at once
+        int occ = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_step_kernel<BT>, BT, sm_off);
+        if (e != cudaSuccess) return cuda_fail(e, "batch step occupancy");
+        if (occ < 1) return set_error(WK_EDEVICE, "batch step kernel: no block fits on an SM");
+        const unsigned gf = (unsigned)std::min<int64_t>(grid, (int64_t)occ * b->sms);
+        // the barrier words start at zero in every batch (a wait that ran out leaves them unbalanced)
+        if ((e = cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned int), st)) != cudaSuccess)
+            return cuda_fail(e, "batch barrier reset");
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(gf);
+        cfg.blockDim = dim3(BT);
+        cfg.dynamicSmemBytes = sm_off;
+        cfg.stream = st;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        for (int s = 0; s < b->max_steps; ++s) {
+            StepIO io = make_io(b, s, Q);
+            if ((e = cudaLaunchKernelEx(&cfg, batch_step_kernel<BT>, io, t.rounds, t.split, b->d_bar)) != cudaSuccess)
+                return cuda_fail(e, "batch step launch");
+        }
+    } else {
+        for (int s = 0; s < b->max_steps; ++s) {
+            StepIO io = make_io(b, s, Q);
+            batch_count_kernel<BT><<<grid, BT, sm_off, st>>>(io, t.rounds);
+            batch_scan_kernel<BT><<<1, 1024, 0, st>>>(io, t.rounds);
+            batch_write_kernel<BT><<<grid, BT, sm_off, st>>>(io, t.rounds, t.split);
+        }
+    }
+    return WK_OK;
+}
+
 // kernels of one batch: the layout init, then per step three kernels or one
 int64_t batch_kernels(const wk_batch *b, const BatchTune &t) {
     return 1 + (t.fused ? 1 : 3) * (int64_t)b->max_steps;
@@ -543,39 +594,8 @@ int enqueue(wk_batch *b, int Q, const BatchTune &t, cudaStream_t st) {
     const int64_t full = (int64_t)b->sms * t.blocks_per_sm;
     const unsigned grid = (unsigned)std::min<int64_t>(full, std::max<int64_t>(b->sms / 4, 2 * (int64_t)Q));
     const size_t sm_off = sizeof(int64_t) * (size_t)(Q + 1);
-    if (t.fused) {
-        // every block of a cooperative launch must be resident at once
-        int occ = 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_step_kernel, kBT, sm_off);
-        if (e != cudaSuccess) return cuda_fail(e, "batch step occupancy");
-        if (occ < 1) return set_error(WK_EDEVICE, "batch step kernel: no block fits on an SM");
-        const unsigned gf = (unsigned)std::min<int64_t>(grid, (int64_t)occ * b->sms);
-        // the barrier words start at zero in every batch (a wait that ran out leaves them unbalanced)
-        if ((e = cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned int), st)) != cudaSuccess)
-            return cuda_fail(e, "batch barrier reset");
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeCooperative;
-        attr[0].val.cooperative = 1;
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(gf);
-        cfg.blockDim = dim3(kBT);
-        cfg.dynamicSmemBytes = sm_off;
-        cfg.stream = st;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        for (int s = 0; s < b->max_steps; ++s) {
-            StepIO io = make_io(b, s, Q);
-            if ((e = cudaLaunchKernelEx(&cfg, batch_step_kernel, io, t.rounds, t.split, b->d_bar)) != cudaSuccess)
-                return cuda_fail(e, "batch step launch");
-        }
-    } else {
-        for (int s = 0; s < b->max_steps; ++s) {
-            StepIO io = make_io(b, s, Q);
-            batch_count_kernel<<<grid, kBT, sm_off, st>>>(io, t.rounds);
-            batch_scan_kernel<<<1, 1024, 0, st>>>(io, t.rounds);
-            batch_write_kernel<<<grid, kBT, sm_off, st>>>(io, t.rounds, t.split);
-        }
-    }
+    const int st2 = t.bt == 128 ? enqueue_steps<128>(b, Q, t, grid, sm_off, st) : enqueue_steps<256>(b, Q, t, grid, sm_off, st);
+    if (st2) return st2;
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "batch launch");
     b->kernels += batch_kernels(b, t);
@@ -643,7 +663,7 @@ extern "C" int wk_batch_set_tuning(wk_batch *b, int32_t blocks_per_sm, int32_t r
     if (!b || blocks_per_sm < 1 || blocks_per_sm > 16 || rows_per_warp < 32 || rows_per_warp > 256 ||
         rows_per_warp % 32 || split_ints < 1)
         return set_error(WK_EINVAL, "wk_batch_set_tuning: blocks/SM 1..16, rows/warp 32..256 (x32), split >= 1");
-    b->tune = BatchTune{blocks_per_sm, rows_per_warp / 32, split_ints, b->tune.fused};
+    b->tune = BatchTune{blocks_per_sm, rows_per_warp / 32, split_ints, b->tune.fused, b->tune.bt};
     return WK_OK;
 }
 
@@ -654,6 +674,14 @@ extern "C" int wk_batch_set_fused(wk_batch *b, int32_t fused) {
 }
 
 extern "C" int wk_batch_get_fused(wk_batch *b) { return b ? b->tune.fused : 0; }
+
+extern "C" int wk_batch_set_block_threads(wk_batch *b, int32_t threads) {
+    if (!b || (threads != 128 && threads != 256)) return set_error(WK_EINVAL, "wk_batch_set_block_threads: 128 or 256");
+    b->tune.bt = threads;
+    return WK_OK;
+}
+
+extern "C" int wk_batch_get_block_threads(wk_batch *b) { return b ? b->tune.bt : 0; }
 
 extern "C" int wk_batch_get_tuning(wk_batch *b, int32_t *blocks_per_sm, int32_t *rows_per_warp, int32_t *split_ints) {
     if (!b || !blocks_per_sm || !rows_per_warp || !split_ints) return set_error(WK_EINVAL, "wk_batch_get_tuning: null");
@@ -830,8 +858,8 @@ extern "C" int wk_batch_download(wk_batch *b, int32_t *host, int64_t cap, int64_
 }
 
 // Autotuner: time the batch with every candidate (three kernels or one per
-// step, blocks/SM, rows/warp, split) on the given queries (CUDA events, best
-// of `reps` after a warm run) and keep the fastest.  A one-kernel candidate
+// step, 128 or 256 threads a block, blocks/SM, rows/warp, split) on the given
+// queries (CUDA events, best of `reps` after a warm run) and keep the fastest.  A one-kernel candidate
 // the device refuses (its cooperative launch, or its capture into a graph) is
 // skipped.  Writes the chosen candidate's time.
 extern "C" int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const int32_t *n_patterns, int32_t nq,
@@ -847,10 +875,11 @@ extern "C" int wk_batch_autotune(wk_batch *b, const int64_t *cmd_chains, const i
     BatchTune keep = b->tune;
     b->form_best_ms[0] = b->form_best_ms[1] = -1.0;
     for (int fu = 0; fu < 2; ++fu)
+    for (int bt : {256, 128})
     for (int bl : kBlocks)
         for (int rw : kRows)
             for (int sp : kSplit) {
-                b->tune = BatchTune{bl, rw / 32, sp, fu};
+                b->tune = BatchTune{bl, rw / 32, sp, fu, bt};
                 int st = wk_batch_run(b, cmd_chains, n_patterns, nq, 1);   // builds the graph
                 if (st && fu && st != WK_EOVERFLOW && st != WK_ETIMEDOUT) {
                     cudaGetLastError();
