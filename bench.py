@@ -531,6 +531,9 @@ def run_gb300(args, dist):
                        "rows_in_mean": float(np.mean([op["rows_in"] for op in ops])),
                        "rows_out_mean": float(np.mean([op["rows_out"] for op in ops])),
                        "ms_mean": ms / len(ops),
+                       # the device's idle time between the op's kernels (a k2u op's
+                       # group-sum readback and expansion launch)
+                       "idle_ms_mean": float(np.mean([max(op["span_ms"] - op["ms"], 0.0) for op in ops])),
                        "gbs": sum(op["alg_bytes"] for op in ops) / (ms / 1000.0) / 1e9 if ms > 0 else None})
 
     # ---- the filter group: the same shapes closed by known_to_known /

@@ -445,6 +445,9 @@ typedef struct {
     int32_t kind;          /* 0 k2u, 1 k2k, 2 k2c, 3 i2u, 4 c2u            */
     int64_t alg_bytes;     /* algorithmic bytes per the roofline formulas   */
     int64_t kernels;       /* kernel launches of the op                     */
+    double span_ms;        /* first kernel's start to last kernel's end: ms
+                              plus the device's idle time between the op's
+                              kernels (the host round trip of a k2u op)     */
 } wk_op_stats;
 int wk_enable_timing(wk_ctx *ctx, int enable);
 int wk_last_op_stats(wk_ctx *ctx, wk_op_stats *st);

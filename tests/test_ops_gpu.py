@@ -276,7 +276,7 @@ def test_kernel_launch_count_and_timing(gpu_small, golden_small):
     st = gpu_small.last_op_stats()
     gpu_small.enable_timing(False)
     assert gpu_small.kernel_launches() > before
-    assert st["kernels"] == 2 and st["ms"] > 0 and st["ms_main"] > 0   # k2u: count + expand
+    assert st["kernels"] == 3 and st["ms"] > 0 and st["ms_main"] > 0   # k2u: count + publish + expand
     assert st["rows_out"] == q["rows"]
 
 

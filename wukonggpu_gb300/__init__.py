@@ -63,7 +63,8 @@ class wk_seg_layout(C.Structure):
 
 class wk_op_stats(C.Structure):
     _fields_ = [("ms", C.c_double), ("ms_main", C.c_double), ("rows_in", C.c_int64), ("rows_out", C.c_int64),
-                ("cols_in", C.c_int32), ("kind", C.c_int32), ("alg_bytes", C.c_int64), ("kernels", C.c_int64)]
+                ("cols_in", C.c_int32), ("kind", C.c_int32), ("alg_bytes", C.c_int64), ("kernels", C.c_int64),
+                ("span_ms", C.c_double)]
 
 
 class wk_server_config(C.Structure):

@@ -209,6 +209,16 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
     }
 }
 
+// One CTA, stream-ordered behind a count kernel: copies the op's error word
+// and group sums into pinned host memory, fences them system-wide, then writes
+// the sequence number the host waits for.
+__global__ void __launch_bounds__(kThreads) publish_kernel(const Publish pub) {
+    for (long long w = threadIdx.x; w < pub.n; w += blockDim.x) pub.dst[2 + w] = __ldcg(pub.src + w);
+    __threadfence_system();
+    __syncthreads();
+    if (threadIdx.x == 0) *(volatile unsigned long long *)pub.dst = pub.seq;
+}
+
 // ------------------------------------------------------- k2u slice location
 static_assert(kThreads == (1 << kGroupShift), "one thread per group and per block of a group");
 
@@ -815,6 +825,8 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t 
 #undef WK_COUNT
 }
 
+void launch_publish(const Publish &pub, cudaStream_t st) { publish_kernel<<<1, kThreads, 0, st>>>(pub); }
+
 void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
                             const unsigned long long *blk_sum, const unsigned long long *group_sums,
                             const GroupTable &gt, unsigned long long slices, int32_t *out, cudaStream_t st) {
@@ -874,6 +886,7 @@ int preload_k2u_kernels() {
     get((const void *)k2u_count_kernel<true, false, 1>);
     get((const void *)k2u_count_kernel<true, true, 1>);
     get((const void *)k2u_count_kernel<true, true, 2>);
+    get((const void *)publish_kernel);
     get((const void *)k2u_expand_kernel<0>);
     get((const void *)k2u_expand_kernel<2>);
     get((const void *)k2u_expand_kernel<3>);

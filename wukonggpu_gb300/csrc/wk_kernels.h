@@ -41,6 +41,19 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t 
                       uint32_t *off, unsigned long long *blk_sum, unsigned long long *group_sums, int *err, bool func,
                       unsigned long long *clear, int64_t nclear, int sms, cudaStream_t st);
 
+// The op's error word and group sums (n words from src) for the host: a
+// one-CTA kernel, stream-ordered behind the count, copies them into
+// dst[2 .. 2 + n) of pinned, device-mapped host memory and then writes seq
+// into dst[0], so a host that sees seq there reads the op's totals without a
+// device-to-host copy or a stream synchronisation.
+struct Publish {
+    const unsigned long long *src;
+    unsigned long long *dst;
+    long long n;
+    unsigned long long seq;
+};
+void launch_publish(const Publish &pub, cudaStream_t st);
+
 // Load every k2u count and expansion kernel on the current device (they load
 // lazily, at first launch, otherwise); returns a cudaError_t.
 int preload_k2u_kernels();

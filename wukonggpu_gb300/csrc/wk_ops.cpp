@@ -87,6 +87,9 @@ struct OpClock {
         }
         ctx->last.ms = tot;
         ctx->last.ms_main = main;
+        float span = 0.f;
+        if (ctx->tn >= 2) cudaEventElapsedTime(&span, ctx->tev[0], ctx->tev[(size_t)ctx->tn - 1]);
+        ctx->last.span_ms = span;
     }
 };
 
@@ -112,13 +115,22 @@ int ensure_seg(wk_ctx *ctx, int id, PredView *pv) {
     return WK_OK;
 }
 
-int read_totals(wk_ctx *ctx, int *err_flag) {
-    cudaError_t e = cudaMemcpyAsync(ctx->h_scal, ctx->dscal.ptr, 32, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "totals readback");
-    e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "op sync");
-    *err_flag = (int)(ctx->h_scal[0] & 0xffffffffull);
-    return WK_OK;
+
+// Wait until the publish kernel of sequence number seq has written its copy
+// into ctx->h_gs.  The wait ends with the stream's work: the stream is polled
+// between reads, and a stream that has finished (or failed) without the
+// number there is an error.
+int wait_published(wk_ctx *ctx, unsigned long long seq) {
+    for (unsigned int i = 1;; ++i) {
+        if (__atomic_load_n(ctx->h_gs, __ATOMIC_ACQUIRE) == seq) return WK_OK;
+        if ((i & 255u) == 0u) {
+            const cudaError_t e = cudaStreamQuery(ctx->stream);
+            if (e == cudaErrorNotReady) continue;
+            if (e != cudaSuccess) return cuda_fail(e, "op sync");
+            if (__atomic_load_n(ctx->h_gs, __ATOMIC_ACQUIRE) == seq) return WK_OK;
+            return set_error(WK_EDEVICE, "op finished without publishing its totals");
+        }
+    }
 }
 
 int fail_corrupt(wk_ctx *ctx) {
@@ -139,16 +151,22 @@ int reserve_gsum(wk_ctx *ctx, int64_t groups) {
     if (st) return st;
     cudaError_t e = cudaMemsetAsync(ctx->gsum.ptr, 0, ctx->gsum.cap, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "k2u: clear group sums");
+    // every count kernel that published into the old copy has been waited for
     if (ctx->h_gs) cudaFreeHost(ctx->h_gs);
-    ctx->h_gs = nullptr;
+    ctx->h_gs = ctx->h_gs_dev = nullptr;
     ctx->h_gs_bytes = 0;
-    e = cudaHostAlloc((void **)&ctx->h_gs, buf_bytes, cudaHostAllocDefault);
+    e = cudaHostAlloc((void **)&ctx->h_gs, 16 + buf_bytes, cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+        std::memset(ctx->h_gs, 0, 16 + buf_bytes);   // no sequence number yet
+        e = cudaHostGetDevicePointer((void **)&ctx->h_gs_dev, ctx->h_gs, 0);
+    }
     if (e != cudaSuccess) {
-        ctx->h_gs = nullptr;
+        if (ctx->h_gs) cudaFreeHost(ctx->h_gs);
+        ctx->h_gs = ctx->h_gs_dev = nullptr;
         ctx->gs_groups = 0;
         return cuda_fail(e, "k2u: pinned group sums");
     }
-    ctx->h_gs_bytes = buf_bytes;
+    ctx->h_gs_bytes = 16 + buf_bytes;
     ctx->gs_groups = want;
     ctx->gs_par = 0;
     ctx->gs_used[0] = ctx->gs_used[1] = 0;
@@ -227,19 +245,24 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
         const int par = ctx->gs_par;
         gs = gsum_buffer(ctx, par);
         if ((st = clk.begin())) return st;
+        // the op's error flags and group sums come to the host through pinned
+        // memory (a one-CTA kernel behind the count); the host adds up the totals
+        const dev::Publish pub{gs, ctx->h_gs_dev, 2 + 2 * groups, ++ctx->pub_seq};
         dev::launch_k2u_count(h->data, R, C, scol, dir, pv, ctx->deg.as<uint32_t>(), ctx->off.as<uint32_t>(),
                               ctx->blk_sum.as<unsigned long long>(), gs + 2, reinterpret_cast<int *>(gs), func,
                               gsum_buffer(ctx, par ^ 1), 2 + 2 * ctx->gs_used[par ^ 1], ctx->sms, ctx->stream);
         if ((st = launch_check("k2u count")) || (st = clk.end(false))) return st;
+        // outside the count's timing events: the op's device span counts it,
+        // the count kernel's time does not
+        dev::launch_publish(pub, ctx->stream);
+        if ((st = launch_check("k2u publish"))) return st;
+        ++ctx->launches;
+        ++ctx->last.kernels;
         ctx->gs_par = par ^ 1;
         ctx->gs_used[par ^ 1] = 0;
         ctx->gs_used[par] = groups;
-        // the op's error flags and group sums: the host adds up the totals
-        cudaError_t e = cudaMemcpyAsync(ctx->h_gs, gs, (size_t)(16 + 16 * groups), cudaMemcpyDeviceToHost,
-                                        ctx->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "k2u: group sums readback");
-        if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(e, "op sync");
-        errf = (int)(ctx->h_gs[0] & 0xffffffffull);
+        if ((st = wait_published(ctx, pub.seq))) return st;
+        errf = (int)(ctx->h_gs[2] & 0xffffffffull);
         if (!(func && (errf & 8))) break;
         func = false;   // the next count adds into the other, cleared buffer
     }
@@ -255,8 +278,8 @@ int op_k2u(wk_ctx *ctx, wk_history *h, int scol, uint32_t pid, uint32_t dir) {
             gt.out[g] = rows_out;
             gt.sl[g] = (unsigned int)slices;
         }
-        rows_out += ctx->h_gs[2 + 2 * g];
-        slices += ctx->h_gs[3 + 2 * g];
+        rows_out += ctx->h_gs[4 + 2 * g];
+        slices += ctx->h_gs[5 + 2 * g];
     }
     if (slices >> 32) gt.n = 0;   // not reached: a slice holds up to 8192 of the output rows
     if (gt.n) {
@@ -338,11 +361,17 @@ int op_filter(wk_ctx *ctx, wk_history *h, int scol, int ecol, int32_t end_const,
     dev::launch_filter_write(h->data, R, C, ctx->mask.as<uint32_t>(), ctx->blk_nz.as<unsigned int>(), gs,
                              ob.as<int32_t>(), ctx->stream);
     if ((st = launch_check("filter write")) || (st = clk.end(false))) return st;
-    int errf = 0;
-    if ((st = read_totals(ctx, &errf))) return st;
-    if (errf) return fail_corrupt(ctx);
-    const int64_t E = (int64_t)ctx->h_scal[1];
-    const int64_t nz = (int64_t)ctx->h_scal[2];
+    // the error word and totals come to the host through pinned memory, as a
+    // k2u op's group sums do
+    const dev::Publish pub{ctx->dscal.as<unsigned long long>(), ctx->h_gs_dev, 4, ++ctx->pub_seq};
+    dev::launch_publish(pub, ctx->stream);
+    if ((st = launch_check("filter publish"))) return st;
+    ++ctx->launches;
+    ++ctx->last.kernels;
+    if ((st = wait_published(ctx, pub.seq))) return st;
+    if (ctx->h_gs[2] & 0xffffffffull) return fail_corrupt(ctx);
+    const int64_t E = (int64_t)ctx->h_gs[3];
+    const int64_t nz = (int64_t)ctx->h_gs[4];
     clk.finish();
     ctx->last.rows_out = nz;
     ctx->last.alg_bytes = 4 * R * C + 16 * R + 4 * E + 4 * nz * C;

@@ -89,8 +89,12 @@ struct wk_ctx {
     int64_t gs_groups = 0;           // groups per buffer
     int gs_par = 0;                  // the buffer the next count kernel adds into
     int64_t gs_used[2] = {0, 0};     // groups written into each buffer since it was cleared
-    unsigned long long *h_gs = nullptr;   // pinned copy of one buffer
+    // pinned, device-mapped host words: [0] the sequence number of the last
+    // count kernel that published, then a copy of its sums buffer from [2]
+    unsigned long long *h_gs = nullptr;
+    unsigned long long *h_gs_dev = nullptr;   // its device address
     size_t h_gs_bytes = 0;
+    unsigned long long pub_seq = 0;  // the last count kernel's sequence number
     wk::DevBuf dscal;                // [0] error flags, [8..32) totals
     // wk_history_partition: rows per (owner, tile) and their scan's block
     // sums, and the parts' bounds (grown on demand, kept for the next call)
