@@ -66,9 +66,9 @@ def parse():
     ap.add_argument("--serving-scale", type=float, default=1.0,
                     help="entity scale of the serving section's own graph (1.0 = 20M entities, 1e9 triples); "
                          "0 serves on the single-query graph")
-    ap.add_argument("--heavy-workers", type=int, default=3,
-                    help="contexts running heavy requests in the serving loop (2, 3, 4 and 6 measured; 3 serves "
-                         "the most at the baseline's p99)")
+    ap.add_argument("--heavy-workers", type=int, default=2,
+                    help="contexts running heavy requests in the serving loop (2, 3, 4 and 6 measured; with 2 the "
+                         "light requests' p99 stays lowest at middle rates)")
     ap.add_argument("--one-query", type=int, default=-1,
                     help="run query N of the mix once, op by op, print each op's stats and exit "
                          "(a fixed launch sequence for ncu captures)")
@@ -1039,7 +1039,7 @@ def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2,
            "baseline_capacity_qps": cap0,
            "plan_us": {"statistics": t_stats * 1e6, "learned_batched": t_learned * 1e6},
            "heavy_plans_checked": {"plans": checked, "bindings_differ": mismatched}, "sweep": []}
-    for f in (0.9, 1.5, 2.0, 3.0, 5.0, 7.0, 9.0, 11.0, 13.0):
+    for f in (0.9, 1.5, 2.0, 3.0, 5.0, 6.0, 7.0, 8.0, 9.0, 11.0, 13.0):
         rate = f * cap0
         row = {"rate_qps": rate, "query_at_a_time_stats": run(0, stats_plans, rate) if f <= 1.5 else None,
                "batched_learned": run(1, learned_plans, rate)}
