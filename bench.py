@@ -379,8 +379,9 @@ def run_reference(args, dist):
 
 def run_one_query(args):
     """Query `args.one_query` of the mix, once, op by op with per-kernel timing.
-    Kernel launches: the start op's copy, then two per k2u op (count, expand)
-    and two per filter op (probe, write), in pattern order."""
+    Kernel launches: the start op's copy, then three per k2u op (count,
+    publish, expand) and three per filter op (probe, write, publish), in
+    pattern order."""
     import wukonggpu_gb300 as W
     from wukonggpu_gb300 import build as wb
     from wukonggpu_gb300 import workloads
