@@ -75,6 +75,46 @@ def test_k2u_random_histories(gpu_small, small_graph, small_oracle, R, C):
         assert got.shape == exp.shape and np.array_equal(got, exp), (pid, d, scol)
 
 
+def test_interleaved_op_sizes_on_a_fresh_context(small_graph, small_oracle):
+    """One new context, ops of growing and shrinking size: each op's totals
+    reach the host through pinned memory, whose buffer grows when an op has
+    more groups than any before it (1, 3, 1, 3 and 11 groups here, k2u and
+    k2k ops alternating)."""
+    g, s, p, o = small_graph
+    rc = W.RCache(device=0)
+    rc.build_store_graph(g)
+    rng = np.random.default_rng(77)
+    verts = np.unique(s)
+    m = p == 2
+    es, eo = s[m], o[m]
+    try:
+        for R, kind in ((1000, "k2u"), (700_001, "k2u"), (3000, "k2u"), (700_001, "k2k"), (2_800_003, "k2u"),
+                        (5, "k2k"), (2_800_003, "k2k"), (1, "k2u")):
+            C = 3
+            h = _random_history(rng, verts, R, C, miss_frac=0.1)
+            if kind == "k2k":   # rows that are real edges, so that some are kept
+                idx = rng.integers(0, len(es), size=R)
+                real = rng.random(R) < 0.5
+                h[real, 0] = es[idx[real]]
+                h[real, 1] = eo[idx[real]]
+            req = W.Request([])
+            rc.upload_history(req, h)
+            if kind == "k2u":
+                rc.known_to_unknown(req, -2, W.OUT, 2)
+                exp, _ = small_oracle.step(h, False, -2, 2, W.OUT, -C - 1)
+            else:
+                rc.known_to_known(req, -1, W.OUT, 2, -2)
+                exp, _ = small_oracle.step(h, False, -1, 2, W.OUT, -2)
+            st = rc.last_op_stats()
+            got = rc.download(req)
+            assert np.array_equal(got.reshape(exp.shape), exp), (R, kind)
+            # the op's two kernels and the publish kernel; a k2u op with no
+            # output rows launches no expansion
+            assert st["kernels"] == (3 if kind == "k2k" or len(exp) else 2), (R, kind)
+    finally:
+        rc.close()
+
+
 @pytest.mark.parametrize("R", [1, 33, 1025, 50_000, 700_001])   # 700,001 rows: 684 blocks in 3 groups of 256
 @pytest.mark.parametrize("C", [2, 5, 11])
 def test_k2k_k2c_random_histories(gpu_small, small_graph, small_oracle, R, C):
