@@ -90,3 +90,21 @@ def test_graph_generator_rejects_bad_specs(lib_built):
     bad = W.graph_spec(1, 1000, 3, [dict(kind=7, count=2)])
     with pytest.raises(W.WkError):
         W.Graph(bad)
+
+
+def test_batch_results_are_views_of_the_packed_array():
+    """A batch's per-query tables index into one packed host array: query i
+    has rows[i] rows of cols[i] columns from offset offs[i]."""
+    import numpy as np
+    buf = np.arange(40, dtype=np.int32)
+    rows = np.array([2, 0, 3, 1], np.int64)
+    cols = np.array([2, 3, 1, 4], np.int32)
+    offs = np.array([0, 4, 4, 7], np.int64)
+    res = W.BatchResults(buf, rows, cols, offs)
+    assert len(res) == 4
+    assert [t.shape for t in res] == [(2, 2), (0, 3), (3, 1), (1, 4)]
+    assert res[0].tolist() == [[0, 1], [2, 3]] and res[-1].tolist() == [[7, 8, 9, 10]]
+    assert [t.shape for t in res[1:3]] == [(0, 3), (3, 1)]
+    assert np.shares_memory(res[2], buf)
+    with pytest.raises(IndexError):
+        res[4]

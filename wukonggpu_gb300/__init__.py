@@ -16,6 +16,7 @@ There is no CPU fallback: if the library is missing every entry point raises.
 from __future__ import annotations
 
 import ctypes as C
+import collections.abc
 import itertools
 import os
 from pathlib import Path
@@ -572,6 +573,29 @@ class RCache:
             pass
 
 
+
+class BatchResults(collections.abc.Sequence):
+    """The per-query tables of one batch: query i's rows are a (rows, cols)
+    view into the packed host array, made when the query is indexed."""
+
+    def __init__(self, buf: np.ndarray, rows: np.ndarray, cols: np.ndarray, offs: np.ndarray):
+        self._buf, self._rows, self._cols, self._offs = buf, rows, cols, offs
+
+    def __len__(self) -> int:
+        return len(self._rows)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self[j] for j in range(*i.indices(len(self)))]
+        n = len(self._rows)
+        if i < 0:
+            i += n
+        if not 0 <= i < n:
+            raise IndexError(i)
+        r, c, o = int(self._rows[i]), int(self._cols[i]), int(self._offs[i])
+        return self._buf[o:o + r * c].reshape(-1, max(c, 1))
+
+
 class Batch:
     """Batched execution of constant-start queries (one CUDA graph per batch shape)."""
 
@@ -594,8 +618,10 @@ class Batch:
                                            len(npat), 1 if use_graph else 0))
         return len(npat)
 
-    def download(self, nq: int, into: "PinnedBuffer | None" = None):
-        """Per-query result tables of the last run (numpy views into one packed array)."""
+    def download(self, nq: int, into: "PinnedBuffer | None" = None) -> "BatchResults":
+        """Per-query result tables of the last run: every result is copied to
+        host memory (into `into` when it is large enough), and the returned
+        sequence gives each query's table as a numpy view into that array."""
         lib = load_library()
         tot = C.c_int64()
         _check(lib.wk_batch_download(self._h, None, 0, C.byref(tot)))
@@ -609,10 +635,7 @@ class Batch:
         offs = np.empty(nq, np.int64)
         _check(lib.wk_batch_layouts(self._h, nq, rows.ctypes.data_as(_I64P), cols.ctypes.data_as(_I32P),
                                     offs.ctypes.data_as(_I64P)))
-        width = np.maximum(cols, 1).tolist()
-        ends = (offs + rows * cols).tolist()
-        out = [buf[a:e].reshape(-1, w) for a, e, w in zip(offs.tolist(), ends, width)]
-        return out
+        return BatchResults(buf, rows, cols, offs)
 
     def set_tuning(self, blocks_per_sm: int, rows_per_warp: int, split_ints: int):
         _check(load_library().wk_batch_set_tuning(self._h, blocks_per_sm, rows_per_warp, split_ints))
