@@ -115,7 +115,6 @@ int ensure_seg(wk_ctx *ctx, int id, PredView *pv) {
     return WK_OK;
 }
 
-
 // Wait until the publish kernel of sequence number seq has written its copy
 // into ctx->h_gs.  The wait ends with the stream's work: the stream is polled
 // between reads, and a stream that has finished (or failed) without the
@@ -151,7 +150,7 @@ int reserve_gsum(wk_ctx *ctx, int64_t groups) {
     if (st) return st;
     cudaError_t e = cudaMemsetAsync(ctx->gsum.ptr, 0, ctx->gsum.cap, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "k2u: clear group sums");
-    // every count kernel that published into the old copy has been waited for
+    // every publish into the old copy has been waited for
     if (ctx->h_gs) cudaFreeHost(ctx->h_gs);
     ctx->h_gs = ctx->h_gs_dev = nullptr;
     ctx->h_gs_bytes = 0;
