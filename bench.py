@@ -255,8 +255,16 @@ def cpu_leg(rc, g, queries, nthreads: int, batch_sample=None, extra=None):
         del table
         if list(grows) != list(orows) or gd != od:
             bad.append({"query": name, "gpu_rows": [int(x) for x in grows], "oracle_rows": [int(x) for x in orows]})
-    cpu = {"value": len(queries) / secs, "unit": "queries/s", "cores": nthreads, "kind": "port",
-           "sample": f"one pass over the {len(queries)}-query mix on the full graph, {nthreads} threads",
+    # two more timed passes, so the sample is about 10-30 s of CPU work
+    passes = 3
+    for _ in range(passes - 1):
+        for _, q in queries:
+            a = time.perf_counter()
+            table, _ = orc.execute(q, nthreads=nthreads)
+            secs += time.perf_counter() - a
+            del table
+    cpu = {"value": passes * len(queries) / secs, "unit": "queries/s", "cores": nthreads, "kind": "port",
+           "sample": f"{passes} passes over the {len(queries)}-query mix on the full graph, {nthreads} threads",
            "seconds": secs, "oracle_build_s": build_s}
     parity = {"single_query_mix": {"queries": len(queries), "mismatched": len(bad), "compared": "per-step rows and "
                                    "order-independent digest of the final table", "mismatches": bad[:5]}}
