@@ -108,7 +108,7 @@ int ensure_seg(wk_ctx *ctx, int id, PredView *pv) {
     if (ds.pool) {
         std::vector<int> prot = ctx->protect;
         prot.push_back(id);
-        int st = ds.ensure(id, prot, ctx->stream, ctx->stream, nullptr);
+        int st = ds.ensure(id, prot, ctx->query_rest, ctx->stream, ctx->stream, nullptr);
         if (st) return st;
     }
     *pv = ds.views[(size_t)id];
@@ -491,17 +491,26 @@ extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history
     if (ctx->device < 0) return set_error(WK_EDEVICE, "wk_execute: host-only context");
     wk_history_init(h);
     ctx->protect.clear();
+    ctx->query_rest.clear();
     ctx->qstats.clear();
     DeviceStore &ds = *ctx->store;
     int st = WK_OK;
     for (int i = 0; i < n && st == WK_OK; ++i) {
         const int64_t start = cmd[i * 4], pid = cmd[i * 4 + 1], d = cmd[i * 4 + 2], end = cmd[i * 4 + 3];
+        if (ds.pool) {
+            // the segments of steps i.. (an index start's segment is its index id)
+            ctx->query_rest.clear();
+            for (int k = i; k < n; ++k) {
+                const int64_t sid = (k == 0 && is_tpid(cmd[0])) ? cmd[0] : cmd[k * 4 + 1];
+                if (sid >= 1 && sid <= ds.hs->num_ids) ctx->query_rest.push_back((int)sid);
+            }
+        }
         if (ds.pool && ctx->cfg.enable_prefetch && i + 1 < n) {
             const int64_t np = cmd[(i + 1) * 4 + 1];
             const int64_t cp = (i == 0 && is_tpid(cmd[0])) ? cmd[0] : pid;
             if (np >= 1 && np <= ds.hs->num_ids && cp >= 1 && cp <= ds.hs->num_ids) {
                 std::vector<int> prot{(int)cp, (int)np};
-                ds.ensure((int)np, prot, ctx->side, ctx->stream, ctx->use_ready);
+                ds.ensure((int)np, prot, ctx->query_rest, ctx->side, ctx->stream, ctx->use_ready);
                 ctx->protect = prot;
             }
         }
@@ -533,6 +542,7 @@ extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history
         if (st == WK_OK && ctx->timing) ctx->qstats.push_back(ctx->last);
     }
     ctx->protect.clear();
+    ctx->query_rest.clear();
     return st;
 }
 

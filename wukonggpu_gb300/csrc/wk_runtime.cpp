@@ -179,15 +179,26 @@ int DeviceStore::compact(cudaStream_t use_st, cudaStream_t copy_st) {
 }
 
 // Make segment `id` resident (ShardManager::load_predicate,
-// core/shard_manager.hpp:473-555).  Eviction takes the least recently used
-// segment that is not protected (the reference evicts non-query predicates
-// first).  The copy is issued on `copy_st`; `use_st` is made to wait for it.
-int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t copy_st, cudaStream_t use_st,
-                        cudaEvent_t use_ready) {
+// core/shard_manager.hpp:473-555).  Eviction never takes a protected segment.
+// Like the reference, which evicts predicates outside the query first and the
+// query's own last (evict_kcache_blocks / evict_vcache_blocks,
+// core/shard_manager.hpp:130-295), it takes a segment that the query's
+// remaining steps (`avoid`) use only when no other will do.  Among the rest it
+// takes the least requested segment, the most recently used one on a tie:
+// a mix that cycles through its queries then keeps a fixed set of segments
+// instead of evicting each one just before it comes round again (least
+// recently used would), and a skewed mix keeps its frequent segments.
+// Request counts halve every 4096 requests, so past popularity fades.  The
+// copy is issued on `copy_st`; `use_st` is made to wait for it.
+int DeviceStore::ensure(int id, const std::vector<int> &protect, const std::vector<int> &avoid, cudaStream_t copy_st,
+                        cudaStream_t use_st, cudaEvent_t use_ready) {
     if (!pool) return WK_OK;
     Resident &r = res[(size_t)id];
     ++clock;
     ++requests;
+    if ((requests & 4095) == 0)
+        for (Resident &x : res) x.uses >>= 1;
+    if (r.uses < UINT32_MAX) ++r.uses;
     if (r.resident) {
         ++hits;
         r.last_use = clock;
@@ -212,12 +223,24 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, cudaStream_t co
             continue;
         }
         int victim = -1;
-        uint64_t oldest = ~0ull;
+        bool v_needed = true;
+        uint32_t v_uses = 0;
+        uint64_t v_last = 0;
         for (int v = 1; v <= hs->num_ids; ++v) {
             const Resident &x = res[(size_t)v];
             if (!x.resident || x.bytes == 0) continue;
             if (std::find(protect.begin(), protect.end(), v) != protect.end()) continue;
-            if (x.last_use < oldest) { oldest = x.last_use; victim = v; }
+            const bool needed = std::find(avoid.begin(), avoid.end(), v) != avoid.end();
+            // order: not needed by the query's remaining steps, fewer requests, more recent use
+            const bool better = victim < 0 || (needed != v_needed ? !needed
+                                                                  : (x.uses != v_uses ? x.uses < v_uses
+                                                                                      : x.last_use > v_last));
+            if (better) {
+                victim = v;
+                v_needed = needed;
+                v_uses = x.uses;
+                v_last = x.last_use;
+            }
         }
         if (victim < 0)
             return set_error(WK_ENOMEM,

@@ -37,6 +37,7 @@ struct DeviceStore {
     struct Resident {
         bool resident = false;
         uint64_t off = 0, bytes = 0, last_use = 0;
+        uint32_t uses = 0;   // requests since load or the last halving (eviction by frequency)
         cudaEvent_t ev = nullptr;   // completion of the segment's copy
     };
     int device = 0;
@@ -64,8 +65,8 @@ struct DeviceStore {
     void pool_free(uint64_t off, uint64_t n);
     uint64_t pool_free_bytes() const;
     int compact(cudaStream_t use_st, cudaStream_t copy_st);
-    int ensure(int id, const std::vector<int> &protect, cudaStream_t copy_st, cudaStream_t use_st,
-               cudaEvent_t use_ready);
+    int ensure(int id, const std::vector<int> &protect, const std::vector<int> &avoid, cudaStream_t copy_st,
+               cudaStream_t use_st, cudaEvent_t use_ready);
 };
 
 }  // namespace wk
@@ -112,8 +113,10 @@ struct wk_ctx {
     int64_t row_limit = INT64_MAX;   // wk_set_row_limit
     cudaEvent_t tm0 = nullptr, tm1 = nullptr;   // wk_timer_begin / wk_timer_end
 
-    // query-level state (segment cache protection / prefetch)
-    std::vector<int> protect;
+    // query-level state (segment cache protection / prefetch): segments that
+    // must stay (the current step's and the prefetched one), and the segments
+    // the query's remaining steps use, evicted only when nothing else can be
+    std::vector<int> protect, query_rest;
 
     // injected allocation failures still to come (wk_ctx_inject_alloc_failure)
     std::atomic<int> inject_alloc_fail{0};
