@@ -278,9 +278,10 @@ def test_fragmented_segment_cache_compacts(small_graph, small_oracle):
     core/shard_manager.hpp:78-128; here a segment is one range, moved down).
 
     Budget 5 MiB; segments 2, 3 and 6 (about 1.6 MB each) are loaded in that
-    order, then a query steps through 3 and prefetches the type segment (2.4
-    MB): evicting 2 and 6 frees 3.6 MB in two ranges of at most 2.0 MB around
-    3, which is protected."""
+    order, then a query steps through 3 and then the type segment (2.4 MB),
+    with 3 still protected (the prefetch finds no free space and leaves the
+    load to the step): evicting 2 and 6 frees 3.6 MB in two ranges of at most
+    2.0 MB around 3."""
     g, s, p, o = small_graph
     host = W.RCache(device=-1)
     host.build_store(s, p, o, g.num_ids)

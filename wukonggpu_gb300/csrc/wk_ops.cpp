@@ -510,7 +510,7 @@ extern "C" int wk_execute(wk_ctx *ctx, const int64_t *cmd, int32_t n, wk_history
             const int64_t cp = (i == 0 && is_tpid(cmd[0])) ? cmd[0] : pid;
             if (np >= 1 && np <= ds.hs->num_ids && cp >= 1 && cp <= ds.hs->num_ids) {
                 std::vector<int> prot{(int)cp, (int)np};
-                ds.ensure((int)np, prot, ctx->query_rest, ctx->side, ctx->stream, ctx->use_ready);
+                ds.ensure((int)np, prot, ctx->query_rest, ctx->side, ctx->stream, ctx->use_ready, false);
                 ctx->protect = prot;
             }
         }

@@ -189,16 +189,21 @@ int DeviceStore::compact(cudaStream_t use_st, cudaStream_t copy_st) {
 // instead of evicting each one just before it comes round again (least
 // recently used would), and a skewed mix keeps its frequent segments.
 // Request counts halve every 4096 requests, so past popularity fades.  The
-// copy is issued on `copy_st`; `use_st` is made to wait for it.
+// copy is issued on `copy_st`; `use_st` is made to wait for it.  With
+// may_evict false (a prefetch) the segment loads only into free space: no
+// segment is evicted or moved, and the step's own request loads it otherwise.
 int DeviceStore::ensure(int id, const std::vector<int> &protect, const std::vector<int> &avoid, cudaStream_t copy_st,
-                        cudaStream_t use_st, cudaEvent_t use_ready) {
+                        cudaStream_t use_st, cudaEvent_t use_ready, bool may_evict) {
     if (!pool) return WK_OK;
     Resident &r = res[(size_t)id];
+    if (!may_evict && r.resident) return WK_OK;   // a prefetch of a resident segment: nothing to do
     ++clock;
-    ++requests;
-    if ((requests & 4095) == 0)
-        for (Resident &x : res) x.uses >>= 1;
-    if (r.uses < UINT32_MAX) ++r.uses;
+    if (may_evict) {   // a step's request (a prefetch is not one)
+        ++requests;
+        if ((requests & 4095) == 0)
+            for (Resident &x : res) x.uses >>= 1;
+        if (r.uses < UINT32_MAX) ++r.uses;
+    }
     if (r.resident) {
         ++hits;
         r.last_use = clock;
@@ -216,6 +221,7 @@ int DeviceStore::ensure(int id, const std::vector<int> &protect, const std::vect
                          (unsigned long long)need, (unsigned long long)pool_bytes);
     uint64_t off = 0;
     while (!pool_alloc(need, &off)) {
+        if (!may_evict) return WK_OK;
         // free bytes enough but split into ranges: compact rather than evict
         if (pool_free_bytes() >= need) {
             int st = compact(use_st, copy_st);

@@ -66,7 +66,7 @@ struct DeviceStore {
     uint64_t pool_free_bytes() const;
     int compact(cudaStream_t use_st, cudaStream_t copy_st);
     int ensure(int id, const std::vector<int> &protect, const std::vector<int> &avoid, cudaStream_t copy_st,
-               cudaStream_t use_st, cudaEvent_t use_ready);
+               cudaStream_t use_st, cudaEvent_t use_ready, bool may_evict = true);
 };
 
 }  // namespace wk
