@@ -117,18 +117,18 @@ int ensure_seg(wk_ctx *ctx, int id, PredView *pv) {
 
 // Wait until the publish kernel of sequence number seq has written its copy
 // into ctx->h_gs.  The wait ends with the stream's work: the stream is polled
-// between reads, and a stream that has finished (or failed) without the
-// number there is an error.
+// every 4096 reads of the word (a few microseconds; no clock is read, as a
+// clock read can enter the kernel and cost the thread its core), and a stream
+// that has finished (or failed) without the number there is an error.
 int wait_published(wk_ctx *ctx, unsigned long long seq) {
     for (unsigned int i = 1;; ++i) {
         if (__atomic_load_n(ctx->h_gs, __ATOMIC_ACQUIRE) == seq) return WK_OK;
-        if ((i & 255u) == 0u) {
-            const cudaError_t e = cudaStreamQuery(ctx->stream);
-            if (e == cudaErrorNotReady) continue;
-            if (e != cudaSuccess) return cuda_fail(e, "op sync");
-            if (__atomic_load_n(ctx->h_gs, __ATOMIC_ACQUIRE) == seq) return WK_OK;
-            return set_error(WK_EDEVICE, "op finished without publishing its totals");
-        }
+        if ((i & 4095u) != 0u) continue;
+        const cudaError_t e = cudaStreamQuery(ctx->stream);
+        if (e == cudaErrorNotReady) continue;
+        if (e != cudaSuccess) return cuda_fail(e, "op sync");
+        if (__atomic_load_n(ctx->h_gs, __ATOMIC_ACQUIRE) == seq) return WK_OK;
+        return set_error(WK_EDEVICE, "op finished without publishing its totals");
     }
 }
 
