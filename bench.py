@@ -360,8 +360,9 @@ def run_reference(args, dist):
     queries = workloads.scale_queries()
     nthreads = os.cpu_count() or 1
     orc = oracle.Oracle(s, p, o, g.num_ids)
-    for _ in range(args.warmup):
-        orc.execute(queries[0][1], nthreads=nthreads)
+    for _ in range(args.warmup):   # untimed steps: passes over the mix
+        for _, q in queries:
+            orc.execute(q, nthreads=nthreads)
     lat = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
