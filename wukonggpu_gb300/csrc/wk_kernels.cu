@@ -65,6 +65,13 @@ __device__ __forceinline__ unsigned long long slices_of(unsigned long long t) {
     return t == 0ull ? 0ull : (t + 3ull + kSliceRows - 1) / kSliceRows;
 }
 
+// Programmatic dependent launch: a count kernel is launched so that its CTAs
+// may be placed while the previous op's expansion finishes its last wave;
+// each CTA first waits (in hardware) until that kernel has completed and its
+// writes are visible.  An expansion CTA allows the launch once it runs.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_dependent_grid() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 // A warp owns kRounds * 32 consecutive rows.  Their start vertices are loaded
 // first (kRounds independent coalesced loads), then each round of 32 rows is
 // probed, so the history read does not sit in front of every bucket read.
@@ -87,6 +94,7 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
                  unsigned long long *__restrict__ blk_sum, unsigned long long *__restrict__ group_sums, int *err,
                  unsigned long long *__restrict__ clear, int64_t nclear) {
     constexpr int NR = kRounds * BPC;   // rounds of 32 rows per warp
+    wait_prior_grid();   // before anything is read or cleared
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t b0 = (int64_t)blockIdx.x * BPC;
     // the other sums buffer, read by the previous op's expansion, is cleared
@@ -430,6 +438,7 @@ k2u_expand_kernel(const int32_t *__restrict__ hist, int64_t R, int C_rt, const i
     __shared__ uint32_t s_w[2][kThreads / 32];
     const int C = W >= 2 ? W - 1 : C_rt;
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    allow_dependent_grid();
 
     // 1. the slice's block, the block's output prefix and count
     const SliceLoc loc = locate_slice(blockIdx.x, blk_sum, group_sums, ngroups, nblk, gt);
@@ -531,6 +540,7 @@ k2u_expand_func_kernel(const int32_t *__restrict__ hist, int64_t R, const int32_
     __shared__ int32_t rows[kRowsPerBlock * kPitch];
     __shared__ uint32_t s_w[kThreads / 32];
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    allow_dependent_grid();
 
     // the block (every non-empty block has one slice)
     const SliceLoc loc = locate_slice(blockIdx.x, blk_sum, group_sums, ngroups, nblk, gt);
@@ -808,9 +818,20 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t 
     // two blocks per CTA once the op has enough blocks to fill the GPU with half as many CTAs
     if (sms < 1) sms = 1;
     const bool pair = dense && nb >= 16u * (unsigned int)sms;
-#define WK_COUNT(F, D, B) \
-    k2u_count_kernel<F, D, B><<<(nb + B - 1) / B, kThreads, 0, st>>>(hist, R, C, scol, dir, pv, deg, off, blk_sum, \
-                                                                     group_sums, err, clear, nclear)
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+#define WK_COUNT(F, D, B)                                                                                         \
+    do {                                                                                                         \
+        cfg.gridDim = dim3((nb + B - 1) / B);                                                                    \
+        cudaLaunchKernelEx(&cfg, k2u_count_kernel<F, D, B>, hist, R, C, scol, dir, pv, deg, off, blk_sum,         \
+                           group_sums, err, clear, nclear);                                                      \
+    } while (0)
     if (func && dense) {
         if (pair) WK_COUNT(true, true, 2);
         else WK_COUNT(true, true, 1);
