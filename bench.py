@@ -1049,7 +1049,7 @@ def section_serving(rc, layout, est, n_req: int = 20000, heavy_workers: int = 2,
            "baseline_capacity_qps": cap0,
            "plan_us": {"statistics": t_stats * 1e6, "learned_batched": t_learned * 1e6},
            "heavy_plans_checked": {"plans": checked, "bindings_differ": mismatched}, "sweep": []}
-    for f in (0.9, 1.5, 2.0, 3.0, 5.0, 6.0, 7.0, 8.0, 9.0, 11.0, 13.0):
+    for f in (0.9, 1.5, 2.0, 3.0, 5.0, 6.0, 6.5, 7.0, 7.5, 8.0, 9.0, 11.0, 13.0):
         rate = f * cap0
         row = {"rate_qps": rate, "query_at_a_time_stats": run(0, stats_plans, rate) if f <= 1.5 else None,
                "batched_learned": run(1, learned_plans, rate)}
