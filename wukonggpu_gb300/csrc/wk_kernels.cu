@@ -95,6 +95,7 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
                  unsigned long long *__restrict__ clear, int64_t nclear) {
     constexpr int NR = kRounds * BPC;   // rounds of 32 rows per warp
     wait_prior_grid();   // before anything is read or cleared
+    allow_dependent_grid();   // the publish kernel behind it
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t b0 = (int64_t)blockIdx.x * BPC;
     // the other sums buffer, read by the previous op's expansion, is cleared
@@ -221,6 +222,7 @@ k2u_count_kernel(const int32_t *__restrict__ hist, int64_t R, int C, int scol, u
 // and group sums into pinned host memory, fences them system-wide, then writes
 // the sequence number the host waits for.
 __global__ void __launch_bounds__(kThreads) publish_kernel(const Publish pub) {
+    wait_prior_grid();   // the count kernel's sums are complete
     for (long long w = threadIdx.x; w < pub.n; w += blockDim.x) pub.dst[2 + w] = __ldcg(pub.src + w);
     __threadfence_system();
     __syncthreads();
@@ -846,7 +848,19 @@ void launch_k2u_count(const int32_t *hist, int64_t R, int C, int scol, uint32_t 
 #undef WK_COUNT
 }
 
-void launch_publish(const Publish &pub, cudaStream_t st) { publish_kernel<<<1, kThreads, 0, st>>>(pub); }
+// launched so that its one CTA is in place when the count kernel finishes
+void launch_publish(const Publish &pub, cudaStream_t st) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, publish_kernel, pub);
+}
 
 void launch_k2u_expand_func(const int32_t *hist, int64_t R, int C, const int32_t *nbr,
                             const unsigned long long *blk_sum, const unsigned long long *group_sums,
