@@ -66,9 +66,11 @@ __device__ __forceinline__ unsigned long long slices_of(unsigned long long t) {
 }
 
 // Programmatic dependent launch: a count kernel is launched so that its CTAs
-// may be placed while the previous op's expansion finishes its last wave;
-// each CTA first waits (in hardware) until that kernel has completed and its
-// writes are visible.  An expansion CTA allows the launch once it runs.
+// may be placed while the previous op's expansion finishes its last wave, and
+// the publish kernel so that its CTA is in place when the count finishes.
+// Each CTA of such a kernel first waits (in hardware) until the previous grid
+// has completed and its writes are visible; expansion and count CTAs allow
+// the dependent launch as soon as they run.
 __device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void allow_dependent_grid() { asm volatile("griddepcontrol.launch_dependents;"); }
 
